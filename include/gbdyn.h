@@ -1,0 +1,153 @@
+/*
+ * gbdyn.h -- C ABI of the GB300 (sm_103a) float64 dynamic step of TM5 as pydyn transcribes it.
+ *
+ * Every entry point returns GB_OK (0) or a status code; gb_last_error() gives the message of
+ * the last failure on the calling thread.  Arrays are device memory described by gb_view:
+ * a pointer plus up to four extents and element strides (the layout of a NumPy view of a
+ * C-contiguous pydyn array, any strides).  Work is enqueued on the context's one stream and
+ * returns without waiting; errors found on the device (a sub-cycle cap reached, non-zero halo
+ * faces, a search that would not converge) land in a device status word that gb_sync() reads.
+ *
+ * The reference interface each entry point replaces is named beside it, by file:line inside
+ * the pydyn project (pydyn/kernels.py, pydyn/zoom/..., pydyn/cfl.py, pydyn/diffusion.py,
+ * pydyn/chem.py); the device port of pydyn (pydyn/gpu/kernels.py) had the same roles.
+ */
+#ifndef GBDYN_H
+#define GBDYN_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* status codes (bit flags in the device status word) */
+enum {
+    GB_OK = 0,
+    GB_ECFL = 1,      /* a sub-cycle cap was reached: pydyn.kernels.CFLError (kernels.py:60) */
+    GB_EHALO = 2,     /* non-zero polar / boundary faces: the ValueError of kernels.py:233,301 */
+    GB_ELEVELS = 4,   /* rebin levels not strictly descending: chem.py:47-49 */
+    GB_ESEARCH = 8,   /* a region-wide sub-cycle search did not settle in its rounds */
+    GB_EARG = 16,     /* bad argument (host side) */
+    GB_ECUDA = 32,    /* a CUDA runtime call failed */
+    GB_ETIMEOUT = 64  /* a bounded device wait ran out */
+};
+
+typedef struct gb_ctx gb_ctx;
+
+/* A strided float64 (or int32) device array of rank <= 4; unused axes have n = 1, s = 0. */
+typedef struct {
+    void *p;
+    int64_t n[4];
+    int64_t s[4]; /* element strides */
+} gb_view;
+
+/* ------------------------------------------------------------------ context, memory, stream */
+int gb_create(int device, gb_ctx **out);
+void gb_destroy(gb_ctx *ctx);
+const char *gb_last_error(void);
+int gb_alloc(gb_ctx *ctx, size_t bytes, void **dptr);
+int gb_free(gb_ctx *ctx, void *dptr);
+int gb_put(gb_ctx *ctx, void *dst, const void *src, size_t bytes);      /* host -> device, async */
+int gb_get(gb_ctx *ctx, void *dst, const void *src, size_t bytes);      /* device -> host, waits */
+int gb_copy_d2d(gb_ctx *ctx, void *dst, const void *src, size_t bytes); /* async */
+int gb_host_alloc(size_t bytes, void **hptr);                           /* pinned host memory */
+int gb_host_free(void *hptr);
+int gb_stream_sync(gb_ctx *ctx);   /* wait for the stream */
+int gb_sync(gb_ctx *ctx);          /* wait for the stream, then read and clear the status word */
+int gb_status_peek(gb_ctx *ctx, int *word); /* read the status word without clearing it */
+int64_t gb_launches(gb_ctx *ctx);  /* kernels this context has launched (graph replays count theirs) */
+void *gb_stream(gb_ctx *ctx);      /* the cudaStream_t work is enqueued on */
+
+/* CUDA graphs of enqueued work: a whole step is captured once and replayed. */
+int gb_capture_begin(gb_ctx *ctx);
+int gb_capture_end(gb_ctx *ctx, void **graph);
+int gb_graph_launch(gb_ctx *ctx, void *graph);
+int gb_graph_destroy(void *graph);
+
+/* Timing: events recorded on the context's stream. */
+int gb_event_create(void **ev);
+int gb_event_record(gb_ctx *ctx, void *ev);
+int gb_event_elapsed_ms(void *start, void *stop, float *ms);
+int gb_event_destroy(void *ev);
+
+/* The Check_CFL rehearsal flag: the mass-only kernels set it on a failed operator, and every
+ * later rehearsal kernel returns without work while it is set (advectm_cfl's early return,
+ * zoom/check_cfl.py:222-236). */
+int gb_cfl_reset(gb_ctx *ctx);
+int gb_cfl_failed(gb_ctx *ctx, int *failed); /* waits for the stream */
+
+/* ------------------------------------------------------------------ box statements
+ * Elementwise statements on views of equal extents (dst may alias a source exactly).
+ * op: 0 dst = a; 1 dst = a * x; 2 dst = a / x; 3 dst = x (fill); 4 dst = a + b; 5 dst = a - b;
+ *     6 dst = a * b; 7 dst = a / b; 8 dst = (a * x) / y (the progressive rescale, ops.py:304);
+ *     9 dst = x * a + y * b (time interpolation, balance.py:63); 10 dst = x * a (scalar first)
+ * These carry the exchange, save/restore and halo statements of pydyn/zoom (exchange.py,
+ * host.py:56-70); evaluation per element is the NumPy statement's. */
+int gb_box(gb_ctx *ctx, int op, const gb_view *dst, const gb_view *a, const gb_view *b, double x,
+           double y);
+/* dst = seqsum of src over `axis` (src's extent along it), accumulated in index order
+ * (ops.seqsum, ops.py:235); dst has src's extents with that axis dropped (n = 1). */
+int gb_seqsum(gb_ctx *ctx, const gb_view *dst, const gb_view *src, int axis, double post_mul);
+
+/* ------------------------------------------------------------------ advection (pydyn/kernels.py)
+ * x: dynamu on every (j, l) row of a region (kernels.py:129-220, redgrid.py:56-110,
+ * zoom/advect.py:237-275).  m (im, jm, lm), tracers (im, jm, lm, nt) sharing strides,
+ * am (im+1, jm, lm).  clust (jm) int32 device array: the reduced-grid cluster size of each
+ * latitude (1 = uniform), or NULL.  halo: 1 also writes the periodic halos m/rm..(0, j) and
+ * (im+1, j) as zoom/advect.py:257-272 does (the views must then sit inside halo'd arrays).
+ * nloop_out (jm*lm int32) / amax_out (jm*lm float64): optional device outputs per row. */
+int gb_advect_x(gb_ctx *ctx, const gb_view *m, const gb_view *rm, const gb_view *rxm,
+                const gb_view *rym, const gb_view *rzm, const gb_view *am, const int32_t *clust,
+                int halo, int js, int je, int limits, int max_nloop, int32_t *nloop_out,
+                double *amax_out);
+/* y: dynamv (kernels.py:223-291 + zoom/advect.py:201-226).  m (im, jm, lm), bm (im, jm+1, lm);
+ * bm_full: the whole halo'd bm whose every face of each layer is rescaled with it (or NULL);
+ * bm_full_l0: the level of bm_full that is bm's level 0.  nloop_out: lm int32 (optional). */
+int gb_advect_y(gb_ctx *ctx, const gb_view *m, const gb_view *rm, const gb_view *rxm,
+                const gb_view *rym, const gb_view *rzm, const gb_view *bm, const gb_view *bm_full,
+                int bm_full_l0, int limits, int max_nloop, int32_t *nloop_out);
+/* z: dynamw (kernels.py:295-346).  cm (im, jm, lm+1); cm is left bitwise as it was.
+ * n_out: 1 int32 (optional). */
+int gb_advect_z(gb_ctx *ctx, const gb_view *m, const gb_view *rm, const gb_view *rxm,
+                const gb_view *rym, const gb_view *rzm, const gb_view *cm, int limits,
+                int iter_limit, int32_t *n_out);
+
+/* z on a scope: the search looks at every column of m (im, jm, lm), the sub-steps run on the
+ * columns [si0, si1) x [sj0, sj1) (0-based, half-open) -- a child's dynamw
+ * (zoom/advect.py:444-472, column_trial :415-441). */
+int gb_advect_z_scope(gb_ctx *ctx, const gb_view *m, const gb_view *rm, const gb_view *rxm,
+                      const gb_view *rym, const gb_view *rzm, const gb_view *cm, int si0, int si1,
+                      int sj0, int sj1, int limits, int iter_limit);
+
+/* ------------------------------------------------------------------ Check_CFL mass kernels (pydyn/cfl.py)
+ * dynamum (cfl.py:140) with the region-1 halos of zoom/check_cfl.py:94-110 when halo = 1. */
+int gb_cfl_x(gb_ctx *ctx, const gb_view *m, const gb_view *am, const int32_t *clust, int halo,
+             int js, int je, int max_nloop);
+/* dynamvm (cfl.py:170) */
+int gb_cfl_y(gb_ctx *ctx, const gb_view *m, const gb_view *bm, int max_nloop);
+/* dynamwm / zoom _dynamwm (cfl.py:186, zoom/check_cfl.py:206-216): the Courant search over the
+ * whole m (im, jm, lm) under cm (im, jm, lm+1), the mass advanced on the scope
+ * [si0, si1) x [sj0, sj1) (0-based, half-open) when every column passes. */
+int gb_cfl_z(gb_ctx *ctx, const gb_view *m, const gb_view *cm, int si0, int si1, int sj0, int sj1,
+             int iter_limit);
+
+/* ------------------------------------------------------------------ mass fluxes, pressure
+ * dynam0 (kernels.py:102-125, zoom/massflow.py:188-203): am = dt pu, bm = dt pv and cm from the
+ * column convergence.  pu (im+1, jm, lm), pv (im, jm+1, lm), bt (lm+1) device; am (im+1, jm, lm),
+ * bm (im, jm+1, lm), cm (im, jm, lm+1) destination views. */
+int gb_fluxes_from_meteo(gb_ctx *ctx, const gb_view *pu, const gb_view *pv, const double *bt,
+                         double dt, const gb_view *am, const gb_view *bm, const gb_view *cm);
+/* m2phlb1 / m2phlb (zoom/massflow.py:24-56): sp = seqsum_l(m) g / dxyp(j), phlb = at + bt sp.
+ * m (im, jm, lm); sp (im, jm); phlb (im, jm, lm+1); dxyp (jm); at, bt (lm+1).  ring: for a
+ * child, the ring cells' p rescaled by dxyp(j) xr yr / dxyp_parent(jpar) -- ring_xr, ring_yr,
+ * jbeg and dxyp_parent given (ring_xr = 0: region 1, no rescale). */
+int gb_m2phlb(gb_ctx *ctx, const gb_view *m, const gb_view *sp, const gb_view *phlb,
+              const double *dxyp, const double *at, const double *bt, int ring_xr, int ring_yr,
+              int jbeg, const double *dxyp_parent);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* GBDYN_H */

@@ -1,0 +1,32 @@
+"""ORACLE build recipe: compile oracle/src/*.c into oracle/_build/liboracle.so with gcc,
+-O2 and no floating-point contraction (-ffp-contract=off), so that every element is the
+IEEE result of the reference's own operation order on any host (x86-64 or aarch64).
+The transcendental functions come from the package's host math library (libgbmath.so), the
+same library the reference is pointed at through its pydyn.ops.use_libm hook when the golden
+fixtures are made."""
+
+import subprocess
+from pathlib import Path
+
+HERE = Path(__file__).resolve().parent
+SRC = HERE / "src"
+OUT = HERE / "_build"
+LIB = OUT / "liboracle.so"
+CFLAGS = ["-O2", "-fPIC", "-ffp-contract=off", "-fno-fast-math", "-std=c11", "-Wall"]
+
+
+def build():
+    OUT.mkdir(exist_ok=True)
+    srcs = sorted(SRC.glob("*.c"))
+    heads = sorted(SRC.glob("*.h"))
+    if LIB.exists() and all(s.stat().st_mtime <= LIB.stat().st_mtime for s in [*srcs, *heads]):
+        return LIB
+    cmd = ["gcc", *CFLAGS, "-shared", "-o", str(LIB), *map(str, srcs), "-lm"]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"oracle build failed:\n{r.stderr}")
+    return LIB
+
+
+if __name__ == "__main__":
+    print(build())

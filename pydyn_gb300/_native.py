@@ -1,0 +1,132 @@
+"""ctypes binding of libgbdyn.so (include/gbdyn.h).  There is no fallback: without the built
+library, or without a CUDA device, every call raises."""
+
+import ctypes
+from pathlib import Path
+
+import numpy as np
+
+from .build import LIBGBDYN, LIBGBMATH
+
+GB_OK, GB_ECFL, GB_EHALO, GB_ELEVELS, GB_ESEARCH, GB_EARG, GB_ECUDA, GB_ETIMEOUT = 0, 1, 2, 4, 8, 16, 32, 64
+
+
+class GBView(ctypes.Structure):
+    """gb_view: pointer, extents and element strides of a device array of rank <= 4."""
+
+    _fields_ = [("p", ctypes.c_void_p), ("n", ctypes.c_int64 * 4), ("s", ctypes.c_int64 * 4)]
+
+
+class CFLError(RuntimeError):
+    """A sub-cycle cap was reached (pydyn.kernels.CFLError, kernels.py:60-61)."""
+
+
+class DeviceError(RuntimeError):
+    """A failure reported by the device library."""
+
+
+_P = ctypes.POINTER(GBView)
+_VP = ctypes.c_void_p
+_I = ctypes.c_int
+_D = ctypes.c_double
+
+# name -> (restype, argtypes); every entry point include/gbdyn.h declares
+SIGNATURES = {
+    "gb_create": (_I, [_I, ctypes.POINTER(_VP)]),
+    "gb_destroy": (None, [_VP]),
+    "gb_last_error": (ctypes.c_char_p, []),
+    "gb_alloc": (_I, [_VP, ctypes.c_size_t, ctypes.POINTER(_VP)]),
+    "gb_free": (_I, [_VP, _VP]),
+    "gb_put": (_I, [_VP, _VP, _VP, ctypes.c_size_t]),
+    "gb_get": (_I, [_VP, _VP, _VP, ctypes.c_size_t]),
+    "gb_copy_d2d": (_I, [_VP, _VP, _VP, ctypes.c_size_t]),
+    "gb_host_alloc": (_I, [ctypes.c_size_t, ctypes.POINTER(_VP)]),
+    "gb_host_free": (_I, [_VP]),
+    "gb_stream_sync": (_I, [_VP]),
+    "gb_sync": (_I, [_VP]),
+    "gb_status_peek": (_I, [_VP, ctypes.POINTER(_I)]),
+    "gb_launches": (ctypes.c_int64, [_VP]),
+    "gb_stream": (_VP, [_VP]),
+    "gb_capture_begin": (_I, [_VP]),
+    "gb_capture_end": (_I, [_VP, ctypes.POINTER(_VP)]),
+    "gb_graph_launch": (_I, [_VP, _VP]),
+    "gb_graph_destroy": (_I, [_VP]),
+    "gb_event_create": (_I, [ctypes.POINTER(_VP)]),
+    "gb_event_record": (_I, [_VP, _VP]),
+    "gb_event_elapsed_ms": (_I, [_VP, _VP, ctypes.POINTER(ctypes.c_float)]),
+    "gb_event_destroy": (_I, [_VP]),
+    "gb_cfl_reset": (_I, [_VP]),
+    "gb_cfl_failed": (_I, [_VP, ctypes.POINTER(_I)]),
+    "gb_box": (_I, [_VP, _I, _P, _P, _P, _D, _D]),
+    "gb_seqsum": (_I, [_VP, _P, _P, _I, _D]),
+    "gb_advect_x": (_I, [_VP, _P, _P, _P, _P, _P, _P, _VP, _I, _I, _I, _I, _I, _VP, _VP]),
+    "gb_advect_y": (_I, [_VP, _P, _P, _P, _P, _P, _P, _P, _I, _I, _I, _VP]),
+    "gb_advect_z": (_I, [_VP, _P, _P, _P, _P, _P, _P, _I, _I, _VP]),
+    "gb_advect_z_scope": (_I, [_VP, _P, _P, _P, _P, _P, _P, _I, _I, _I, _I, _I, _I]),
+    "gb_cfl_x": (_I, [_VP, _P, _P, _VP, _I, _I, _I, _I]),
+    "gb_cfl_y": (_I, [_VP, _P, _P, _I]),
+    "gb_cfl_z": (_I, [_VP, _P, _P, _I, _I, _I, _I, _I]),
+    "gb_fluxes_from_meteo": (_I, [_VP, _P, _P, _VP, _D, _P, _P, _P]),
+    "gb_m2phlb": (_I, [_VP, _P, _P, _P, _VP, _VP, _VP, _I, _I, _I, _VP]),
+}
+
+_LIB = []
+
+
+def lib():
+    """The loaded libgbdyn.so with its prototypes set; raises if it was not built."""
+    if not _LIB:
+        path = Path(LIBGBDYN)
+        if not path.exists():
+            raise RuntimeError(f"pydyn_gb300: {path} is not built (run pydyn_gb300.build.build())")
+        L = ctypes.CDLL(str(path))
+        for name, (res, args) in SIGNATURES.items():
+            f = getattr(L, name)
+            f.restype, f.argtypes = res, args
+        _LIB.append(L)
+    return _LIB[0]
+
+
+def last_error():
+    msg = lib().gb_last_error()
+    return msg.decode() if msg else ""
+
+
+def check(rc, what=""):
+    """Raise for a non-zero status of a host-side call."""
+    if rc == GB_OK:
+        return
+    if rc & GB_ECFL:
+        raise CFLError(f"{what}: {last_error()}")
+    if rc & GB_EHALO:
+        raise ValueError(f"{what}: {last_error()}")
+    raise DeviceError(f"{what} failed ({rc}): {last_error()}")
+
+
+_MATH = []
+
+
+def mathlib():
+    """libgbmath.so: the host build of the device's transcendental functions."""
+    if not _MATH:
+        path = Path(LIBGBMATH)
+        if not path.exists():
+            raise RuntimeError(f"pydyn_gb300: {path} is not built")
+        L = ctypes.CDLL(str(path))
+        for name, nargs in (("exp", 1), ("log", 1), ("pow", 2), ("cos", 1), ("sin", 1)):
+            f = getattr(L, name)
+            f.restype, f.argtypes = ctypes.c_double, [ctypes.c_double] * nargs
+        _MATH.append(L)
+    return _MATH[0]
+
+
+def host_math(name, *arrays):
+    """Apply libgbmath's `name` elementwise on the host (float64 arrays, broadcast)."""
+    f = getattr(mathlib(), name)
+    arrs = np.broadcast_arrays(*(np.asarray(a, dtype=np.float64) for a in arrays))
+    out = np.empty(arrs[0].shape)
+    flat = [a.ravel() for a in arrs]
+    o = out.ravel()
+    for k in range(o.size):
+        o[k] = f(*(float(a[k]) for a in flat))
+    return out

@@ -1,0 +1,280 @@
+// dynamu: zonal slopes advection of every (j, l) row of a region, one warp per row.
+//
+// A row is staged in shared memory (lanes across its cells), clustered onto the reduced grid
+// when its latitude is reduced, searched for its smallest CFL-safe sub-cycle count (warp
+// vote), advanced through all its sub-steps on chip, split back onto the uniform cells and
+// written once.  Reference: pydyn kernels.py:129-220 (_advect_rows_x, subcycle_rows,
+// _substeps_x), redgrid.py:56-110 (uni2red, uni2red_mf, red2uni), zoom/advect.py:237-275
+// (_dynamu_region1's halos), cfl.py:140-167 (dynamum, the mass-only rehearsal).
+#include "gb_common.cuh"
+
+namespace {
+
+constexpr int WARPS = 4;
+
+struct XArgs {
+    DV m, q[4], am;
+    const int32_t *clust;
+    int im, jm, lm, nt;
+    int halo, js, je;    // halo writes on rows js..je (1-based, inclusive)
+    int limits, nmax;    // nmax = max_nloop - 1
+    int restore_am;      // 1: am = a * nloop written back (no reduced grid); 0: am untouched
+    int ncell;           // smem cells per array (im + 2)
+    int32_t *nloop_out;
+    double *amax_out;
+    gb_ctl *ctl;
+};
+
+__device__ __forceinline__ double &AT(const DV &v, int64_t i, int64_t j, int64_t l) {
+    return v.p[i * v.s0 + j * v.s1 + l * v.s2];
+}
+__device__ __forceinline__ double &AT4(const DV &v, int64_t i, int64_t j, int64_t l, int64_t t) {
+    return v.p[i * v.s0 + j * v.s1 + l * v.s2 + t * v.s3];
+}
+
+// The per-row CFL search (kernels.py:169-199, periodic): the smallest nloop for which nloop
+// trial sub-steps of the mass stay under |Courant| < 1 on every face (division form,
+// ops.py:267-270), the faces rescaled by (n-1)/n per retry.  Returns nloop, or nmax + 1.
+__device__ int row_search(double *m_s, double *mx_s, double *a_s, int n, int nmax, int lane, double &amax_out) {
+    int nloop = 1;
+    while (true) {
+        for (int k = lane; k < n; k += GB_WARP) mx_s[k] = m_s[k];
+        __syncwarp();
+        bool ok = true;
+        double amax = 0.0;
+        for (int s = 0; s < nloop; ++s) {
+            bool lok = true;
+            double cmax = 0.0;
+            for (int k = lane; k <= n; k += GB_WARP) {
+                double f = a_s[k];
+                int up = (f >= 0.0) ? (k == 0 ? n - 1 : k - 1) : (k == n ? 0 : k);
+                double c = fabs(f / mx_s[up]);
+                lok = lok && (c < 1.0);
+                cmax = (c > cmax) ? c : cmax;
+            }
+            ok = __all_sync(FULL_MASK, lok);
+            if (!ok) break;
+            for (int o = 16; o > 0; o >>= 1) {
+                double other = __shfl_xor_sync(FULL_MASK, cmax, o);
+                cmax = (other > cmax) ? other : cmax;
+            }
+            amax = (amax > cmax) ? amax : cmax;
+            __syncwarp();
+            for (int k = lane; k < n; k += GB_WARP) mx_s[k] = (mx_s[k] + a_s[k]) - a_s[k + 1];
+            __syncwarp();
+        }
+        if (ok) {
+            amax_out = amax;
+            return nloop;
+        }
+        nloop += 1;
+        for (int k = lane; k <= n; k += GB_WARP) a_s[k] = (a_s[k] * (double)(nloop - 1)) / (double)nloop;
+        __syncwarp();
+        if (nloop > nmax) {
+            amax_out = 0.0;
+            return nloop;
+        }
+    }
+}
+
+template <bool MASS_ONLY>
+__global__ void __launch_bounds__(WARPS * 32) k_advect_x(XArgs A) {
+    extern __shared__ double smem[];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int64_t row = (int64_t)blockIdx.x * WARPS + warp;
+    if (row >= (int64_t)A.jm * A.lm) return;
+    if (MASS_ONLY && __shfl_sync(FULL_MASK, *(volatile int *)&A.ctl->cfl_failed, 0)) return;
+    const int j = (int)(row / A.lm), l = (int)(row % A.lm);
+    const int nt = MASS_ONLY ? 0 : A.nt;
+    const int NC = A.ncell;
+    const int per_warp = NC * (4 + 8 * nt);
+    double *m_s = smem + (size_t)warp * per_warp;
+    double *mx_s = m_s + NC;
+    double *minv_s = mx_s + NC;
+    double *a_s = minv_s + NC;
+    double *q_s = a_s + NC;          // [4][nt][NC]: rm, rxm, rym, rzm
+    double *f_s = q_s + 4 * nt * NC; // [4][nt][NC]: f, pf, fy, fz
+    auto Q = [&](int w, int t) { return q_s + (size_t)(w * nt + t) * NC; };
+    auto F = [&](int w, int t) { return f_s + (size_t)(w * nt + t) * NC; };
+
+    const int c = (A.clust && A.clust[j] > 1) ? A.clust[j] : 1;
+    const int n = A.im / c;
+    const bool reduced = c > 1;
+
+    // ---- stage the row: cluster sums onto the reduced cells (uni2red, seqsum in order)
+    for (int k = lane; k < n; k += GB_WARP) {
+        double acc = AT(A.m, (int64_t)k * c, j, l);
+        for (int cc = 1; cc < c; ++cc) acc = acc + AT(A.m, (int64_t)k * c + cc, j, l);
+        m_s[k] = acc;
+        for (int w = 0; w < 4; ++w)
+            for (int t = 0; t < nt; ++t) {
+                double s = AT4(A.q[w], (int64_t)k * c, j, l, t);
+                for (int cc = 1; cc < c; ++cc) s = s + AT4(A.q[w], (int64_t)k * c + cc, j, l, t);
+                Q(w, t)[k] = s;
+            }
+    }
+    // faces: a(i) = am(i c) for i = 1..n, a(0) = a(n) on a reduced row (uni2red_mf)
+    for (int k = lane; k <= n; k += GB_WARP) {
+        int src = (k == 0) ? (reduced ? n * c : 0) : k * c;
+        a_s[k] = AT(A.am, src, j, l);
+    }
+    __syncwarp();
+
+    if (!MASS_ONLY && A.limits)
+        for (int t = 0; t < nt; ++t)
+            for (int k = lane; k < n; k += GB_WARP) Q(1, t)[k] = np_limit(Q(1, t)[k], Q(0, t)[k]);
+
+    double amax = 0.0;
+    const int nloop = row_search(m_s, mx_s, a_s, n, A.nmax, lane, amax);
+    if (nloop > A.nmax) {
+        if (lane == 0) {
+            if (MASS_ONLY)
+                atomicExch(&A.ctl->cfl_failed, 1);
+            else
+                raise_status(A.ctl, GB_ECFL);
+            if (A.nloop_out) A.nloop_out[row] = nloop;
+        }
+        return;
+    }
+
+    if (MASS_ONLY) {
+        for (int s = 0; s < nloop; ++s) {
+            for (int k = lane; k < n; k += GB_WARP) m_s[k] = (m_s[k] + a_s[k]) - a_s[k + 1];
+            __syncwarp();
+        }
+    } else {
+        for (int k = lane; k < n; k += GB_WARP) minv_s[k] = 1.0 / m_s[k];
+        __syncwarp();
+        for (int s = 0; s < nloop; ++s) {
+            // faces 1..n; face 0 is the periodic seam, a copy of face n
+            for (int k = lane + 1; k <= n; k += GB_WARP) {
+                double f = a_s[k];
+                int up = (f >= 0.0) ? k - 1 : (k == n ? 0 : k);
+                double alpha = f * minv_s[up];  // the reciprocal form of production dynamu
+                for (int t = 0; t < nt; ++t) {
+                    double ff, pf, fy, fz;
+                    slopes_flux(f, alpha, Q(0, t)[up], Q(1, t)[up], Q(2, t)[up], Q(3, t)[up], ff, pf, fy, fz);
+                    F(0, t)[k] = ff; F(1, t)[k] = pf; F(2, t)[k] = fy; F(3, t)[k] = fz;
+                }
+            }
+            __syncwarp();
+            for (int i = lane; i < n; i += GB_WARP) {
+                const int lo = (i == 0) ? n : i;
+                const double mo = m_s[i], alo = a_s[i], ahi = a_s[i + 1];
+                const double mn = (mo + alo) - ahi;
+                for (int t = 0; t < nt; ++t) {
+                    double *f = F(0, t), *pf = F(1, t), *fy = F(2, t), *fz = F(3, t);
+                    double rmn = Q(0, t)[i] - (f[i + 1] - f[lo]);
+                    double rxn = along_slope(Q(1, t)[i], pf[lo], pf[i + 1], alo, ahi, rmn, f[lo], f[i + 1], mo, mn);
+                    if (A.limits) rxn = np_limit(rxn, rmn);
+                    Q(0, t)[i] = rmn;
+                    Q(1, t)[i] = rxn;
+                    Q(2, t)[i] = Q(2, t)[i] - (fy[i + 1] - fy[lo]);
+                    Q(3, t)[i] = Q(3, t)[i] - (fz[i + 1] - fz[lo]);
+                }
+                m_s[i] = mn;
+                minv_s[i] = 1.0 / mn;
+            }
+            __syncwarp();
+        }
+    }
+
+    if (A.nloop_out && lane == 0) A.nloop_out[row] = nloop;
+    if (A.amax_out && lane == 0) A.amax_out[row] = amax;
+
+    if (A.restore_am)  // "restore old am": a * nloop, not an exact round trip
+        for (int k = lane; k <= n; k += GB_WARP) AT(A.am, k, j, l) = a_s[k] * (double)nloop;
+
+    const bool in_scope = (j + 1 >= A.js) && (j + 1 <= A.je);
+    if (!reduced) {
+        for (int i = lane; i < n; i += GB_WARP) {
+            AT(A.m, i, j, l) = m_s[i];
+            for (int w = 0; w < 4; ++w)
+                for (int t = 0; t < nt; ++t) AT4(A.q[w], i, j, l, t) = Q(w, t)[i];
+        }
+        if (A.halo && in_scope && lane == 0) {  // q(0) = q(im), q(im+1) = q(1)
+            AT(A.m, -1, j, l) = m_s[n - 1];
+            AT(A.m, n, j, l) = m_s[0];
+            for (int w = 0; w < 4; ++w)
+                for (int t = 0; t < nt; ++t) {
+                    AT4(A.q[w], -1, j, l, t) = Q(w, t)[n - 1];
+                    AT4(A.q[w], n, j, l, t) = Q(w, t)[0];
+                }
+        }
+    } else {
+        // red2uni: the uniform mass update with the untouched am, and every cell of a cluster
+        // given its share m_uni(i) / m(cluster) of the cluster's tracers
+        const int im = A.im;
+        for (int i = lane; i < im; i += GB_WARP) {
+            const int k = i / c;
+            double mun = (AT(A.m, i, j, l) + AT(A.am, i, j, l)) - AT(A.am, i + 1, j, l);
+            double sc = mun / m_s[k];
+            for (int w = 0; w < 4; ++w)
+                for (int t = 0; t < nt; ++t) AT4(A.q[w], i, j, l, t) = sc * Q(w, t)[k];
+            AT(A.m, i, j, l) = mun;
+            if (A.halo && i == im - 1 && (MASS_ONLY ? in_scope : true)) {  // q(0) = q(im) after red2uni
+                AT(A.m, -1, j, l) = mun;
+                for (int w = 0; w < 4; ++w)
+                    for (int t = 0; t < nt; ++t) AT4(A.q[w], -1, j, l, t) = sc * Q(w, t)[k];
+            }
+        }
+    }
+}
+
+int launch_x(gb_ctx *ctx, XArgs &A, bool mass_only) {
+    A.ncell = A.im + 2;
+    const int nt = mass_only ? 0 : A.nt;
+    size_t smem = (size_t)WARPS * A.ncell * (4 + 8 * nt) * sizeof(double);
+    int64_t rows = (int64_t)A.jm * A.lm;
+    int blocks = (int)((rows + WARPS - 1) / WARPS);
+    if (blocks == 0) return GB_OK;
+    if (mass_only) {
+        GB_CHECK_CUDA(cudaFuncSetAttribute(k_advect_x<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        k_advect_x<true><<<blocks, WARPS * 32, smem, ctx->stream>>>(A);
+    } else {
+        GB_CHECK_CUDA(cudaFuncSetAttribute(k_advect_x<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        k_advect_x<false><<<blocks, WARPS * 32, smem, ctx->stream>>>(A);
+    }
+    return gb_after_launch(ctx, mass_only ? "cfl_x" : "advect_x");
+}
+
+}  // namespace
+
+extern "C" int gb_advect_x(gb_ctx *ctx, const gb_view *m, const gb_view *rm, const gb_view *rxm,
+                           const gb_view *rym, const gb_view *rzm, const gb_view *am,
+                           const int32_t *clust, int halo, int js, int je, int limits, int max_nloop,
+                           int32_t *nloop_out, double *amax_out) {
+    if (!ctx || !m || !rm || !rxm || !rym || !rzm || !am) return GB_EARG;
+    XArgs A{};
+    A.m = dv(m);
+    A.q[0] = dv(rm); A.q[1] = dv(rxm); A.q[2] = dv(rym); A.q[3] = dv(rzm);
+    A.am = dv(am);
+    A.clust = clust;
+    A.im = (int)m->n[0]; A.jm = (int)m->n[1]; A.lm = (int)m->n[2]; A.nt = (int)rm->n[3];
+    if (am->n[0] != A.im + 1) {
+        gb_set_error("gb_advect_x: am must have im+1 faces");
+        return GB_EARG;
+    }
+    A.halo = halo; A.js = js; A.je = je;
+    A.limits = limits; A.nmax = max_nloop - 1;
+    A.restore_am = clust ? 0 : 1;
+    A.nloop_out = nloop_out; A.amax_out = amax_out;
+    A.ctl = ctx->ctl;
+    return launch_x(ctx, A, false);
+}
+
+extern "C" int gb_cfl_x(gb_ctx *ctx, const gb_view *m, const gb_view *am, const int32_t *clust, int halo,
+                        int js, int je, int max_nloop) {
+    if (!ctx || !m || !am) return GB_EARG;
+    XArgs A{};
+    A.m = dv(m);
+    for (int w = 0; w < 4; ++w) A.q[w] = A.m;
+    A.am = dv(am);
+    A.clust = clust;
+    A.im = (int)m->n[0]; A.jm = (int)m->n[1]; A.lm = (int)m->n[2]; A.nt = 0;
+    A.halo = halo; A.js = js; A.je = je;
+    A.limits = 0; A.nmax = max_nloop - 1;
+    A.restore_am = clust ? 0 : 1;
+    A.ctl = ctx->ctl;
+    return launch_x(ctx, A, true);
+}

@@ -1,0 +1,122 @@
+// Shared pieces of the gbdyn kernels: the context, device views, the status word, and the
+// per-element arithmetic of the slopes scheme in NumPy's evaluation order.
+//
+// Every kernel is float64 and compiled with -fmad=false: no multiply-add contraction, no
+// reassociation, IEEE division and square root.  That is what makes each element's value the
+// one the NumPy reference computes.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <cstdint>
+#include <cstdio>
+#include <string>
+
+#include "../../include/gbdyn.h"
+
+// ------------------------------------------------------------------ context
+struct gb_ctl {         // device-resident control block, one per context
+    int status;         // GB_* error bits, or-ed by kernels
+    int cfl_failed;     // Check_CFL rehearsal: an operator exceeded its cap
+    int zsearch_n[8];   // z search rounds: candidate n_advz after each round
+    int zsearch_changed[8];
+    int ysearch_fail;   // scratch
+    int pad[5];
+    double stats[4];
+};
+
+struct gb_ctx {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    gb_ctl *ctl = nullptr;         // device
+    int32_t *scratch_i = nullptr;  // per-op integer scratch (layer nloops, ...)
+    size_t scratch_i_n = 0;
+    int64_t launches = 0;
+    bool capturing = false;
+    int64_t capture_launches = 0;
+};
+
+void gb_set_error(const std::string &msg);
+int gb_cuda_fail(cudaError_t e, const char *what);
+int gb_after_launch(gb_ctx *ctx, const char *what);
+int32_t *gb_scratch_i(gb_ctx *ctx, size_t n);
+
+#define GB_CHECK_CUDA(call)                                   \
+    do {                                                      \
+        cudaError_t e_ = (call);                              \
+        if (e_ != cudaSuccess) return gb_cuda_fail(e_, #call); \
+    } while (0)
+
+// ------------------------------------------------------------------ views
+struct DV {  // device view of a float64 array, rank <= 4
+    double *p;
+    int64_t n0, n1, n2, n3;
+    int64_t s0, s1, s2, s3;
+};
+
+static inline DV dv(const gb_view *v) {
+    DV d;
+    d.p = (double *)v->p;
+    d.n0 = v->n[0]; d.n1 = v->n[1]; d.n2 = v->n[2]; d.n3 = v->n[3];
+    d.s0 = v->s[0]; d.s1 = v->s[1]; d.s2 = v->s[2]; d.s3 = v->s[3];
+    return d;
+}
+
+// ------------------------------------------------------------------ NumPy's element rules
+// np.clip(s, -|r|, |r|) exactly as NumPy evaluates it: a NaN in s wins, then max with the lower
+// bound ((s > lo) ? s : lo), then a NaN wins again, then min with the upper bound.
+__device__ __forceinline__ double np_limit(double s, double r) {
+    double hi = fabs(r);
+    double lo = -hi;
+    double t = isnan(s) ? s : (s > lo ? s : lo);
+    return isnan(t) ? t : (t < hi ? t : hi);
+}
+
+// np.maximum(a, b): NaN in a, else NaN in b, else (a > b ? a : b).
+__device__ __forceinline__ double np_max(double a, double b) {
+    return isnan(a) ? a : (isnan(b) ? b : (a > b ? a : b));
+}
+__device__ __forceinline__ double np_min(double a, double b) {
+    return isnan(a) ? a : (isnan(b) ? b : (a < b ? a : b));
+}
+
+// Tracer fluxes of the slopes scheme through one face (pydyn kernels.py:75-84): the flux,
+// its Courant number c and the upwind cell's mass rm_u, along-slope s_u and cross slopes.
+__device__ __forceinline__ void slopes_flux(double flux, double c, double rm_u, double s_u,
+                                            double t_u, double w_u, double &f, double &pf,
+                                            double &ft, double &fw) {
+    double ff;
+    if (flux >= 0.0)
+        ff = c * (rm_u + (1.0 - c) * s_u);
+    else
+        ff = c * (rm_u - (1.0 + c) * s_u);
+    f = ff;
+    pf = flux * (c * c * s_u - 3.0 * ff);
+    ft = c * t_u;
+    fw = c * w_u;
+}
+
+// The along-flow slope after one sub-step (kernels.py:87-92):
+// s + (pf_lo - pf_hi - (lo - hi) s + 3 ((lo + hi) rm_new - (f_lo + f_hi) m_old)) / m_new
+__device__ __forceinline__ double along_slope(double s, double pf_lo, double pf_hi, double lo,
+                                              double hi, double rm_new, double f_lo, double f_hi,
+                                              double m_old, double m_new) {
+    double num = ((pf_lo - pf_hi) - (lo - hi) * s) + 3.0 * ((lo + hi) * rm_new - (f_lo + f_hi) * m_old);
+    return s + num / m_new;
+}
+
+// The progressive rescale of dynamu / dynamv (ops.py:304-307): f * (n - 1) / n, evaluated
+// left to right, applied once per retry n = 2 .. nloop.
+__device__ __forceinline__ double progressive_chain(double f, int nloop) {
+    for (int n = 2; n <= nloop; ++n) f = (f * (double)(n - 1)) / (double)n;
+    return f;
+}
+
+__device__ __forceinline__ void raise_status(gb_ctl *ctl, int bits) { atomicOr(&ctl->status, bits); }
+
+// max of non-negative doubles through their bit patterns (order-free)
+__device__ __forceinline__ void atomic_max_nonneg(double *addr, double v) {
+    atomicMax((unsigned long long *)addr, (unsigned long long)__double_as_longlong(v));
+}
+
+#define GB_WARP 32
+#define FULL_MASK 0xffffffffu

@@ -1,0 +1,306 @@
+// The context of the C ABI: device memory, the one stream, the device status word, CUDA graph
+// capture and the generic box statements (strided elementwise statements and ordered sums) that
+// carry the zoom exchange.
+#include "gb_common.cuh"
+
+#include <mutex>
+#include <new>
+
+static thread_local std::string g_last_error;
+
+void gb_set_error(const std::string &msg) { g_last_error = msg; }
+
+int gb_cuda_fail(cudaError_t e, const char *what) {
+    g_last_error = std::string(what) + ": " + cudaGetErrorString(e);
+    return GB_ECUDA;
+}
+
+int gb_after_launch(gb_ctx *ctx, const char *what) {
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return gb_cuda_fail(e, what);
+    ctx->launches += 1;
+    if (ctx->capturing) ctx->capture_launches += 1;
+    return GB_OK;
+}
+
+int32_t *gb_scratch_i(gb_ctx *ctx, size_t n) {
+    if (n <= ctx->scratch_i_n) return ctx->scratch_i;
+    return nullptr;  // grown only outside capture, by gb_create's fixed size
+}
+
+extern "C" const char *gb_last_error(void) { return g_last_error.c_str(); }
+
+extern "C" int gb_create(int device, gb_ctx **out) {
+    if (!out) return GB_EARG;
+    GB_CHECK_CUDA(cudaSetDevice(device));
+    gb_ctx *ctx = new (std::nothrow) gb_ctx();
+    if (!ctx) return GB_EARG;
+    ctx->device = device;
+    cudaError_t e = cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaMalloc(&ctx->ctl, sizeof(gb_ctl));
+    if (e == cudaSuccess) e = cudaMemset(ctx->ctl, 0, sizeof(gb_ctl));
+    ctx->scratch_i_n = 1 << 16;
+    if (e == cudaSuccess) e = cudaMalloc(&ctx->scratch_i, ctx->scratch_i_n * sizeof(int32_t));
+    if (e == cudaSuccess) e = cudaMemset(ctx->scratch_i, 0, ctx->scratch_i_n * sizeof(int32_t));
+    if (e != cudaSuccess) {
+        delete ctx;
+        return gb_cuda_fail(e, "gb_create");
+    }
+    *out = ctx;
+    return GB_OK;
+}
+
+extern "C" void gb_destroy(gb_ctx *ctx) {
+    if (!ctx) return;
+    cudaSetDevice(ctx->device);
+    if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+    if (ctx->ctl) cudaFree(ctx->ctl);
+    if (ctx->scratch_i) cudaFree(ctx->scratch_i);
+    if (ctx->stream) cudaStreamDestroy(ctx->stream);
+    delete ctx;
+}
+
+extern "C" int gb_alloc(gb_ctx *ctx, size_t bytes, void **dptr) {
+    if (!ctx || !dptr) return GB_EARG;
+    GB_CHECK_CUDA(cudaMalloc(dptr, bytes ? bytes : 8));
+    GB_CHECK_CUDA(cudaMemset(*dptr, 0, bytes ? bytes : 8));
+    return GB_OK;
+}
+
+extern "C" int gb_free(gb_ctx *ctx, void *dptr) {
+    (void)ctx;
+    GB_CHECK_CUDA(cudaFree(dptr));
+    return GB_OK;
+}
+
+extern "C" int gb_put(gb_ctx *ctx, void *dst, const void *src, size_t bytes) {
+    GB_CHECK_CUDA(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, ctx->stream));
+    return GB_OK;
+}
+
+extern "C" int gb_get(gb_ctx *ctx, void *dst, const void *src, size_t bytes) {
+    GB_CHECK_CUDA(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, ctx->stream));
+    GB_CHECK_CUDA(cudaStreamSynchronize(ctx->stream));
+    return GB_OK;
+}
+
+extern "C" int gb_copy_d2d(gb_ctx *ctx, void *dst, const void *src, size_t bytes) {
+    GB_CHECK_CUDA(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToDevice, ctx->stream));
+    return GB_OK;
+}
+
+extern "C" int gb_stream_sync(gb_ctx *ctx) {
+    GB_CHECK_CUDA(cudaStreamSynchronize(ctx->stream));
+    return GB_OK;
+}
+
+extern "C" int gb_host_alloc(size_t bytes, void **hptr) {
+    GB_CHECK_CUDA(cudaMallocHost(hptr, bytes ? bytes : 8));
+    return GB_OK;
+}
+
+extern "C" int gb_host_free(void *hptr) {
+    GB_CHECK_CUDA(cudaFreeHost(hptr));
+    return GB_OK;
+}
+
+extern "C" int gb_status_peek(gb_ctx *ctx, int *word) {
+    int w = 0;
+    GB_CHECK_CUDA(cudaMemcpyAsync(&w, &ctx->ctl->status, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+    GB_CHECK_CUDA(cudaStreamSynchronize(ctx->stream));
+    *word = w;
+    return GB_OK;
+}
+
+extern "C" int gb_sync(gb_ctx *ctx) {
+    int w = 0;
+    GB_CHECK_CUDA(cudaStreamSynchronize(ctx->stream));
+    GB_CHECK_CUDA(cudaMemcpy(&w, &ctx->ctl->status, sizeof(int), cudaMemcpyDeviceToHost));
+    if (w) {
+        int zero = 0;
+        GB_CHECK_CUDA(cudaMemcpy(&ctx->ctl->status, &zero, sizeof(int), cudaMemcpyHostToDevice));
+        std::string msg;
+        if (w & GB_ECFL) msg += "sub-cycle cap reached (CFL); ";
+        if (w & GB_EHALO) msg += "non-zero boundary faces; ";
+        if (w & GB_ELEVELS) msg += "levels not strictly descending; ";
+        if (w & GB_ESEARCH) msg += "sub-cycle search did not settle; ";
+        if (w & GB_ETIMEOUT) msg += "device wait timed out; ";
+        gb_set_error(msg);
+    }
+    return w;
+}
+
+extern "C" int64_t gb_launches(gb_ctx *ctx) { return ctx->launches; }
+
+extern "C" void *gb_stream(gb_ctx *ctx) { return (void *)ctx->stream; }
+
+// ------------------------------------------------------------------ graphs
+struct gb_graph {
+    cudaGraph_t graph;
+    cudaGraphExec_t exec;
+    int64_t launches;
+};
+
+extern "C" int gb_capture_begin(gb_ctx *ctx) {
+    GB_CHECK_CUDA(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
+    ctx->capturing = true;
+    ctx->capture_launches = 0;
+    return GB_OK;
+}
+
+extern "C" int gb_capture_end(gb_ctx *ctx, void **out) {
+    gb_graph *g = new gb_graph();
+    ctx->capturing = false;
+    cudaError_t e = cudaStreamEndCapture(ctx->stream, &g->graph);
+    if (e != cudaSuccess) {
+        delete g;
+        return gb_cuda_fail(e, "cudaStreamEndCapture");
+    }
+    e = cudaGraphInstantiate(&g->exec, g->graph, 0);
+    if (e != cudaSuccess) {
+        cudaGraphDestroy(g->graph);
+        delete g;
+        return gb_cuda_fail(e, "cudaGraphInstantiate");
+    }
+    g->launches = ctx->capture_launches;
+    ctx->launches -= ctx->capture_launches;  // counted when replayed
+    *out = g;
+    return GB_OK;
+}
+
+extern "C" int gb_graph_launch(gb_ctx *ctx, void *graph) {
+    gb_graph *g = (gb_graph *)graph;
+    GB_CHECK_CUDA(cudaGraphLaunch(g->exec, ctx->stream));
+    ctx->launches += g->launches;
+    return GB_OK;
+}
+
+extern "C" int gb_graph_destroy(void *graph) {
+    gb_graph *g = (gb_graph *)graph;
+    if (!g) return GB_OK;
+    cudaGraphExecDestroy(g->exec);
+    cudaGraphDestroy(g->graph);
+    delete g;
+    return GB_OK;
+}
+
+// ------------------------------------------------------------------ events
+extern "C" int gb_event_create(void **ev) {
+    cudaEvent_t e;
+    GB_CHECK_CUDA(cudaEventCreate(&e));
+    *ev = (void *)e;
+    return GB_OK;
+}
+extern "C" int gb_event_record(gb_ctx *ctx, void *ev) {
+    GB_CHECK_CUDA(cudaEventRecord((cudaEvent_t)ev, ctx->stream));
+    return GB_OK;
+}
+extern "C" int gb_event_elapsed_ms(void *start, void *stop, float *ms) {
+    GB_CHECK_CUDA(cudaEventSynchronize((cudaEvent_t)stop));
+    GB_CHECK_CUDA(cudaEventElapsedTime(ms, (cudaEvent_t)start, (cudaEvent_t)stop));
+    return GB_OK;
+}
+extern "C" int gb_event_destroy(void *ev) {
+    GB_CHECK_CUDA(cudaEventDestroy((cudaEvent_t)ev));
+    return GB_OK;
+}
+
+// ------------------------------------------------------------------ Check_CFL flag
+__global__ void k_cfl_reset(gb_ctl *ctl) { ctl->cfl_failed = 0; }
+
+extern "C" int gb_cfl_reset(gb_ctx *ctx) {
+    k_cfl_reset<<<1, 1, 0, ctx->stream>>>(ctx->ctl);
+    return gb_after_launch(ctx, "cfl_reset");
+}
+
+extern "C" int gb_cfl_failed(gb_ctx *ctx, int *failed) {
+    int w = 0;
+    GB_CHECK_CUDA(cudaMemcpyAsync(&w, &ctx->ctl->cfl_failed, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+    GB_CHECK_CUDA(cudaStreamSynchronize(ctx->stream));
+    *failed = w;
+    return GB_OK;
+}
+
+// ------------------------------------------------------------------ box statements
+__device__ __forceinline__ int64_t off4(const DV &v, int64_t i0, int64_t i1, int64_t i2, int64_t i3) {
+    return i0 * v.s0 + i1 * v.s1 + i2 * v.s2 + i3 * v.s3;
+}
+
+__global__ void k_box(int op, DV d, DV a, DV b, double x, double y, int64_t total) {
+    int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    for (; k < total; k += stride) {
+        int64_t r = k;
+        int64_t i3 = r % d.n3; r /= d.n3;
+        int64_t i2 = r % d.n2; r /= d.n2;
+        int64_t i1 = r % d.n1; r /= d.n1;
+        int64_t i0 = r;
+        double va = (op != 3) ? a.p[off4(a, i0, i1, i2, i3)] : 0.0;
+        double vb = (op >= 4 && op <= 7) || op == 9 ? b.p[off4(b, i0, i1, i2, i3)] : 0.0;
+        double out;
+        switch (op) {
+            case 0: out = va; break;
+            case 1: out = va * x; break;
+            case 2: out = va / x; break;
+            case 3: out = x; break;
+            case 4: out = va + vb; break;
+            case 5: out = va - vb; break;
+            case 6: out = va * vb; break;
+            case 7: out = va / vb; break;
+            case 8: out = (va * x) / y; break;
+            case 9: out = x * va + y * vb; break;
+            case 10: out = x * va; break;
+            default: out = va; break;
+        }
+        d.p[off4(d, i0, i1, i2, i3)] = out;
+    }
+}
+
+static int launch_grid(int64_t total) {
+    int64_t blocks = (total + 255) / 256;
+    if (blocks > 152 * 16) blocks = 152 * 16;
+    if (blocks < 1) blocks = 1;
+    return (int)blocks;
+}
+
+extern "C" int gb_box(gb_ctx *ctx, int op, const gb_view *dst, const gb_view *a, const gb_view *b,
+                      double x, double y) {
+    if (!dst) return GB_EARG;
+    DV d = dv(dst);
+    DV va = a ? dv(a) : d;
+    DV vb = b ? dv(b) : d;
+    int64_t total = d.n0 * d.n1 * d.n2 * d.n3;
+    if (total <= 0) return GB_OK;
+    k_box<<<launch_grid(total), 256, 0, ctx->stream>>>(op, d, va, vb, x, y, total);
+    return gb_after_launch(ctx, "box");
+}
+
+// dst[...] = seqsum over `axis` of src (accumulated in index order), times post_mul if != 1
+__global__ void k_seqsum(DV d, DV s, int axis, int64_t len, double post_mul, int use_mul, int64_t total) {
+    int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    int64_t sstep = axis == 0 ? s.s0 : axis == 1 ? s.s1 : axis == 2 ? s.s2 : s.s3;
+    for (; k < total; k += stride) {
+        int64_t r = k;
+        int64_t i3 = r % d.n3; r /= d.n3;
+        int64_t i2 = r % d.n2; r /= d.n2;
+        int64_t i1 = r % d.n1; r /= d.n1;
+        int64_t i0 = r;
+        const double *q = s.p + off4(s, i0, i1, i2, i3);
+        double acc = q[0];
+        for (int64_t t = 1; t < len; ++t) acc = acc + q[t * sstep];
+        if (use_mul) acc = acc * post_mul;
+        d.p[off4(d, i0, i1, i2, i3)] = acc;
+    }
+}
+
+extern "C" int gb_seqsum(gb_ctx *ctx, const gb_view *dst, const gb_view *src, int axis, double post_mul) {
+    if (!dst || !src || axis < 0 || axis > 3) return GB_EARG;
+    DV d = dv(dst), s = dv(src);
+    int64_t len = src->n[axis];
+    // the destination iterates src's other axes; the summed axis has extent 1 there
+    int64_t total = d.n0 * d.n1 * d.n2 * d.n3;
+    if (total <= 0) return GB_OK;
+    k_seqsum<<<launch_grid(total), 256, 0, ctx->stream>>>(d, s, axis, len, post_mul, post_mul != 1.0, total);
+    return gb_after_launch(ctx, "seqsum");
+}

@@ -1,0 +1,93 @@
+// dynam0 and m2phlb: the per-half-step mass fluxes from the meteo fluxes, and the surface
+// pressure / half-level pressures from the column mass.
+// Reference: pydyn kernels.py:102-125 (fluxes_from_meteo), ops.py:273-274 (convergence),
+// zoom/massflow.py:24-56 (m2phlb1, m2phlb), balance.py:222-226.
+#include "gb_common.cuh"
+
+namespace {
+
+constexpr double GRAV = 9.80665;  // Binas, balance.py
+
+__device__ __forceinline__ double &AT(const DV &v, int64_t i, int64_t j, int64_t l) {
+    return v.p[i * v.s0 + j * v.s1 + l * v.s2];
+}
+
+// One thread per (i, j) of the face grid [0, im] x [0, jm]: its am column (j < jm), its bm
+// column (i < im) and, for a cell column, cm from the convergence distributed by the hybrid b.
+__global__ void k_fluxes(DV pu, DV pv, const double *bt, double dt, DV am, DV bm, DV cm, int im, int jm, int lm) {
+    int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (k >= (int64_t)(im + 1) * (jm + 1)) return;
+    const int i = (int)(k / (jm + 1)), j = (int)(k % (jm + 1));
+    if (j < jm)
+        for (int l = 0; l < lm; ++l) AT(am, i, j, l) = dt * AT(pu, i, j, l);
+    if (i < im)
+        for (int l = 0; l < lm; ++l) AT(bm, i, j, l) = dt * AT(pv, i, j, l);
+    if (i < im && j < jm) {
+        // conv = pu(i-1) - pu(i) + pv(j) - pv(j+1); pit = its column sum, bottom-up
+        double pit = 0.0;
+        for (int l = 0; l < lm; ++l) {
+            double c = ((AT(pu, i, j, l) - AT(pu, i + 1, j, l)) + AT(pv, i, j, l)) - AT(pv, i, j + 1, l);
+            pit = (l == 0) ? c : pit + c;
+        }
+        // sd(l) from the top down; cm = -dt sd on the interior interfaces
+        double sd = 0.0;
+        AT(cm, i, j, lm) = 0.0;
+        for (int l = lm - 1; l >= 1; --l) {
+            double c = ((AT(pu, i, j, l) - AT(pu, i + 1, j, l)) + AT(pv, i, j, l)) - AT(pv, i, j + 1, l);
+            if (l == lm - 1)
+                sd = c - (bt[lm - 1] - bt[lm]) * pit;
+            else
+                sd = (sd + c) - (bt[l] - bt[l + 1]) * pit;
+            AT(cm, i, j, l) = (-dt) * sd;
+        }
+        AT(cm, i, j, 0) = 0.0;
+    }
+}
+
+__global__ void k_m2phlb(DV m, DV sp, DV phlb, const double *dxyp, const double *at, const double *bt, int im,
+                         int jm, int lm, int xr, int yr, int jbeg, const double *dxyp_parent) {
+    int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (k >= (int64_t)im * jm) return;
+    const int i = (int)(k / jm), j = (int)(k % jm);
+    double acc = AT(m, i, j, 0);
+    for (int l = 1; l < lm; ++l) acc = acc + AT(m, i, j, l);
+    double p = (acc * GRAV) / dxyp[j];
+    if (xr > 0) {
+        // the child's ring: rescaled to the parent cell's area (Fortran i, j from 1)
+        const int fi = i + 1, fj = j + 1;
+        const bool interior = (xr < fi && fi < im - xr + 1) && (yr < fj && fj < jm - yr + 1);
+        if (!interior) {
+            const int jpar = jbeg + (fj - 1) / yr;  // 1-based parent row
+            p = (((p * dxyp[j]) * (double)xr) * (double)yr) / dxyp_parent[jpar - 1];
+        }
+    }
+    sp.p[i * sp.s0 + j * sp.s1] = p;
+    for (int l = 0; l <= lm; ++l) AT(phlb, i, j, l) = at[l] + bt[l] * p;
+}
+
+}  // namespace
+
+extern "C" int gb_fluxes_from_meteo(gb_ctx *ctx, const gb_view *pu, const gb_view *pv, const double *bt, double dt,
+                                    const gb_view *am, const gb_view *bm, const gb_view *cm) {
+    if (!ctx || !pu || !pv || !bt || !am || !bm || !cm) return GB_EARG;
+    const int im = (int)pv->n[0], jm = (int)pu->n[1], lm = (int)pu->n[2];
+    if (pu->n[0] != im + 1 || pv->n[1] != jm + 1 || cm->n[2] != lm + 1) {
+        gb_set_error("gb_fluxes_from_meteo: inconsistent shapes");
+        return GB_EARG;
+    }
+    int64_t total = (int64_t)(im + 1) * (jm + 1);
+    k_fluxes<<<(int)((total + 127) / 128), 128, 0, ctx->stream>>>(dv(pu), dv(pv), bt, dt, dv(am), dv(bm), dv(cm), im,
+                                                                  jm, lm);
+    return gb_after_launch(ctx, "fluxes_from_meteo");
+}
+
+extern "C" int gb_m2phlb(gb_ctx *ctx, const gb_view *m, const gb_view *sp, const gb_view *phlb, const double *dxyp,
+                         const double *at, const double *bt, int ring_xr, int ring_yr, int jbeg,
+                         const double *dxyp_parent) {
+    if (!ctx || !m || !sp || !phlb || !dxyp || !at || !bt) return GB_EARG;
+    const int im = (int)m->n[0], jm = (int)m->n[1], lm = (int)m->n[2];
+    int64_t total = (int64_t)im * jm;
+    k_m2phlb<<<(int)((total + 127) / 128), 128, 0, ctx->stream>>>(dv(m), dv(sp), dv(phlb), dxyp, at, bt, im, jm, lm,
+                                                                  ring_xr, ring_yr, jbeg, dxyp_parent);
+    return gb_after_launch(ctx, "m2phlb");
+}

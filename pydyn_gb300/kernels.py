@@ -1,0 +1,129 @@
+"""pydyn.kernels / pydyn.cfl on device arrays: the same calls and in-place semantics, the work
+done by the sm_103a kernels of libgbdyn.  Each function takes the DevArray views the reference
+function takes (any strides) and leaves them as the reference leaves them.  Nothing comes back
+to the host but what the caller asks for; errors found on the device (a sub-cycle cap, non-zero
+boundary faces) are raised at the next `Device.sync()`, or at once with `sync=True`.
+
+Sub-cycle caps are the reference's defaults: x 50, y 10, z 15 (kernels.py:129,223,295) and
+Check_CFL's 10, 1, 1 (cfl.py:136)."""
+
+import ctypes
+
+import numpy as np
+
+from . import _native as N
+from .device import DevArray, views
+
+MAX_NLOOP_X, MAX_NLOOP_Y, ITER_LIMIT_Z = 50, 10, 15
+CFL_MAX_NLOOP_X, CFL_MAX_NLOOP_Y, CFL_MAX_NLOOP_Z = 10, 1, 1
+
+__all__ = [
+    "advect_x",
+    "advect_y",
+    "advect_z",
+    "cfl_x",
+    "cfl_y",
+    "cfl_z",
+    "fluxes_from_meteo",
+    "m2phlb",
+]
+
+
+def _lib(a):
+    return a.dev.L, a.dev.h
+
+
+def _tracer_strides(*qs):
+    st = {q.strides for q in qs}
+    if len(st) != 1:
+        raise ValueError("pydyn_gb300: rm, rxm, rym, rzm views must share their strides")
+
+
+def _done(dev, rc, what, sync):
+    N.check(rc, what)
+    if sync:
+        dev.sync()
+
+
+def advect_x(m, rm, rxm, rym, rzm, am, clust=None, halo=False, js=1, je=None, limits=True,
+             max_nloop=MAX_NLOOP_X, nloop=None, amax=None, sync=False):
+    """dynamu on every (j, l) row (kernels.advect_x :129; with `clust` the reduced grid of
+    redgrid.advect_x_reduced :93; with `halo` the periodic halos of zoom _dynamu_region1 :237).
+    clust: DevArray (jm,) int32 of cluster sizes or None.  nloop/amax: optional DevArray
+    outputs (jm*lm,) of each row's sub-cycle count and largest Courant number."""
+    _tracer_strides(rm, rxm, rym, rzm)
+    L, h = _lib(m)
+    je = m.shape[1] if je is None else je
+    rc = L.gb_advect_x(h, *views(m, rm, rxm, rym, rzm, am), None if clust is None else clust.ptr, int(halo), js, je,
+                       int(limits), max_nloop, None if nloop is None else nloop.ptr,
+                       None if amax is None else amax.ptr)  # fmt: skip
+    _done(m.dev, rc, "advect_x", sync)
+
+
+def advect_y(m, rm, rxm, rym, rzm, bm, bm_full=None, bm_full_l0=0, limits=True, max_nloop=MAX_NLOOP_Y,
+             nloop=None, sync=False):
+    """dynamv (kernels.advect_y :223), the layers' nloop on the device; bm_full: region 1's
+    halo'd bm whose outside faces are rescaled with each layer (zoom _rescale_layer_halo :212)."""
+    _tracer_strides(rm, rxm, rym, rzm)
+    L, h = _lib(m)
+    rc = L.gb_advect_y(h, *views(m, rm, rxm, rym, rzm, bm, bm_full), bm_full_l0, int(limits), max_nloop,
+                       None if nloop is None else nloop.ptr)  # fmt: skip
+    _done(m.dev, rc, "advect_y", sync)
+
+
+def advect_z(m, rm, rxm, rym, rzm, cm, scope=None, limits=True, iter_limit=ITER_LIMIT_Z, sync=False):
+    """dynamw (kernels.advect_z :295); scope (si0, si1, sj0, sj1), 0-based half-open: the columns
+    the trial mass and the sub-steps act on, the search looking at every column (zoom
+    _dynamw_child :444)."""
+    _tracer_strides(rm, rxm, rym, rzm)
+    L, h = _lib(m)
+    im, jm = m.shape[0], m.shape[1]
+    si0, si1, sj0, sj1 = (0, im, 0, jm) if scope is None else scope
+    rc = L.gb_advect_z_scope(h, *views(m, rm, rxm, rym, rzm, cm), si0, si1, sj0, sj1, int(limits), iter_limit)
+    _done(m.dev, rc, "advect_z", sync)
+
+
+def cfl_x(m, am, clust=None, halo=False, js=1, je=None, max_nloop=CFL_MAX_NLOOP_X):
+    """cfl.dynamum (:140) with the region-1 halos of zoom/check_cfl.py:94-110; a failure sets
+    the device's Check_CFL flag (Device.cfl_failed)."""
+    L, h = _lib(m)
+    je = m.shape[1] if je is None else je
+    N.check(L.gb_cfl_x(h, *views(m, am), None if clust is None else clust.ptr, int(halo), js, je, max_nloop),
+            "cfl_x")
+
+
+def cfl_y(m, bm, max_nloop=CFL_MAX_NLOOP_Y):
+    """cfl.dynamvm (:170)."""
+    L, h = _lib(m)
+    N.check(L.gb_cfl_y(h, *views(m, bm), max_nloop), "cfl_y")
+
+
+def cfl_z(m, cm, scope=None, iter_limit=CFL_MAX_NLOOP_Z):
+    """cfl.dynamwm / zoom _dynamwm (cfl.py:186, zoom/check_cfl.py:206)."""
+    L, h = _lib(m)
+    im, jm = m.shape[0], m.shape[1]
+    si0, si1, sj0, sj1 = (0, im, 0, jm) if scope is None else scope
+    N.check(L.gb_cfl_z(h, *views(m, cm), si0, si1, sj0, sj1, iter_limit), "cfl_z")
+
+
+def fluxes_from_meteo(pu, pv, bt, dt, am, bm, cm):
+    """kernels.fluxes_from_meteo (:102) into am, bm, cm (DevArray views); bt a DevArray (lm+1)."""
+    L, h = _lib(pu)
+    N.check(L.gb_fluxes_from_meteo(h, *views(pu, pv), bt.ptr, float(dt), *views(am, bm, cm)), "fluxes_from_meteo")
+
+
+def m2phlb(m, sp, phlb, dxyp, at, bt, ring=None):
+    """zoom m2phlb1 (massflow.py:24) -- ring = (xr, yr, jbeg, dxyp_parent) for m2phlb (:35).
+    m (im, jm, lm), sp (im, jm), phlb (im, jm, lm+1); dxyp, at, bt, dxyp_parent DevArrays."""
+    L, h = _lib(m)
+    xr, yr, jbeg, par = (0, 0, 0, None) if ring is None else ring
+    N.check(L.gb_m2phlb(h, *views(m, sp, phlb), dxyp.ptr, at.ptr, bt.ptr, xr, yr, jbeg,
+                        None if par is None else par.ptr), "m2phlb")  # fmt: skip
+
+
+def to_device(dev, arr, dtype=np.float64):
+    """A DevArray copy of a host array (0-based bounds)."""
+    return DevArray.from_host(dev, np.asarray(arr, dtype=dtype))
+
+
+_ = ctypes
