@@ -1,0 +1,318 @@
+"""Benchmark: simulated years per wall-clock hour of the dynamic step on one GB300.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--config NAME] [--impl gbdyn|reference]
+
+A step is one read interval of one simulated hour (ndyn = nread = 3600 s): Check_CFL's mass-only
+rehearsal on a copy of the air mass, then the step itself -- Setup_MassFlow and the operator
+sequence xyzvsc | csvzyx on every region of the tree (with physics: Calc_Kzz, convection, CH4
+emission and chemistry) -- replayed as one captured CUDA graph.  The metric is pydyn's own
+(pydyn gpu/bench.py:262, forward.py:518): 3600 * 3600 / (365 * 86400 * wall seconds per step).
+
+value: device time (CUDA events on the context's stream) of K replays, inputs resident in HBM,
+L2 flushed between replays (a 256 MiB write).  e2e: the same steps through the public API with
+the step's meteo copied in from pinned host memory and the step's tracer mass copied out, timed
+on the host clock.  roofline: the body that takes the most device time in an eagerly enqueued
+interval, its algorithmic bytes (per cell per application: x, y 2(2+4nt), z (2+4nt)+(1+4nt),
+v 6+8nt, c 3+8nt, m2phlb 2, dynam0 5 values of 8 bytes) over its measured time, against the
+measured HBM copy bandwidth.  cpu_baseline: the oracle (a scalar C restatement of pydyn) on this
+host's cores on a bounded sample of the same workload.
+
+--impl reference runs the CPU reference arm: the oracle port of pydyn (the Python reference
+itself cannot be installed where this runs) on the same workload, with the same metric.
+With N > 1 (torchrun), every rank runs an independent replica of the workload (the step has no
+data-parallel split; the runs are independent members) and rank 0 reports the whole-job rate."""
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+SECONDS_A_YEAR = 365.0 * 86400.0
+WORKLOADS = {
+    # name: (tree, levels, physics, seed)
+    "glb6x4": ("glb6x4", 25, False, 11),
+    "glb3x2-adv": ("glb3x2", 34, False, 21),
+}
+DEFAULT = "glb3x2-adv"
+BYTES_PER_CELL = {"_dynamu_region1": 12, "_dynamv_region1": 12, "_dynamw_region1": 11, "_dynamu_child": 12,
+                  "_dynamv_child": 12, "_dynamw_child": 11, "convec_region": 14, "chemistry_region": 11,
+                  "m2phlb1": 2, "m2phlb": 2, "dynam0": 5}  # fmt: skip  (values of 8 bytes at nt = 1)
+
+
+def sim_years_per_hour(seconds_per_step, step_seconds=3600.0):
+    return 3600.0 * step_seconds / (SECONDS_A_YEAR * seconds_per_step)
+
+
+def peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+class Clocks:
+    """nvidia-smi samples (200 ms) of SM clock and throttle reasons during the timed region."""
+
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+             "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+             "clocks_event_reasons.sw_power_cap")  # fmt: skip
+
+    def __init__(self, index=0):
+        self.index = index
+        self.proc = None
+        self.path = Path(tempfile.mkstemp(suffix=".csv")[1])
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.QUERY}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)  # fmt: skip
+        except OSError:
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        if self.proc is not None:
+            self.proc.terminate()
+            self.proc.wait(timeout=10)
+        return False
+
+    def summary(self):
+        rows = []
+        for line in self.path.read_text().splitlines() if self.path.exists() else []:
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) >= 9:
+                rows.append(parts)
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no nvidia-smi samples"]}
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+        names = ("hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap")
+        reasons = sorted({n for r in rows for n, v in zip(names, r[5:9], strict=False) if v.lower() == "active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(rows)}  # fmt: skip
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    return ws, int(os.environ.get("RANK", "0")), int(os.environ.get("LOCAL_RANK", "0"))
+
+
+def max_over_ranks(x, ws):
+    if ws == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+
+    t = torch.tensor([x], dtype=torch.float64, device="cuda")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def barrier(ws):
+    if ws > 1:
+        import torch.distributed as dist
+
+        dist.barrier()
+
+
+def cpu_baseline(workload, seconds=15.0):
+    """The oracle on this host: whole intervals of the same workload until ~`seconds` pass."""
+    from oracle.forward import OracleRun
+
+    tree, lm, physics, seed = WORKLOADS[workload]
+    orc = OracleRun(tree, lm, seed)
+    t0 = time.perf_counter()
+    n = 0
+    while n < 1 or (time.perf_counter() - t0 < seconds and n < 50):
+        orc.interval()
+        n += 1
+    per = (time.perf_counter() - t0) / n
+    return {"value": sim_years_per_hour(per), "unit": "sim-years/hour", "cores": 1, "kind": "port",
+            "sample": f"{n} whole intervals of {workload} on one host thread ({per:.3f} s each)"}  # fmt: skip
+
+
+def run_reference(args, ws, rank):
+    """--impl reference: the CPU reference arm on rank 0 (the oracle port of pydyn)."""
+    if rank != 0:
+        return
+    from __graft_entry__ import build
+
+    build()
+    from oracle.forward import OracleRun
+
+    tree, lm, physics, seed = WORKLOADS[args.config]
+    orc = OracleRun(tree, lm, seed)
+    for _ in range(args.warmup):
+        orc.interval()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        orc.interval()
+    per = (time.perf_counter() - t0) / args.steps
+    v = sim_years_per_hour(per)
+    line = {
+        "impl": "reference", "metric": f"sim-years/hour {args.config} FP64-bitwise", "value": v,
+        "unit": "sim-years/hour", "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": per * 1e3, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f64", "data": "synthetic", "config": {"workload": args.config, "tree": tree, "levels": lm},
+        "cpu_baseline": {"value": v, "unit": "sim-years/hour", "cores": 1, "kind": "port",
+                         "sample": f"{args.steps} whole intervals of {args.config} (oracle, one host thread)"},
+        "e2e": {"value": v, "unit": "sim-years/hour", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }  # fmt: skip
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser(description=__doc__.split("\n")[0])
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--config", default=DEFAULT, choices=sorted(WORKLOADS))
+    ap.add_argument("--impl", default="gbdyn", choices=("gbdyn", "reference"))
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    ws, rank, local = dist_env()
+    if ws > 1:
+        import torch
+        import torch.distributed as dist
+
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    if args.impl == "reference":
+        run_reference(args, ws, rank)
+        return
+    args.warmup = max(args.warmup, 3)
+
+    from __graft_entry__ import build
+
+    build()
+    from pydyn_gb300.device import DevArray, Device
+    from pydyn_gb300.forward import Forward
+    from pydyn_gb300.profile import BodyProfiler
+
+    tree, lm, physics, seed = WORKLOADS[args.config]
+    dev = Device(local)
+    fw = Forward(dev, tree, lm, seed=seed + rank)
+
+    # per-body device time of one eager interval: the roofline's dominant body
+    with BodyProfiler(dev) as prof:
+        fw.interval(graph=False)
+    bodies = prof.report()
+
+    for _ in range(args.warmup):
+        fw.interval(graph=True)
+    flush = DevArray.zeros(dev, (0, 32 * 1024 * 1024 - 1))  # 256 MiB > the 129 MB L2
+    evs = [(dev.event(), dev.event()) for _ in range(args.steps)]
+    n0 = dev.launches()
+    barrier(ws)
+    dev.sync()
+    t_wall = time.perf_counter()
+    with Clocks(local) as clk:
+        t = fw.t
+        for k in range(args.steps):
+            flush.fill(float(k))
+            a, b = evs[k]
+            a.record()
+            fw.enqueue_interval_async(t)
+            b.record()
+            t += fw.nread
+        dev.sync()
+    wall = time.perf_counter() - t_wall
+    launches = dev.launches() - n0 - args.steps  # the flushes are not the step's
+    if dev.cfl_failed():
+        raise RuntimeError("bench: Check_CFL rejected ndyn = nread inside the timed region")
+    fw.t = t
+    ms = [a.elapsed_ms(b) for a, b in evs]
+    sec_per_step = max_over_ranks(sum(ms) / len(ms) / 1e3, ws)
+
+    # e2e: host buffers through the public API, the step's meteo in and tracer mass out
+    host_in = {r: [np.ascontiguousarray(x) for x in fw.met.fluxes(r, 1)] for r in fw.zoom.regions()}
+    pinned_in, pinned_out = {}, {}
+    from pydyn_gb300.hostbuf import PinnedArray
+
+    for r in fw.zoom.regions():
+        pinned_in[r] = [PinnedArray.copy_of(x) for x in host_in[r]]
+        rm = fw.st[r]["rm"]
+        g = fw.zoom.g(r)
+        pinned_out[r] = PinnedArray.empty((g.im, g.jm, lm, 1))
+    h2d = sum(p.nbytes for v in pinned_in.values() for p in v)
+    d2h = sum(p.nbytes for p in pinned_out.values())
+    barrier(ws)
+    dev.sync()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        for r in fw.zoom.regions():
+            pu1, pv1 = fw.meteo[r][1]
+            pinned_in[r][0].to_device(dev, pu1)
+            pinned_in[r][1].to_device(dev, pv1)
+        fw.enqueue_interval_async(fw.t)
+        fw.t += fw.nread
+        for r in fw.zoom.regions():
+            g = fw.zoom.g(r)
+            pinned_out[r].from_device(dev, fw.st[r]["rm"][1 : g.im, 1 : g.jm, 1:lm])
+        dev.sync()
+    e2e_sec = max_over_ranks((time.perf_counter() - t0) / args.steps, ws)
+    if dev.cfl_failed():
+        raise RuntimeError("bench: Check_CFL rejected ndyn = nread in the e2e loop")
+
+    # roofline of the dominant body
+    hbm, how = peaks()
+    name, (calls, total_ms, nlaunch) = max(bodies.items(), key=lambda kv: kv[1][1])
+    cells = {r: fw.zoom.g(r).im * fw.zoom.g(r).jm * lm for r in fw.zoom.regions()}
+    per_call_bytes = 8 * BYTES_PER_CELL.get(name, 0) * cells[1]
+    achieved = per_call_bytes / (total_ms / calls / 1e3) / 1e9 if per_call_bytes else None
+    roof = {"bound": "hbm", "kernel": name, "achieved": achieved, "peak": hbm, "unit": "GB/s",
+            "frac": achieved / hbm if achieved else None, "traffic": None, "peak_source": how,
+            "bytes_per_launch": per_call_bytes, "ms_per_launch": total_ms / calls,
+            "note": "float64 with no contraction: the FP64 pipe (500 G DMUL/DADD/s measured) bounds the step"}  # fmt: skip
+
+    step_bytes = sum(n * (2 * fw.zoom.g(r).tref * 37 * 8 + 40 + 248) for r, n in cells.items())
+    total_time = sum(v[1] for v in bodies.values())
+    line = {
+        "metric": "sim-years/hour glb3x2+nam1x1 FP64-bitwise" if "nam" in tree else f"sim-years/hour {args.config} FP64-bitwise",
+        "value": sim_years_per_hour(sec_per_step) * ws,
+        "unit": "sim-years/hour",
+        "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": sec_per_step * 1e3,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (seeded meteo of the configuration's shape; pydyn_gb300.synth)",
+        "config": {"workload": args.config, "tree": tree, "levels": lm, "nt": 1, "physics": physics,
+                   "step": "Check_CFL rehearsal + Setup_MassFlow + xyzvsc|csvzyx, one CUDA graph",
+                   "l2": "flushed between timed steps (256 MiB write)", "parallelism": f"replicas x{ws}"},
+        "roofline": roof,
+        "step_bytes": step_bytes,
+        "step_hbm_frac": step_bytes / sec_per_step / 1e9 / hbm,
+        "e2e": {"value": sim_years_per_hour(e2e_sec) * ws, "unit": "sim-years/hour", "h2d_bytes_per_step": h2d,
+                "d2h_bytes_per_step": d2h},
+        "gpu_launches": launches,
+        "clocks": clk.summary(),
+        "wall_s": wall,
+        "bodies_ms": {k: round(v[1], 4) for k, v in sorted(bodies.items(), key=lambda kv: -kv[1][1])},
+        "eager_interval_ms": total_time,
+    }  # fmt: skip
+    if rank == 0 and not args.no_cpu_baseline:
+        line["cpu_baseline"] = cpu_baseline(args.config)
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    fw.close()
+    dev.close()
+    if ws > 1:
+        import torch.distributed as dist
+
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

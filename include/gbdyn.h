@@ -51,6 +51,7 @@ int gb_alloc(gb_ctx *ctx, size_t bytes, void **dptr);
 int gb_free(gb_ctx *ctx, void *dptr);
 int gb_put(gb_ctx *ctx, void *dst, const void *src, size_t bytes);      /* host -> device, async */
 int gb_get(gb_ctx *ctx, void *dst, const void *src, size_t bytes);      /* device -> host, waits */
+int gb_get_async(gb_ctx *ctx, void *dst, const void *src, size_t bytes); /* device -> pinned host */
 int gb_copy_d2d(gb_ctx *ctx, void *dst, const void *src, size_t bytes); /* async */
 int gb_host_alloc(size_t bytes, void **hptr);                           /* pinned host memory */
 int gb_host_free(void *hptr);
@@ -87,6 +88,9 @@ int gb_cfl_failed(gb_ctx *ctx, int *failed); /* waits for the stream */
  * host.py:56-70); evaluation per element is the NumPy statement's. */
 int gb_box(gb_ctx *ctx, int op, const gb_view *dst, const gb_view *a, const gb_view *b, double x,
            double y);
+/* dst = w[0] a + w[1] b, the weights read from device memory when the kernel runs, so that a
+ * captured step replays with each step's weights (balance.py:63 time_interpolation). */
+int gb_interp(gb_ctx *ctx, const gb_view *dst, const gb_view *a, const gb_view *b, const double *w);
 /* dst = seqsum of src over `axis` (src's extent along it), accumulated in index order
  * (ops.seqsum, ops.py:235); dst has src's extents with that axis dropped (n = 1). */
 int gb_seqsum(gb_ctx *ctx, const gb_view *dst, const gb_view *src, int axis, double post_mul);

@@ -39,6 +39,7 @@ SIGNATURES = {
     "gb_free": (_I, [_VP, _VP]),
     "gb_put": (_I, [_VP, _VP, _VP, ctypes.c_size_t]),
     "gb_get": (_I, [_VP, _VP, _VP, ctypes.c_size_t]),
+    "gb_get_async": (_I, [_VP, _VP, _VP, ctypes.c_size_t]),
     "gb_copy_d2d": (_I, [_VP, _VP, _VP, ctypes.c_size_t]),
     "gb_host_alloc": (_I, [ctypes.c_size_t, ctypes.POINTER(_VP)]),
     "gb_host_free": (_I, [_VP]),
@@ -59,6 +60,7 @@ SIGNATURES = {
     "gb_cfl_failed": (_I, [_VP, ctypes.POINTER(_I)]),
     "gb_box": (_I, [_VP, _I, _P, _P, _P, _D, _D]),
     "gb_seqsum": (_I, [_VP, _P, _P, _I, _D]),
+    "gb_interp": (_I, [_VP, _P, _P, _P, _VP]),
     "gb_advect_x": (_I, [_VP, _P, _P, _P, _P, _P, _P, _VP, _I, _I, _I, _I, _I, _VP, _VP]),
     "gb_advect_y": (_I, [_VP, _P, _P, _P, _P, _P, _P, _P, _I, _I, _I, _VP]),
     "gb_advect_z": (_I, [_VP, _P, _P, _P, _P, _P, _P, _I, _I, _VP]),

@@ -84,6 +84,11 @@ extern "C" int gb_get(gb_ctx *ctx, void *dst, const void *src, size_t bytes) {
     return GB_OK;
 }
 
+extern "C" int gb_get_async(gb_ctx *ctx, void *dst, const void *src, size_t bytes) {
+    GB_CHECK_CUDA(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, ctx->stream));
+    return GB_OK;
+}
+
 extern "C" int gb_copy_d2d(gb_ctx *ctx, void *dst, const void *src, size_t bytes) {
     GB_CHECK_CUDA(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToDevice, ctx->stream));
     return GB_OK;
@@ -273,6 +278,30 @@ extern "C" int gb_box(gb_ctx *ctx, int op, const gb_view *dst, const gb_view *a,
     if (total <= 0) return GB_OK;
     k_box<<<launch_grid(total), 256, 0, ctx->stream>>>(op, d, va, vb, x, y, total);
     return gb_after_launch(ctx, "box");
+}
+
+// dst = w[0] a + w[1] b with the weights read from device memory (balance.time_interpolation)
+__global__ void k_interp(DV d, DV a, DV b, const double *w, int64_t total) {
+    int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    const double w1 = w[0], w2 = w[1];
+    for (; k < total; k += stride) {
+        int64_t r = k;
+        int64_t i3 = r % d.n3; r /= d.n3;
+        int64_t i2 = r % d.n2; r /= d.n2;
+        int64_t i1 = r % d.n1; r /= d.n1;
+        int64_t i0 = r;
+        d.p[off4(d, i0, i1, i2, i3)] = w1 * a.p[off4(a, i0, i1, i2, i3)] + w2 * b.p[off4(b, i0, i1, i2, i3)];
+    }
+}
+
+extern "C" int gb_interp(gb_ctx *ctx, const gb_view *dst, const gb_view *a, const gb_view *b, const double *w) {
+    if (!dst || !a || !b || !w) return GB_EARG;
+    DV d = dv(dst);
+    int64_t total = d.n0 * d.n1 * d.n2 * d.n3;
+    if (total <= 0) return GB_OK;
+    k_interp<<<launch_grid(total), 256, 0, ctx->stream>>>(d, dv(a), dv(b), w, total);
+    return gb_after_launch(ctx, "interp");
 }
 
 // dst[...] = seqsum over `axis` of src (accumulated in index order), times post_mul if != 1

@@ -1,0 +1,188 @@
+"""The dynamic step as a run performs it, on the device (pydyn forward.py:388-451, Forward._carry
+and Forward._step, recomposed for a region tree): for every read interval, Check_CFL rehearses
+the interval's steps on a copy of the air mass and decides ndyn; then each step interpolates
+the meteo fluxes to its middle, runs Setup_MassFlow, (with physics) Calc_Kzz, and the operator
+sequence with sources and chemistry at each half step.
+
+A step never waits for the device.  `interval(graph=True)` replays the interval (Check_CFL +
+one step at ndyn = nread) as one captured CUDA graph; the step runs speculatively next to the
+rehearsal, from a device copy of the state taken at the interval's start, and the host reads
+the rehearsal's one flag after the replay -- if it failed, the state is put back and the
+interval is redone uncaptured with ndyn reduced, as Check_CFL decides.
+
+The meteo of a configuration (pydyn_gb300.synth) is two flux instants per region, six hours
+apart; a step at time t interpolates them with weights held in device memory, so the captured
+graph serves every step."""
+
+import numpy as np
+
+from . import driver as D
+from . import synth
+from .device import DevArray
+from .state import TRACERS, ZoomState
+
+WINDOW = 6 * 3600.0
+SPECULATED = ("m", *TRACERS, "sp", "phlb")
+
+
+def weights(t):
+    """(alfa1, alfa2) of the two meteo instants at time t (s): a triangle wave between them."""
+    cycle = t / WINDOW
+    k = int(np.floor(cycle))
+    frac = cycle - k
+    return (1.0 - frac, frac) if k % 2 == 0 else (frac, 1.0 - frac)
+
+
+class Forward:
+    """A configuration's run on one device: the state, the Check_CFL copy, the meteo instants."""
+
+    def __init__(self, dev, config="glb6x4", lm=25, seed=0, nt=1, ndyn=3600, nread=3600, limits=True, physics=None,
+                 umax=40.0):  # fmt: skip
+        self.dev = dev
+        self.zoom, self.met, fields = synth.case(config, lm, seed, nt, umax=umax)
+        self.st = ZoomState.from_host(dev, self.zoom, fields)
+        self.cfl_st = ZoomState.zeros(dev, self.zoom, nt)
+        for r in self.zoom.regions():
+            self.cfl_st[r]["dxyp"].assign(self.st[r]["dxyp"])
+        self.ndyn_max, self.nread, self.limits = ndyn, nread, limits
+        self.t = 0.0
+        self.meteo = {}
+        for r in self.zoom.regions():
+            pair = [self.met.fluxes(r, k) for k in (0, 1)]
+            self.meteo[r] = [(DevArray.from_host(dev, pu), DevArray.from_host(dev, pv)) for pu, pv in pair]
+        self.w = DevArray.zeros(dev, (0, 1))
+        self.physics = physics
+        self.graphs = {}
+        self.last = {}
+
+    # -------------------------------------------------------------- meteo
+    def put_weights(self, t):
+        self.w.upload(np.array(weights(t)))
+
+    def interpolate(self, st):
+        """pu, pv of every region from the meteo instants with the device-held weights."""
+        for r in self.zoom.regions():
+            (pu0, pv0), (pu1, pv1) = self.meteo[r]
+            _interp(st[r]["pu"], pu0, pu1, self.w)
+            _interp(st[r]["pv"], pv0, pv1, self.w)
+
+    # -------------------------------------------------------------- Check_CFL, the step
+    def _rehearse(self, st, i, n, ndyn):
+        D.setup_massflow(self.zoom, st, ndyn)
+        run = D._CFLRun(self.zoom)
+        D.determine_cfl_iter(self.zoom, st, run, 1)
+        D.determine_cfl_iter(self.zoom, st, run, 1)
+
+    def check_cfl(self, t0):
+        """Check_CFL on the copy of m and sp (Forward._carry); (ndyn, n, iterations)."""
+        for r in self.zoom.regions():
+            for name in ("m", "sp"):
+                self.cfl_st[r][name].assign(self.st[r][name])
+
+        def interpolate(zoom, st, i, ndyn):
+            self.put_weights(t0 + (i - 0.5) * ndyn)
+            self.interpolate(st)
+
+        return D.check_cfl_zoom(self.zoom, self.cfl_st, self.ndyn_max, self.nread // self.ndyn_max, self.nread,
+                                interpolate)  # fmt: skip
+
+    def step(self, t0, ndyn):
+        """One step from t0 (Forward._step): meteo at the middle, Setup_MassFlow, the sequence."""
+        self.put_weights(t0 + ndyn / 2.0)
+        self.enqueue_step(ndyn)
+
+    def enqueue_step(self, ndyn):
+        st = self.st
+        self.interpolate(st)
+        D.setup_massflow(self.zoom, st, ndyn)
+        kw = {"limits": self.limits}
+        conv = None
+        if self.physics is not None:
+            conv, kw2 = self.physics.prepare(self, ndyn)
+            kw.update(kw2)
+        D.step(self.zoom, st, conv, ndyn, **kw)
+
+    def interval(self, graph=False):
+        """One read interval: Check_CFL, then its steps.  Returns (ndyn, n)."""
+        t0 = self.t
+        if graph:
+            return self._interval_graph(t0)
+        ndyn, n, _ = self.check_cfl(t0)
+        for s in range(n):
+            self.step(t0 + s * ndyn, ndyn)
+        self.dev.sync()
+        self.t = t0 + self.nread
+        return ndyn, n
+
+    # -------------------------------------------------------------- the captured interval
+    def _enqueue_interval(self):
+        """Check_CFL's rehearsal of one step at ndyn = nread and that step, speculatively."""
+        zoom, cst, st = self.zoom, self.cfl_st, self.st
+        lib = st.lib
+        for r in zoom.regions():
+            for name in SPECULATED:
+                self._spec[(r, name)].assign(st[r][name])
+            for name in ("m", "sp"):
+                cst[r][name].assign(st[r][name])
+        lib.save(cst, "check_cfl", ("m", "am", "bm", "cm"))
+        lib.cfl_begin(cst)
+        self.interpolate(cst)
+        self._rehearse(cst, 1, 1, self.nread)
+        lib.restore(cst, "check_cfl")
+        self.enqueue_step(self.nread)
+
+    def _interval_graph(self, t0):
+        if self.nread // self.ndyn_max != 1:
+            raise NotImplementedError("the captured interval is one step at ndyn = nread")
+        if "interval" not in self.graphs:
+            # the first interval runs uncaptured: every device constant and scratch array the
+            # bodies create lazily exists before capture (allocation is not capturable)
+            out = self.interval(graph=False)
+            self._spec = {(r, k): DevArray.zeros(self.dev, *((lo, lo + n - 1) for lo, n in
+                                                         zip(a.lower, a.shape, strict=True)))
+                          for r in self.zoom.regions() for k, a in self.st[r].items() if k in SPECULATED}  # fmt: skip
+            self.st.lib.save(self.cfl_st, "check_cfl", ("m", "am", "bm", "cm"))
+            self.dev.sync()
+            with self.dev.capture() as g:
+                self._enqueue_interval()
+            self.graphs["interval"] = g
+            return out
+        self.put_weights(t0 + self.nread / 2.0)
+        self.graphs["interval"].launch()
+        if self.dev.cfl_failed():  # the speculation was wrong: back to the interval's start
+            for (r, k), a in self._spec.items():
+                self.st[r][k].assign(a)
+            self.dev.sync()
+            return self.interval(graph=False)
+        self.dev.sync()
+        self.t = t0 + self.nread
+        return self.nread, 1
+
+    def close(self):
+        """Give the device memory of both states, the meteo and the graphs back."""
+        self.graphs.clear()
+        for s in (self.st, self.cfl_st):
+            s.free()
+        for pairs in self.meteo.values():
+            for pu, pv in pairs:
+                pu.free()
+                pv.free()
+        for a in getattr(self, "_spec", {}).values():
+            a.free()
+        self.w.free()
+
+    def enqueue_interval_async(self, t0):
+        """The captured interval, launched without any host read (the benchmark's timed loop;
+        the rehearsal flag is read once after the loop)."""
+        self.put_weights(t0 + self.nread / 2.0)
+        self.graphs["interval"].launch()
+
+
+def _interp(dst, a, b, w):
+    import ctypes
+
+    L = dst.dev.L
+    from . import _native as N
+
+    vd, va, vb = dst.view(), a.view(), b.view()
+    N.check(L.gb_interp(dst.dev.h, ctypes.byref(vd), ctypes.byref(va), ctypes.byref(vb), w.ptr), "gb_interp")

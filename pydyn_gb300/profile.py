@@ -1,0 +1,64 @@
+"""Per-body device time of one eagerly enqueued interval: every body the driver calls through
+`st.lib` is bracketed by CUDA events on the context's stream (pydyn's CudaBackend
+profile_begin/end has the same role, gpu/backend.py:634-651)."""
+
+import functools
+from collections import defaultdict
+
+from . import zoom as Z
+
+
+class BodyProfiler:
+    """Wrap the lib's bodies with event pairs while active; report {name: [ms per call]}."""
+
+    WRAPPED = ("_dynamu_region1", "_dynamv_region1", "_dynamw_region1", "_dynamu_child", "_dynamv_child",
+               "_dynamw_child", "_dynamum_region1", "_dynamvm_region1", "_dynamwm", "_dynamum_child",
+               "_dynamvm_child", "dynam0", "m2phlb1", "m2phlb", "convec_region", "sources_region",
+               "chemistry_region", "put_xedges", "put_yedges", "mix_edges", "update_parent", "_coarsen_block",
+               "coarsen_ambm", "_uncompress_xedges", "_uncompress_yedges", "save", "restore")  # fmt: skip
+
+    def __init__(self, dev):
+        self.dev = dev
+        self.pairs = defaultdict(list)
+        self.launches = defaultdict(int)
+        self._saved = {}
+
+    def __enter__(self):
+        for name in self.WRAPPED:
+            f = getattr(Z, name, None)
+            if f is None or name in self._saved:
+                continue
+            self._saved[name] = f
+            setattr(Z, name, self._wrap(name, f))
+        return self
+
+    def __exit__(self, *exc):
+        for name, f in self._saved.items():
+            setattr(Z, name, f)
+        self._saved.clear()
+        return False
+
+    def _wrap(self, name, f):
+        dev = self.dev
+
+        @functools.wraps(f)
+        def call(*a, **k):
+            e0, e1 = dev.event(), dev.event()
+            n0 = dev.launches()
+            e0.record()
+            out = f(*a, **k)
+            e1.record()
+            self.pairs[name].append((e0, e1))
+            self.launches[name] += dev.launches() - n0
+            return out
+
+        return call
+
+    def report(self):
+        """{body: (calls, total ms, kernel launches)}."""
+        self.dev.sync()
+        out = {}
+        for name, pairs in self.pairs.items():
+            ms = [a.elapsed_ms(b) for a, b in pairs]
+            out[name] = (len(ms), sum(ms), self.launches[name])
+        return out

@@ -101,7 +101,8 @@ class ZoomState:
             for a in f.values():
                 a.free()
         for a in self.consts.values():
-            a.free()
+            for x in a if isinstance(a, tuple) else (a,):
+                x.free()
         for d in self.saved.values():
             for a in d.values():
                 a.free()

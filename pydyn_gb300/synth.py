@@ -1,0 +1,268 @@
+"""Seeded synthetic inputs of the benchmark configurations, identical to the bit on any host.
+
+The generator uses NumPy's PCG64 stream (`Generator.random`, `integers`) and only IEEE-exact
+operations (+ - * /, sqrt, ldexp): its own sine, cosine and exponential below are polynomial
+evaluations after an exact range reduction, so that the x86 container that makes the golden
+fixtures and the aarch64 GPU machine regenerate the same bits (NumPy's vectorised transcendentals
+differ between the two).  Reductions use math.fsum (exactly rounded).
+
+Configurations (dims as the benchmark names them):
+    glb6x4      60 x 45 x 25, reduced grid jred (1, 2, 3, 45) clustsize (60, 20, 10, 60)
+    glb3x2      120 x 90 x 34, reduced grid of the production fixture
+    glb3x2+nam1x1  the above with a 90 x 70 child at 140W-50W, 10N-80N, xref 3, yref 2, tref 2
+
+Air mass from a surface pressure of 1e5 Pa +- 2 % smooth noise on hybrid a / b levels; mass
+fluxes from a seeded streamfunction of eight low spherical modes (winds up to 40 m/s, so the
+horizontal flow is divergence-free up to rounding) plus a small seeded velocity potential (so
+the vertical flux the column balance makes is not zero and z sub-cycles); two meteo instants six
+hours apart that each step interpolates between.  Tracer: mixing ratio 1.8e-6 plus a Gaussian
+blob of 2e-7, slopes zero."""
+
+import math
+
+import numpy as np
+
+from .tree import RedGrid, Region, Zoom
+
+AE = 6.371e6
+GRAV = 9.80665
+PI = 3.14159265358979  # the reference's PI (balance.py), a default-real literal
+
+G6_JRED, G6_CLUST = (1, 2, 3, 45), (60, 20, 10, 60)
+G3_JRED = (1, 2, 3, 4, 5, 6, 7, 84, 85, 86, 87, 88, 89, 90)
+G3_CLUST = (40, 8, 8, 4, 4, 4, 2, 2, 4, 4, 4, 8, 8, 40)
+
+
+# ------------------------------------------------------------------ deterministic elementary functions
+def _poly(x, coeffs):
+    acc = np.full_like(x, coeffs[-1])
+    for c in coeffs[-2::-1]:
+        acc = acc * x + c
+    return acc
+
+
+_SIN = [(-1.0) ** k / math.factorial(2 * k + 1) for k in range(11)]
+_COS = [(-1.0) ** k / math.factorial(2 * k) for k in range(11)]
+_HALF_PI_HI = 1.5707963267341256  # pi/2 split so that k * HI is exact for |k| < 2**20
+_HALF_PI_LO = 6.077100506506192e-11
+
+
+def sin_cos(x):
+    """(sin x, cos x) to ~1 ulp for |x| < 1e5, by quadrant reduction and Taylor series."""
+    x = np.asarray(x, dtype=np.float64)
+    k = np.floor(x / (_HALF_PI_HI + _HALF_PI_LO) + 0.5)
+    r = (x - k * _HALF_PI_HI) - k * _HALF_PI_LO
+    r2 = r * r
+    s = r * _poly(r2, _SIN)
+    c = _poly(r2, _COS)
+    q = np.mod(k, 4.0)
+    sin = np.where(q == 0, s, np.where(q == 1, c, np.where(q == 2, -s, -c)))
+    cos = np.where(q == 0, c, np.where(q == 1, -s, np.where(q == 2, -c, s)))
+    return sin, cos
+
+
+_EXP = [1.0 / math.factorial(k) for k in range(16)]
+_LN2 = 0.6931471805599453
+
+
+def exp(x):
+    """e**x to ~1 ulp for moderate x: x = k ln2 + r, a Taylor series of r, ldexp."""
+    x = np.asarray(x, dtype=np.float64)
+    k = np.floor(x / _LN2 + 0.5)
+    r = x - k * _LN2
+    return np.ldexp(_poly(r, _EXP), k.astype(np.int64))
+
+
+def _normalise(a):
+    top = max(abs(float(a.max())), abs(float(a.min())))
+    return a / top if top > 0 else a
+
+
+# ------------------------------------------------------------------ grids and levels
+def levels(lm, top=2000.0):
+    """Hybrid coefficients at the lm+1 interfaces, surface first: a from `top` Pa... down to 0
+    at the model top with b 1 -> 0 (the benchmark's fixed a / b)."""
+    frac = np.array([(lm - l) / lm for l in range(lm + 1)])
+    at = top * np.array([l / lm for l in range(lm + 1)]) * frac * 4.0
+    bt = frac * frac
+    at[0], at[lm], bt[lm] = 0.0, 0.0, 0.0
+    return at, bt
+
+
+def cell_area(g):
+    """dxyp (jm): AE^2 dlon (sin(lat north) - sin(lat south)) of the region's rows."""
+    dx, dy = (g.xend - g.xbeg) / g.im, (g.yend - g.ybeg) / g.jm
+    edges = np.array([g.ybeg + dy * j for j in range(g.jm + 1)]) * (PI / 180.0)
+    s, _ = sin_cos(edges)
+    return (AE * AE * (dx * PI / 180.0)) * (s[1:] - s[:-1])
+
+
+def glb6x4():
+    g = Region("glb6x4", 60, 45, xcyc=1, touch_sp=1, touch_np=1, redgrid=RedGrid(60, 45, G6_JRED, G6_CLUST))
+    return [g]
+
+
+def glb3x2():
+    g = Region("glb3x2", 120, 90, xcyc=1, touch_sp=1, touch_np=1, redgrid=RedGrid(120, 90, G3_JRED, G3_CLUST))
+    return [g]
+
+
+def nam1x1():
+    return Region("nam1x1", 90, 70, xbeg=-140, xend=-50, ybeg=10, yend=80, xref=3, yref=2, tref=2, parent=1)
+
+
+def tree(name, lm):
+    regions = {"glb6x4": glb6x4, "glb3x2": glb3x2, "glb3x2+nam1x1": lambda: [*glb3x2(), nam1x1()]}[name]()
+    at, bt = levels(lm)
+    return Zoom(regions, lm, at, bt)
+
+
+# ------------------------------------------------------------------ fields on a region
+def _centres(g):
+    dx, dy = (g.xend - g.xbeg) / g.im, (g.yend - g.ybeg) / g.jm
+    lon = np.array([g.xbeg + dx * (i + 0.5) for i in range(g.im)])
+    lat = np.array([g.ybeg + dy * (j + 0.5) for j in range(g.jm)])
+    return lon * (PI / 180.0), lat * (PI / 180.0)
+
+
+def _corners(g):
+    dx, dy = (g.xend - g.xbeg) / g.im, (g.yend - g.ybeg) / g.jm
+    lon = np.array([g.xbeg + dx * i for i in range(g.im + 1)])
+    lat = np.array([g.ybeg + dy * j for j in range(g.jm + 1)])
+    return lon * (PI / 180.0), lat * (PI / 180.0)
+
+
+class Modes:
+    """A seeded sum of low spherical modes cos(lat)^p cos(m lon + a) sin(n lat + b)."""
+
+    def __init__(self, rng, count=8):
+        r = rng.random((count, 6))
+        self.m = np.floor(r[:, 0] * 3.0) + 1.0
+        self.n = np.floor(r[:, 1] * 3.0) + 1.0
+        self.a = r[:, 2] * (2 * PI)
+        self.b = r[:, 3] * (2 * PI)
+        self.w = r[:, 4] * 2.0 - 1.0
+
+    def __call__(self, lon, lat):
+        lon, lat = np.broadcast_arrays(np.asarray(lon, dtype=float), np.asarray(lat, dtype=float))
+        _, clat = sin_cos(lat)
+        out = np.zeros(lon.shape)
+        for m, n, a, b, w in zip(self.m, self.n, self.a, self.b, self.w, strict=True):
+            _, c = sin_cos(m * lon + a)
+            s, _ = sin_cos(n * lat + b)
+            out = out + w * (clat * c * s)
+        return out
+
+
+class Meteo:
+    """The meteo of one configuration: surface pressure, streamfunction and potential modes
+    per meteo instant, the region geometry, and the mass fluxes pu, pv of every region."""
+
+    def __init__(self, zoom, seed, umax=40.0, chi_frac=0.05, wind_scale=1.0):
+        self.zoom = zoom
+        rng = np.random.default_rng(seed)
+        self.sp_modes = Modes(rng, 6)
+        self.psi = [Modes(rng, 8), Modes(rng, 8)]  # two meteo instants
+        self.chi = [Modes(rng, 8), Modes(rng, 8)]
+        self.level_w = 0.4 + 0.6 * rng.random(zoom.lm)
+        self.level_sign = np.where(rng.random(zoom.lm) < 0.15, -1.0, 1.0)
+        self.umax, self.chi_frac, self.wind_scale = umax, chi_frac, wind_scale
+        self.blob = rng.random(3)
+
+    def surface_pressure(self, g):
+        lon, lat = _centres(g)
+        noise = _normalise(self.sp_modes(lon[:, None], lat[None, :]))
+        return 1.0e5 * (1.0 + 0.02 * noise)
+
+    def mass(self, g, sp):
+        """m (im, jm, lm): the hybrid layer's pressure difference times the cell area over g."""
+        at, bt = self.zoom.at, self.zoom.bt
+        dxyp = cell_area(g)
+        dp = (at[None, None, :-1] - at[None, None, 1:]) + (bt[None, None, :-1] - bt[None, None, 1:]) * sp[..., None]
+        return dp * dxyp[None, :, None] / GRAV
+
+    def fluxes(self, r, instant):
+        """(pu (im+1, jm, lm), pv (im, jm+1, lm)) in kg/s of region r at a meteo instant."""
+        g = self.zoom.g(r)
+        lonc, latc = _corners(g)
+        lon, lat = _centres(g)
+        psi = self.psi[instant](lonc[:, None], latc[None, :])  # (im+1, jm+1) corners
+        chi = self.chi[instant](lon[:, None], lat[None, :])  # (im, jm) centres
+        dx, dy = (g.xend - g.xbeg) / g.im, (g.yend - g.ybeg) / g.jm
+        dyy = AE * dy * (PI / 180.0)
+        _, clat = sin_cos(lat)
+        dxx = AE * dx * (PI / 180.0) * clat  # (jm,)
+        u_psi = (psi[:, 1:] - psi[:, :-1]) / dyy  # x faces (im+1, jm)
+        # v on y faces: the streamfunction difference along x over the face's own width
+        _, clat_f = sin_cos(latc)
+        dxf = AE * dx * (PI / 180.0) * clat_f  # (jm+1,)
+        dpsi_x = psi[1:, :] - psi[:-1, :]  # (im, jm+1)
+        v_psi = -np.where(np.abs(dxf) > 1.0, dpsi_x / np.where(np.abs(dxf) > 1.0, dxf, 1.0)[None, :], 0.0)
+        scale = self.umax / max(float(np.abs(u_psi).max()), float(np.abs(v_psi).max()))
+        # velocity potential: gradient between neighbouring centres
+        chi_w = np.concatenate([chi[-1:], chi, chi[:1]], axis=0) if g.xcyc else np.concatenate([chi[:1], chi, chi[-1:]])
+        u_chi = (chi_w[1:] - chi_w[:-1]) / dxx[None, :]
+        v_chi = np.zeros((g.im, g.jm + 1))
+        v_chi[:, 1:-1] = (chi[:, 1:] - chi[:, :-1]) / dyy
+        cs = self.chi_frac * self.umax / max(float(np.abs(u_chi).max()), float(np.abs(v_chi).max()), 1e-300)
+        u = (u_psi * scale + u_chi * cs) * self.wind_scale
+        v = (v_psi * scale + v_chi * cs) * self.wind_scale
+        if g.xcyc:
+            u[g.im] = u[0]
+        if g.touch_sp:
+            v[:, 0] = 0.0
+        if g.touch_np:
+            v[:, g.jm] = 0.0
+        # mass flux = wind * (layer pressure thickness / g) * face length, per level
+        at, bt = self.zoom.at, self.zoom.bt
+        dp = (at[:-1] - at[1:]) + (bt[:-1] - bt[1:]) * 1.0e5
+        w = self.level_w * self.level_sign * dp / GRAV
+        pu = (u * dyy)[..., None] * w[None, None, :]
+        pv = (v * dxf[None, :])[..., None] * w[None, None, :]
+        return pu, pv
+
+    def tracer(self, r, m):
+        """rm (im, jm, lm, 1): m times 1.8e-6 plus a 2e-7 Gaussian blob."""
+        g = self.zoom.g(r)
+        lon, lat = _centres(g)
+        slon, clon = sin_cos(lon)
+        slat, clat = sin_cos(lat)
+        b = self.blob
+        blon, blat = (b[0] * 2.0 - 1.0) * PI, (b[1] - 0.5) * PI * 0.6
+        (sb,), (cb,) = sin_cos(np.array([blon]))
+        (sa,), (ca,) = sin_cos(np.array([blat]))
+        x0, y0, z0 = ca * cb, ca * sb, sa
+        x = clat[None, :] * clon[:, None]
+        y = clat[None, :] * slon[:, None]
+        z = np.broadcast_to(slat[None, :], x.shape)
+        d2 = (x - x0) * (x - x0) + (y - y0) * (y - y0) + (z - z0) * (z - z0)
+        sigma2 = 0.08 + 0.1 * b[2]
+        mix = 1.8e-6 + 2.0e-7 * exp(-d2 / (2.0 * sigma2))
+        return (m * mix[..., None])[..., None]
+
+
+def case(name, lm, seed=0, nt=1, umax=40.0):
+    """(zoom, meteo, {r: {field: host array}}): the initial state of every region in the
+    declared (halo'd) shapes: m and rm from the meteo's surface pressure, slopes zero, dxyp.
+    pu / pv are set per step by the run (interpolated between the meteo instants)."""
+    from .state import bounds
+
+    zoom = tree(name, lm)
+    met = Meteo(zoom, seed, umax=umax)
+    fields = {}
+    for r in zoom.regions():
+        g = zoom.g(r)
+        sp = met.surface_pressure(g)
+        m = met.mass(g, sp)
+        rm = met.tracer(r, m)
+        if nt > 1:
+            rm = np.concatenate([rm * (k + 1) for k in range(nt)], axis=3)
+        f = {}
+        for fname in ("m", "rm", "rxm", "rym", "rzm", "dxyp"):
+            shape = tuple(hi - lo + 1 for lo, hi in bounds(fname, g.im, g.jm, lm, nt))
+            f[fname] = np.zeros(shape)
+        f["m"][2 : g.im + 2, 2 : g.jm + 2] = m
+        f["rm"][2 : g.im + 2, 2 : g.jm + 2] = rm
+        f["dxyp"][:] = cell_area(g)
+        fields[r] = f
+    return zoom, met, fields

@@ -105,6 +105,107 @@ def kernel_cases():
     return cases
 
 
+STATE_FIELDS = ("m", "rm", "rxm", "rym", "rzm", "am", "bm", "cm", "pu", "pv", "sp", "phlb")
+
+
+def digest(fields_by_region):
+    """sha1 over every state array of every region (bit patterns, fixed order)."""
+    import hashlib
+
+    h = hashlib.sha1()
+    for r in sorted(fields_by_region):
+        for name in STATE_FIELDS:
+            h.update(np.ascontiguousarray(fields_by_region[r][name], dtype="<f8").tobytes())
+    return h.hexdigest()
+
+
+def reference_run(config, lm, seed, nsteps, nt=1, physics=None, keep=None, umax=40.0):
+    """pydyn's own driver (zoom.check_cfl_zoom on a copy of m and sp, then setup_massflow and
+    zoom.step, as pydyn forward.py:388-451 runs an interval of one step) on the synthetic case
+    of pydyn_gb300.synth.  Returns [(ndyn, n, digest)] per interval; keep: a list that receives
+    the full host state after each interval."""
+    _reference()
+    sys.path.insert(0, str(HERE.parents[1]))
+    from pydyn import redgrid as RG
+    from pydyn import zoom as Z
+
+    from pydyn_gb300 import forward, synth
+
+    zoom, met, fields = synth.case(config, lm, seed, nt, umax=umax)
+    regions = []
+    for g in zoom.region[1:]:
+        kw = {k: getattr(g, k) for k in g.__dataclass_fields__ if k != "redgrid"}
+        rg = None
+        if g.redgrid is not None:
+            rg = RG.RedGrid(g.im, g.jm, [b[0] + 1 for b in g.redgrid.bands], [b[1] for b in g.redgrid.bands])
+        regions.append(Z.Region(**kw, redgrid=rg))
+    zref = Z.Zoom(regions, lm, zoom.at, zoom.bt)
+    st, cst = Z.ZoomState.zeros(zref, nt), Z.ZoomState.zeros(zref, nt)
+    for r, f in fields.items():
+        for name, a in f.items():
+            st[r][name].data[...] = a
+        cst[r]["dxyp"].data[...] = f["dxyp"]
+    meteo = {r: [met.fluxes(r, k) for k in (0, 1)] for r in zref.regions()}
+
+    def interp(s, t):
+        a1, a2 = forward.weights(t)
+        for r in zref.regions():
+            (pu0, pv0), (pu1, pv1) = meteo[r]
+            s[r]["pu"].data[...] = a1 * pu0 + a2 * pu1
+            s[r]["pv"].data[...] = a1 * pv0 + a2 * pv1
+
+    conv = {r: None for r in zref.regions()}
+    out, t = [], 0.0
+    for _ in range(nsteps):
+        for r in zref.regions():
+            for name in ("m", "sp"):
+                cst[r][name].data[...] = st[r][name].data
+        t0 = t
+        ndyn, n, _ = Z.check_cfl_zoom(zref, cst, 3600, 1, 3600, lambda z, s, i, nd: interp(s, t0 + (i - 0.5) * nd))
+        for k in range(n):
+            interp(st, t0 + k * ndyn + ndyn / 2.0)
+            Z.setup_massflow(zref, st, ndyn)
+            kw = {}
+            if physics is not None:
+                conv, kw = physics(zref, st, ndyn)
+            else:
+                conv = {r: _no_convection(zref, r) for r in zref.regions()}
+            Z.step(zref, st, conv, ndyn, limits=True, **kw)
+        t = t0 + 3600.0
+        host = {r: {name: st[r][name].data for name in STATE_FIELDS} for r in zref.regions()}
+        out.append((ndyn, n, digest(host)))
+        if keep is not None:
+            keep.append({r: {k: v.copy() for k, v in f.items()} for r, f in host.items()})
+    return out
+
+
+def _no_convection(zoom, r):
+    """convection over no level: the `v` operator of an advection-only run is then a no-op."""
+    g = zoom.g(r)
+    z = np.zeros((g.im, g.jm, 0))
+    c = np.zeros((g.im, g.jm), dtype=np.int32)
+    return {"entu": z, "detu": z, "entd": z, "detd": z, "dkg": z, "cloud_top": c, "cloud_lfs": c, "lmax": 0}
+
+
+STEP_RUNS = {  # name: (tree, lm, seed, intervals, umax)
+    "config0": ("glb6x4", 25, 11, 24, 40.0),
+    "config0-strong": ("glb6x4", 25, 12, 6, 160.0),
+}
+
+
+def step_goldens():
+    import time
+
+    res = {}
+    for name, (config, lm, seed, nsteps, umax) in STEP_RUNS.items():
+        t = time.perf_counter()
+        runs = reference_run(config, lm, seed, nsteps, umax=umax)
+        res[name] = {"config": config, "lm": lm, "seed": seed, "umax": umax, "steps": [list(x) for x in runs],
+                     "reference_seconds_per_interval": (time.perf_counter() - t) / nsteps}  # fmt: skip
+        print(name, runs[-1], res[name]["reference_seconds_per_interval"])
+    return res
+
+
 def save(cases, path):
     flat = {}
     for name, (ins, outs, meta) in cases.items():
@@ -135,3 +236,9 @@ if __name__ == "__main__":
     if "kernels" in what:
         save(kernel_cases(), HERE / "kernels.npz")
         print("wrote", HERE / "kernels.npz")
+    if "steps" in what:
+        path = HERE / "steps.json"
+        old = json.loads(path.read_text()) if path.exists() else {}
+        old.update(step_goldens())
+        path.write_text(json.dumps(old, indent=1) + "\n")
+        print("wrote", path)
