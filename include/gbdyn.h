@@ -125,6 +125,18 @@ int gb_advect_z_scope(gb_ctx *ctx, const gb_view *m, const gb_view *rm, const gb
                       const gb_view *rym, const gb_view *rzm, const gb_view *cm, int si0, int si1,
                       int sj0, int sj1, int limits, int iter_limit);
 
+/* A child's held-end rows: m (n, nj, nl) cells is-1..ie+1 whose two ends are held, am (n-1, nj,
+ * nl) the interior faces (zoom/advect.py:278-345 _dynamu_child, _rows_child, _substeps_child). */
+int gb_advect_x_held(gb_ctx *ctx, const gb_view *m, const gb_view *rm, const gb_view *rxm,
+                     const gb_view *rym, const gb_view *rzm, const gb_view *am, int limits,
+                     int max_nloop);
+/* A child's held-end columns: m (ni, n, nl), bm (ni, n-1, nl); bm_full the whole halo'd bm,
+ * own[4] (int32 device) the inclusive (i0, i1, j0, j1) box of its faces the columns own
+ * (zoom/advect.py:348-412 _dynamv_child). */
+int gb_advect_y_held(gb_ctx *ctx, const gb_view *m, const gb_view *rm, const gb_view *rxm,
+                     const gb_view *rym, const gb_view *rzm, const gb_view *bm, const gb_view *bm_full,
+                     int bm_full_l0, const int32_t *own, int limits, int max_nloop);
+
 /* ------------------------------------------------------------------ Check_CFL mass kernels (pydyn/cfl.py)
  * dynamum (cfl.py:140) with the region-1 halos of zoom/check_cfl.py:94-110 when halo = 1. */
 int gb_cfl_x(gb_ctx *ctx, const gb_view *m, const gb_view *am, const int32_t *clust, int halo,
@@ -136,6 +148,40 @@ int gb_cfl_y(gb_ctx *ctx, const gb_view *m, const gb_view *bm, int max_nloop);
  * [si0, si1) x [sj0, sj1) (0-based, half-open) when every column passes. */
 int gb_cfl_z(gb_ctx *ctx, const gb_view *m, const gb_view *cm, int si0, int si1, int sj0, int sj1,
              int iter_limit);
+
+/* a child's dynamum / dynamvm (zoom/check_cfl.py:113-193) on held rows / columns */
+int gb_cfl_x_held(gb_ctx *ctx, const gb_view *m, const gb_view *am, int max_nloop);
+int gb_cfl_y_held(gb_ctx *ctx, const gb_view *m, const gb_view *bm, const gb_view *bm_full,
+                  int bm_full_l0, const int32_t *own, int max_nloop);
+
+/* ------------------------------------------------------------------ the zoom exchange
+ * Region arguments are arrays of eight gb_views of the whole (halo'd) arrays m, rm, rxm, rym,
+ * rzm, am, bm, cm; indices are Fortran (pydyn zoom/exchange.py, zoom/massflow.py). */
+/* put_xedges / putm_xedges (exchange.py:17-60) */
+int gb_put_xedges(gb_ctx *ctx, const gb_view *parent, const gb_view *child, int ib, int ie, int jbeg,
+                  int lbeg, int xr, int yr, int zr, double yzref, double xyzref, int tracers);
+/* put_yedges / putm_yedges (exchange.py:63-105) */
+int gb_put_yedges(gb_ctx *ctx, const gb_view *parent, const gb_view *child, int jb, int je, int ibeg,
+                  int lbeg, int xr, int yr, int zr, double xzref, double xyzref, int tracers);
+/* _compress_xedges / _uncompress_xedges (exchange.py:108-141) on rows js..je, levels ls..le */
+int gb_compress_xedges(gb_ctx *ctx, const gb_view *region, int xr, int js, int je, int ls, int le,
+                       int tracers, int uncompress);
+/* _compress_yedges / _uncompress_yedges (exchange.py:144-175) on columns is..ie */
+int gb_compress_yedges(gb_ctx *ctx, const gb_view *region, int yr, int is, int ie, int ls, int le,
+                       int tracers, int uncompress);
+/* mix_edges / mixm_edges (exchange.py:178-229) */
+int gb_mix_edges(gb_ctx *ctx, const gb_view *region, int xr, int yr, int xedges, int ysp, int ynp,
+                 int tracers);
+/* update_parent / updatem_parent (exchange.py:233-258) */
+int gb_update_parent(gb_ctx *ctx, const gb_view *parent, const gb_view *child, int ib, int jb, int xr,
+                     int yr, int tracers);
+/* _coarsen_block (zoom/massflow.py:334-397) */
+int gb_coarsen_block(gb_ctx *ctx, const gb_view *parent, const gb_view *child, int ib, int jb, int lb,
+                     int xr, int yr, double tr);
+/* coarsen_ambm (zoom/massflow.py:400-428) */
+int gb_coarsen_ambm(gb_ctx *ctx, const gb_view *parent, const gb_view *child, int ib, int ie, int jb,
+                    int je, int lb, int le, int xr, int yr, int zr, int xedges, int sp_edge,
+                    int np_edge);
 
 /* ------------------------------------------------------------------ mass fluxes, pressure
  * dynam0 (kernels.py:102-125, zoom/massflow.py:188-203): am = dt pu, bm = dt pv and cm from the

@@ -40,6 +40,8 @@ def lib():
         L.or_advect_y.argtypes = [P, P, P, P, P, P, P, I, I, I, I, i32]
         L.or_advect_z.argtypes = [P, P, P, P, P, P, I, I, I, I, I, I, I, i32]
         L.or_fluxes_from_meteo.argtypes = [P, P, ctypes.c_void_p, ctypes.c_double, P, P, P]
+        L.or_advect_x_held.argtypes = [P, P, P, P, P, P, I, I, I]
+        L.or_advect_y_held.argtypes = [P, P, P, P, P, P, P, I, I, I, I]
         L.or_m2phlb.argtypes = [P, P, P, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, I, I, I, ctypes.c_void_p]
         _LIB.append(L)
     return _LIB[0]
@@ -113,6 +115,27 @@ def advect_z(m, rm, rxm, rym, rzm, cm, scope=None, limits=True, iter_limit=15, m
             return None
         raise CFLError("dynamw: too many CFL violations!")
     return int(n[0])
+
+
+def advect_x_held(m, rm, rxm, rym, rzm, am, limits=True, max_nloop=50, mass_only=False):
+    """A child's held-end rows (zoom/advect.py:278-345; check_cfl.py:113-137 with mass_only):
+    m (n, nj, nl), am (n-1, nj, nl).  False when a row exceeded its cap (mass_only)."""
+    q = [x if x is not None else m for x in (rm, rxm, rym, rzm)]
+    rc = lib().or_advect_x_held(*map(_ref, [ov(m), *map(ov, q), ov(am)]), int(limits), max_nloop, int(mass_only))
+    if rc and not mass_only:
+        raise CFLError("dynuamu: nloop too high")
+    return not rc
+
+
+def advect_y_held(m, rm, rxm, rym, rzm, bm, full, full_l0, limits=True, max_nloop=10, mass_only=False):
+    """A child's held-end columns (zoom/advect.py:348-412; check_cfl.py:162-193 with mass_only):
+    m (ni, n, nl), bm (ni, n-1, nl) the scope's faces, full the whole halo'd bm."""
+    q = [x if x is not None else m for x in (rm, rxm, rym, rzm)]
+    rc = lib().or_advect_y_held(*map(_ref, [ov(m), *map(ov, q), ov(bm), ov(full)]), full_l0, int(limits), max_nloop,
+                                int(mass_only))  # fmt: skip
+    if rc and not mass_only:
+        raise CFLError("nloop too high in dynamv")
+    return not rc
 
 
 def fluxes_from_meteo(pu, pv, bt, dt, am, bm, cm):

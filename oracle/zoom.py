@@ -9,6 +9,7 @@ import sys
 
 import numpy as np
 
+from . import exchange as X
 from . import kernels as O
 
 TRACERS = ("rm", "rxm", "rym", "rzm")
@@ -198,37 +199,136 @@ def scale(st, names, factor):
             f[k].data[...] = f[k].data * factor
 
 
-# ------------------------------------------------------------------ the children's exchange: none on a single region
-class _Nothing:
+# ------------------------------------------------------------------ the children (zoom/advect.py, check_cfl.py, exchange.py)
+class _OuterFaces:
+    """outer_{x,y}_faces_zeroed (zoom/advect.py:117-151): a child's outer interface fluxes zeroed
+    around its advection in the second half of the parent step, restored after."""
+
+    def __init__(self, arr, planes):
+        self.arr, self.planes, self.kept = arr, planes, []
+
     def __enter__(self):
+        for ix in self.planes:
+            self.kept.append((ix, self.arr[ix].copy()))
+            self.arr[ix] = 0.0
         return self
 
     def __exit__(self, *a):
+        for ix, v in self.kept:
+            self.arr[ix] = v
         return False
 
 
 def outer_x_faces_zeroed(zoom, st, region, second):
-    if region != 1:
-        raise NotImplementedError("oracle: children")
-    return _Nothing()
+    g = zoom.g(region)
+    if region == 1 or not (second and g.im // g.xref < zoom.g(1).im):
+        return _OuterFaces(None, [])
+    xr = zoom.ref(region, "x")
+    return _OuterFaces(st[region]["am"], [(xr - 1, slice(None), slice(None)), (g.im - xr + 1, slice(None), slice(None))])
 
 
 def outer_y_faces_zeroed(zoom, st, region, second):
-    if region != 1:
-        raise NotImplementedError("oracle: children")
-    return _Nothing()
+    g = zoom.g(region)
+    if region == 1 or not second:
+        return _OuterFaces(None, [])
+    yr = zoom.ref(region, "y")
+    planes = []
+    if g.touch_sp != 1:
+        planes.append((slice(None), yr, slice(None)))
+    if g.touch_np != 1:
+        planes.append((slice(None), g.jm - yr + 2, slice(None)))
+    return _OuterFaces(st[region]["bm"], planes)
 
 
 def put_xedges(zoom, st, region, tracers=True):
-    if zoom.children[region]:
-        raise NotImplementedError("oracle: children")
+    X.put_xedges(zoom, st, region, tracers)
 
 
 def put_yedges(zoom, st, region, tracers=True):
-    if zoom.children[region]:
-        raise NotImplementedError("oracle: children")
+    X.put_yedges(zoom, st, region, tracers)
+
+
+def mix_edges(zoom, st, region, tracers=True):
+    X.mix_edges(zoom, st, region, tracers)
+
+
+def update_parent(zoom, st, region, tracers=True):
+    X.update_parent(zoom, st, region, tracers)
+
+
+def _uncompress_xedges(zoom, st, region, js, je, ls, le, tracers=True):
+    X.uncompress_xedges(zoom, st, region, js, je, ls, le, tracers)
+
+
+def _uncompress_yedges(zoom, st, region, is_, ie, ls, le, tracers=True):
+    X.uncompress_yedges(zoom, st, region, is_, ie, ls, le, tracers)
+
+
+def _coarsen_block(zoom, st, region):
+    X.coarsen_block(zoom, st, region)
 
 
 def coarsen_ambm(zoom, st, region):
-    if zoom.children[region]:
-        raise NotImplementedError("oracle: children")
+    X.coarsen_ambm(zoom, st, region)
+
+
+def _dynamu_child(zoom, st, region, js, je, ls, le, limits, stats, max_nloop=50):
+    X.compress_xedges(zoom, st, region, js, je, ls, le)
+    g, f = zoom.g(region), st[region]
+    xr = zoom.ref(region, "x")
+    is_, ie = xr, g.im - xr + 1
+    cells = (slice(is_ - 1, ie + 1), slice(js, je), slice(ls, le))
+    O.advect_x_held(f["m"][cells], *(f[q][cells] for q in TRACERS), f["am"][is_ - 1 : ie, js:je, ls:le],
+                    limits=limits, max_nloop=max_nloop)  # fmt: skip
+
+
+def _dynamv_child(zoom, st, region, is_, ie, ls, le, limits, stats, max_nloop=10):
+    X.compress_yedges(zoom, st, region, is_, ie, ls, le)
+    g, f = zoom.g(region), st[region]
+    yr = zoom.ref(region, "y")
+    js, je = yr, g.jm - yr + 1
+    cells = (slice(is_, ie), slice(js - 1, je + 1), slice(ls, le))
+    O.advect_y_held(f["m"][cells], *(f[q][cells] for q in TRACERS), f["bm"][is_:ie, js : je + 1, ls:le],
+                    f["bm"].data, ls, limits=limits, max_nloop=max_nloop)  # fmt: skip
+
+
+def _dynamw_child(zoom, st, region, is_, ie, js, je, limits, stats, iter_limit=15):
+    g, f, lm = zoom.g(region), st[region], zoom.lm
+    m, *q = _interior(st, region)
+    O.advect_z(m, *q, f["cm"][1 : g.im, 1 : g.jm, 0:lm], scope=(is_ - 1, ie, js - 1, je), limits=limits,
+               iter_limit=iter_limit)  # fmt: skip
+
+
+def _dynamum_child(zoom, st, region, js, je, ls, le, max_nloop):
+    if st.cfl_failed:
+        return False
+    X.compress_xedges(zoom, st, region, js, je, ls, le, tracers=False)
+    g, f = zoom.g(region), st[region]
+    xr = zoom.ref(region, "x")
+    is_, ie = xr, g.im - xr + 1
+    ok = O.advect_x_held(f["m"][is_ - 1 : ie + 1, js:je, ls:le], None, None, None, None,
+                         f["am"][is_ - 1 : ie, js:je, ls:le], max_nloop=max_nloop, mass_only=True)  # fmt: skip
+    if not ok:
+        st.cfl_failed = True
+        return False
+    X.uncompress_xedges(zoom, st, region, js, je, ls, le, tracers=False)
+    X.mix_edges(zoom, st, region, tracers=False)
+    return True
+
+
+def _dynamvm_child(zoom, st, region, is_, ie, ls, le, max_nloop):
+    if st.cfl_failed:
+        return False
+    X.compress_yedges(zoom, st, region, is_, ie, ls, le, tracers=False)
+    g, f = zoom.g(region), st[region]
+    yr = zoom.ref(region, "y")
+    js, je = yr, g.jm - yr + 1
+    ok = O.advect_y_held(f["m"][is_:ie, js - 1 : je + 1, ls:le], None, None, None, None,
+                         f["bm"][is_:ie, js : je + 1, ls:le], f["bm"].data, ls, max_nloop=max_nloop,
+                         mass_only=True)  # fmt: skip
+    if not ok:
+        st.cfl_failed = True
+        return False
+    X.uncompress_yedges(zoom, st, region, is_, ie, ls, le, tracers=False)
+    X.mix_edges(zoom, st, region, tracers=False)
+    return True

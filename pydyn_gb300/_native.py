@@ -68,6 +68,18 @@ SIGNATURES = {
     "gb_cfl_x": (_I, [_VP, _P, _P, _VP, _I, _I, _I, _I]),
     "gb_cfl_y": (_I, [_VP, _P, _P, _I]),
     "gb_cfl_z": (_I, [_VP, _P, _P, _I, _I, _I, _I, _I]),
+    "gb_advect_x_held": (_I, [_VP, _P, _P, _P, _P, _P, _P, _I, _I]),
+    "gb_advect_y_held": (_I, [_VP, _P, _P, _P, _P, _P, _P, _P, _I, _VP, _I, _I]),
+    "gb_cfl_x_held": (_I, [_VP, _P, _P, _I]),
+    "gb_cfl_y_held": (_I, [_VP, _P, _P, _P, _I, _VP, _I]),
+    "gb_put_xedges": (_I, [_VP, _P, _P, _I, _I, _I, _I, _I, _I, _I, _D, _D, _I]),
+    "gb_put_yedges": (_I, [_VP, _P, _P, _I, _I, _I, _I, _I, _I, _I, _D, _D, _I]),
+    "gb_compress_xedges": (_I, [_VP, _P, _I, _I, _I, _I, _I, _I, _I]),
+    "gb_compress_yedges": (_I, [_VP, _P, _I, _I, _I, _I, _I, _I, _I]),
+    "gb_mix_edges": (_I, [_VP, _P, _I, _I, _I, _I, _I, _I]),
+    "gb_update_parent": (_I, [_VP, _P, _P, _I, _I, _I, _I, _I]),
+    "gb_coarsen_block": (_I, [_VP, _P, _P, _I, _I, _I, _I, _I, _D]),
+    "gb_coarsen_ambm": (_I, [_VP, _P, _P, _I, _I, _I, _I, _I, _I, _I, _I, _I, _I, _I, _I]),
     "gb_fluxes_from_meteo": (_I, [_VP, _P, _P, _VP, _D, _P, _P, _P]),
     "gb_m2phlb": (_I, [_VP, _P, _P, _P, _VP, _VP, _VP, _I, _I, _I, _VP]),
 }

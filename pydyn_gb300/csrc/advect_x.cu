@@ -3,9 +3,15 @@
 // A row is staged in shared memory (lanes across its cells), clustered onto the reduced grid
 // when its latitude is reduced, searched for its smallest CFL-safe sub-cycle count (warp
 // vote), advanced through all its sub-steps on chip, split back onto the uniform cells and
-// written once.  Reference: pydyn kernels.py:129-220 (_advect_rows_x, subcycle_rows,
-// _substeps_x), redgrid.py:56-110 (uni2red, uni2red_mf, red2uni), zoom/advect.py:237-275
-// (_dynamu_region1's halos), cfl.py:140-167 (dynamum, the mass-only rehearsal).
+// written once.  Two row kinds:
+//   periodic  region 1: n cells, n+1 faces, face 0 the seam copy of face n
+//   held      a child: n cells of which the two ends are held (the parent's, put there by
+//             put_xedges), n-1 interior faces; shared memory keeps the periodic indexing (face
+//             k between cells k-1 and k, k = 1 .. n-1)
+// Reference: pydyn kernels.py:129-220 (_advect_rows_x, subcycle_rows, _substeps_x),
+// redgrid.py:56-110 (uni2red, uni2red_mf, red2uni), zoom/advect.py:237-345 (_dynamu_region1's
+// halos, _dynamu_child, _rows_child, _substeps_child), cfl.py:140-167 (dynamum) and
+// zoom/check_cfl.py:113-137 (_dynamum_child).
 #include "gb_common.cuh"
 
 namespace {
@@ -15,11 +21,12 @@ constexpr int WARPS = 4;
 struct XArgs {
     DV m, q[4], am;
     const int32_t *clust;
-    int im, jm, lm, nt;
+    int n0, nj, nl, nt;  // view extents: cells per row, rows (j), levels
     int halo, js, je;    // halo writes on rows js..je (1-based, inclusive)
     int limits, nmax;    // nmax = max_nloop - 1
-    int restore_am;      // 1: am = a * nloop written back (no reduced grid); 0: am untouched
-    int ncell;           // smem cells per array (im + 2)
+    int restore_am;      // 1: am = a * nloop written back; 0: am untouched (reduced grid)
+    int held;            // child rows
+    int ncell;           // smem cells per array (n0 + 2)
     int32_t *nloop_out;
     double *amax_out;
     gb_ctl *ctl;
@@ -32,10 +39,14 @@ __device__ __forceinline__ double &AT4(const DV &v, int64_t i, int64_t j, int64_
     return v.p[i * v.s0 + j * v.s1 + l * v.s2 + t * v.s3];
 }
 
-// The per-row CFL search (kernels.py:169-199, periodic): the smallest nloop for which nloop
-// trial sub-steps of the mass stay under |Courant| < 1 on every face (division form,
-// ops.py:267-270), the faces rescaled by (n-1)/n per retry.  Returns nloop, or nmax + 1.
-__device__ int row_search(double *m_s, double *mx_s, double *a_s, int n, int nmax, int lane, double &amax_out) {
+// The per-row CFL search (kernels.py:169-199): the smallest nloop for which nloop trial
+// sub-steps of the mass stay under |Courant| < 1 on every face (division form,
+// ops.py:267-270), the faces rescaled by (n-1)/n per retry.  Faces k0..k1, cells i0..i1 move.
+// Returns nloop, or nmax + 1.
+__device__ int row_search(double *m_s, double *mx_s, double *a_s, int n, bool held, int nmax, int lane,
+                          double &amax_out) {
+    const int k0 = held ? 1 : 0, k1 = held ? n - 1 : n;
+    const int i0 = held ? 1 : 0, i1 = held ? n - 1 : n;  // cells [i0, i1)
     int nloop = 1;
     while (true) {
         for (int k = lane; k < n; k += GB_WARP) mx_s[k] = m_s[k];
@@ -45,7 +56,7 @@ __device__ int row_search(double *m_s, double *mx_s, double *a_s, int n, int nma
         for (int s = 0; s < nloop; ++s) {
             bool lok = true;
             double cmax = 0.0;
-            for (int k = lane; k <= n; k += GB_WARP) {
+            for (int k = k0 + lane; k <= k1; k += GB_WARP) {
                 double f = a_s[k];
                 int up = (f >= 0.0) ? (k == 0 ? n - 1 : k - 1) : (k == n ? 0 : k);
                 double c = fabs(f / mx_s[up]);
@@ -60,7 +71,7 @@ __device__ int row_search(double *m_s, double *mx_s, double *a_s, int n, int nma
             }
             amax = (amax > cmax) ? amax : cmax;
             __syncwarp();
-            for (int k = lane; k < n; k += GB_WARP) mx_s[k] = (mx_s[k] + a_s[k]) - a_s[k + 1];
+            for (int k = i0 + lane; k < i1; k += GB_WARP) mx_s[k] = (mx_s[k] + a_s[k]) - a_s[k + 1];
             __syncwarp();
         }
         if (ok) {
@@ -68,7 +79,7 @@ __device__ int row_search(double *m_s, double *mx_s, double *a_s, int n, int nma
             return nloop;
         }
         nloop += 1;
-        for (int k = lane; k <= n; k += GB_WARP) a_s[k] = (a_s[k] * (double)(nloop - 1)) / (double)nloop;
+        for (int k = k0 + lane; k <= k1; k += GB_WARP) a_s[k] = (a_s[k] * (double)(nloop - 1)) / (double)nloop;
         __syncwarp();
         if (nloop > nmax) {
             amax_out = 0.0;
@@ -82,12 +93,13 @@ __global__ void __launch_bounds__(WARPS * 32) k_advect_x(XArgs A) {
     extern __shared__ double smem[];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int64_t row = (int64_t)blockIdx.x * WARPS + warp;
-    if (row >= (int64_t)A.jm * A.lm) return;
+    if (row >= (int64_t)A.nj * A.nl) return;
     if (MASS_ONLY && __shfl_sync(FULL_MASK, *(volatile int *)&A.ctl->cfl_failed, 0)) return;
-    const int j = (int)(row / A.lm), l = (int)(row % A.lm);
+    const int j = (int)(row / A.nl), l = (int)(row % A.nl);
     const int nt = MASS_ONLY ? 0 : A.nt;
     const int NC = A.ncell;
     const int per_warp = NC * (4 + 8 * nt);
+    const bool held = A.held != 0;
     double *m_s = smem + (size_t)warp * per_warp;
     double *mx_s = m_s + NC;
     double *minv_s = mx_s + NC;
@@ -97,8 +109,8 @@ __global__ void __launch_bounds__(WARPS * 32) k_advect_x(XArgs A) {
     auto Q = [&](int w, int t) { return q_s + (size_t)(w * nt + t) * NC; };
     auto F = [&](int w, int t) { return f_s + (size_t)(w * nt + t) * NC; };
 
-    const int c = (A.clust && A.clust[j] > 1) ? A.clust[j] : 1;
-    const int n = A.im / c;
+    const int c = (!held && A.clust && A.clust[j] > 1) ? A.clust[j] : 1;
+    const int n = A.n0 / c;
     const bool reduced = c > 1;
 
     // ---- stage the row: cluster sums onto the reduced cells (uni2red, seqsum in order)
@@ -113,19 +125,22 @@ __global__ void __launch_bounds__(WARPS * 32) k_advect_x(XArgs A) {
                 Q(w, t)[k] = s;
             }
     }
-    // faces: a(i) = am(i c) for i = 1..n, a(0) = a(n) on a reduced row (uni2red_mf)
-    for (int k = lane; k <= n; k += GB_WARP) {
-        int src = (k == 0) ? (reduced ? n * c : 0) : k * c;
-        a_s[k] = AT(A.am, src, j, l);
+    if (held) {  // n-1 interior faces, face k between cells k-1 and k
+        for (int k = 1 + lane; k < n; k += GB_WARP) a_s[k] = AT(A.am, k - 1, j, l);
+    } else {     // a(i) = am(i c), i = 1..n; a(0) = a(n) on a reduced row (uni2red_mf)
+        for (int k = lane; k <= n; k += GB_WARP) {
+            int src = (k == 0) ? (reduced ? n * c : 0) : k * c;
+            a_s[k] = AT(A.am, src, j, l);
+        }
     }
     __syncwarp();
 
-    if (!MASS_ONLY && A.limits)
+    if (!MASS_ONLY && A.limits)  // every cell of the row, a child's held ends included
         for (int t = 0; t < nt; ++t)
             for (int k = lane; k < n; k += GB_WARP) Q(1, t)[k] = np_limit(Q(1, t)[k], Q(0, t)[k]);
 
     double amax = 0.0;
-    const int nloop = row_search(m_s, mx_s, a_s, n, A.nmax, lane, amax);
+    const int nloop = row_search(m_s, mx_s, a_s, n, held, A.nmax, lane, amax);
     if (nloop > A.nmax) {
         if (lane == 0) {
             if (MASS_ONLY)
@@ -137,17 +152,18 @@ __global__ void __launch_bounds__(WARPS * 32) k_advect_x(XArgs A) {
         return;
     }
 
+    const int i0 = held ? 1 : 0, i1 = held ? n - 1 : n;  // the cells that move
     if (MASS_ONLY) {
         for (int s = 0; s < nloop; ++s) {
-            for (int k = lane; k < n; k += GB_WARP) m_s[k] = (m_s[k] + a_s[k]) - a_s[k + 1];
+            for (int k = i0 + lane; k < i1; k += GB_WARP) m_s[k] = (m_s[k] + a_s[k]) - a_s[k + 1];
             __syncwarp();
         }
     } else {
         for (int k = lane; k < n; k += GB_WARP) minv_s[k] = 1.0 / m_s[k];
         __syncwarp();
+        const int k0 = 1, k1 = held ? n - 1 : n;  // periodic: face 0 is the seam copy of face n
         for (int s = 0; s < nloop; ++s) {
-            // faces 1..n; face 0 is the periodic seam, a copy of face n
-            for (int k = lane + 1; k <= n; k += GB_WARP) {
+            for (int k = k0 + lane; k <= k1; k += GB_WARP) {
                 double f = a_s[k];
                 int up = (f >= 0.0) ? k - 1 : (k == n ? 0 : k);
                 double alpha = f * minv_s[up];  // the reciprocal form of production dynamu
@@ -158,7 +174,7 @@ __global__ void __launch_bounds__(WARPS * 32) k_advect_x(XArgs A) {
                 }
             }
             __syncwarp();
-            for (int i = lane; i < n; i += GB_WARP) {
+            for (int i = i0 + lane; i < i1; i += GB_WARP) {
                 const int lo = (i == 0) ? n : i;
                 const double mo = m_s[i], alo = a_s[i], ahi = a_s[i + 1];
                 const double mn = (mo + alo) - ahi;
@@ -182,16 +198,25 @@ __global__ void __launch_bounds__(WARPS * 32) k_advect_x(XArgs A) {
     if (A.nloop_out && lane == 0) A.nloop_out[row] = nloop;
     if (A.amax_out && lane == 0) A.amax_out[row] = amax;
 
-    if (A.restore_am)  // "restore old am": a * nloop, not an exact round trip
-        for (int k = lane; k <= n; k += GB_WARP) AT(A.am, k, j, l) = a_s[k] * (double)nloop;
+    if (A.restore_am) {  // "restore old am": a * nloop, not an exact round trip
+        if (held)
+            for (int k = 1 + lane; k < n; k += GB_WARP) AT(A.am, k - 1, j, l) = a_s[k] * (double)nloop;
+        else
+            for (int k = lane; k <= n; k += GB_WARP) AT(A.am, k, j, l) = a_s[k] * (double)nloop;
+    }
 
     const bool in_scope = (j + 1 >= A.js) && (j + 1 <= A.je);
     if (!reduced) {
-        for (int i = lane; i < n; i += GB_WARP) {
+        for (int i = i0 + lane; i < i1; i += GB_WARP) {
             AT(A.m, i, j, l) = m_s[i];
             for (int w = 0; w < 4; ++w)
                 for (int t = 0; t < nt; ++t) AT4(A.q[w], i, j, l, t) = Q(w, t)[i];
         }
+        if (held && A.limits && !MASS_ONLY && lane == 0)  // the held ends keep their limited rxm
+            for (int t = 0; t < nt; ++t) {
+                AT4(A.q[1], 0, j, l, t) = Q(1, t)[0];
+                AT4(A.q[1], n - 1, j, l, t) = Q(1, t)[n - 1];
+            }
         if (A.halo && in_scope && lane == 0) {  // q(0) = q(im), q(im+1) = q(1)
             AT(A.m, -1, j, l) = m_s[n - 1];
             AT(A.m, n, j, l) = m_s[0];
@@ -204,7 +229,7 @@ __global__ void __launch_bounds__(WARPS * 32) k_advect_x(XArgs A) {
     } else {
         // red2uni: the uniform mass update with the untouched am, and every cell of a cluster
         // given its share m_uni(i) / m(cluster) of the cluster's tracers
-        const int im = A.im;
+        const int im = A.n0;
         for (int i = lane; i < im; i += GB_WARP) {
             const int k = i / c;
             double mun = (AT(A.m, i, j, l) + AT(A.am, i, j, l)) - AT(A.am, i + 1, j, l);
@@ -222,10 +247,10 @@ __global__ void __launch_bounds__(WARPS * 32) k_advect_x(XArgs A) {
 }
 
 int launch_x(gb_ctx *ctx, XArgs &A, bool mass_only) {
-    A.ncell = A.im + 2;
+    A.ncell = A.n0 + 2;
     const int nt = mass_only ? 0 : A.nt;
     size_t smem = (size_t)WARPS * A.ncell * (4 + 8 * nt) * sizeof(double);
-    int64_t rows = (int64_t)A.jm * A.lm;
+    int64_t rows = (int64_t)A.nj * A.nl;
     int blocks = (int)((rows + WARPS - 1) / WARPS);
     if (blocks == 0) return GB_OK;
     if (mass_only) {
@@ -238,6 +263,22 @@ int launch_x(gb_ctx *ctx, XArgs &A, bool mass_only) {
     return gb_after_launch(ctx, mass_only ? "cfl_x" : "advect_x");
 }
 
+int setup(XArgs &A, const gb_view *m, const gb_view *am, int held) {
+    A.m = dv(m);
+    A.am = dv(am);
+    A.n0 = (int)m->n[0]; A.nj = (int)m->n[1]; A.nl = (int)m->n[2];
+    A.held = held;
+    if (!held && am->n[0] != A.n0 + 1) {
+        gb_set_error("gb_advect_x: a periodic row has im+1 faces");
+        return GB_EARG;
+    }
+    if (held && (am->n[0] != A.n0 - 1 || A.n0 < 3)) {
+        gb_set_error("gb_advect_x_held: a held row of n >= 3 cells has n-1 faces");
+        return GB_EARG;
+    }
+    return GB_OK;
+}
+
 }  // namespace
 
 extern "C" int gb_advect_x(gb_ctx *ctx, const gb_view *m, const gb_view *rm, const gb_view *rxm,
@@ -246,15 +287,10 @@ extern "C" int gb_advect_x(gb_ctx *ctx, const gb_view *m, const gb_view *rm, con
                            int32_t *nloop_out, double *amax_out) {
     if (!ctx || !m || !rm || !rxm || !rym || !rzm || !am) return GB_EARG;
     XArgs A{};
-    A.m = dv(m);
+    if (int rc = setup(A, m, am, 0)) return rc;
     A.q[0] = dv(rm); A.q[1] = dv(rxm); A.q[2] = dv(rym); A.q[3] = dv(rzm);
-    A.am = dv(am);
     A.clust = clust;
-    A.im = (int)m->n[0]; A.jm = (int)m->n[1]; A.lm = (int)m->n[2]; A.nt = (int)rm->n[3];
-    if (am->n[0] != A.im + 1) {
-        gb_set_error("gb_advect_x: am must have im+1 faces");
-        return GB_EARG;
-    }
+    A.nt = (int)rm->n[3];
     A.halo = halo; A.js = js; A.je = je;
     A.limits = limits; A.nmax = max_nloop - 1;
     A.restore_am = clust ? 0 : 1;
@@ -263,18 +299,45 @@ extern "C" int gb_advect_x(gb_ctx *ctx, const gb_view *m, const gb_view *rm, con
     return launch_x(ctx, A, false);
 }
 
+extern "C" int gb_advect_x_held(gb_ctx *ctx, const gb_view *m, const gb_view *rm, const gb_view *rxm,
+                                const gb_view *rym, const gb_view *rzm, const gb_view *am, int limits,
+                                int max_nloop) {
+    if (!ctx || !m || !rm || !rxm || !rym || !rzm || !am) return GB_EARG;
+    XArgs A{};
+    if (int rc = setup(A, m, am, 1)) return rc;
+    A.q[0] = dv(rm); A.q[1] = dv(rxm); A.q[2] = dv(rym); A.q[3] = dv(rzm);
+    A.nt = (int)rm->n[3];
+    A.limits = limits; A.nmax = max_nloop - 1;
+    A.restore_am = 1;
+    A.js = 1; A.je = 0;
+    A.ctl = ctx->ctl;
+    return launch_x(ctx, A, false);
+}
+
 extern "C" int gb_cfl_x(gb_ctx *ctx, const gb_view *m, const gb_view *am, const int32_t *clust, int halo,
                         int js, int je, int max_nloop) {
     if (!ctx || !m || !am) return GB_EARG;
     XArgs A{};
-    A.m = dv(m);
+    if (int rc = setup(A, m, am, 0)) return rc;
     for (int w = 0; w < 4; ++w) A.q[w] = A.m;
-    A.am = dv(am);
     A.clust = clust;
-    A.im = (int)m->n[0]; A.jm = (int)m->n[1]; A.lm = (int)m->n[2]; A.nt = 0;
+    A.nt = 0;
     A.halo = halo; A.js = js; A.je = je;
     A.limits = 0; A.nmax = max_nloop - 1;
     A.restore_am = clust ? 0 : 1;
+    A.ctl = ctx->ctl;
+    return launch_x(ctx, A, true);
+}
+
+extern "C" int gb_cfl_x_held(gb_ctx *ctx, const gb_view *m, const gb_view *am, int max_nloop) {
+    if (!ctx || !m || !am) return GB_EARG;
+    XArgs A{};
+    if (int rc = setup(A, m, am, 1)) return rc;
+    for (int w = 0; w < 4; ++w) A.q[w] = A.m;
+    A.nt = 0;
+    A.limits = 0; A.nmax = max_nloop - 1;
+    A.restore_am = 1;
+    A.js = 1; A.je = 0;
     A.ctl = ctx->ctl;
     return launch_x(ctx, A, true);
 }

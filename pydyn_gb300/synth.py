@@ -111,8 +111,25 @@ def nam1x1():
     return Region("nam1x1", 90, 70, xbeg=-140, xend=-50, ybeg=10, yend=80, xref=3, yref=2, tref=2, parent=1)
 
 
+def two():
+    """A 24 x 18 parent (15 x 10 degrees) and one child at nam1x1's refinements (xref 3,
+    yref 2, tref 2): the shape of the reference's small tree tests."""
+    glb = Region("glb", 24, 18, xcyc=1, touch_sp=1, touch_np=1)
+    child = Region("child", 24, 16, xbeg=-105, xend=15, ybeg=-30, yend=50, xref=3, yref=2, tref=2, parent=1)
+    return [glb, child]
+
+
+def three():
+    """A grandchild: region 2 at 2 x 2 / tref 2, region 3 at 3 x 2 / tref 2 relative to it."""
+    glb = Region("glb", 24, 18, xcyc=1, touch_sp=1, touch_np=1)
+    mid = Region("mid", 16, 16, xbeg=-90, xend=30, ybeg=-40, yend=40, xref=2, yref=2, tref=2, parent=1)
+    fine = Region("fine", 30, 16, xbeg=-75, xend=0, ybeg=-20, yend=20, xref=6, yref=4, tref=4, parent=2)
+    return [glb, mid, fine]
+
+
 def tree(name, lm):
-    regions = {"glb6x4": glb6x4, "glb3x2": glb3x2, "glb3x2+nam1x1": lambda: [*glb3x2(), nam1x1()]}[name]()
+    regions = {"glb6x4": glb6x4, "glb3x2": glb3x2, "glb3x2+nam1x1": lambda: [*glb3x2(), nam1x1()], "two": two,
+               "three": three}[name]()  # fmt: skip
     at, bt = levels(lm)
     return Zoom(regions, lm, at, bt)
 

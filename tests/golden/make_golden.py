@@ -190,6 +190,10 @@ def _no_convection(zoom, r):
 STEP_RUNS = {  # name: (tree, lm, seed, intervals, umax)
     "config0": ("glb6x4", 25, 11, 24, 40.0),
     "config0-strong": ("glb6x4", 25, 12, 6, 160.0),
+    "two": ("two", 5, 13, 6, 40.0),
+    "two-strong": ("two", 5, 14, 6, 120.0),
+    "three": ("three", 4, 15, 4, 40.0),
+    "config2-adv": ("glb3x2+nam1x1", 34, 31, 3, 40.0),
 }
 
 
