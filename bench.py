@@ -43,8 +43,9 @@ WORKLOADS = {
     # name: (tree, levels, physics, seed)
     "glb6x4": ("glb6x4", 25, False, 11),
     "glb3x2-adv": ("glb3x2", 34, False, 21),
+    "glb3x2+nam1x1-adv": ("glb3x2+nam1x1", 34, False, 31),
 }
-DEFAULT = "glb3x2-adv"
+DEFAULT = "glb3x2+nam1x1-adv"
 BYTES_PER_CELL = {"_dynamu_region1": 12, "_dynamv_region1": 12, "_dynamw_region1": 11, "_dynamu_child": 12,
                   "_dynamv_child": 12, "_dynamw_child": 11, "convec_region": 14, "chemistry_region": 11,
                   "m2phlb1": 2, "m2phlb": 2, "dynam0": 5}  # fmt: skip  (values of 8 bytes at nt = 1)
@@ -271,7 +272,8 @@ def main():
     hbm, how = peaks()
     name, (calls, total_ms, nlaunch) = max(bodies.items(), key=lambda kv: kv[1][1])
     cells = {r: fw.zoom.g(r).im * fw.zoom.g(r).jm * lm for r in fw.zoom.regions()}
-    per_call_bytes = 8 * BYTES_PER_CELL.get(name, 0) * cells[1]
+    body, _, region = name.partition("@")
+    per_call_bytes = 8 * BYTES_PER_CELL.get(body, 0) * cells[int(region) if region else 1]
     achieved = per_call_bytes / (total_ms / calls / 1e3) / 1e9 if per_call_bytes else None
     roof = {"bound": "hbm", "kernel": name, "achieved": achieved, "peak": hbm, "unit": "GB/s",
             "frac": achieved / hbm if achieved else None, "traffic": None, "peak_source": how,

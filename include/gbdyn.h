@@ -131,7 +131,7 @@ int gb_advect_x_held(gb_ctx *ctx, const gb_view *m, const gb_view *rm, const gb_
                      const gb_view *rym, const gb_view *rzm, const gb_view *am, int limits,
                      int max_nloop);
 /* A child's held-end columns: m (ni, n, nl), bm (ni, n-1, nl); bm_full the whole halo'd bm,
- * own[4] (int32 device) the inclusive (i0, i1, j0, j1) box of its faces the columns own
+ * own[4] (int32, host memory) the inclusive (i0, i1, j0, j1) box of its faces the columns own
  * (zoom/advect.py:348-412 _dynamv_child). */
 int gb_advect_y_held(gb_ctx *ctx, const gb_view *m, const gb_view *rm, const gb_view *rxm,
                      const gb_view *rym, const gb_view *rzm, const gb_view *bm, const gb_view *bm_full,

@@ -13,13 +13,22 @@ from .device import views
 from .state import TRACERS
 
 
+class _HostBox:
+    """The inclusive (i0, i1, j0, j1) face box a child's columns own: a host int32[4]."""
+
+    def __init__(self, box):
+        self.arr = (ctypes.c_int32 * 4)(*box)
+
+    @property
+    def ptr(self):
+        return ctypes.addressof(self.arr)
+
+
 def _own_box(st, key, box):
     k = ("own", key)
     if k not in st.consts:
-        from .device import DevArray
-
-        st.consts[k] = DevArray.from_host(st.dev, np.asarray(box, dtype=np.int32))
-    return st.consts[k]
+        st.consts[k] = (_HostBox(box),)
+    return st.consts[k][0]
 
 
 def dynamu(zoom, st, region, js, je, ls, le, limits, max_nloop):

@@ -48,8 +48,10 @@ class BodyProfiler:
             e0.record()
             out = f(*a, **k)
             e1.record()
-            self.pairs[name].append((e0, e1))
-            self.launches[name] += dev.launches() - n0
+            region = a[2] if len(a) > 2 and isinstance(a[2], int) else (1 if name.endswith("region1") else None)
+            key = name if region is None else f"{name}@{region}"
+            self.pairs[key].append((e0, e1))
+            self.launches[key] += dev.launches() - n0
             return out
 
         return call

@@ -102,7 +102,8 @@ class ZoomState:
                 a.free()
         for a in self.consts.values():
             for x in a if isinstance(a, tuple) else (a,):
-                x.free()
+                if isinstance(x, DevArray):
+                    x.free()
         for d in self.saved.values():
             for a in d.values():
                 a.free()

@@ -180,7 +180,12 @@ class Meteo:
         rng = np.random.default_rng(seed)
         self.sp_modes = Modes(rng, 6)
         self.psi = [Modes(rng, 8), Modes(rng, 8)]  # two meteo instants
-        self.chi = [Modes(rng, 8), Modes(rng, 8)]
+        # the divergent part changes sign between the instants, so that the convergence a cell
+        # sees averages out over the interpolation cycle and no column drains over a long run
+        chi = Modes(rng, 8)
+        neg = Modes.__new__(Modes)
+        neg.m, neg.n, neg.a, neg.b, neg.w = chi.m, chi.n, chi.a, chi.b, -chi.w
+        self.chi = [chi, neg]
         self.level_w = 0.4 + 0.6 * rng.random(zoom.lm)
         self.level_sign = np.where(rng.random(zoom.lm) < 0.15, -1.0, 1.0)
         self.umax, self.chi_frac, self.wind_scale = umax, chi_frac, wind_scale
