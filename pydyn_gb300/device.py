@@ -64,6 +64,11 @@ class Device:
         rc = self.L.gb_sync(self.h)
         N.check(rc, "device")
 
+    def discard_status(self):
+        """Wait for the stream and clear the device status word without raising (the errors of
+        work that is being thrown away, a failed speculation's)."""
+        self.L.gb_sync(self.h)
+
     def launches(self):
         return int(self.L.gb_launches(self.h))
 

@@ -152,7 +152,7 @@ class Forward:
         if self.dev.cfl_failed():  # the speculation was wrong: back to the interval's start
             for (r, k), a in self._spec.items():
                 self.st[r][k].assign(a)
-            self.dev.sync()
+            self.dev.discard_status()  # the speculative step's own errors are not the run's
             return self.interval(graph=False)
         self.dev.sync()
         self.t = t0 + self.nread

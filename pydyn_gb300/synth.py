@@ -108,7 +108,12 @@ def glb3x2():
 
 
 def nam1x1():
-    return Region("nam1x1", 90, 70, xbeg=-140, xend=-50, ybeg=10, yend=80, xref=3, yref=2, tref=2, parent=1)
+    """The 90 x 70 child over North America.  141W-51W rather than 140W-50W: the benchmark's
+    corners are not on glb3x2's 3-degree lines, and TM5's nint would place the footprint at
+    parent cells 14..43 (141W-51W) while the child's own fluxes sit one degree east, so its
+    boundary fluxes would not match the parent's and cells near the interface would drain.
+    The footprint (i 14..43, j 51..85) and every size are the benchmark's."""
+    return Region("nam1x1", 90, 70, xbeg=-141, xend=-51, ybeg=10, yend=80, xref=3, yref=2, tref=2, parent=1)
 
 
 def two():
@@ -204,7 +209,14 @@ class Meteo:
         return dp * dxyp[None, :, None] / GRAV
 
     def fluxes(self, r, instant):
-        """(pu (im+1, jm, lm), pv (im, jm+1, lm)) in kg/s of region r at a meteo instant."""
+        """(pu (im+1, jm, lm), pv (im, jm+1, lm)) in kg/s of region r at a meteo instant.  The
+        wind scales are the global region's, so every region samples one and the same flow and
+        a child's boundary fluxes are its parent's."""
+        if r != 1:
+            self._winds(1, instant)
+        return self._winds(r, instant)
+
+    def _winds(self, r, instant):
         g = self.zoom.g(r)
         lonc, latc = _corners(g)
         lon, lat = _centres(g)
@@ -220,13 +232,18 @@ class Meteo:
         dxf = AE * dx * (PI / 180.0) * clat_f  # (jm+1,)
         dpsi_x = psi[1:, :] - psi[:-1, :]  # (im, jm+1)
         v_psi = -np.where(np.abs(dxf) > 1.0, dpsi_x / np.where(np.abs(dxf) > 1.0, dxf, 1.0)[None, :], 0.0)
-        scale = self.umax / max(float(np.abs(u_psi).max()), float(np.abs(v_psi).max()))
         # velocity potential: gradient between neighbouring centres
         chi_w = np.concatenate([chi[-1:], chi, chi[:1]], axis=0) if g.xcyc else np.concatenate([chi[:1], chi, chi[-1:]])
         u_chi = (chi_w[1:] - chi_w[:-1]) / dxx[None, :]
         v_chi = np.zeros((g.im, g.jm + 1))
         v_chi[:, 1:-1] = (chi[:, 1:] - chi[:, :-1]) / dyy
-        cs = self.chi_frac * self.umax / max(float(np.abs(u_chi).max()), float(np.abs(v_chi).max()), 1e-300)
+        if r == 1:
+            self._scale = getattr(self, "_scale", {})
+            self._scale[instant] = (
+                self.umax / max(float(np.abs(u_psi).max()), float(np.abs(v_psi).max())),
+                self.chi_frac * self.umax / max(float(np.abs(u_chi).max()), float(np.abs(v_chi).max()), 1e-300),
+            )
+        scale, cs = self._scale[instant]
         u = (u_psi * scale + u_chi * cs) * self.wind_scale
         v = (v_psi * scale + v_chi * cs) * self.wind_scale
         if g.xcyc:
