@@ -64,3 +64,41 @@ class BodyProfiler:
             ms = [a.elapsed_ms(b) for a, b in pairs]
             out[name] = (len(ms), sum(ms), self.launches[name])
         return out
+
+
+def main(argv=None):
+    """One eagerly enqueued interval of a configuration -- every kernel launched once, no graph,
+    no pinned copies -- for a launch list under a profiler:
+
+        python -m pydyn_gb300.profile --config glb3x2+nam1x1 --levels 34 --intervals 1
+    """
+    import argparse
+    import sys
+    from pathlib import Path
+
+    sys.path.insert(0, str(Path(__file__).resolve().parents[1]))
+    ap = argparse.ArgumentParser(description=main.__doc__.split("\n")[0])
+    ap.add_argument("--config", default="glb3x2+nam1x1")
+    ap.add_argument("--levels", type=int, default=34)
+    ap.add_argument("--seed", type=int, default=31)
+    ap.add_argument("--intervals", type=int, default=1)
+    a = ap.parse_args(argv)
+    from __graft_entry__ import build
+
+    build()
+    from .device import Device
+    from .forward import Forward
+
+    dev = Device(0)
+    fw = Forward(dev, a.config, a.levels, a.seed)
+    n0 = dev.launches()
+    for _ in range(a.intervals):
+        fw.interval(graph=False)
+    dev.sync()
+    print(f"{a.intervals} interval(s) of {a.config}: {dev.launches() - n0} kernel launches")
+    fw.close()
+    dev.close()
+
+
+if __name__ == "__main__":
+    main()
