@@ -183,6 +183,21 @@ int gb_coarsen_ambm(gb_ctx *ctx, const gb_view *parent, const gb_view *child, in
                     int je, int lb, int le, int xr, int yr, int zr, int xedges, int sp_edge,
                     int np_edge);
 
+/* ------------------------------------------------------------------ convection (pydyn/kernels.py)
+ * convec on the listed owned columns (kernels.py:350-457, zoom/physics.py:33-52): m and tracers
+ * the region's interior views (im, jm, lm[, nt]); entu, detu, entd, detd (im, jm, >= lmax);
+ * dkg (im, jm, >= lmax); cloud_top / cloud_lfs (im, jm) int32 device arrays with element
+ * strides ts0, ts1 (1-based levels, 0 = no cloud); cols: ncol (i, j) int32 pairs, 0-based;
+ * dt = nconv / (2 tref).  cache_inv (ncol*lmax*lmax), cache_m (ncol*lmax), cache_tag (ncol)
+ * and epoch (1 int32, all device) keep each column's inverse for the next call in the same
+ * epoch whose air mass is bitwise unchanged; NULL cache_inv disables the reuse. */
+int gb_convec(gb_ctx *ctx, const gb_view *m, const gb_view *rm, const gb_view *rxm, const gb_view *rym,
+              const gb_view *rzm, const gb_view *entu, const gb_view *detu, const gb_view *entd,
+              const gb_view *detd, const gb_view *dkg, const int32_t *cloud_top,
+              const int32_t *cloud_lfs, int64_t ts0, int64_t ts1, const int32_t *cols, int ncol,
+              double dt, int lmax, double *cache_inv, double *cache_m, int32_t *cache_tag,
+              const int32_t *epoch);
+
 /* ------------------------------------------------------------------ mass fluxes, pressure
  * dynam0 (kernels.py:102-125, zoom/massflow.py:188-203): am = dt pu, bm = dt pv and cm from the
  * column convergence.  pu (im+1, jm, lm), pv (im, jm+1, lm), bt (lm+1) device; am (im+1, jm, lm),

@@ -41,6 +41,8 @@ def lib():
         L.or_advect_z.argtypes = [P, P, P, P, P, P, I, I, I, I, I, I, I, i32]
         L.or_fluxes_from_meteo.argtypes = [P, P, ctypes.c_void_p, ctypes.c_double, P, P, P]
         L.or_advect_x_held.argtypes = [P, P, P, P, P, P, I, I, I]
+        L.or_convec.argtypes = [P, P, P, P, P, P, P, P, P, P, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int64,
+                                ctypes.c_int64, ctypes.c_void_p, I, ctypes.c_double, I]
         L.or_advect_y_held.argtypes = [P, P, P, P, P, P, P, I, I, I, I]
         L.or_m2phlb.argtypes = [P, P, P, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, I, I, I, ctypes.c_void_p]
         _LIB.append(L)
@@ -136,6 +138,22 @@ def advect_y_held(m, rm, rxm, rym, rzm, bm, full, full_l0, limits=True, max_nloo
     if rc and not mass_only:
         raise CFLError("nloop too high in dynamv")
     return not rc
+
+
+def convec(m, rm, rxm, rym, rzm, entu, detu, entd, detd, cloud_top, cloud_lfs, dkg, dt, lmax, cols=None):
+    """kernels.convec (kernels.py:423-457) with the Crout inverse, on the listed (i, j) columns
+    (default every column of m (im, jm, lm))."""
+    im, jm = m.shape[0], m.shape[1]
+    if cols is None:
+        cols = np.array([(i, j) for i in range(im) for j in range(jm)], dtype=np.int32)
+    cols = np.ascontiguousarray(cols, dtype=np.int32)
+    top = np.asarray(cloud_top)
+    lfs = np.asarray(cloud_lfs)
+    if top.dtype != np.int32 or lfs.dtype != np.int32 or top.strides != lfs.strides:
+        top, lfs = np.ascontiguousarray(top, dtype=np.int32), np.ascontiguousarray(lfs, dtype=np.int32)
+    lib().or_convec(*map(_ref, map(ov, (m, rm, rxm, rym, rzm, entu, detu, entd, detd, dkg))), top.ctypes.data,
+                    lfs.ctypes.data, top.strides[0] // 4, top.strides[1] // 4, cols.ctypes.data, len(cols),
+                    float(dt), int(lmax))  # fmt: skip
 
 
 def fluxes_from_meteo(pu, pv, bt, dt, am, bm, cm):

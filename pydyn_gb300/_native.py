@@ -80,6 +80,8 @@ SIGNATURES = {
     "gb_update_parent": (_I, [_VP, _P, _P, _I, _I, _I, _I, _I]),
     "gb_coarsen_block": (_I, [_VP, _P, _P, _I, _I, _I, _I, _I, _D]),
     "gb_coarsen_ambm": (_I, [_VP, _P, _P, _I, _I, _I, _I, _I, _I, _I, _I, _I, _I, _I, _I]),
+    "gb_convec": (_I, [_VP, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P, _VP, _VP, ctypes.c_int64, ctypes.c_int64, _VP, _I,
+                       _D, _I, _VP, _VP, _VP, _VP]),
     "gb_fluxes_from_meteo": (_I, [_VP, _P, _P, _VP, _D, _P, _P, _P]),
     "gb_m2phlb": (_I, [_VP, _P, _P, _P, _VP, _VP, _VP, _I, _I, _I, _VP]),
 }

@@ -121,6 +121,21 @@ def m2phlb(m, sp, phlb, dxyp, at, bt, ring=None):
                         None if par is None else par.ptr), "m2phlb")  # fmt: skip
 
 
+def convec(m, rm, rxm, rym, rzm, entu, detu, entd, detd, dkg, cloud_top, cloud_lfs, cols, dt, lmax, cache=None):
+    """kernels.convec (:423) on the listed owned columns: cols a DevArray (ncol, 2) int32 of
+    0-based (i, j); cloud_top / cloud_lfs DevArrays (im, jm) int32; cache: None or
+    (inv, m, tag, epoch) DevArrays keeping each column's inverse for the paired call."""
+    _tracer_strides(rm, rxm, rym, rzm)
+    if cloud_top.strides != cloud_lfs.strides:
+        raise ValueError("convec: cloud_top and cloud_lfs must share their strides")
+    L, h = _lib(m)
+    ncol = cols.shape[0]
+    c = (None, None, None, None) if cache is None else tuple(x.ptr for x in cache)
+    N.check(L.gb_convec(h, *views(m, rm, rxm, rym, rzm, entu, detu, entd, detd, dkg), cloud_top.ptr, cloud_lfs.ptr,
+                        cloud_top.strides[0], cloud_top.strides[1], cols.ptr, ncol, float(dt), int(lmax), *c),
+            "convec")  # fmt: skip
+
+
 def to_device(dev, arr, dtype=np.float64):
     """A DevArray copy of a host array (0-based bounds)."""
     return DevArray.from_host(dev, np.asarray(arr, dtype=dtype))

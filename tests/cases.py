@@ -42,6 +42,11 @@ def run_oracle(ins, meta):
             sp, phlb = np.zeros(m.shape[:2]), np.zeros((*m.shape[:2], m.shape[2] + 1))
             O.m2phlb(m, sp, phlb, a["dxyp"], a["at"], a["bt"])
             return {"sp": sp, "phlb": phlb}, None
+        elif op == "convec":
+            q = [a[k] for k in TRACERS]
+            O.convec(a["m"], *q, a["entu"], a["detu"], a["entd"], a["detd"], a["cloud_top"], a["cloud_lfs"], a["dkg"],
+                     meta["dt"], meta["lmax"])  # fmt: skip
+            return {k: a[k] for k in ("m", *TRACERS)}, None
         else:
             raise KeyError(op)
         if r is None:
@@ -102,6 +107,15 @@ def run_device(dev, ins, meta):
             K.m2phlb(m, sp, phlb, d["dxyp"], d["at"], d["bt"])
             dev.sync()
             return {"sp": sp.host(), "phlb": phlb.host()}, None
+        if op == "convec":
+            im, jm = d["m"].shape[0], d["m"].shape[1]
+            cols = DevArray.from_host(dev, np.array([(i, j) for i in range(im) for j in range(jm)], dtype=np.int32))
+            q = [d[k] for k in TRACERS]
+            K.convec(d["m"], *q, d["entu"], d["detu"], d["entd"], d["detd"], d["dkg"], d["cloud_top"], d["cloud_lfs"],
+                     cols, meta["dt"], meta["lmax"])  # fmt: skip
+            dev.sync()
+            cols.free()
+            return {k: d[k].host() for k in ("m", *TRACERS)}, None
         raise KeyError(op)
     except N.CFLError:
         return {}, "CFLError"

@@ -89,6 +89,18 @@ def kernel_cases():
         put(f"cflz{tag}", {"m": s.m, "flux": cm}, {"m": m3, "flux": c3} if r else {}, op="cflz",
             error=None if r else "fail")
 
+    # convection with diffusion (kernels.convec, the Crout inverse), the reference test's variants
+    for k, kw in enumerate(({}, {"lfs_above_top": True}, {"strong_detu": True}, {"top_max": 3})):
+        rng = np.random.default_rng(60 + k)
+        lmax = 10
+        s = synth.state(rng, 8, 6, 12, 2)
+        conv = synth.convection(rng, s.m, lmax, 1800.0, **kw)
+        st = s.copy()
+        kernels.convec(st.m, st.rm, st.rxm, st.rym, st.rzm, **conv, dt=1800.0, lmax=lmax)
+        ins = {"m": s.m, "rm": s.rm, "rxm": s.rxm, "rym": s.rym, "rzm": s.rzm, **conv}
+        put(f"convec{k}", ins, {"m": st.m, "rm": st.rm, "rxm": st.rxm, "rym": st.rym, "rzm": st.rzm}, op="convec",
+            lmax=lmax, dt=1800.0)
+
     # dynam0 and m2phlb1
     rng = np.random.default_rng(7)
     IM, JM, LM = 10, 8, 6

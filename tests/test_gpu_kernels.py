@@ -49,6 +49,62 @@ def _state(rng, im, jm, lm, nt, cfl):
     return {"m": m, "rm": rm, "rxm": slopes[0], "rym": slopes[1], "rzm": slopes[2]}, (am, bm, cm)
 
 
+def _convection(rng, m, lmax, dt, frac=0.4):
+    """Seeded convection inputs in kernels.convec's layout: a fraction of the columns convective
+    with cloud tops in 10..30 (a smooth updraft flux peaking mid-cloud, a downdraft a third as
+    strong below the level of free sinking), the rest diffusion only; dkg everywhere."""
+    im, jm, lm = m.shape
+    top = np.where(rng.random((im, jm)) < frac, rng.integers(10, 31, (im, jm)), 0).astype(np.int32)
+    top = np.minimum(top, lmax).astype(np.int32)
+    lfs = np.where(top > 0, rng.integers(2, np.maximum(top, 3)), 0).astype(np.int32)
+    k = np.arange(lm + 1)[None, None, :]
+    T = np.maximum(top, 1)[..., None]
+    flux = np.where(k <= T, np.sin(np.pi * np.minimum(k, T) / T) ** 2, 0.0) * (0.05 * m.mean(axis=2, keepdims=True) / dt)
+    d = np.diff(flux, axis=2)
+    noise = 1.0 + 0.2 * rng.random(m.shape)
+    entu, detu = np.maximum(d, 0.0) * noise, np.maximum(-d, 0.0) * noise
+    entd, detd = 0.3 * detu[..., ::-1].copy(), 0.3 * entu[..., ::-1].copy()
+    dkg = 0.02 * m[..., :lmax] / dt * rng.random((im, jm, lmax))
+    return {"entu": entu, "detu": detu, "entd": entd, "detd": detd, "dkg": dkg, "cloud_top": top, "cloud_lfs": lfs}
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize(("shape", "lmax"), [((120, 90, 34, 1), 34), ((90, 70, 34, 1), 26), ((40, 30, 60, 2), 60)])
+def test_convec_matches_oracle_at_size(dev, shape, lmax):
+    """Convection on every column, then again on the same air mass: the second call reuses the
+    kept inverses, and both equal the oracle's two applications bitwise."""
+    from oracle import kernels as O
+
+    from pydyn_gb300 import kernels as K
+    from pydyn_gb300.device import DevArray
+
+    im, jm, lm, nt = shape
+    rng = np.random.default_rng(zlib.crc32(repr(shape).encode()))
+    st, _ = _state(rng, im, jm, lm, nt, 0.5)
+    conv = _convection(rng, st["m"], lmax, 1800.0)
+    want = {k: v.copy() for k, v in st.items()}
+    for _ in range(2):
+        O.convec(want["m"], *(want[q] for q in TRACERS), conv["entu"], conv["detu"], conv["entd"], conv["detd"],
+                 conv["cloud_top"], conv["cloud_lfs"], conv["dkg"], 1800.0, lmax)  # fmt: skip
+    d = {k: DevArray.from_host(dev, v) for k, v in {**st, **conv}.items()}
+    ncol = im * jm
+    cols = DevArray.from_host(dev, np.array([(i, j) for i in range(im) for j in range(jm)], dtype=np.int32))
+    cache = (DevArray.zeros(dev, (0, ncol * lmax * lmax - 1)), DevArray.zeros(dev, (0, ncol * lmax - 1)),
+             DevArray.zeros(dev, (0, ncol - 1), dtype=np.int32), DevArray.from_host(dev, np.array([7], np.int32)))
+    before = dev.launches()
+    for _ in range(2):
+        K.convec(d["m"], *(d[q] for q in TRACERS), d["entu"], d["detu"], d["entd"], d["detd"], d["dkg"],
+                 d["cloud_top"], d["cloud_lfs"], cols, 1800.0, lmax, cache=cache)  # fmt: skip
+    dev.sync()
+    assert dev.launches() - before == 2
+    tags = cache[2].host()
+    assert (tags == 7).all()
+    for k in ("m", *TRACERS):
+        assert_bitwise(d[k].host(), want[k], f"convec.{k}")
+    for a in (*d.values(), cols, *cache):
+        a.free()
+
+
 @pytest.mark.gpu
 @pytest.mark.parametrize("shape", [(120, 90, 34, 1), (60, 45, 25, 2), (90, 70, 34, 1)])
 @pytest.mark.parametrize("cfl", [0.3, 1.6])
