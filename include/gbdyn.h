@@ -212,6 +212,10 @@ int gb_m2phlb(gb_ctx *ctx, const gb_view *m, const gb_view *sp, const gb_view *p
               const double *dxyp, const double *at, const double *bt, int ring_xr, int ring_yr,
               int jbeg, const double *dxyp_parent);
 
+/* The device build of the library's exp / log / pow / cos / sin (op 0..4) on n values: the
+ * check that it equals the host build (libgbmath.so) bit for bit.  No reference counterpart. */
+int gb_math_eval(gb_ctx *ctx, int op, const double *x, const double *y, double *out, int64_t n);
+
 #ifdef __cplusplus
 }
 #endif

@@ -91,3 +91,29 @@ extern "C" int gb_m2phlb(gb_ctx *ctx, const gb_view *m, const gb_view *sp, const
                                                                   ring_xr, ring_yr, jbeg, dxyp_parent);
     return gb_after_launch(ctx, "m2phlb");
 }
+
+// ------------------------------------------------------------------ the device math, for tests
+#include "gbmath.h"
+
+namespace {
+__global__ void k_math_eval(int op, const double *x, const double *y, double *out, int64_t n) {
+    int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    double r;
+    switch (op) {
+        case 0: r = gbm_exp(x[k]); break;
+        case 1: r = gbm_log(x[k]); break;
+        case 2: r = gbm_pow(x[k], y[k]); break;
+        case 3: r = gbm_cos(x[k]); break;
+        default: r = gbm_sin(x[k]); break;
+    }
+    out[k] = r;
+}
+}  // namespace
+
+extern "C" int gb_math_eval(gb_ctx *ctx, int op, const double *x, const double *y, double *out, int64_t n) {
+    if (!ctx || !x || !y || !out || n < 0) return GB_EARG;
+    if (n == 0) return GB_OK;
+    k_math_eval<<<(int)((n + 127) / 128), 128, 0, ctx->stream>>>(op, x, y, out, n);
+    return gb_after_launch(ctx, "math_eval");
+}

@@ -1,0 +1,82 @@
+"""The package's host math library (libgbmath.so, the host build of csrc/gbmath.h) against the C
+library: within 1 ulp on the arguments the dynamic step's Kzz and chemistry pass (and wider
+ranges), C99 special values; the device build equals the host build bit for bit (GPU test)."""
+
+import math
+
+import numpy as np
+import pytest
+
+from conftest import bits
+
+
+def ulps(a, b):
+    def ordered(x):
+        i = np.asarray(x, dtype="<f8").view(np.int64)
+        return np.where(i < 0, np.iinfo(np.int64).min - i, i)
+
+    return np.abs(ordered(a) - ordered(b))
+
+
+def _cases(rng):
+    return {
+        "exp": [(x,) for x in np.concatenate([rng.uniform(-700, 700, 4000), rng.uniform(-2, 2, 4000),
+                                             rng.uniform(-1e-8, 1e-8, 500)])],
+        "log": [(x,) for x in np.concatenate([np.exp(rng.uniform(-700, 700, 4000)), rng.uniform(0.5, 2.0, 4000),
+                                             1.0 + rng.uniform(-1e-7, 1e-7, 500), [5e-320, 1e-310]])],
+        "pow": [(x, y) for x, y in zip(rng.uniform(0.1, 10, 4000), rng.uniform(-5, 5, 4000), strict=True)]
+        + [(x, 1.0 / 3.0) for x in rng.uniform(1e-6, 1e3, 2000)]
+        + [(x, 1.37) for x in rng.uniform(0.6, 1.1, 2000)]
+        + [(x, 0.2857) for x in rng.uniform(0.01, 100.0, 2000)]
+        + [(x, y) for x, y in zip(rng.uniform(0.99, 1.01, 1000), rng.uniform(-3e3, 3e3, 1000), strict=True)],
+        "cos": [(x,) for x in np.concatenate([rng.uniform(-1.6, 1.6, 4000), rng.uniform(-100, 100, 2000)])],
+        "sin": [(x,) for x in np.concatenate([rng.uniform(-1.6, 1.6, 4000), rng.uniform(-100, 100, 2000)])],
+    }
+
+
+@pytest.mark.parametrize("name", ["exp", "log", "pow", "cos", "sin"])
+def test_within_one_ulp_of_the_c_library(built, name):
+    from pydyn_gb300 import _native as N
+
+    f = getattr(N.mathlib(), name)
+    rng = np.random.default_rng(7)
+    args = _cases(rng)[name]
+    ours = np.array([f(*a) for a in args])
+    theirs = np.array([getattr(math, name)(*a) for a in args])
+    d = ulps(ours, theirs)
+    assert d.max() <= 1, f"{name}: {d.max()} ulp at {args[int(d.argmax())]}"
+
+
+def test_special_values(built):
+    from pydyn_gb300 import _native as N
+
+    L = N.mathlib()
+    inf, nan = math.inf, math.nan
+    assert L.exp(0.0) == 1.0 and L.exp(-inf) == 0.0 and L.exp(inf) == inf and L.exp(800.0) == inf
+    assert L.exp(-800.0) == 0.0 and math.isnan(L.exp(nan))
+    assert L.log(1.0) == 0.0 and L.log(0.0) == -inf and math.isnan(L.log(-1.0)) and L.log(inf) == inf
+    assert L.pow(1.0, nan) == 1.0 and L.pow(2.0, 0.0) == 1.0 and L.pow(-8.0, 1.0 / 3.0) != L.pow(-8.0, 1.0 / 3.0)
+    assert L.pow(-2.0, 3.0) == -8.0 and L.pow(0.0, -1.0) == inf and L.pow(4.0, 0.5) == 2.0
+    assert L.pow(2.0, -1075.0) == 0.0 and L.pow(2.0, 1024.0) == inf and L.pow(2.0, -1074.0) == 5e-324
+    assert L.cos(0.0) == 1.0 and L.sin(0.0) == 0.0 and bits(L.sin(-0.0)) == bits(-0.0)
+
+
+@pytest.mark.gpu
+def test_device_math_equals_host_math(dev):
+    from pydyn_gb300 import _native as N
+    from pydyn_gb300.device import DevArray
+
+    L = N.mathlib()
+    rng = np.random.default_rng(11)
+    for op, name in enumerate(("exp", "log", "pow", "cos", "sin")):
+        args = _cases(rng)[name]
+        x = np.array([a[0] for a in args])
+        y = np.array([a[1] if len(a) > 1 else 0.0 for a in args])
+        dx, dy = DevArray.from_host(dev, x), DevArray.from_host(dev, y)
+        out = DevArray.zeros(dev, (0, len(x) - 1))
+        N.check(dev.L.gb_math_eval(dev.h, op, dx.ptr, dy.ptr, out.ptr, len(x)), "gb_math_eval")
+        got = out.host()
+        want = np.array([getattr(L, name)(*a) for a in args])
+        assert (bits(got) == bits(want)).all(), name
+        for a in (dx, dy, out):
+            a.free()
