@@ -198,6 +198,17 @@ int gb_convec(gb_ctx *ctx, const gb_view *m, const gb_view *rm, const gb_view *r
               double dt, int lmax, double *cache_inv, double *cache_m, int32_t *cache_tag,
               const int32_t *epoch);
 
+/* Calc_Kzz (diffusion.py:266-276, the zoom driver's Kzz body at zoom/driver.py:186-200): the
+ * vertical diffusion exchange rate dkg (im, jm, lmax_conv) of every column, zero at lmax_conv-1.
+ * spm, sp (im, jm) the surface pressure of the previous / current instant; pu (im+1, jm, lm),
+ * pv (im, jm+1, lm); t, q (im, jm, lm); surface: 10 (im, jm) views in the order oro, lsm, sr,
+ * srols, u10m, v10m, sshf, slhf, ewss, nsss; at, bt (lm+1), dxyp (jm) device; dx, dy, ybeg the
+ * region's grid in degrees.  pblh (im, jm) receives the boundary-layer height if not NULL. */
+int gb_calc_kzz(gb_ctx *ctx, const gb_view *spm, const gb_view *sp, const gb_view *pu,
+                const gb_view *pv, const gb_view *t, const gb_view *q, const gb_view *surface,
+                const double *at, const double *bt, const double *dxyp, int lmax_conv, double dx,
+                double dy, double ybeg, const gb_view *dkg, const gb_view *pblh);
+
 /* ------------------------------------------------------------------ mass fluxes, pressure
  * dynam0 (kernels.py:102-125, zoom/massflow.py:188-203): am = dt pu, bm = dt pv and cm from the
  * column convergence.  pu (im+1, jm, lm), pv (im, jm+1, lm), bt (lm+1) device; am (im+1, jm, lm),

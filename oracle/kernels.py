@@ -41,6 +41,8 @@ def lib():
         L.or_advect_z.argtypes = [P, P, P, P, P, P, I, I, I, I, I, I, I, i32]
         L.or_fluxes_from_meteo.argtypes = [P, P, ctypes.c_void_p, ctypes.c_double, P, P, P]
         L.or_advect_x_held.argtypes = [P, P, P, P, P, P, I, I, I]
+        D, VP = ctypes.c_double, ctypes.c_void_p
+        L.or_calc_kzz.argtypes = [P, P, P, P, P, P, P, VP, VP, VP, I, D, D, D, P, P]
         L.or_convec.argtypes = [P, P, P, P, P, P, P, P, P, P, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int64,
                                 ctypes.c_int64, ctypes.c_void_p, I, ctypes.c_double, I]
         L.or_advect_y_held.argtypes = [P, P, P, P, P, P, P, I, I, I, I]
@@ -154,6 +156,21 @@ def convec(m, rm, rxm, rym, rzm, entu, detu, entd, detd, cloud_top, cloud_lfs, d
     lib().or_convec(*map(_ref, map(ov, (m, rm, rxm, rym, rzm, entu, detu, entd, detd, dkg))), top.ctypes.data,
                     lfs.ctypes.data, top.strides[0] // 4, top.strides[1] // 4, cols.ctypes.data, len(cols),
                     float(dt), int(lmax))  # fmt: skip
+
+
+KZZ_SURFACE = ("oro", "lsm", "sr", "srols", "u10m", "v10m", "sshf", "slhf", "ewss", "nsss")
+
+
+def calc_kzz(spm, sp, pu, pv, t, q, surface, at, bt, dxyp, lmax_conv, dx=6.0, dy=4.0, ybeg=-90.0):
+    """diffusion.calc_kzz (diffusion.py:266-276): (dkg (im, jm, lmax_conv), pblh (im, jm))."""
+    im, jm = t.shape[0], t.shape[1]
+    dkg = np.zeros((im, jm, lmax_conv))
+    pblh = np.zeros((im, jm))
+    surf = (OV * 10)(*[ov(np.asarray(surface[k], dtype=np.float64)) for k in KZZ_SURFACE])
+    arrs = [np.ascontiguousarray(a, dtype=np.float64) for a in (at, bt, dxyp)]
+    lib().or_calc_kzz(*map(_ref, map(ov, (spm, sp, pu, pv, t, q))), surf, *(a.ctypes.data for a in arrs),
+                      int(lmax_conv), float(dx), float(dy), float(ybeg), _ref(ov(dkg)), _ref(ov(pblh)))  # fmt: skip
+    return dkg, pblh
 
 
 def fluxes_from_meteo(pu, pv, bt, dt, am, bm, cm):

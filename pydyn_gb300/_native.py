@@ -82,7 +82,8 @@ SIGNATURES = {
     "gb_coarsen_ambm": (_I, [_VP, _P, _P, _I, _I, _I, _I, _I, _I, _I, _I, _I, _I, _I, _I]),
     "gb_convec": (_I, [_VP, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P, _VP, _VP, ctypes.c_int64, ctypes.c_int64, _VP, _I,
                        _D, _I, _VP, _VP, _VP, _VP]),
-    "gb_math_eval": (_I, [_VP, _I, _VP, _VP, _VP, ctypes.c_int64]),
+    "gb_calc_kzz": (_I, [_VP, _P, _P, _P, _P, _P, _P, _P, _VP, _VP, _VP, _I, _D, _D, _D, _P, _P]),
+    "gb_math_eval":(_I, [_VP, _I, _VP, _VP, _VP, ctypes.c_int64]),
     "gb_fluxes_from_meteo": (_I, [_VP, _P, _P, _VP, _D, _P, _P, _P]),
     "gb_m2phlb": (_I, [_VP, _P, _P, _P, _VP, _VP, _VP, _I, _I, _I, _VP]),
 }

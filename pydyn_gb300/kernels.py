@@ -136,6 +136,24 @@ def convec(m, rm, rxm, rym, rzm, entu, detu, entd, detd, dkg, cloud_top, cloud_l
             "convec")  # fmt: skip
 
 
+KZZ_SURFACE = ("oro", "lsm", "sr", "srols", "u10m", "v10m", "sshf", "slhf", "ewss", "nsss")
+
+
+def calc_kzz(spm, sp, pu, pv, t, q, surface, at, bt, dxyp, lmax_conv, dx, dy, ybeg, dkg, pblh=None):
+    """diffusion.calc_kzz (diffusion.py:266-276) into dkg (im, jm, lmax_conv) and, if given,
+    pblh (im, jm).  surface: the 10 (im, jm) DevArrays in KZZ_SURFACE order (or a mapping of
+    those names); at, bt (lm+1) and dxyp (jm) contiguous DevArrays."""
+    if isinstance(surface, dict):
+        surface = [surface[k] for k in KZZ_SURFACE]
+    if len(surface) != len(KZZ_SURFACE):
+        raise ValueError(f"calc_kzz: {len(KZZ_SURFACE)} surface fields, got {len(surface)}")
+    L, h = _lib(t)
+    surf = (N.GBView * len(KZZ_SURFACE))(*(s.view() for s in surface))
+    N.check(L.gb_calc_kzz(h, *views(spm, sp, pu, pv, t, q), surf, at.ptr, bt.ptr, dxyp.ptr, int(lmax_conv),
+                          float(dx), float(dy), float(ybeg), *views(dkg, pblh)),
+            "calc_kzz")  # fmt: skip
+
+
 def to_device(dev, arr, dtype=np.float64):
     """A DevArray copy of a host array (0-based bounds)."""
     return DevArray.from_host(dev, np.asarray(arr, dtype=dtype))

@@ -47,6 +47,11 @@ def run_oracle(ins, meta):
             O.convec(a["m"], *q, a["entu"], a["detu"], a["entd"], a["detd"], a["cloud_top"], a["cloud_lfs"], a["dkg"],
                      meta["dt"], meta["lmax"])  # fmt: skip
             return {k: a[k] for k in ("m", *TRACERS)}, None
+        elif op == "kzz":
+            surface = {k: a[f"surface.{k}"] for k in O.KZZ_SURFACE}
+            dkg, pblh = O.calc_kzz(a["spm"], a["sp"], a["pu"], a["pv"], a["t"], a["q"], surface, a["at"], a["bt"],
+                                   a["dxyp"], meta["lmax"], meta["dx"], meta["dy"], meta["ybeg"])  # fmt: skip
+            return {"dkg": dkg, "pblh": pblh}, None
         else:
             raise KeyError(op)
         if r is None:
@@ -116,6 +121,18 @@ def run_device(dev, ins, meta):
             dev.sync()
             cols.free()
             return {k: d[k].host() for k in ("m", *TRACERS)}, None
+        if op == "kzz":
+            im, jm = d["t"].shape[0], d["t"].shape[1]
+            dkg = DevArray.zeros(dev, (0, im - 1), (0, jm - 1), (0, meta["lmax"] - 1))
+            pblh = DevArray.zeros(dev, (0, im - 1), (0, jm - 1))
+            surface = [d[f"surface.{k}"] for k in K.KZZ_SURFACE]
+            K.calc_kzz(d["spm"], d["sp"], d["pu"], d["pv"], d["t"], d["q"], surface, d["at"], d["bt"], d["dxyp"],
+                       meta["lmax"], meta["dx"], meta["dy"], meta["ybeg"], dkg, pblh)  # fmt: skip
+            dev.sync()
+            out = {"dkg": dkg.host(), "pblh": pblh.host()}
+            dkg.free()
+            pblh.free()
+            return out, None
         raise KeyError(op)
     except N.CFLError:
         return {}, "CFLError"

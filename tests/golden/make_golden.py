@@ -30,6 +30,14 @@ def _reference():
     return pydyn
 
 
+def _gbmath():
+    """libgbmath.so (built here if needed): the exp / log / pow / cos the device computes."""
+    sys.path.insert(0, str(HERE.parents[1]))
+    from pydyn_gb300.build import build
+
+    return build()[1]
+
+
 def kernel_cases():
     _reference()
     from pydyn import balance, cfl, kernels, redgrid, synth
@@ -100,6 +108,24 @@ def kernel_cases():
         ins = {"m": s.m, "rm": s.rm, "rxm": s.rxm, "rym": s.rym, "rzm": s.rzm, **conv}
         put(f"convec{k}", ins, {"m": st.m, "rm": st.rm, "rxm": st.rxm, "rym": st.rym, "rzm": st.rzm}, op="convec",
             lmax=lmax, dt=1800.0)
+
+    # Calc_Kzz (diffusion.calc_kzz on pydyn.synth.kzz_inputs), pydyn's libm routed through the
+    # package's gbmath so that the fixtures hold the bits the device must reproduce
+    from pydyn import diffusion, ops
+
+    ops.use_libm(str(_gbmath()))
+    for k, (im, jm, lm, lmax, spm_scale) in enumerate(((12, 9, 8, 6, None), (16, 10, 34, 26, 1.003),
+                                                      (12, 9, 8, 8, 0.998), (10, 6, 25, 25, None))):  # fmt: skip
+        rng = np.random.default_rng(80 + k)
+        args, grid = synth.kzz_inputs(rng, im, jm, lm, lmax)
+        args = list(args)
+        if spm_scale is not None:  # spm (the step's middle) apart from sp (its start)
+            args[0] = args[1] * spm_scale
+        dkg, parts = diffusion.calc_kzz(*args, **grid)
+        spm, sp, pu, pv, t, q, surface, at, bt, dxyp, _ = args
+        ins = {"spm": spm, "sp": sp, "pu": pu, "pv": pv, "t": t, "q": q, "at": at, "bt": bt, "dxyp": dxyp,
+               **{f"surface.{name}": surface[name] for name in surface}}  # fmt: skip
+        put(f"kzz{k}", ins, {"dkg": dkg, "pblh": parts["pblh"]}, op="kzz", lmax=lmax, **grid)
 
     # dynam0 and m2phlb1
     rng = np.random.default_rng(7)
