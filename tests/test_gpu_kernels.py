@@ -105,6 +105,57 @@ def test_convec_matches_oracle_at_size(dev, shape, lmax):
         a.free()
 
 
+def _kzz_inputs(rng, im, jm, lm):
+    """Calc_Kzz inputs on a global grid: a warm surface under a stable lapse rate, humidity
+    falling with height, heat fluxes of both signs (some columns convective), land and sea."""
+    at = 1.0e4 * np.sin(np.linspace(0.0, np.pi, lm + 1))
+    bt = np.linspace(1.0, 0.0, lm + 1) ** 2
+    sp = rng.uniform(9.5e4, 1.02e5, (im, jm))
+    z = np.cumsum(np.full((im, jm, lm), 12000.0 / lm), axis=-1)
+    t = 295.0 - 6.5e-3 * z + rng.uniform(-1.0, 1.0, (im, jm, lm))
+    q = 1e-2 * np.exp(-z / 2500.0) * rng.uniform(0.5, 1.0, (im, jm, lm))
+    pu = rng.uniform(-3e9, 3e9, (im + 1, jm, lm))
+    pv = rng.uniform(-1e9, 1e9, (im, jm + 1, lm))
+    surface = {"oro": rng.uniform(0.0, 2e4, (im, jm)), "lsm": rng.choice([0.0, 30.0, 100.0], (im, jm)),
+               "sr": rng.uniform(1e-4, 0.5, (im, jm)), "srols": rng.uniform(1e-3, 1.0, (im, jm)),
+               "u10m": rng.uniform(-8.0, 8.0, (im, jm)), "v10m": rng.uniform(-8.0, 8.0, (im, jm)),
+               "sshf": rng.uniform(-200.0, 80.0, (im, jm)), "slhf": rng.uniform(-150.0, 20.0, (im, jm)),
+               "ewss": rng.uniform(-0.2, 0.2, (im, jm)), "nsss": rng.uniform(-0.2, 0.2, (im, jm))}  # fmt: skip
+    dy = 180.0 / jm
+    lat = np.radians(-90.0 + dy * np.arange(jm + 1))
+    dxyp = np.radians(360.0 / im) * np.diff(np.sin(lat)) * 6.371e6**2
+    return sp * rng.uniform(0.998, 1.002, (im, jm)), sp, pu, pv, t, q, surface, at, bt, dxyp
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize(("shape", "lmax"), [((120, 90, 34), 34), ((90, 70, 34), 26), ((60, 45, 25), 25)])
+def test_calc_kzz_matches_oracle_at_size(dev, shape, lmax):
+    """Calc_Kzz over every column of a benchmark-sized region: dkg and pblh bitwise."""
+    from oracle import kernels as O
+
+    from pydyn_gb300 import kernels as K
+    from pydyn_gb300.device import DevArray
+
+    im, jm, lm = shape
+    rng = np.random.default_rng(zlib.crc32(repr(("kzz", shape)).encode()))
+    spm, sp, pu, pv, t, q, surface, at, bt, dxyp = _kzz_inputs(rng, im, jm, lm)
+    dx, dy = 360.0 / im, 180.0 / jm
+    want_dkg, want_pblh = O.calc_kzz(spm, sp, pu, pv, t, q, surface, at, bt, dxyp, lmax, dx, dy, -90.0)
+    d = {k: DevArray.from_host(dev, v) for k, v in {"spm": spm, "sp": sp, "pu": pu, "pv": pv, "t": t, "q": q,
+                                                    "at": at, "bt": bt, "dxyp": dxyp}.items()}  # fmt: skip
+    ds = {k: DevArray.from_host(dev, v) for k, v in surface.items()}
+    dkg = DevArray.zeros(dev, (0, im - 1), (0, jm - 1), (0, lmax - 1))
+    pblh = DevArray.zeros(dev, (0, im - 1), (0, jm - 1))
+    K.calc_kzz(d["spm"], d["sp"], d["pu"], d["pv"], d["t"], d["q"], ds, d["at"], d["bt"], d["dxyp"], lmax, dx, dy,
+               -90.0, dkg, pblh)  # fmt: skip
+    dev.sync()
+    assert_bitwise(dkg.host(), want_dkg, "kzz.dkg")
+    assert_bitwise(pblh.host(), want_pblh, "kzz.pblh")
+    assert (want_dkg[..., : lmax - 1] > 0.0).mean() > 0.5
+    for a in (*d.values(), *ds.values(), dkg, pblh):
+        a.free()
+
+
 @pytest.mark.gpu
 @pytest.mark.parametrize("shape", [(120, 90, 34, 1), (60, 45, 25, 2), (90, 70, 34, 1)])
 @pytest.mark.parametrize("cfl", [0.3, 1.6])
