@@ -90,7 +90,12 @@ __global__ void __launch_bounds__(SEARCH_THREADS) k_y_search(YArgs A) {
         s_halo = 0;
     }
     __syncthreads();
-    if (s_abort) return;
+    // every exit writes the layer's count, so that k_y_steps never reads one of an earlier call;
+    // a count above nmax leaves the layer untouched
+    if (s_abort) {
+        if (threadIdx.x == 0) A.nloop[l] = A.nmax + 1;
+        return;
+    }
 
     // region 1's polar outer faces must carry nothing (kernels.py:233-234); dynamvm does not check
     if (!A.mass_only && !A.held)
@@ -98,7 +103,10 @@ __global__ void __launch_bounds__(SEARCH_THREADS) k_y_search(YArgs A) {
             if (AT(A.bm, i, 0, l) != 0.0 || AT(A.bm, i, A.nc, l) != 0.0) s_halo = 1;
     __syncthreads();
     if (s_halo) {
-        if (threadIdx.x == 0) raise_status(A.ctl, GB_EHALO);
+        if (threadIdx.x == 0) {
+            A.nloop[l] = A.nmax + 1;
+            raise_status(A.ctl, GB_EHALO);
+        }
         return;
     }
 
