@@ -87,3 +87,21 @@ def test_tree_equals_the_reference(make):
     for r in ours.regions():
         assert (ours.zoomed[r] == theirs.zoomed[r]).all()
         assert (ours.edge[r] == theirs.edge[r]).all()
+
+
+def test_the_device_module_has_every_body_the_driver_runs():
+    """The driver runs st.lib's bodies: pydyn_gb300.zoom has each name of pydyn's zoom.host.BODIES
+    (the list pydyn's tests/test_gpu.py:64-70 checks its own device module against)."""
+    from pydyn_gb300 import zoom as gz
+
+    assert [n for n in gz.BODIES if not callable(getattr(gz, n, None))] == []
+
+
+@pytest.mark.skipif(not (REF / "pydyn").is_dir(), reason="the pydyn reference is not on this machine")
+def test_the_body_names_are_the_reference_s():
+    sys.path.insert(0, str(REF))
+    from pydyn.zoom import host
+
+    from pydyn_gb300 import zoom as gz
+
+    assert sorted(gz.BODIES) == sorted(host.BODIES)
