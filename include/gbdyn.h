@@ -112,6 +112,23 @@ int gb_advect_x(gb_ctx *ctx, const gb_view *m, const gb_view *rm, const gb_view 
 int gb_advect_y(gb_ctx *ctx, const gb_view *m, const gb_view *rm, const gb_view *rxm,
                 const gb_view *rym, const gb_view *rzm, const gb_view *bm, const gb_view *bm_full,
                 int bm_full_l0, int limits, int max_nloop, int32_t *nloop_out);
+/* gb_advect_y without an allocation.  No counterpart in the reference.  The same arguments and
+ * results as gb_advect_y; its per-layer sub-cycle counts are kept in a fixed device array of
+ * GB_NOALLOC_MAX_LEVELS int32 (4 KiB) compiled into the library, not in the context's scratch.
+ * For callers that must not allocate device memory while they run: a host whose own allocator
+ * has reserved the device's free memory, or a loop that cannot take the device-wide
+ * synchronisation an allocation may cause.  The call allocates nothing (no cudaMalloc, no
+ * library that allocates).  More than GB_NOALLOC_MAX_LEVELS levels return GB_EARG.  Nothing in
+ * the array must start at zero: each call writes every count it reads.  The array is one per
+ * device, shared by every context and stream: calls that can overlap (two streams, two host
+ * threads) race on it and must be serialised by the caller.  The first call on a device looks
+ * the array's address up (cudaGetSymbolAddress); make it before any stream capture begins.
+ * The current device must be the context's. */
+#define GB_NOALLOC_MAX_LEVELS 1024
+int gb_advect_y_noalloc(gb_ctx *ctx, const gb_view *m, const gb_view *rm, const gb_view *rxm,
+                        const gb_view *rym, const gb_view *rzm, const gb_view *bm,
+                        const gb_view *bm_full, int bm_full_l0, int limits, int max_nloop,
+                        int32_t *nloop_out);
 /* z: dynamw (kernels.py:295-346).  cm (im, jm, lm+1); cm is left bitwise as it was.
  * n_out: 1 int32 (optional). */
 int gb_advect_z(gb_ctx *ctx, const gb_view *m, const gb_view *rm, const gb_view *rxm,

@@ -63,6 +63,7 @@ SIGNATURES = {
     "gb_interp": (_I, [_VP, _P, _P, _P, _VP]),
     "gb_advect_x": (_I, [_VP, _P, _P, _P, _P, _P, _P, _VP, _I, _I, _I, _I, _I, _VP, _VP]),
     "gb_advect_y": (_I, [_VP, _P, _P, _P, _P, _P, _P, _P, _I, _I, _I, _VP]),
+    "gb_advect_y_noalloc": (_I, [_VP, _P, _P, _P, _P, _P, _P, _P, _I, _I, _I, _VP]),
     "gb_advect_z": (_I, [_VP, _P, _P, _P, _P, _P, _P, _I, _I, _VP]),
     "gb_advect_z_scope": (_I, [_VP, _P, _P, _P, _P, _P, _P, _I, _I, _I, _I, _I, _I]),
     "gb_cfl_x": (_I, [_VP, _P, _P, _VP, _I, _I, _I, _I]),

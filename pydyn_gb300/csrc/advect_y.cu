@@ -15,6 +15,8 @@
 // (subcycles, _trial), zoom/advect.py:201-226 (_dynamv_region1, _rescale_layer_halo),
 // zoom/advect.py:348-412 (_dynamv_child), cfl.py:170-183 (dynamvm) and zoom/check_cfl.py:162-193
 // (_dynamvm_child).
+#include <atomic>
+
 #include "gb_common.cuh"
 
 namespace {
@@ -270,9 +272,9 @@ __global__ void __launch_bounds__(STEP_WARPS * 32) k_y_steps(YArgs A) {
     for (int k = kf0 + lane; k <= kf1; k += GB_WARP) BF(A, i, k, l) = b_s[k] * (double)nloop;
 }
 
-int launch_y(gb_ctx *ctx, YArgs &A) {
+int launch_y(gb_ctx *ctx, YArgs &A, int32_t *scratch = nullptr) {
     A.ncell = A.nc + 2;
-    A.nloop = gb_scratch_i(ctx, A.nl);
+    A.nloop = scratch ? scratch : gb_scratch_i(ctx, A.nl);
     if (!A.nloop) {
         gb_set_error("gb_advect_y: too many levels for the scratch");
         return GB_EARG;
@@ -339,6 +341,59 @@ extern "C" int gb_advect_y(gb_ctx *ctx, const gb_view *m, const gb_view *rm, con
     A.nloop_out = nloop_out;
     A.ctl = ctx->ctl;
     return launch_y(ctx, A);
+}
+
+// ------------------------------------------------------------------ gb_advect_y_noalloc
+// The per-layer sub-cycle counts live in this array, compiled into the library, instead of in
+// the context's scratch.  Nothing in it has to start at zero: the search kernel writes the count
+// of every layer of a call (on every exit) before the steps kernel of that call reads it.
+namespace {
+__device__ __align__(256) int32_t g_y_nloop_static[GB_NOALLOC_MAX_LEVELS];
+
+constexpr int MAX_DEVICES = 64;
+std::atomic<int32_t *> g_y_nloop_addr[MAX_DEVICES];
+
+// the array's device address on the current device, looked up on the first call there
+int y_static_scratch(gb_ctx *ctx, int32_t **out) {
+    int cur = -1;
+    GB_CHECK_CUDA(cudaGetDevice(&cur));
+    if (cur != ctx->device || cur < 0 || cur >= MAX_DEVICES) {
+        gb_set_error("gb_advect_y_noalloc: the current device is not the context's (or above 63)");
+        return GB_EARG;
+    }
+    int32_t *p = g_y_nloop_addr[cur].load(std::memory_order_acquire);
+    if (!p) {
+        void *addr = nullptr;
+        GB_CHECK_CUDA(cudaGetSymbolAddress(&addr, g_y_nloop_static));
+        p = static_cast<int32_t *>(addr);
+        g_y_nloop_addr[cur].store(p, std::memory_order_release);
+    }
+    *out = p;
+    return GB_OK;
+}
+}  // namespace
+
+extern "C" int gb_advect_y_noalloc(gb_ctx *ctx, const gb_view *m, const gb_view *rm, const gb_view *rxm,
+                                   const gb_view *rym, const gb_view *rzm, const gb_view *bm,
+                                   const gb_view *bm_full, int bm_full_l0, int limits, int max_nloop,
+                                   int32_t *nloop_out) {
+    if (!ctx || !m || !rm || !rxm || !rym || !rzm || !bm) return GB_EARG;
+    if (m->n[2] < 1 || m->n[2] > GB_NOALLOC_MAX_LEVELS) {
+        gb_set_error("gb_advect_y_noalloc: " + std::to_string(m->n[2]) + " levels; this entry point takes 1 to " +
+                     std::to_string(GB_NOALLOC_MAX_LEVELS));
+        return GB_EARG;
+    }
+    int32_t *scratch = nullptr;
+    if (int rc = y_static_scratch(ctx, &scratch)) return rc;
+    YArgs A{};
+    const int32_t own[4] = {1, (int32_t)m->n[0], 1, (int32_t)m->n[1] + 1};
+    if (int rc = setup(A, m, bm, bm_full, bm_full_l0, own, 0)) return rc;
+    A.q[0] = dv(rm); A.q[1] = dv(rxm); A.q[2] = dv(rym); A.q[3] = dv(rzm);
+    A.nt = (int)rm->n[3];
+    A.limits = limits; A.nmax = max_nloop - 1;
+    A.nloop_out = nloop_out;
+    A.ctl = ctx->ctl;
+    return launch_y(ctx, A, scratch);
 }
 
 extern "C" int gb_advect_y_held(gb_ctx *ctx, const gb_view *m, const gb_view *rm, const gb_view *rxm,
