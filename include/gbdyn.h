@@ -91,6 +91,9 @@ int gb_box(gb_ctx *ctx, int op, const gb_view *dst, const gb_view *a, const gb_v
 /* dst = w[0] a + w[1] b, the weights read from device memory when the kernel runs, so that a
  * captured step replays with each step's weights (balance.py:63 time_interpolation). */
 int gb_interp(gb_ctx *ctx, const gb_view *dst, const gb_view *a, const gb_view *b, const double *w);
+/* counter[0] += delta on the stream (device int32): a step counter that a captured step
+ * advances each time it replays (convection's inverse cache epoch). */
+int gb_iadd(gb_ctx *ctx, int32_t *counter, int delta);
 /* dst = seqsum of src over `axis` (src's extent along it), accumulated in index order
  * (ops.seqsum, ops.py:235); dst has src's extents with that axis dropped (n = 1). */
 int gb_seqsum(gb_ctx *ctx, const gb_view *dst, const gb_view *src, int axis, double post_mul);
@@ -225,6 +228,38 @@ int gb_calc_kzz(gb_ctx *ctx, const gb_view *spm, const gb_view *sp, const gb_vie
                 const gb_view *pv, const gb_view *t, const gb_view *q, const gb_view *surface,
                 const double *at, const double *bt, const double *dxyp, int lmax_conv, double dx,
                 double dy, double ybeg, const gb_view *dkg, const gb_view *pblh);
+
+/* CH4 loss rates and decay (chem.py:114-170, loss_rates + decay) of every column of a region:
+ * temper, oh_3d (im, jm, lm); phlb (im, jm, lm+1) half levels; lat (jm) radians, device;
+ * strat_press (hPa), strat_oh, strat_cl, strat_od (jm, ns >= 2) zonal columns; pl_trop, cl_trop
+ * (im, jm, ntrop) the tropospheric Cl column (both NULL: not applied); soil (im, jm) or NULL;
+ * oh_factor (im) device, a per-longitude multiplier of oh_3d, or NULL.  Outputs loss
+ * (im, jm, lm, 4) and decay (im, jm, lm) = exp(-(sum of the rates) dt_sec), either NULL.
+ * Levels that are not strictly descending raise GB_ELEVELS (chem.py:47-49). */
+int gb_loss_rates(gb_ctx *ctx, const gb_view *temper, const gb_view *phlb, const double *lat,
+                  const gb_view *strat_press, const gb_view *strat_oh, const gb_view *strat_cl,
+                  const gb_view *strat_od, const gb_view *oh_3d, const gb_view *pl_trop,
+                  const gb_view *cl_trop, const gb_view *soil, const double *oh_factor,
+                  double oh_scale, double cl_scale, double o1d_scale, double soil_rate,
+                  double dt_sec, const gb_view *loss, const gb_view *decay);
+/* chemistry_region (zoom/physics.py:67-78 with chem.loss_rates, decay, apply_decay): the same
+ * inputs; on the listed columns cols (ncol, 2) int32 0-based (i, j), device, rm, rxm, rym, rzm
+ * (im, jm, lm, nt) of every tracer t whose bit t-1 is set in tracer_mask are multiplied by the
+ * cell's decay.  The other columns are left as they are (the reference's factor 1.0). */
+int gb_chemistry(gb_ctx *ctx, const gb_view *temper, const gb_view *phlb, const double *lat,
+                 const gb_view *strat_press, const gb_view *strat_oh, const gb_view *strat_cl,
+                 const gb_view *strat_od, const gb_view *oh_3d, const gb_view *pl_trop,
+                 const gb_view *cl_trop, const gb_view *soil, const double *oh_factor,
+                 double oh_scale, double cl_scale, double o1d_scale, double soil_rate,
+                 double dt_sec, const int32_t *cols, int ncol, uint32_t tracer_mask,
+                 const gb_view *rm, const gb_view *rxm, const gb_view *rym, const gb_view *rzm);
+/* sources_region (zoom/physics.py:55-64, emission_data do_add_2d): on the listed columns
+ * cols (ncol, 2) int32 device, rm(level, tracer) += x and rzm(level, tracer) -= x, level and
+ * tracer 1-based, x = (flux(i, j) area(j)) scale with area (jm) device, or x = flux(i, j) when
+ * area is NULL.  rm, rzm (im, jm, lm, nt); flux (im, jm). */
+int gb_sources(gb_ctx *ctx, const gb_view *rm, const gb_view *rzm, const gb_view *flux,
+               const double *area, double scale, int level, int tracer, const int32_t *cols,
+               int ncol);
 
 /* ------------------------------------------------------------------ mass fluxes, pressure
  * dynam0 (kernels.py:102-125, zoom/massflow.py:188-203): am = dt pu, bm = dt pv and cm from the

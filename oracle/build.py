@@ -1,9 +1,9 @@
 """ORACLE build recipe: compile oracle/src/*.c into oracle/_build/liboracle.so with gcc,
 -O2 and no floating-point contraction (-ffp-contract=off), so that every element is the
 IEEE result of the reference's own operation order on any host (x86-64 or aarch64).
-The transcendental functions come from the package's host math library (libgbmath.so), the
-same library the reference is pointed at through its pydyn.ops.use_libm hook when the golden
-fixtures are made."""
+The transcendental functions are the package's gbmath.h (compiled in from its source), the
+functions the reference is pointed at through its pydyn.ops.use_libm hook (as libgbmath.so)
+when the golden fixtures are made."""
 
 import subprocess
 from pathlib import Path
@@ -18,7 +18,7 @@ CFLAGS = ["-O2", "-fPIC", "-ffp-contract=off", "-fno-fast-math", "-std=c11", "-W
 def build():
     OUT.mkdir(exist_ok=True)
     srcs = sorted(SRC.glob("*.c"))
-    heads = sorted(SRC.glob("*.h"))
+    heads = [*sorted(SRC.glob("*.h")), HERE.parent / "pydyn_gb300" / "csrc" / "gbmath.h"]
     if LIB.exists() and all(s.stat().st_mtime <= LIB.stat().st_mtime for s in [*srcs, *heads]):
         return LIB
     cmd = ["gcc", *CFLAGS, "-shared", "-o", str(LIB), *map(str, srcs), "-lm"]

@@ -25,14 +25,19 @@ def digest(st):
 
 
 class OracleRun:
-    def __init__(self, config, lm, seed, nt=1, umax=40.0, physics=None):
+    def __init__(self, config, lm, seed, nt=1, umax=40.0, physics=False, lmax=None):
         self.zoom, self.met, fields = synth.case(config, lm, seed, nt, umax=umax)
         self.st, self.cst = HostState(self.zoom, nt), HostState(self.zoom, nt)
         self.st.load(fields)
         for r in self.zoom.regions():
             self.cst[r]["dxyp"].data[...] = fields[r]["dxyp"]
         self.meteo = {r: [self.met.fluxes(r, k) for k in (0, 1)] for r in self.zoom.regions()}
-        self.physics = physics
+        self.physics = None
+        if physics:
+            from .physics import OraclePhysics
+
+            self.physics = OraclePhysics(self.zoom, self.met, seed, lm if lmax is None else lmax)
+            self.physics.init(self.st)
         self.t = 0.0
 
     def interpolate(self, st, t):
@@ -52,7 +57,7 @@ class OracleRun:
         for k in range(n):
             self.interpolate(st, t0 + k * ndyn + ndyn / 2.0)
             D.setup_massflow(zoom, st, ndyn)
-            conv, kw = (None, {}) if self.physics is None else self.physics(self, ndyn)
+            conv, kw = (None, {}) if self.physics is None else self.physics.step(st, t0 + k * ndyn, ndyn)
             D.step(zoom, st, conv, ndyn, limits=True, **kw)
         self.t = t0 + nread
         return ndyn, n

@@ -43,6 +43,7 @@ def lib():
         L.or_advect_x_held.argtypes = [P, P, P, P, P, P, I, I, I]
         D, VP = ctypes.c_double, ctypes.c_void_p
         L.or_calc_kzz.argtypes = [P, P, P, P, P, P, P, VP, VP, VP, I, D, D, D, P, P]
+        L.or_loss_rates.argtypes = [P, P, VP, P, P, P, P, P, P, P, P, VP, D, D, D, D, D, P, P]
         L.or_convec.argtypes = [P, P, P, P, P, P, P, P, P, P, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int64,
                                 ctypes.c_int64, ctypes.c_void_p, I, ctypes.c_double, I]
         L.or_advect_y_held.argtypes = [P, P, P, P, P, P, P, I, I, I, I]
@@ -171,6 +172,28 @@ def calc_kzz(spm, sp, pu, pv, t, q, surface, at, bt, dxyp, lmax_conv, dx=6.0, dy
     lib().or_calc_kzz(*map(_ref, map(ov, (spm, sp, pu, pv, t, q))), surf, *(a.ctypes.data for a in arrs),
                       int(lmax_conv), float(dx), float(dy), float(ybeg), _ref(ov(dkg)), _ref(ov(pblh)))  # fmt: skip
     return dkg, pblh
+
+
+def loss_rates(temper, phlb, lat, strat_press, strat_oh, strat_cl, strat_od, oh_3d, pl_trop=None, cl_trop=None,
+               soil=None, oh_scale=1.0, cl_scale=1.0, o1d_scale=1.0, soil_rate=0.0, dt=None, oh_factor=None):
+    """chem.loss_rates (chem.py:114-150) and, with dt, chem.decay (:168-170): (loss (im, jm, lm, 4),
+    decay (im, jm, lm) or None).  oh_factor (im): a per-longitude multiplier of oh_3d, or None.
+    Raises ValueError for levels that are not strictly descending (chem.py:47-49)."""
+    im, jm, lm = temper.shape
+    loss = np.zeros((im, jm, lm, 4))
+    decay = None if dt is None else np.zeros((im, jm, lm))
+    f64 = [None if a is None else np.asarray(a, dtype=np.float64) for a in (lat, oh_factor)]
+    lat_c = np.ascontiguousarray(f64[0])
+    fac = None if f64[1] is None else np.ascontiguousarray(f64[1])
+    arrs = [None if a is None else np.asarray(a, dtype=np.float64)
+            for a in (temper, phlb, None, strat_press, strat_oh, strat_cl, strat_od, oh_3d, pl_trop, cl_trop, soil)]
+    views = [ov(a) for a in arrs]  # arrs keeps every converted array alive through the call
+    rc = lib().or_loss_rates(_ref(views[0]), _ref(views[1]), lat_c.ctypes.data, *map(_ref, views[3:]), _ptr(fac),
+                             float(oh_scale), float(cl_scale), float(o1d_scale), float(soil_rate),
+                             float(dt if dt is not None else 0.0), _ref(ov(loss)), _ref(ov(decay)))  # fmt: skip
+    if rc:
+        raise ValueError("rebin: levels not strictly descending")
+    return loss, decay
 
 
 def fluxes_from_meteo(pu, pv, bt, dt, am, bm, cm):

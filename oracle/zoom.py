@@ -332,3 +332,39 @@ def _dynamvm_child(zoom, st, region, is_, ie, ls, le, max_nloop):
     X.uncompress_yedges(zoom, st, region, is_, ie, ls, le, tracers=False)
     X.mix_edges(zoom, st, region, tracers=False)
     return True
+
+
+# ------------------------------------------------------------------ physics (zoom/physics.py)
+def convec_region(zoom, st, region, conv, ndyn, inverse="crout"):
+    """kernels.convec on the owned columns, dt = ndyn / (2 tref) (zoom/physics.py:33-52)."""
+    if conv is None or conv["lmax"] == 0:
+        return
+    cols = np.argwhere(zoom.owned(region)).astype(np.int32)
+    if len(cols) == 0:
+        return
+    dt = ndyn / (2.0 * zoom.g(region).tref)
+    O.convec(*_interior(st, region), conv["entu"], conv["detu"], conv["entd"], conv["detd"], conv["cloud_top"],
+             conv["cloud_lfs"], conv["dkg"], dt, conv["lmax"], cols=cols)  # fmt: skip
+
+
+def sources_region(zoom, st, region, injections):
+    """do_add_2d on the owned cells (zoom/physics.py:55-64)."""
+    g, f = zoom.g(region), st[region]
+    own = zoom.owned(region)
+    for x, level, tracer in injections:
+        rm = f["rm"][1 : g.im, 1 : g.jm, level, tracer]
+        rzm = f["rzm"][1 : g.im, 1 : g.jm, level, tracer]
+        rm[own] = rm[own] + x[own]
+        rzm[own] = rzm[own] - x[own]
+
+
+def chemistry_region(zoom, st, region, decay, tracers):
+    """The scope's decay on the owned cells, factor 1.0 elsewhere (zoom/physics.py:67-78)."""
+    g, f = zoom.g(region), st[region]
+    factor = np.ones((g.im, g.jm, zoom.lm))
+    factor[zoom.scope(region)] = decay
+    factor[~zoom.owned(region)] = 1.0
+    for t in tracers:
+        for name in TRACERS:
+            q = f[name][1 : g.im, 1 : g.jm, 1 : zoom.lm, t]
+            q[...] = q * factor

@@ -61,6 +61,7 @@ SIGNATURES = {
     "gb_box": (_I, [_VP, _I, _P, _P, _P, _D, _D]),
     "gb_seqsum": (_I, [_VP, _P, _P, _I, _D]),
     "gb_interp": (_I, [_VP, _P, _P, _P, _VP]),
+    "gb_iadd": (_I, [_VP, _VP, _I]),
     "gb_advect_x": (_I, [_VP, _P, _P, _P, _P, _P, _P, _VP, _I, _I, _I, _I, _I, _VP, _VP]),
     "gb_advect_y": (_I, [_VP, _P, _P, _P, _P, _P, _P, _P, _I, _I, _I, _VP]),
     "gb_advect_y_noalloc": (_I, [_VP, _P, _P, _P, _P, _P, _P, _P, _I, _I, _I, _VP]),
@@ -84,6 +85,10 @@ SIGNATURES = {
     "gb_convec": (_I, [_VP, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P, _VP, _VP, ctypes.c_int64, ctypes.c_int64, _VP, _I,
                        _D, _I, _VP, _VP, _VP, _VP]),
     "gb_calc_kzz": (_I, [_VP, _P, _P, _P, _P, _P, _P, _P, _VP, _VP, _VP, _I, _D, _D, _D, _P, _P]),
+    "gb_loss_rates": (_I, [_VP, _P, _P, _VP, _P, _P, _P, _P, _P, _P, _P, _P, _VP, _D, _D, _D, _D, _D, _P, _P]),
+    "gb_chemistry": (_I, [_VP, _P, _P, _VP, _P, _P, _P, _P, _P, _P, _P, _P, _VP, _D, _D, _D, _D, _D, _VP, _I,
+                          ctypes.c_uint32, _P, _P, _P, _P]),
+    "gb_sources": (_I, [_VP, _P, _P, _P, _VP, _D, _I, _I, _VP, _I]),
     "gb_math_eval":(_I, [_VP, _I, _VP, _VP, _VP, ctypes.c_int64]),
     "gb_fluxes_from_meteo": (_I, [_VP, _P, _P, _VP, _D, _P, _P, _P]),
     "gb_m2phlb": (_I, [_VP, _P, _P, _P, _VP, _VP, _VP, _I, _I, _I, _VP]),
@@ -117,7 +122,7 @@ def check(rc, what=""):
         return
     if rc & GB_ECFL:
         raise CFLError(f"{what}: {last_error()}")
-    if rc & GB_EHALO:
+    if rc & (GB_EHALO | GB_ELEVELS):
         raise ValueError(f"{what}: {last_error()}")
     raise DeviceError(f"{what} failed ({rc}): {last_error()}")
 

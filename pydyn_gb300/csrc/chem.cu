@@ -1,0 +1,274 @@
+// The CH4 `c` and `s` operators on a region's columns.
+//
+// k_chem: one warp per column.  The lanes stage the column's edges in shared memory -- the
+// zonal loss-rate columns' edges (strat_edges), the tropospheric Cl column's, the model's half
+// levels -- check each is strictly descending (warp vote), then take the levels: the four loss
+// rates, decay = exp(-(((L1 + L2) + L3) + L4) dt), and either the rates and decay written out
+// (gb_loss_rates, every column of the region) or the decay applied to the listed tracers' mass
+// and slopes (gb_chemistry, the columns a region owns).  A rebinned layer sums, in input order
+// from +0.0, data * thickness over the input layers first .. last-1 whose overlap is positive;
+// the terms the reference adds for the others are +0.0, which leave such a sum unchanged.
+// exp / pow / cos are gbmath.h.
+//
+// k_sources: one thread per owned column: rm(level) += x, rzm(level) -= x.
+//
+// Reference: pydyn chem.py:59-178 (rebin_many, strat_edges, tropopause, _column, loss_rates,
+// decay, apply_decay), zoom/physics.py:55-78 (sources_region, chemistry_region).
+#include "gb_common.cuh"
+#include "gbmath.h"
+
+namespace {
+
+constexpr int WARPS = 4;
+
+struct CArgs {
+    DV temper, phlb, soil, oh3d, pltrop, cltrop, sp, soh, scl, sod;
+    const double *lat, *oh_factor;
+    double oh_scale, cl_scale, o1d_scale, soil_rate, dt;
+    int im, jm, lm, ns, ntrop, has_trop, has_soil;
+    const int32_t *cols;  // (ncol, 2) 0-based (i, j), or null: every column
+    int64_t ncol;
+    DV loss, decay;             // gb_loss_rates outputs (either may be absent)
+    DV q[4];                    // gb_chemistry: rm, rxm, rym, rzm
+    uint32_t tracer_mask;       // gb_chemistry: bit t-1 for tracer t
+    int apply;
+    gb_ctl *ctl;
+};
+
+__device__ __forceinline__ double &E2(const DV &v, int64_t a, int64_t b) { return v.p[a * v.s0 + b * v.s1]; }
+__device__ __forceinline__ double &E3(const DV &v, int64_t a, int64_t b, int64_t c) {
+    return v.p[a * v.s0 + b * v.s1 + c * v.s2];
+}
+__device__ __forceinline__ double &E4(const DV &v, int64_t a, int64_t b, int64_t c, int64_t d) {
+    return v.p[a * v.s0 + b * v.s1 + c * v.s2 + d * v.s3];
+}
+
+// rebin_levels(ip_mix) of one output layer [top, bot] from the edges ip[0..nip] (shared memory)
+__device__ double rebin_layer(const double *ip, int nip, const double *data, int64_t stride, double bot,
+                              double top) {
+    int first = 0, last = 0;
+    for (int k = 0; k < nip; ++k) {
+        first += ip[k + 1] >= bot;
+        last += ip[k] > top;
+    }
+    double overlap = 0.0;
+    for (int k = first; k < last; ++k) {
+        const double thickness = np_min(bot, ip[k]) - np_max(top, ip[k + 1]);
+        if (thickness > 0.0) overlap = overlap + data[k * stride] * thickness;
+    }
+    const double width = bot - top;
+    return width > 0.0 ? overlap / width : overlap;
+}
+
+__global__ void __launch_bounds__(WARPS * 32) k_chem(CArgs A) {
+    extern __shared__ double smem[];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int64_t c = (int64_t)blockIdx.x * WARPS + warp;
+    if (c >= A.ncol) return;
+    int i, j;
+    if (A.cols) {
+        i = A.cols[2 * c];
+        j = A.cols[2 * c + 1];
+    } else {
+        i = (int)(c / A.jm);
+        j = (int)(c % A.jm);
+    }
+    const int ns = A.ns, nt = A.ntrop, lm = A.lm;
+    double *edges = smem + (size_t)warp * ((ns + 1) + (nt + 1) + (lm + 1));
+    double *tedges = edges + (ns + 1);
+    double *ph = tedges + (nt + 1);
+
+    // strat_edges (chem.py:91-98): midpoints, a half layer below the first, 0 above the last, x100
+    for (int k = lane; k <= ns; k += 32) {
+        double e;
+        if (k == 0) {
+            const double p0 = E2(A.sp, j, 0), p1 = E2(A.sp, j, 1);
+            e = p0 + 0.5 * (p0 - p1);
+        } else if (k < ns) {
+            e = (E2(A.sp, j, k - 1) + E2(A.sp, j, k)) / 2.0;
+        } else {
+            e = 0.0;
+        }
+        edges[k] = e * 100.0;
+    }
+    if (A.has_trop) {
+        for (int k = lane; k < nt; k += 32) tedges[k] = E3(A.pltrop, i, j, k);
+        if (lane == 0) tedges[nt] = 0.0;
+    }
+    for (int k = lane; k <= lm; k += 32) ph[k] = E3(A.phlb, i, j, k);
+    __syncwarp();
+    bool ok = true;
+    for (int k = lane; k < ns; k += 32) ok = ok && (edges[k + 1] - edges[k] < 0.0);
+    for (int k = lane; k < lm; k += 32) ok = ok && (ph[k + 1] - ph[k] < 0.0);
+    if (A.has_trop)
+        for (int k = lane; k < nt; k += 32) ok = ok && (tedges[k + 1] - tedges[k] < 0.0);
+    if (!__all_sync(FULL_MASK, ok)) {
+        if (lane == 0) raise_status(A.ctl, GB_ELEVELS);
+        return;
+    }
+    const double cl = gbm_cos(A.lat[j]);
+    const double trop = 30000.0 - 21500.0 * (cl * cl);
+    const double *doh = &E2(A.soh, j, 0), *dcl = &E2(A.scl, j, 0), *dod = &E2(A.sod, j, 0);
+
+    for (int l = lane; l < lm; l += 32) {
+        const double bot = ph[l], top = ph[l + 1];
+        const bool below = bot > edges[0];
+        const double s_oh = below ? doh[0] : rebin_layer(edges, ns, doh, A.soh.s1, bot, top);
+        const double s_cl = below ? dcl[0] : rebin_layer(edges, ns, dcl, A.scl.s1, bot, top);
+        const double s_od = below ? dod[0] : rebin_layer(edges, ns, dod, A.sod.s1, bot, top);
+        const double T = E3(A.temper, i, j, l);
+        double trop_cl = 0.0;
+        if (A.has_trop) {
+            const double *dtr = &E3(A.cltrop, i, j, 0);
+            const double v = bot > tedges[0] ? dtr[0] : rebin_layer(tedges, nt, dtr, A.cltrop.s2, bot, top);
+            const double krate = (2.36e-12 * gbm_pow(T / 298.0, 1.37)) * gbm_exp(-939.0 / T);
+            trop_cl = (v * krate) * A.cl_scale;
+        }
+        double oh = E3(A.oh3d, i, j, l);
+        if (A.oh_factor) oh = oh * A.oh_factor[i];
+        const double krate_oh = 2.45e-12 * gbm_exp(-1775.0 / T);
+        const double spiv = (krate_oh * oh) * A.oh_scale;
+        const bool strat = bot < trop;
+        const double L0 = strat ? s_oh : spiv;
+        const double L1 = strat ? s_cl : s_cl + trop_cl;
+        const double L2 = s_od * A.o1d_scale;
+        const double L3 = (A.has_soil && l == 0) ? -(A.soil_rate * E2(A.soil, i, j)) : 0.0;
+        const double d = gbm_exp(-((((L0 + L1) + L2) + L3) * A.dt));
+        if (A.apply) {
+            for (uint32_t mask = A.tracer_mask; mask; mask &= mask - 1) {
+                const int t = __ffs(mask) - 1;
+                for (int w = 0; w < 4; ++w) {
+                    double &x = E4(A.q[w], i, j, l, t);
+                    x = x * d;
+                }
+            }
+        } else {
+            if (A.loss.p) {
+                E4(A.loss, i, j, l, 0) = L0;
+                E4(A.loss, i, j, l, 1) = L1;
+                E4(A.loss, i, j, l, 2) = L2;
+                E4(A.loss, i, j, l, 3) = L3;
+            }
+            if (A.decay.p) E3(A.decay, i, j, l) = d;
+        }
+    }
+}
+
+struct SArgs {
+    DV rm, rzm, flux;
+    const double *area;
+    double scale;
+    int level, tracer;
+    const int32_t *cols;
+    int64_t ncol;
+};
+
+__global__ void k_sources(SArgs A) {
+    const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= A.ncol) return;
+    const int i = A.cols[2 * c], j = A.cols[2 * c + 1];
+    double x = E2(A.flux, i, j);
+    if (A.area) x = (x * A.area[j]) * A.scale;
+    double &rm = E4(A.rm, i, j, A.level, A.tracer);
+    double &rz = E4(A.rzm, i, j, A.level, A.tracer);
+    rm = rm + x;
+    rz = rz - x;
+}
+
+int setup_chem(CArgs &A, const gb_view *temper, const gb_view *phlb, const double *lat, const gb_view *strat_press,
+               const gb_view *strat_oh, const gb_view *strat_cl, const gb_view *strat_od, const gb_view *oh_3d,
+               const gb_view *pl_trop, const gb_view *cl_trop, const gb_view *soil, const double *oh_factor,
+               double oh_scale, double cl_scale, double o1d_scale, double soil_rate, double dt) {
+    if (!temper || !phlb || !lat || !strat_press || !strat_oh || !strat_cl || !strat_od || !oh_3d) return GB_EARG;
+    if ((pl_trop == nullptr) != (cl_trop == nullptr)) {
+        gb_set_error("chemistry: pl_trop and cl_trop go together");
+        return GB_EARG;
+    }
+    A.temper = dv(temper); A.phlb = dv(phlb); A.oh3d = dv(oh_3d);
+    A.sp = dv(strat_press); A.soh = dv(strat_oh); A.scl = dv(strat_cl); A.sod = dv(strat_od);
+    A.im = (int)temper->n[0]; A.jm = (int)temper->n[1]; A.lm = (int)temper->n[2];
+    A.ns = (int)strat_press->n[1];
+    if (A.ns < 2 || phlb->n[2] != A.lm + 1) {
+        gb_set_error("chemistry: need >= 2 zonal levels and phlb of lm+1 half levels");
+        return GB_EARG;
+    }
+    A.has_trop = pl_trop != nullptr;
+    if (A.has_trop) {
+        A.pltrop = dv(pl_trop); A.cltrop = dv(cl_trop);
+        A.ntrop = (int)pl_trop->n[2];
+    }
+    A.has_soil = soil != nullptr;
+    if (A.has_soil) A.soil = dv(soil);
+    A.lat = lat; A.oh_factor = oh_factor;
+    A.oh_scale = oh_scale; A.cl_scale = cl_scale; A.o1d_scale = o1d_scale; A.soil_rate = soil_rate; A.dt = dt;
+    return GB_OK;
+}
+
+int launch_chem(gb_ctx *ctx, CArgs &A) {
+    A.ctl = ctx->ctl;
+    if (A.ncol == 0) return GB_OK;
+    const size_t smem = (size_t)WARPS * ((A.ns + 1) + (A.ntrop + 1) + (A.lm + 1)) * sizeof(double);
+    GB_CHECK_CUDA(cudaFuncSetAttribute(k_chem, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    k_chem<<<(unsigned)((A.ncol + WARPS - 1) / WARPS), WARPS * 32, smem, ctx->stream>>>(A);
+    return gb_after_launch(ctx, A.apply ? "chemistry" : "loss_rates");
+}
+
+}  // namespace
+
+extern "C" int gb_loss_rates(gb_ctx *ctx, const gb_view *temper, const gb_view *phlb, const double *lat,
+                             const gb_view *strat_press, const gb_view *strat_oh, const gb_view *strat_cl,
+                             const gb_view *strat_od, const gb_view *oh_3d, const gb_view *pl_trop,
+                             const gb_view *cl_trop, const gb_view *soil, const double *oh_factor, double oh_scale,
+                             double cl_scale, double o1d_scale, double soil_rate, double dt_sec,
+                             const gb_view *loss, const gb_view *decay) {
+    if (!ctx) return GB_EARG;
+    CArgs A{};
+    if (int rc = setup_chem(A, temper, phlb, lat, strat_press, strat_oh, strat_cl, strat_od, oh_3d, pl_trop, cl_trop,
+                            soil, oh_factor, oh_scale, cl_scale, o1d_scale, soil_rate, dt_sec))
+        return rc;
+    A.loss = loss ? dv(loss) : DV{};
+    A.decay = decay ? dv(decay) : DV{};
+    A.ncol = (int64_t)A.im * A.jm;
+    return launch_chem(ctx, A);
+}
+
+extern "C" int gb_chemistry(gb_ctx *ctx, const gb_view *temper, const gb_view *phlb, const double *lat,
+                            const gb_view *strat_press, const gb_view *strat_oh, const gb_view *strat_cl,
+                            const gb_view *strat_od, const gb_view *oh_3d, const gb_view *pl_trop,
+                            const gb_view *cl_trop, const gb_view *soil, const double *oh_factor, double oh_scale,
+                            double cl_scale, double o1d_scale, double soil_rate, double dt_sec, const int32_t *cols,
+                            int ncol, uint32_t tracer_mask, const gb_view *rm, const gb_view *rxm,
+                            const gb_view *rym, const gb_view *rzm) {
+    if (!ctx || !rm || !rxm || !rym || !rzm || (ncol > 0 && !cols) || ncol < 0) return GB_EARG;
+    CArgs A{};
+    if (int rc = setup_chem(A, temper, phlb, lat, strat_press, strat_oh, strat_cl, strat_od, oh_3d, pl_trop, cl_trop,
+                            soil, oh_factor, oh_scale, cl_scale, o1d_scale, soil_rate, dt_sec))
+        return rc;
+    if (rm->n[3] < 32 && (tracer_mask >> rm->n[3]) != 0) {
+        gb_set_error("gb_chemistry: a tracer of the mask is beyond the arrays' nt");
+        return GB_EARG;
+    }
+    A.q[0] = dv(rm); A.q[1] = dv(rxm); A.q[2] = dv(rym); A.q[3] = dv(rzm);
+    A.tracer_mask = tracer_mask;
+    A.apply = 1;
+    A.cols = cols;
+    A.ncol = ncol;
+    return launch_chem(ctx, A);
+}
+
+extern "C" int gb_sources(gb_ctx *ctx, const gb_view *rm, const gb_view *rzm, const gb_view *flux,
+                          const double *area, double scale, int level, int tracer, const int32_t *cols, int ncol) {
+    if (!ctx || !rm || !rzm || !flux || (ncol > 0 && !cols) || ncol < 0) return GB_EARG;
+    if (level < 1 || level > rm->n[2] || tracer < 1 || tracer > rm->n[3]) {
+        gb_set_error("gb_sources: level or tracer (1-based) outside the arrays");
+        return GB_EARG;
+    }
+    if (ncol == 0) return GB_OK;
+    SArgs A{};
+    A.rm = dv(rm); A.rzm = dv(rzm); A.flux = dv(flux);
+    A.area = area; A.scale = scale;
+    A.level = level - 1; A.tracer = tracer - 1;
+    A.cols = cols; A.ncol = ncol;
+    k_sources<<<(unsigned)((ncol + 127) / 128), 128, 0, ctx->stream>>>(A);
+    return gb_after_launch(ctx, "sources");
+}

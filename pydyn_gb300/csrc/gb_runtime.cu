@@ -295,6 +295,14 @@ __global__ void k_interp(DV d, DV a, DV b, const double *w, int64_t total) {
     }
 }
 
+__global__ void k_iadd(int32_t *p, int delta) { p[0] += delta; }
+
+extern "C" int gb_iadd(gb_ctx *ctx, int32_t *counter, int delta) {
+    if (!ctx || !counter) return GB_EARG;
+    k_iadd<<<1, 1, 0, ctx->stream>>>(counter, delta);
+    return gb_after_launch(ctx, "iadd");
+}
+
 extern "C" int gb_interp(gb_ctx *ctx, const gb_view *dst, const gb_view *a, const gb_view *b, const double *w) {
     if (!dst || !a || !b || !w) return GB_EARG;
     DV d = dv(dst);

@@ -36,8 +36,10 @@ def weights(t):
 class Forward:
     """A configuration's run on one device: the state, the Check_CFL copy, the meteo instants."""
 
-    def __init__(self, dev, config="glb6x4", lm=25, seed=0, nt=1, ndyn=3600, nread=3600, limits=True, physics=None,
-                 umax=40.0):  # fmt: skip
+    def __init__(self, dev, config="glb6x4", lm=25, seed=0, nt=1, ndyn=3600, nread=3600, limits=True, physics=False,
+                 umax=40.0, lmax=None):  # fmt: skip
+        """physics: with convection (Kzz folded in), emission and CH4 chemistry over lmax levels
+        (default lm), on the inputs of pydyn_gb300.synth.Physics; without, advection only."""
         self.dev = dev
         self.zoom, self.met, fields = synth.case(config, lm, seed, nt, umax=umax)
         self.st = ZoomState.from_host(dev, self.zoom, fields)
@@ -51,13 +53,30 @@ class Forward:
             pair = [self.met.fluxes(r, k) for k in (0, 1)]
             self.meteo[r] = [(DevArray.from_host(dev, pu), DevArray.from_host(dev, pv)) for pu, pv in pair]
         self.w = DevArray.zeros(dev, (0, 1))
-        self.physics = physics
+        self.physics = None
+        if physics:
+            from .physics import Physics
+
+            spec = synth.Physics(self.zoom, self.met, seed, lm if lmax is None else lmax)
+            self.physics = Physics(dev, self.zoom, spec, {r: self.st[r]["dxyp"] for r in self.zoom.regions()})
+            self.physics.init_state(self.st)
         self.graphs = {}
         self.last = {}
 
     # -------------------------------------------------------------- meteo
     def put_weights(self, t):
         self.w.upload(np.array(weights(t)))
+
+    def interp_into(self, dst, a, b):
+        """dst = w1 a + w2 b with the device-held weights of the step."""
+        _interp(dst, a, b, self.w)
+
+    def put_step_inputs(self, t0, ndyn):
+        """The step's time-dependent inputs into device memory: the meteo weights at its middle
+        and the physics' OH factors of its half steps."""
+        self.put_weights(t0 + ndyn / 2.0)
+        if self.physics is not None:
+            self.physics.put_factors(t0, ndyn)
 
     def interpolate(self, st):
         """pu, pv of every region from the meteo instants with the device-held weights."""
@@ -88,7 +107,7 @@ class Forward:
 
     def step(self, t0, ndyn):
         """One step from t0 (Forward._step): meteo at the middle, Setup_MassFlow, the sequence."""
-        self.put_weights(t0 + ndyn / 2.0)
+        self.put_step_inputs(t0, ndyn)
         self.enqueue_step(ndyn)
 
     def enqueue_step(self, ndyn):
@@ -147,7 +166,7 @@ class Forward:
                 self._enqueue_interval()
             self.graphs["interval"] = g
             return out
-        self.put_weights(t0 + self.nread / 2.0)
+        self.put_step_inputs(t0, self.nread)
         self.graphs["interval"].launch()
         if self.dev.cfl_failed():  # the speculation was wrong: back to the interval's start
             for (r, k), a in self._spec.items():
@@ -169,12 +188,14 @@ class Forward:
                 pv.free()
         for a in getattr(self, "_spec", {}).values():
             a.free()
+        if self.physics is not None:
+            self.physics.free()
         self.w.free()
 
     def enqueue_interval_async(self, t0):
         """The captured interval, launched without any host read (the benchmark's timed loop;
         the rehearsal flag is read once after the loop)."""
-        self.put_weights(t0 + self.nread / 2.0)
+        self.put_step_inputs(t0, self.nread)
         self.graphs["interval"].launch()
 
 

@@ -154,6 +154,49 @@ def calc_kzz(spm, sp, pu, pv, t, q, surface, at, bt, dxyp, lmax_conv, dx, dy, yb
             "calc_kzz")  # fmt: skip
 
 
+CHEM_FIELDS = ("strat_press", "strat_oh", "strat_cl", "strat_od", "oh_3d", "pl_trop", "cl_trop", "soil")
+
+
+def _chem_args(temper, phlb, lat, fields, oh_factor, oh_scale, cl_scale, o1d_scale, soil_rate, dt):
+    f = {k: fields.get(k) for k in CHEM_FIELDS}
+    return (*views(temper, phlb), lat.ptr, *views(*(f[k] for k in CHEM_FIELDS)),
+            None if oh_factor is None else oh_factor.ptr, float(oh_scale), float(cl_scale), float(o1d_scale),
+            float(soil_rate), float(dt))  # fmt: skip
+
+
+def loss_rates(temper, phlb, lat, fields, dt, loss=None, decay=None, oh_factor=None, oh_scale=1.0, cl_scale=1.0,
+               o1d_scale=1.0, soil_rate=0.0):
+    """chem.loss_rates and chem.decay (chem.py:114-170) of every column into loss (im, jm, lm, 4)
+    and decay (im, jm, lm).  fields: DevArrays by CHEM_FIELDS name (pl_trop / cl_trop and soil
+    optional, as the sinks are on); lat (jm) radians; oh_factor (im) multiplies oh_3d."""
+    L, h = _lib(temper)
+    N.check(L.gb_loss_rates(h, *_chem_args(temper, phlb, lat, fields, oh_factor, oh_scale, cl_scale, o1d_scale,
+                                           soil_rate, dt), *views(loss, decay)), "loss_rates")  # fmt: skip
+
+
+def chemistry(temper, phlb, lat, fields, dt, cols, tracers, rm, rxm, rym, rzm, oh_factor=None, oh_scale=1.0,
+              cl_scale=1.0, o1d_scale=1.0, soil_rate=0.0):
+    """chemistry_region (zoom/physics.py:67): the decay of each listed column's cells applied to
+    the mass and slopes of the (1-based) `tracers`."""
+    _tracer_strides(rm, rxm, rym, rzm)
+    mask = 0
+    for t in tracers:
+        mask |= 1 << (int(t) - 1)
+    L, h = _lib(temper)
+    N.check(L.gb_chemistry(h, *_chem_args(temper, phlb, lat, fields, oh_factor, oh_scale, cl_scale, o1d_scale,
+                                          soil_rate, dt), cols.ptr, cols.shape[0], mask,
+                           *views(rm, rxm, rym, rzm)), "chemistry")  # fmt: skip
+
+
+def sources(rm, rzm, flux, cols, level, tracer, area=None, scale=1.0):
+    """sources_region (zoom/physics.py:55): rm(level) += x, rzm(level) -= x on the listed columns,
+    x = (flux area) scale, or flux itself without area."""
+    _tracer_strides(rm, rzm)
+    L, h = _lib(rm)
+    N.check(L.gb_sources(h, *views(rm, rzm, flux), None if area is None else area.ptr, float(scale), int(level),
+                         int(tracer), cols.ptr, cols.shape[0]), "sources")  # fmt: skip
+
+
 def to_device(dev, arr, dtype=np.float64):
     """A DevArray copy of a host array (0-based bounds)."""
     return DevArray.from_host(dev, np.asarray(arr, dtype=dtype))

@@ -1,0 +1,206 @@
+"""The physics of a step on the device: Calc_Kzz per region at the step's start, and the `v`, `s`
+and `c` operators on the columns each region owns (pydyn zoom/physics.py:33-78, with
+diffusion.calc_kzz, chem.loss_rates / decay and the emission's do_add_2d), recomposed for a
+region tree as pydyn forward.py:411-451 runs them for one region:
+
+    Calc_Kzz     after Setup_MassFlow, on every region: spm the meteo surface pressure at the
+                 step's middle, sp the region's own at the step's start, pu / pv the step's
+    v            kernels.convec on the owned columns, dt = ndyn / (2 tref), dkg the step's; the
+                 inverse of each column is kept for the step's second `v` of the same air mass
+    s            flux x area x dt added to rm and taken from rzm at level 1, tracer 1
+    c            the loss rates and decay exp(-L dt) of each owned cell, applied to the CH4
+                 tracers' mass and slopes; OH carries a diurnal factor at the time of the
+                 region's half step (status // 6) -- put in device memory before each step
+
+Everything a step enqueues reads its time-dependent inputs (weights, OH factors, the step
+counter) from device memory, so one captured graph serves every step."""
+
+import numpy as np
+
+from . import _native as N
+from . import kernels as K
+from .device import DevArray
+from .state import TRACERS
+
+N_OPERATORS = 6
+LEVEL, TRACER, CH4_TRACERS = 1, 1, (1,)
+
+
+def _interior(st, r):
+    g, f, lm = st.zoom.g(r), st[r], st.zoom.lm
+    return [f["m"][1 : g.im, 1 : g.jm, 1:lm], *(f[q][1 : g.im, 1 : g.jm, 1:lm] for q in TRACERS)]
+
+
+class Physics:
+    """The device-resident physics inputs of a run (from a pydyn_gb300.synth.Physics) and the
+    bodies that use them."""
+
+    def __init__(self, dev, zoom, spec, dxyp):
+        """dxyp: {region: DevArray (jm)} the cell areas."""
+        self.dev, self.zoom, self.spec = dev, zoom, spec
+        self.lmax = spec.lmax
+        up = lambda a, dtype=np.float64: DevArray.from_host(dev, np.ascontiguousarray(a, dtype=dtype))  # noqa: E731
+        self.at, self.bt = up(zoom.at), up(zoom.bt)
+        self.epoch = DevArray.from_host(dev, np.zeros(1, dtype=np.int32))
+        self.r = {}
+        for r in zoom.regions():
+            g, R = zoom.g(r), spec.region[r]
+            own = zoom.owned(r)
+            cols = np.argwhere(own).astype(np.int32)
+            ncol = len(cols)
+            d = {
+                "conv": {k: up(v, np.int32 if k.startswith("cloud") else np.float64) for k, v in R["conv"].items()},
+                "t": up(R["kzz"]["t"]), "q": up(R["kzz"]["q"]),
+                "surface": [up(R["kzz"]["surface"][k]) for k in K.KZZ_SURFACE],
+                "spm": [up(s) for s in R["kzz"]["spm"]],
+                "spm_now": DevArray.zeros(dev, (0, g.im - 1), (0, g.jm - 1)),
+                "dkg": DevArray.zeros(dev, (0, g.im - 1), (0, g.jm - 1), (0, self.lmax - 1)),
+                "chem": {k: up(v) for k, v in R["chem"].items()},
+                "flux": up(R["flux"]),
+                "factors": DevArray.zeros(dev, (0, 2 * g.tref - 1), (0, g.im - 1)),
+                "cols": up(cols if ncol else np.zeros((0, 2)), np.int32),
+                "ncol": ncol,
+                "cache": (DevArray.zeros(dev, (0, max(ncol, 1) * self.lmax * self.lmax - 1)),
+                          DevArray.zeros(dev, (0, max(ncol, 1) * self.lmax - 1)),
+                          DevArray.from_host(dev, np.full(max(ncol, 1), -1, dtype=np.int32)), self.epoch),
+                "dxyp": dxyp[r],
+                "grid": ((g.xend - g.xbeg) / g.im, (g.yend - g.ybeg) / g.jm, float(g.ybeg)),
+            }  # fmt: skip
+            self.r[r] = d
+        self.ndyn = None
+
+    # -------------------------------------------------------------- host side, outside capture
+    def init_state(self, st):
+        """sp and phlb of every region from its initial air mass (m2phlb1 / m2phlb), so that the
+        first step's Calc_Kzz and chemistry see the pressures of the state they start from."""
+        for r in self.zoom.regions():
+            if r == 1:
+                st.lib.m2phlb1(self.zoom, st, 1)
+            else:
+                st.lib.m2phlb(self.zoom, st, r)
+
+    def put_factors(self, t0, ndyn):
+        """The OH factors of every region's half steps of the step from t0, into device memory
+        (stream-ordered: a step already enqueued still reads the previous ones)."""
+        for r, d in self.r.items():
+            d["factors"].upload(self.spec.factors(r, t0, ndyn))
+
+    # -------------------------------------------------------------- enqueued (capturable)
+    def prepare(self, fwd, ndyn):
+        """After Setup_MassFlow: the step counter, spm, Calc_Kzz of every region.  Returns the
+        driver's (conv, kwargs)."""
+        self.ndyn = ndyn
+        N.check(self.dev.L.gb_iadd(self.dev.h, self.epoch.ptr, 1), "gb_iadd")
+        st = fwd.st
+        for r, d in self.r.items():
+            g, f = self.zoom.g(r), st[r]
+            fwd.interp_into(d["spm_now"], d["spm"][0], d["spm"][1])
+            dx, dy, ybeg = d["grid"]
+            K.calc_kzz(d["spm_now"], f["sp"][1 : g.im, 1 : g.jm, 1], f["pu"], f["pv"], d["t"], d["q"],
+                       d["surface"], self.at, self.bt, d["dxyp"], self.lmax, dx, dy, ybeg, d["dkg"])  # fmt: skip
+        conv = {r: self for r in self.r}
+        return conv, {"sources": self.sources, "chemistry": self.chemistry}
+
+    def convec_region(self, zoom, st, region, ndyn, inverse="crout"):
+        if inverse != "crout":
+            raise NotImplementedError("convec_region: the device solves with the Crout inverse only")
+        d = self.r[region]
+        if d["ncol"] == 0:
+            return
+        c = d["conv"]
+        dt = ndyn / (2.0 * zoom.g(region).tref)
+        K.convec(*_interior(st, region), c["entu"], c["detu"], c["entd"], c["detd"], d["dkg"], c["cloud_top"],
+                 c["cloud_lfs"], d["cols"], dt, self.lmax, cache=d["cache"])  # fmt: skip
+
+    def sources(self, zoom, st, region):
+        d = self.r[region]
+        if d["ncol"] == 0:
+            return
+        g, f = zoom.g(region), st[region]
+        rm = f["rm"][1 : g.im, 1 : g.jm, 1 : zoom.lm]
+        rzm = f["rzm"][1 : g.im, 1 : g.jm, 1 : zoom.lm]
+        K.sources(rm, rzm, d["flux"], d["cols"], LEVEL, TRACER, area=d["dxyp"],
+                  scale=self.spec.half_step(region, self.ndyn))  # fmt: skip
+
+    def chemistry(self, zoom, st, region):
+        d = self.r[region]
+        if d["ncol"] == 0:
+            return
+        g, f = zoom.g(region), st[region]
+        h = zoom.status[region] // N_OPERATORS
+        c = d["chem"]
+        K.chemistry(d["t"], f["phlb"][1 : g.im, 1 : g.jm, 1 : zoom.lm + 1], c["lat"], c, self.spec.half_step(region,
+                    self.ndyn), d["cols"], CH4_TRACERS, *_interior(st, region)[1:], oh_factor=d["factors"][h],
+                    **self.spec.settings)  # fmt: skip
+
+    def free(self):
+        seen = set()
+
+        def rel(a):
+            if isinstance(a, DevArray) and id(a) not in seen:
+                seen.add(id(a))
+                a.free()
+
+        for d in self.r.values():
+            for k, v in d.items():
+                if k == "dxyp":  # the state's
+                    continue
+                for a in v.values() if isinstance(v, dict) else v if isinstance(v, (list, tuple)) else [v]:
+                    rel(a)
+        for a in (self.at, self.bt, self.epoch):
+            rel(a)
+
+
+def convec_region(zoom, st, region, conv, ndyn, inverse="crout"):
+    """The `v` body (zoom/physics.py:33): conv is the run's Physics."""
+    conv.convec_region(zoom, st, region, ndyn, inverse)
+
+
+def sources_region(zoom, st, region, injections):
+    """The `s` body with explicit injections (zoom/physics.py:55): each (x (im, jm) DevArray kg,
+    level, tracer) added to rm and taken from rzm on the owned cells."""
+    g, f = zoom.g(region), st[region]
+    cols = _owned_cols(zoom, st, region)
+    for x, level, tracer in injections:
+        K.sources(f["rm"][1 : g.im, 1 : g.jm, 1 : zoom.lm], f["rzm"][1 : g.im, 1 : g.jm, 1 : zoom.lm], x, cols, level,
+                  tracer)  # fmt: skip
+
+
+def chemistry_region(zoom, st, region, decay, tracers):
+    """The `c` body with an explicit decay (zoom/physics.py:67): decay, a DevArray over the scope's
+    cells (ni, nj, lm), multiplies the tracers' mass and slopes there, with factor 1.0 on the
+    cells the region does not own (its children's footprints)."""
+    g, f, lm = zoom.g(region), st[region], zoom.lm
+    si, sj = zoom.scope(region)
+    ni, nj = si.stop - si.start, sj.stop - sj.start
+    fac = st.const(region, "chem_factor", lambda: np.ones((ni, nj, lm)))
+    fac.assign(decay.reshape_axes(decay.shape, decay.strides))
+    for i0, i1, j0, j1 in _footprints(zoom, region):
+        fac[i0 - si.start : i1 - si.start, j0 - sj.start : j1 - sj.start].fill(1.0)
+    for t in tracers:
+        for name in TRACERS:
+            q = f[name][si.start + 1 : si.stop, sj.start + 1 : sj.stop, 1:lm, t]
+            q.binary("*", q, fac.reshape_axes(fac.shape, fac.strides, q.lower))
+
+
+def _footprints(zoom, region):
+    """The children's footprints inside the region's scope as inclusive 0-based (i0, i1, j0, j1):
+    together exactly the scope's cells the region does not own."""
+    si, sj = zoom.scope(region)
+    own = zoom.owned(region)
+    boxes, cover = [], np.zeros_like(own)
+    for c in zoom.children[region]:
+        i0, i1 = max(zoom.ibeg[c] - 1, si.start), min(zoom.iend[c] - 1, si.stop - 1)
+        j0, j1 = max(zoom.jbeg[c] - 1, sj.start), min(zoom.jend[c] - 1, sj.stop - 1)
+        if i0 <= i1 and j0 <= j1:
+            boxes.append((i0, i1, j0, j1))
+            cover[i0 : i1 + 1, j0 : j1 + 1] = True
+    scope = np.zeros_like(own)
+    scope[si, sj] = True
+    if not np.array_equal(cover, scope & ~own):
+        raise NotImplementedError("chemistry_region: the scope's unowned cells are not the children's footprints")
+    return boxes
+
+
+def _owned_cols(zoom, st, region):
+    return st.const(region, "owned_cols", lambda: np.argwhere(zoom.owned(region)).astype(np.int32))

@@ -280,6 +280,126 @@ class Meteo:
         return (m * mix[..., None])[..., None]
 
 
+KZZ_SURFACE = ("oro", "lsm", "sr", "srols", "u10m", "v10m", "sshf", "slhf", "ewss", "nsss")
+CHEM_SETTINGS = {"oh_scale": 0.901, "cl_scale": 1.0, "o1d_scale": 1.0, "soil_rate": 2.0e-4}
+
+
+class Physics:
+    """The physics inputs of a configuration, per region, as host arrays:
+
+    conv    entu, detu, entd, detd (im, jm, lmax) kg/s and cloud_top, cloud_lfs (im, jm) int32:
+            40 % of the columns convective with cloud tops at levels 10-30, an updraft flux of
+            up to 0.05 kg m-2 s-1 times the cell area shaped as sin^2 over the cloud (its peak
+            mid-cloud, near 500 hPa), entrainment where it grows and detrainment where it
+            falls, and a downdraft of 0.3 of it below the level of free sinking
+    kzz     t, q (im, jm, lm); the ten surface fields of Calc_Kzz (im, jm); two instants of the
+            surface pressure spm (the meteo's, interpolated to each step's middle)
+    chem    lat (jm) radians; the zonal loss-rate columns strat_press (hPa, descending),
+            strat_oh, strat_cl, strat_od (jm, ns) at 1e-9 - 1e-7 s-1; oh_3d (im, jm, lm) at
+            1e5 - 3e6, times a diurnal factor per longitude (oh_factor); the tropospheric Cl
+            column pl_trop (Pa, descending), cl_trop (im, jm, ntrop); soil (im, jm) on land,
+            a source of at most 1e-8 s-1 at CHEM_SETTINGS' soil_rate
+    emis    flux (im, jm) kg m-2 s-1, log-normal with mean 1e-10 (three times denser on a
+            child), injected at level 1 as flux x area x the region's half step
+
+    The temperature falls from 270-300 K at the surface to about 215 K at the top (200-300 K),
+    so the Kzz boundary layers grow over heated land and stay shallow over the sea."""
+
+    def __init__(self, zoom, met, seed, lmax, ns=24, ntrop=10, child_density=3.0):
+        self.zoom, self.lmax, self.ns, self.ntrop = zoom, lmax, ns, ntrop
+        self.settings = dict(CHEM_SETTINGS)
+        self.region = {}
+        for r in zoom.regions():
+            rng = np.random.default_rng([seed, 7919, r])
+            self.region[r] = self._region(rng, r, met, 1.0 if r == 1 else child_density)
+
+    def _region(self, rng, r, met, density):
+        z, g = self.zoom, self.zoom.g(r)
+        im, jm, lm, lmax = g.im, g.jm, z.lm, self.lmax
+        lon, lat = _centres(g)
+        slat, clat = sin_cos(lat)
+        sp0 = met.surface_pressure(g)
+        # levels: mid-layer sigma of each column
+        at, bt = z.at, z.bt
+        ph = at[None, None, :] + bt[None, None, :] * sp0[..., None]
+        sig = ((ph[..., :-1] + ph[..., 1:]) * 0.5) / sp0[..., None]
+        out = {}
+        # ---- convection
+        u = rng.random((im, jm))
+        top = np.where(rng.random((im, jm)) < 0.4, 10 + np.floor(u * 21.0), 0.0).astype(np.int32)
+        top = np.minimum(top, lmax).astype(np.int32)
+        lfs = np.where(top > 0, 2 + np.floor(rng.random((im, jm)) * np.maximum(top - 2, 1)), 0.0).astype(np.int32)
+        dxyp = cell_area(g)
+        k = np.arange(lmax + 1, dtype=np.float64)[None, None, :]
+        T = np.maximum(top, 1).astype(np.float64)[..., None]
+        s, _ = sin_cos(PI * np.minimum(k, T) / T)
+        peak = 0.05 * rng.random((im, jm)) * dxyp[None, :]
+        flux = np.where((k <= T) & (top[..., None] > 0), s * s, 0.0) * peak[..., None]
+        d = flux[..., 1:] - flux[..., :-1]
+        noise = 1.0 + 0.2 * rng.random((im, jm, lmax))
+        entu, detu = np.maximum(d, 0.0) * noise, np.maximum(-d, 0.0) * noise
+        lev = np.arange(lmax)[None, None, :]
+        down = (lev < lfs[..., None]).astype(np.float64)
+        entd, detd = 0.3 * detu * down, 0.3 * entu * down
+        out["conv"] = {"entu": entu, "detu": detu, "entd": entd, "detd": detd, "cloud_top": top, "cloud_lfs": lfs}
+        # ---- Calc_Kzz
+        ts = 300.0 - 30.0 * (slat * slat)
+        t = 215.0 + (ts[None, :, None] - 215.0) * sig + (rng.random((im, jm, lm)) * 2.0 - 1.0)
+        q = 0.015 * (sig * sig * sig) * (0.5 + 0.5 * rng.random((im, jm, lm))) + 1.0e-6
+        land = _normalise(Modes(rng, 6)(lon[:, None], lat[None, :])) > 0.2
+        r2 = lambda lo, hi: lo + (hi - lo) * rng.random((im, jm))  # noqa: E731
+        surf = {
+            "oro": np.where(land, GRAV * 2000.0 * rng.random((im, jm)), 0.0),
+            "lsm": np.where(land, 100.0, 0.0),
+            "sr": np.where(land, r2(0.05, 0.5), r2(1e-4, 1e-3)),
+            "srols": np.where(land, r2(0.1, 1.0), r2(1e-3, 1e-2)),
+            "u10m": r2(-8.0, 8.0),
+            "v10m": r2(-8.0, 8.0),
+            "sshf": np.where(land, r2(-250.0, 40.0), r2(-30.0, 15.0)),
+            "slhf": np.where(land, r2(-200.0, 0.0), r2(-150.0, 0.0)),
+            "ewss": np.where(land, r2(-0.1, 0.1), r2(-0.3, 0.3)),
+            "nsss": np.where(land, r2(-0.1, 0.1), r2(-0.3, 0.3)),
+        }
+        sp1 = sp0 * (1.0 + 0.003 * _normalise(Modes(rng, 4)(lon[:, None], lat[None, :])))
+        out["kzz"] = {"t": t, "q": q, "surface": surf, "spm": (sp0, sp1)}
+        # ---- chemistry
+        ns, nt = self.ns, self.ntrop
+        kk = np.arange(ns, dtype=np.float64)
+        col = 1000.0 * exp(-kk * (7.6 / (ns - 1)))  # 1000 hPa .. 0.5 hPa, descending
+        press = col[None, :] * (1.0 + 0.01 * rng.random((jm, 1)))
+        strat = {n: 1e-9 + (1e-7 - 1e-9) * rng.random((jm, ns)) for n in ("strat_oh", "strat_cl", "strat_od")}
+        steps = 0.5 + rng.random((im, jm, nt))
+        csum = np.cumsum(steps, axis=-1)
+        pl = 1.0e5 - 9.0e4 * (csum - steps[..., :1]) / (csum[..., -1:] - steps[..., :1])
+        out["chem"] = {
+            "lat": lat, "strat_press": press, **strat,
+            "oh_3d": 1e5 + (3e6 - 1e5) * rng.random((im, jm, lm)),
+            "pl_trop": pl, "cl_trop": 1e3 * rng.random((im, jm, nt)),
+            "soil": np.where(land, 5.0e-5 * rng.random((im, jm)), 0.0),  # soil_rate x soil <= 1e-8 s-1
+        }  # fmt: skip
+        # ---- emission: log-normal (Irwin-Hall normal deviate), mean 1e-10 kg m-2 s-1
+        zdev = rng.random((12, im, jm)).sum(axis=0) - 6.0
+        out["flux"] = density * 1.0e-10 * exp(zdev - 0.5)
+        out["lon"] = lon
+        return out
+
+    def oh_factor(self, r, t):
+        """(im,) the diurnal factor of OH at time t (s) for each longitude of region r: 0.2 at
+        night, up to 1.0 at local noon."""
+        lon = self.region[r]["lon"]
+        _, c = sin_cos(2.0 * PI * (t / 86400.0) + lon - PI)
+        return 0.2 + 0.8 * np.maximum(c, 0.0)
+
+    def half_step(self, r, ndyn):
+        """The region's half step dt = ndyn / (2 tref) (convec_region's, zoom/physics.py:50)."""
+        return ndyn / (2.0 * self.zoom.g(r).tref)
+
+    def factors(self, r, t0, ndyn):
+        """(2 tref, im): the OH factor of each of the region's halves of the step from t0."""
+        dt = self.half_step(r, ndyn)
+        return np.stack([self.oh_factor(r, t0 + h * dt) for h in range(2 * self.zoom.g(r).tref)])
+
+
 def case(name, lm, seed=0, nt=1, umax=40.0):
     """(zoom, meteo, {r: {field: host array}}): the initial state of every region in the
     declared (halo'd) shapes: m and rm from the meteo's surface pressure, slopes zero, dxyp.

@@ -52,6 +52,12 @@ def run_oracle(ins, meta):
             dkg, pblh = O.calc_kzz(a["spm"], a["sp"], a["pu"], a["pv"], a["t"], a["q"], surface, a["at"], a["bt"],
                                    a["dxyp"], meta["lmax"], meta["dx"], meta["dy"], meta["ybeg"])  # fmt: skip
             return {"dkg": dkg, "pblh": pblh}, None
+        elif op == "chem":
+            kw = {k: meta[k] for k in ("oh_scale", "cl_scale", "o1d_scale", "soil_rate") if k in meta}
+            extra = {k: a[k] for k in ("pl_trop", "cl_trop", "soil", "oh_factor") if k in a}
+            loss, decay = O.loss_rates(a["temper"], a["phlb"], a["lat"], a["strat_press"], a["strat_oh"], a["strat_cl"],
+                                       a["strat_od"], a["oh_3d"], **extra, **kw, dt=meta["dt"])  # fmt: skip
+            return {"loss": loss, "decay": decay}, None
         else:
             raise KeyError(op)
         if r is None:
@@ -132,6 +138,18 @@ def run_device(dev, ins, meta):
             out = {"dkg": dkg.host(), "pblh": pblh.host()}
             dkg.free()
             pblh.free()
+            return out, None
+        if op == "chem":
+            im, jm, lm = d["temper"].shape
+            loss = DevArray.zeros(dev, (0, im - 1), (0, jm - 1), (0, lm - 1), (0, 3))
+            decay = DevArray.zeros(dev, (0, im - 1), (0, jm - 1), (0, lm - 1))
+            kw = {k: meta[k] for k in ("oh_scale", "cl_scale", "o1d_scale", "soil_rate") if k in meta}
+            K.loss_rates(d["temper"], d["phlb"], d["lat"], d, meta["dt"], loss=loss, decay=decay,
+                         oh_factor=d.get("oh_factor"), **kw)  # fmt: skip
+            dev.sync()
+            out = {"loss": loss.host(), "decay": decay.host()}
+            loss.free()
+            decay.free()
             return out, None
         raise KeyError(op)
     except N.CFLError:

@@ -38,6 +38,24 @@ def _gbmath():
     return build()[1]
 
 
+def chem_inputs(rng, im, jm, lm, ns, ntrop):
+    """Inputs of chem.loss_rates on a global grid: half levels of a surface pressure falling as
+    sigma**1.5, zonal columns on descending pressures (some below the surface), a tropospheric
+    Cl column on descending pressures, temperatures 200-300 K, OH 1e5-3e6."""
+    sp = rng.uniform(9e4, 1.02e5, (im, jm))
+    phlb = sp[..., None] * np.linspace(1.0, 0.0, lm + 1)[None, None] ** 1.5
+    press = np.sort(rng.uniform(0.5, 1000.0, (jm, ns)), axis=1)[:, ::-1]  # hPa
+    pl = np.sort(rng.uniform(1e4, 1e5, (im, jm, ntrop)), axis=-1)[..., ::-1]
+    return {
+        "temper": rng.uniform(200.0, 300.0, (im, jm, lm)), "phlb": phlb,
+        "lat": np.radians(-90 + 180.0 / jm * (np.arange(jm) + 0.5)), "strat_press": press,
+        "strat_oh": rng.uniform(1e-9, 1e-7, (jm, ns)), "strat_cl": rng.uniform(1e-9, 1e-7, (jm, ns)),
+        "strat_od": rng.uniform(1e-9, 1e-7, (jm, ns)), "oh_3d": rng.uniform(1e5, 3e6, (im, jm, lm)),
+        "pl_trop": np.ascontiguousarray(pl), "cl_trop": rng.uniform(0, 1e3, (im, jm, ntrop)),
+        "soil": rng.uniform(0, 1, (im, jm)),
+    }  # fmt: skip
+
+
 def kernel_cases():
     _reference()
     from pydyn import balance, cfl, kernels, redgrid, synth
@@ -127,6 +145,30 @@ def kernel_cases():
                **{f"surface.{name}": surface[name] for name in surface}}  # fmt: skip
         put(f"kzz{k}", ins, {"dkg": dkg, "pblh": parts["pblh"]}, op="kzz", lmax=lmax, **grid)
 
+    # CH4 loss rates and decay (chem.loss_rates, chem.decay), pydyn's libm routed as above
+    from pydyn import chem
+
+    for k, (im, jm, lm, ns, ntrop, sinks, factor) in enumerate((
+            (10, 8, 20, 12, 5, ("trop", "soil"), False), (10, 8, 20, 12, 5, ("soil",), False),
+            (9, 7, 34, 30, 8, ("trop",), True), (12, 6, 34, 18, 12, ("trop", "soil"), True))):  # fmt: skip
+        rng = np.random.default_rng(90 + k)
+        ins = chem_inputs(rng, im, jm, lm, ns, ntrop)
+        kw = {"oh_scale": 0.901, "cl_scale": 1.1, "o1d_scale": 1.0}
+        if "trop" in sinks:
+            kw.update(pl_trop=ins["pl_trop"], cl_trop=ins["cl_trop"])
+        if "soil" in sinks:
+            kw.update(soil=ins["soil"], soil_rate=2e-4)
+        oh = ins["oh_3d"]
+        if factor:  # the benchmark's diurnal cycle: a per-longitude multiplier of oh_3d
+            ins["oh_factor"] = rng.uniform(0.2, 1.0, im)
+            oh = oh * ins["oh_factor"][:, None, None]
+        base = {n: ins[n] for n in ("temper", "phlb", "lat", "strat_press", "strat_oh", "strat_cl", "strat_od")}
+        loss = chem.loss_rates(**base, oh_3d=oh, **kw)
+        decay = chem.decay(loss, 1800.0)
+        keep = {n: v for n, v in ins.items() if n in (*base, "oh_3d", "oh_factor", *kw)}
+        put(f"chem{k}", keep, {"loss": loss, "decay": decay}, op="chem", dt=1800.0,
+            **{n: v for n, v in kw.items() if isinstance(v, float)})
+
     # dynam0 and m2phlb1
     rng = np.random.default_rng(7)
     IM, JM, LM = 10, 8, 6
@@ -157,7 +199,65 @@ def digest(fields_by_region):
     return h.hexdigest()
 
 
-def reference_run(config, lm, seed, nsteps, nt=1, physics=None, keep=None, umax=40.0):
+class _RefPhysics:
+    """The physics of a step composed from pydyn itself, as pydyn forward.py:411-451 composes it
+    for one region, for every region of the tree: diffusion.calc_kzz after Setup_MassFlow (spm the
+    meteo's at the step's middle, sp the region's at its start), zoom.physics' convec_region,
+    sources_region and chemistry_region on chem.loss_rates / chem.decay, dt = ndyn / (2 tref)
+    per region, OH times the diurnal factor of the region's half step.  pydyn's libm is routed
+    through the package's gbmath."""
+
+    def __init__(self, zref, spec, fields):
+        from pydyn import ops
+
+        ops.use_libm(str(_gbmath()))
+        self.zref, self.spec, self.dxyp = zref, spec, {r: fields[r]["dxyp"] for r in fields}
+
+    def init(self, st):
+        for r in self.zref.regions():
+            if r == 1:
+                st.lib.m2phlb1(self.zref, st, 1)
+            else:
+                st.lib.m2phlb(self.zref, st, r)
+
+    def step(self, st, t0, ndyn):
+        from pydyn import chem, diffusion
+        from pydyn import zoom as Z
+
+        from pydyn_gb300 import forward
+
+        spec, zref = self.spec, self.zref
+        a1, a2 = forward.weights(t0 + ndyn / 2.0)
+        conv = {}
+        for r in zref.regions():
+            g, R = zref.g(r), spec.region[r]
+            k = R["kzz"]
+            spm = a1 * k["spm"][0] + a2 * k["spm"][1]
+            sp = st[r]["sp"][1 : g.im, 1 : g.jm, 1]
+            dx, dy = (g.xend - g.xbeg) / g.im, (g.yend - g.ybeg) / g.jm
+            dkg, _ = diffusion.calc_kzz(spm, sp, st[r]["pu"].data, st[r]["pv"].data, k["t"], k["q"], k["surface"],
+                                        zref.at, zref.bt, self.dxyp[r], spec.lmax, dx=dx, dy=dy, ybeg=float(g.ybeg))  # fmt: skip
+            conv[r] = {**R["conv"], "dkg": dkg, "lmax": spec.lmax}
+
+        def sources(zoom, s, region):
+            x = spec.region[region]["flux"] * self.dxyp[region][None, :] * spec.half_step(region, ndyn)
+            s.lib.sources_region(zoom, s, region, [(x, 1, 1)])
+
+        def chemistry(zoom, s, region):
+            g, R = zoom.g(region), spec.region[region]
+            c = R["chem"]
+            fac = spec.factors(region, t0, ndyn)[zoom.status[region] // 6]
+            phlb = s[region]["phlb"][1 : g.im, 1 : g.jm, 1 : zoom.lm + 1]
+            loss = chem.loss_rates(R["kzz"]["t"], phlb, c["lat"], c["strat_press"], c["strat_oh"], c["strat_cl"],
+                                   c["strat_od"], c["oh_3d"] * fac[:, None, None], pl_trop=c["pl_trop"],
+                                   cl_trop=c["cl_trop"], soil=c["soil"], **spec.settings)  # fmt: skip
+            decay = chem.decay(loss, spec.half_step(region, ndyn))
+            s.lib.chemistry_region(zoom, s, region, decay[Z.scope(zoom, region)], (1,))
+
+        return conv, {"sources": sources, "chemistry": chemistry}
+
+
+def reference_run(config, lm, seed, nsteps, nt=1, physics=False, keep=None, umax=40.0, lmax=None):
     """pydyn's own driver (zoom.check_cfl_zoom on a copy of m and sp, then setup_massflow and
     zoom.step, as pydyn forward.py:388-451 runs an interval of one step) on the synthetic case
     of pydyn_gb300.synth.  Returns [(ndyn, n, digest)] per interval; keep: a list that receives
@@ -192,7 +292,10 @@ def reference_run(config, lm, seed, nsteps, nt=1, physics=None, keep=None, umax=
             s[r]["pu"].data[...] = a1 * pu0 + a2 * pu1
             s[r]["pv"].data[...] = a1 * pv0 + a2 * pv1
 
-    conv = {r: None for r in zref.regions()}
+    phys = None
+    if physics:
+        phys = _RefPhysics(zref, synth.Physics(zoom, met, seed, lm if lmax is None else lmax), fields)
+        phys.init(st)
     out, t = [], 0.0
     for _ in range(nsteps):
         for r in zref.regions():
@@ -204,11 +307,11 @@ def reference_run(config, lm, seed, nsteps, nt=1, physics=None, keep=None, umax=
             interp(st, t0 + k * ndyn + ndyn / 2.0)
             Z.setup_massflow(zref, st, ndyn)
             kw = {}
-            if physics is not None:
-                conv, kw = physics(zref, st, ndyn)
+            if phys is not None:
+                conv, kw = phys.step(st, t0 + k * ndyn, ndyn)
             else:
                 conv = {r: _no_convection(zref, r) for r in zref.regions()}
-            Z.step(zref, st, conv, ndyn, limits=True, **kw)
+            Z.step(zref, st, conv, ndyn, limits=True, inverse="crout", **kw)
         t = t0 + 3600.0
         host = {r: {name: st[r][name].data for name in STATE_FIELDS} for r in zref.regions()}
         out.append((ndyn, n, digest(host)))
@@ -225,25 +328,35 @@ def _no_convection(zoom, r):
     return {"entu": z, "detu": z, "entd": z, "detd": z, "dkg": z, "cloud_top": c, "cloud_lfs": c, "lmax": 0}
 
 
-STEP_RUNS = {  # name: (tree, lm, seed, intervals, umax)
+STEP_RUNS = {  # name: (tree, lm, seed, intervals, umax[, physics lmax, intervals the CPU tests run])
     "config0": ("glb6x4", 25, 11, 24, 40.0),
     "config0-strong": ("glb6x4", 25, 12, 6, 160.0),
     "two": ("two", 5, 13, 6, 40.0),
     "two-strong": ("two", 5, 14, 6, 120.0),
     "three": ("three", 4, 15, 4, 40.0),
     "config2-adv": ("glb3x2+nam1x1", 34, 31, 3, 40.0),
+    "two-phys": ("two", 8, 21, 6, 40.0, 8, 6),
+    "three-phys": ("three", 6, 22, 4, 40.0, 6, 4),
+    "config1": ("glb3x2", 34, 41, 3, 40.0, 34, 1),
+    "config2": ("glb3x2+nam1x1", 34, 42, 2, 40.0, 34, 1),
 }
 
 
-def step_goldens():
+def step_goldens(names=None):
     import time
 
     res = {}
-    for name, (config, lm, seed, nsteps, umax) in STEP_RUNS.items():
+    for name, spec in STEP_RUNS.items():
+        if names and name not in names:
+            continue
+        config, lm, seed, nsteps, umax = spec[:5]
+        lmax = spec[5] if len(spec) > 5 else None
         t = time.perf_counter()
-        runs = reference_run(config, lm, seed, nsteps, umax=umax)
+        runs = reference_run(config, lm, seed, nsteps, umax=umax, physics=lmax is not None, lmax=lmax)
         res[name] = {"config": config, "lm": lm, "seed": seed, "umax": umax, "steps": [list(x) for x in runs],
                      "reference_seconds_per_interval": (time.perf_counter() - t) / nsteps}  # fmt: skip
+        if lmax is not None:
+            res[name].update(physics=True, lmax=lmax, cpu_prefix=spec[6])
         print(name, runs[-1], res[name]["reference_seconds_per_interval"])
     return res
 
@@ -278,9 +391,9 @@ if __name__ == "__main__":
     if "kernels" in what:
         save(kernel_cases(), HERE / "kernels.npz")
         print("wrote", HERE / "kernels.npz")
-    if "steps" in what:
+    if "steps" in what:  # `steps [name ...]`: those runs only, the others kept
         path = HERE / "steps.json"
         old = json.loads(path.read_text()) if path.exists() else {}
-        old.update(step_goldens())
+        old.update(step_goldens([n for n in what if n in STEP_RUNS]))
         path.write_text(json.dumps(old, indent=1) + "\n")
         print("wrote", path)

@@ -157,6 +157,51 @@ def test_calc_kzz_matches_oracle_at_size(dev, shape, lmax):
 
 
 @pytest.mark.gpu
+@pytest.mark.parametrize(("shape", "ns", "ntrop"), [((120, 90, 34, 2), 30, 10), ((90, 70, 34, 1), 18, 6)])
+def test_chemistry_and_sources_on_owned_columns_at_size(dev, shape, ns, ntrop):
+    """The fused chemistry (rates, decay, applied to tracer 1's mass and slopes) and the
+    emission on the owned columns of a benchmark-sized region (a 30 x 35 block not owned, as a
+    child's footprint), against the oracle's rates and NumPy's q * decay and rm + x."""
+    from make_golden import chem_inputs
+    from oracle import kernels as O
+
+    from pydyn_gb300 import kernels as K
+    from pydyn_gb300.device import DevArray
+
+    im, jm, lm, nt = shape
+    rng = np.random.default_rng(zlib.crc32(repr(("chem", shape)).encode()))
+    st, _ = _state(rng, im, jm, lm, nt, 0.5)
+    ins = chem_inputs(rng, im, jm, lm, ns, ntrop)
+    fac = rng.uniform(0.2, 1.0, im)
+    flux = 1e-10 * rng.uniform(0.1, 3.0, (im, jm))
+    area = rng.uniform(1e9, 1e11, jm)
+    own = np.ones((im, jm), dtype=bool)
+    own[13:43, 50:85] = False
+    cols = np.argwhere(own).astype(np.int32)
+    kw = {"oh_scale": 0.901, "cl_scale": 1.0, "o1d_scale": 1.0, "soil_rate": 2e-4}
+    _, decay = O.loss_rates(ins["temper"], ins["phlb"], ins["lat"], ins["strat_press"], ins["strat_oh"],
+                            ins["strat_cl"], ins["strat_od"], ins["oh_3d"], pl_trop=ins["pl_trop"],
+                            cl_trop=ins["cl_trop"], soil=ins["soil"], dt=1800.0, oh_factor=fac, **kw)  # fmt: skip
+    want = {k: v.copy() for k, v in st.items()}
+    x = flux * area[None, :] * 1800.0
+    want["rm"][..., 0, 0][own] = want["rm"][..., 0, 0][own] + x[own]
+    want["rzm"][..., 0, 0][own] = want["rzm"][..., 0, 0][own] - x[own]
+    for q in TRACERS:
+        want[q][..., 0][own] = want[q][..., 0][own] * decay[own]
+    d = {k: DevArray.from_host(dev, v) for k, v in {**st, **ins, "fac": fac, "flux": flux, "area": area}.items()}
+    dcols = DevArray.from_host(dev, cols)
+    K.sources(d["rm"], d["rzm"], d["flux"], dcols, 1, 1, area=d["area"], scale=1800.0)
+    K.chemistry(d["temper"], d["phlb"], d["lat"], d, 1800.0, dcols, (1,), *(d[q] for q in TRACERS),
+                oh_factor=d["fac"], **kw)  # fmt: skip
+    dev.sync()
+    for k in ("m", *TRACERS):
+        assert_bitwise(d[k].host(), want[k], f"chem.{k}")
+    assert (decay < 1.0).mean() > 0.5
+    for a in (*d.values(), dcols):
+        a.free()
+
+
+@pytest.mark.gpu
 @pytest.mark.parametrize("shape", [(120, 90, 34, 1), (60, 45, 25, 2), (90, 70, 34, 1)])
 @pytest.mark.parametrize("cfl", [0.3, 1.6])
 @pytest.mark.parametrize("op", ["x", "y", "z", "xred"])

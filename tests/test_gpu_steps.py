@@ -25,9 +25,8 @@ def test_intervals_match_reference(dev, name, graph):
     from pydyn_gb300.forward import Forward
 
     run = GOLDEN[name]
-    if run.get("physics"):
-        pytest.skip("physics runs are in their own test")
-    fw = Forward(dev, run["config"], run["lm"], run["seed"], umax=run.get("umax", 40.0))
+    fw = Forward(dev, run["config"], run["lm"], run["seed"], umax=run.get("umax", 40.0),
+                 physics=run.get("physics", False), lmax=run.get("lmax"))  # fmt: skip
     for k, (ndyn, n, want) in enumerate(run["steps"]):
         got_ndyn, got_n = fw.interval(graph=graph)
         assert (got_ndyn, got_n) == (ndyn, n), f"interval {k}: Check_CFL chose {got_ndyn, got_n}, reference {ndyn, n}"

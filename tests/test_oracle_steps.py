@@ -14,10 +14,9 @@ def test_oracle_intervals_match_reference(built, name):
     from oracle.forward import OracleRun, digest
 
     run = GOLDEN[name]
-    if run.get("physics"):
-        pytest.skip("physics runs have their own test")
     steps = run["steps"][: run.get("cpu_prefix", 8)]
-    orc = OracleRun(run["config"], run["lm"], run["seed"], umax=run.get("umax", 40.0))
+    orc = OracleRun(run["config"], run["lm"], run["seed"], umax=run.get("umax", 40.0), physics=run.get("physics", False),
+                    lmax=run.get("lmax"))  # fmt: skip
     for k, (ndyn, n, want) in enumerate(steps):
         assert orc.interval() == (ndyn, n), f"interval {k}"
         assert digest(orc.st) == want, f"{name}: interval {k} differs from the reference"
