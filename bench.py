@@ -40,15 +40,26 @@ sys.path.insert(0, str(ROOT))
 
 SECONDS_A_YEAR = 365.0 * 86400.0
 WORKLOADS = {
-    # name: (tree, levels, physics, seed)
-    "glb6x4": ("glb6x4", 25, False, 11),
-    "glb3x2-adv": ("glb3x2", 34, False, 21),
-    "glb3x2+nam1x1-adv": ("glb3x2+nam1x1", 34, False, 31),
+    # name: (tree, levels, physics, seed, convection levels)
+    "glb6x4": ("glb6x4", 25, False, 11, None),
+    "glb3x2-adv": ("glb3x2", 34, False, 21, None),
+    "glb3x2+nam1x1-adv": ("glb3x2+nam1x1", 34, False, 31, None),
+    "glb3x2": ("glb3x2", 34, True, 41, 34),
+    "glb3x2+nam1x1": ("glb3x2+nam1x1", 34, True, 42, 34),
 }
-DEFAULT = "glb3x2+nam1x1-adv"
+DEFAULT = "glb3x2+nam1x1"
 BYTES_PER_CELL = {"_dynamu_region1": 12, "_dynamv_region1": 12, "_dynamw_region1": 11, "_dynamu_child": 12,
                   "_dynamv_child": 12, "_dynamw_child": 11, "convec_region": 14, "chemistry_region": 11,
-                  "m2phlb1": 2, "m2phlb": 2, "dynam0": 5}  # fmt: skip  (values of 8 bytes at nt = 1)
+                  "sources_region": 4, "calc_kzz": 5, "m2phlb1": 2, "m2phlb": 2,
+                  "dynam0": 5}  # fmt: skip  (values of 8 bytes per cell and application at nt = 1)
+FP64_PEAK = 500.0  # G DMUL or DADD per second, measured on this GB300 (profiles/fp64_throughput_gb300.md)
+
+
+def metric_name(workload):
+    """The headline metric's name for the full-physics glb3x2 + nam1x1 tree, else the workload's."""
+    if workload == "glb3x2+nam1x1":
+        return "sim-years/hour glb3×2+nam1×1 FP64-bitwise"
+    return f"sim-years/hour {workload} FP64-bitwise"
 
 
 def sim_years_per_hour(seconds_per_step, step_seconds=3600.0):
@@ -133,8 +144,8 @@ def cpu_baseline(workload, seconds=15.0):
     """The oracle on this host: whole intervals of the same workload until ~`seconds` pass."""
     from oracle.forward import OracleRun
 
-    tree, lm, physics, seed = WORKLOADS[workload]
-    orc = OracleRun(tree, lm, seed)
+    tree, lm, physics, seed, lmax = WORKLOADS[workload]
+    orc = OracleRun(tree, lm, seed, physics=physics, lmax=lmax)
     t0 = time.perf_counter()
     n = 0
     while n < 1 or (time.perf_counter() - t0 < seconds and n < 50):
@@ -154,8 +165,8 @@ def run_reference(args, ws, rank):
     build()
     from oracle.forward import OracleRun
 
-    tree, lm, physics, seed = WORKLOADS[args.config]
-    orc = OracleRun(tree, lm, seed)
+    tree, lm, physics, seed, lmax = WORKLOADS[args.config]
+    orc = OracleRun(tree, lm, seed, physics=physics, lmax=lmax)
     for _ in range(args.warmup):
         orc.interval()
     t0 = time.perf_counter()
@@ -164,10 +175,11 @@ def run_reference(args, ws, rank):
     per = (time.perf_counter() - t0) / args.steps
     v = sim_years_per_hour(per)
     line = {
-        "impl": "reference", "metric": f"sim-years/hour {args.config} FP64-bitwise", "value": v,
+        "impl": "reference", "metric": metric_name(args.config), "value": v,
         "unit": "sim-years/hour", "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": per * 1e3, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-        "dtype": "f64", "data": "synthetic", "config": {"workload": args.config, "tree": tree, "levels": lm},
+        "dtype": "f64", "data": "synthetic",
+        "config": {"workload": args.config, "tree": tree, "levels": lm, "physics": physics, "lmax": lmax},
         "cpu_baseline": {"value": v, "unit": "sim-years/hour", "cores": 1, "kind": "port",
                          "sample": f"{args.steps} whole intervals of {args.config} (oracle, one host thread)"},
         "e2e": {"value": v, "unit": "sim-years/hour", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
@@ -203,12 +215,12 @@ def main():
     from pydyn_gb300.forward import Forward
     from pydyn_gb300.profile import BodyProfiler
 
-    tree, lm, physics, seed = WORKLOADS[args.config]
+    tree, lm, physics, seed, lmax = WORKLOADS[args.config]
     dev = Device(local)
-    fw = Forward(dev, tree, lm, seed=seed + rank)
+    fw = Forward(dev, tree, lm, seed=seed, physics=physics, lmax=lmax)  # every replica runs the same case
 
     # per-body device time of one eager interval: the roofline's dominant body
-    with BodyProfiler(dev) as prof:
+    with BodyProfiler(dev, fw.physics) as prof:
         fw.interval(graph=False)
     bodies = prof.report()
 
@@ -279,18 +291,30 @@ def main():
             "frac": achieved / hbm if achieved else None, "traffic": None, "peak_source": how,
             "bytes_per_launch": per_call_bytes, "ms_per_launch": total_ms / calls,
             "note": "float64 with no contraction: the FP64 pipe (500 G DMUL/DADD/s measured) bounds the step"}  # fmt: skip
+    if body == "convec_region" and fw.physics is not None:
+        # the explicit Crout inverse: (8/3) lmax^3 flops per column on its first call of a step (the
+        # second call of the same air mass reuses it: 2 lmax^2 nt for the tracer product only)
+        ncol = fw.physics.r[int(region) if region else 1]["ncol"]
+        pairs = calls // 2  # each pair of calls on one air mass computes one inverse per column
+        flops = pairs * ncol * ((8.0 / 3.0) * lmax**3 + 2.0 * 2.0 * lmax * lmax)
+        gflops = flops / (total_ms / 1e3) / 1e9
+        roof["fp64"] = {"achieved_gflops": gflops, "peak_gflops": FP64_PEAK, "frac": gflops / FP64_PEAK,
+                        "flops_per_interval": flops,
+                        "note": "(8/3) lmax^3 per column inverse, 2 lmax^2 per call's product; peak = the "
+                                "measured DMUL/DADD issue rate"}  # fmt: skip
 
-    step_bytes = sum(n * (2 * fw.zoom.g(r).tref * 37 * 8 + 40 + 248) for r, n in cells.items())
+    b_half = (496 if physics else 296)  # bytes per cell per half step at nt = 1
+    step_bytes = sum(n * (2 * fw.zoom.g(r).tref * b_half + 40 + (40 if physics else 0) + 248) for r, n in cells.items())
     total_time = sum(v[1] for v in bodies.values())
     line = {
-        "metric": "sim-years/hour glb3x2+nam1x1 FP64-bitwise" if "nam" in tree else f"sim-years/hour {args.config} FP64-bitwise",
+        "metric": metric_name(args.config),
         "value": sim_years_per_hour(sec_per_step) * ws,
         "unit": "sim-years/hour",
         "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": sec_per_step * 1e3,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
         "data": "synthetic (seeded meteo of the configuration's shape; pydyn_gb300.synth)",
-        "config": {"workload": args.config, "tree": tree, "levels": lm, "nt": 1, "physics": physics,
+        "config": {"workload": args.config, "tree": tree, "levels": lm, "nt": 1, "physics": physics, "lmax": lmax,
                    "step": "Check_CFL rehearsal + Setup_MassFlow + xyzvsc|csvzyx, one CUDA graph",
                    "l2": "flushed between timed steps (256 MiB write)", "parallelism": f"replicas x{ws}"},
         "roofline": roof,

@@ -17,8 +17,12 @@ class BodyProfiler:
                "chemistry_region", "put_xedges", "put_yedges", "mix_edges", "update_parent", "_coarsen_block",
                "coarsen_ambm", "_uncompress_xedges", "_uncompress_yedges", "save", "restore")  # fmt: skip
 
-    def __init__(self, dev):
+    # a run's physics object: its per-step preparation (Calc_Kzz) and its `s` / `c` callbacks
+    PHYSICS = {"prepare": "calc_kzz", "sources": "sources_region", "chemistry": "chemistry_region"}
+
+    def __init__(self, dev, physics=None):
         self.dev = dev
+        self.physics = physics
         self.pairs = defaultdict(list)
         self.launches = defaultdict(int)
         self._saved = {}
@@ -30,12 +34,18 @@ class BodyProfiler:
                 continue
             self._saved[name] = f
             setattr(Z, name, self._wrap(name, f))
+        if self.physics is not None:
+            for attr, name in self.PHYSICS.items():
+                setattr(self.physics, attr, self._wrap(name, getattr(self.physics, attr)))
         return self
 
     def __exit__(self, *exc):
         for name, f in self._saved.items():
             setattr(Z, name, f)
         self._saved.clear()
+        if self.physics is not None:
+            for attr in self.PHYSICS:
+                self.physics.__dict__.pop(attr, None)
         return False
 
     def _wrap(self, name, f):
@@ -80,8 +90,10 @@ def main(argv=None):
     ap = argparse.ArgumentParser(description=main.__doc__.split("\n")[0])
     ap.add_argument("--config", default="glb3x2+nam1x1")
     ap.add_argument("--levels", type=int, default=34)
-    ap.add_argument("--seed", type=int, default=31)
+    ap.add_argument("--seed", type=int, default=42)
     ap.add_argument("--intervals", type=int, default=1)
+    ap.add_argument("--physics", type=int, default=1, help="1: convection, Kzz, emission, chemistry; 0: advection")
+    ap.add_argument("--lmax", type=int, default=None)
     a = ap.parse_args(argv)
     from __graft_entry__ import build
 
@@ -90,7 +102,7 @@ def main(argv=None):
     from .forward import Forward
 
     dev = Device(0)
-    fw = Forward(dev, a.config, a.levels, a.seed)
+    fw = Forward(dev, a.config, a.levels, a.seed, physics=bool(a.physics), lmax=a.lmax)
     n0 = dev.launches()
     for _ in range(a.intervals):
         fw.interval(graph=False)
