@@ -1,14 +1,14 @@
 // The CH4 `c` and `s` operators on a region's columns.
 //
-// k_chem: one warp per column.  The lanes stage the column's edges in shared memory -- the
-// zonal loss-rate columns' edges (strat_edges), the tropospheric Cl column's, the model's half
-// levels -- check each is strictly descending (warp vote), then take the levels: the four loss
-// rates, decay = exp(-(((L1 + L2) + L3) + L4) dt), and either the rates and decay written out
-// (gb_loss_rates, every column of the region) or the decay applied to the listed tracers' mass
-// and slopes (gb_chemistry, the columns a region owns).  A rebinned layer sums, in input order
-// from +0.0, data * thickness over the input layers first .. last-1 whose overlap is positive;
-// the terms the reference adds for the others are +0.0, which leave such a sum unchanged.
-// exp / pow / cos are gbmath.h.
+// k_chem_rows: thread per latitude -- the zonal loss-rate columns' edges (strat_edges), checked
+// strictly descending, and the tropopause pressure.  k_chem: thread per (column, level) -- the
+// cell's half levels and tropospheric Cl edges checked, the four loss rates, decay =
+// exp(-(((L1 + L2) + L3) + L4) dt), and either the rates and decay written out (gb_loss_rates,
+// every column of the region) or the decay applied to the listed tracers' mass and slopes
+// (gb_chemistry, the columns a region owns).  A rebinned layer sums, in input order from +0.0,
+// data * thickness over the input layers first .. last-1 whose overlap is positive; the terms
+// the reference adds for the others are +0.0, which leave such a sum unchanged.  exp / pow /
+// cos are gbmath.h.
 //
 // k_sources: one thread per owned column: rm(level) += x, rzm(level) -= x.
 //
@@ -19,7 +19,7 @@
 
 namespace {
 
-constexpr int WARPS = 4;
+constexpr int CELL_THREADS = 128;
 
 struct CArgs {
     DV temper, phlb, soil, oh3d, pltrop, cltrop, sp, soh, scl, sod;
@@ -32,6 +32,7 @@ struct CArgs {
     DV q[4];                    // gb_chemistry: rm, rxm, rym, rzm
     uint32_t tracer_mask;       // gb_chemistry: bit t-1 for tracer t
     int apply;
+    double *edges, *trop;       // work space: (jm, ns + 1) zonal edges, (jm) tropopause
     gb_ctl *ctl;
 };
 
@@ -43,9 +44,17 @@ __device__ __forceinline__ double &E4(const DV &v, int64_t a, int64_t b, int64_t
     return v.p[a * v.s0 + b * v.s1 + c * v.s2 + d * v.s3];
 }
 
-// rebin_levels(ip_mix) of one output layer [top, bot] from the edges ip[0..nip] (shared memory)
-__device__ double rebin_layer(const double *ip, int nip, const double *data, int64_t stride, double bot,
-                              double top) {
+// the tropospheric Cl column's edges: pl_trop(i, j, 0 .. ntrop-1), then 0 (chem.py:135)
+struct TropEdges {
+    const double *p;
+    int64_t s;
+    int n;
+    __device__ double operator[](int k) const { return k < n ? p[k * s] : 0.0; }
+};
+
+// rebin_levels(ip_mix) of one output layer [top, bot] from the edges ip[0..nip]
+template <class Edges>
+__device__ double rebin_layer(const Edges &ip, int nip, const double *data, int64_t stride, double bot, double top) {
     int first = 0, last = 0;
     for (int k = 0; k < nip; ++k) {
         first += ip[k + 1] >= bot;
@@ -60,26 +69,15 @@ __device__ double rebin_layer(const double *ip, int nip, const double *data, int
     return width > 0.0 ? overlap / width : overlap;
 }
 
-__global__ void __launch_bounds__(WARPS * 32) k_chem(CArgs A) {
-    extern __shared__ double smem[];
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int64_t c = (int64_t)blockIdx.x * WARPS + warp;
-    if (c >= A.ncol) return;
-    int i, j;
-    if (A.cols) {
-        i = A.cols[2 * c];
-        j = A.cols[2 * c + 1];
-    } else {
-        i = (int)(c / A.jm);
-        j = (int)(c % A.jm);
-    }
-    const int ns = A.ns, nt = A.ntrop, lm = A.lm;
-    double *edges = smem + (size_t)warp * ((ns + 1) + (nt + 1) + (lm + 1));
-    double *tedges = edges + (ns + 1);
-    double *ph = tedges + (nt + 1);
-
-    // strat_edges (chem.py:91-98): midpoints, a half layer below the first, 0 above the last, x100
-    for (int k = lane; k <= ns; k += 32) {
+// thread per latitude: the zonal columns' edges (strat_edges, chem.py:91-98: midpoints, a half
+// layer below the first, 0 above the last, x100) and the tropopause pressure (chem.py:101-104)
+__global__ void k_chem_rows(CArgs A) {
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= A.jm) return;
+    const int ns = A.ns;
+    double *edges = A.edges + (int64_t)j * (ns + 1);
+    bool ok = true;
+    for (int k = 0; k <= ns; ++k) {
         double e;
         if (k == 0) {
             const double p0 = E2(A.sp, j, 0), p1 = E2(A.sp, j, 1);
@@ -90,28 +88,45 @@ __global__ void __launch_bounds__(WARPS * 32) k_chem(CArgs A) {
             e = 0.0;
         }
         edges[k] = e * 100.0;
+        if (k > 0) ok = ok && (edges[k] - edges[k - 1] < 0.0);
     }
+    if (!ok) raise_status(A.ctl, GB_ELEVELS);
+    const double cl = gbm_cos(A.lat[j]);
+    A.trop[j] = 30000.0 - 21500.0 * (cl * cl);
+}
+
+// thread per (column, level): the four rates, the decay, and its use
+__global__ void __launch_bounds__(CELL_THREADS) k_chem(CArgs A) {
+    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const int lm = A.lm;
+    if (t >= A.ncol * lm) return;
+    const int64_t c = t / lm;
+    const int l = (int)(t % lm);
+    int i, j;
+    if (A.cols) {
+        i = A.cols[2 * c];
+        j = A.cols[2 * c + 1];
+    } else {
+        i = (int)(c / A.jm);
+        j = (int)(c % A.jm);
+    }
+    const int ns = A.ns, nt = A.ntrop;
+    const double *edges = A.edges + (int64_t)j * (ns + 1);
+    const double bot = E3(A.phlb, i, j, l), top = E3(A.phlb, i, j, l + 1);
+    bool ok = top - bot < 0.0;
+    TropEdges tedges{nullptr, 0, 0};
     if (A.has_trop) {
-        for (int k = lane; k < nt; k += 32) tedges[k] = E3(A.pltrop, i, j, k);
-        if (lane == 0) tedges[nt] = 0.0;
+        tedges = TropEdges{&E3(A.pltrop, i, j, 0), A.pltrop.s2, nt};
+        for (int k = 0; k < nt; ++k) ok = ok && (tedges[k + 1] - tedges[k] < 0.0);
     }
-    for (int k = lane; k <= lm; k += 32) ph[k] = E3(A.phlb, i, j, k);
-    __syncwarp();
-    bool ok = true;
-    for (int k = lane; k < ns; k += 32) ok = ok && (edges[k + 1] - edges[k] < 0.0);
-    for (int k = lane; k < lm; k += 32) ok = ok && (ph[k + 1] - ph[k] < 0.0);
-    if (A.has_trop)
-        for (int k = lane; k < nt; k += 32) ok = ok && (tedges[k + 1] - tedges[k] < 0.0);
-    if (!__all_sync(FULL_MASK, ok)) {
-        if (lane == 0) raise_status(A.ctl, GB_ELEVELS);
+    if (!ok) {
+        raise_status(A.ctl, GB_ELEVELS);
         return;
     }
-    const double cl = gbm_cos(A.lat[j]);
-    const double trop = 30000.0 - 21500.0 * (cl * cl);
+    const double trop = A.trop[j];
     const double *doh = &E2(A.soh, j, 0), *dcl = &E2(A.scl, j, 0), *dod = &E2(A.sod, j, 0);
 
-    for (int l = lane; l < lm; l += 32) {
-        const double bot = ph[l], top = ph[l + 1];
+    {
         const bool below = bot > edges[0];
         const double s_oh = below ? doh[0] : rebin_layer(edges, ns, doh, A.soh.s1, bot, top);
         const double s_cl = below ? dcl[0] : rebin_layer(edges, ns, dcl, A.scl.s1, bot, top);
@@ -207,9 +222,14 @@ int setup_chem(CArgs &A, const gb_view *temper, const gb_view *phlb, const doubl
 int launch_chem(gb_ctx *ctx, CArgs &A) {
     A.ctl = ctx->ctl;
     if (A.ncol == 0) return GB_OK;
-    const size_t smem = (size_t)WARPS * ((A.ns + 1) + (A.ntrop + 1) + (A.lm + 1)) * sizeof(double);
-    GB_CHECK_CUDA(cudaFuncSetAttribute(k_chem, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    k_chem<<<(unsigned)((A.ncol + WARPS - 1) / WARPS), WARPS * 32, smem, ctx->stream>>>(A);
+    double *w = gb_work(ctx, (size_t)A.jm * (A.ns + 2) * sizeof(double));
+    if (!w) return GB_ECUDA;
+    A.edges = w;
+    A.trop = w + (size_t)A.jm * (A.ns + 1);
+    k_chem_rows<<<(unsigned)((A.jm + 127) / 128), 128, 0, ctx->stream>>>(A);
+    if (int rc = gb_after_launch(ctx, "chem_rows")) return rc;
+    const int64_t cells = A.ncol * A.lm;
+    k_chem<<<(unsigned)((cells + CELL_THREADS - 1) / CELL_THREADS), CELL_THREADS, 0, ctx->stream>>>(A);
     return gb_after_launch(ctx, A.apply ? "chemistry" : "loss_rates");
 }
 

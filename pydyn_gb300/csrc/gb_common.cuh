@@ -30,6 +30,8 @@ struct gb_ctx {
     gb_ctl *ctl = nullptr;         // device
     int32_t *scratch_i = nullptr;  // per-op integer scratch (layer nloops, ...)
     size_t scratch_i_n = 0;
+    double *work = nullptr;        // per-op float64 work space, grown outside capture (gb_work)
+    size_t work_bytes = 0;
     int64_t launches = 0;
     bool capturing = false;
     int64_t capture_launches = 0;
@@ -39,6 +41,7 @@ void gb_set_error(const std::string &msg);
 int gb_cuda_fail(cudaError_t e, const char *what);
 int gb_after_launch(gb_ctx *ctx, const char *what);
 int32_t *gb_scratch_i(gb_ctx *ctx, size_t n);
+double *gb_work(gb_ctx *ctx, size_t bytes);  // nullptr (error set) if it cannot be had
 
 #define GB_CHECK_CUDA(call)                                   \
     do {                                                      \

@@ -28,6 +28,27 @@ int32_t *gb_scratch_i(gb_ctx *ctx, size_t n) {
     return nullptr;  // grown only outside capture, by gb_create's fixed size
 }
 
+double *gb_work(gb_ctx *ctx, size_t bytes) {
+    if (bytes <= ctx->work_bytes) return ctx->work;
+    if (ctx->capturing) {  // an allocation would end the capture: the first uncaptured call sizes it
+        gb_set_error("work space of " + std::to_string(bytes) + " bytes needed inside a capture; run the "
+                     "operator once before capturing");
+        return nullptr;
+    }
+    cudaError_t e = cudaStreamSynchronize(ctx->stream);  // the old space may still be read
+    if (e == cudaSuccess && ctx->work) e = cudaFree(ctx->work);
+    ctx->work = nullptr;
+    ctx->work_bytes = 0;
+    if (e == cudaSuccess) e = cudaMalloc(&ctx->work, bytes);
+    if (e != cudaSuccess) {
+        gb_cuda_fail(e, "gb_work");
+        ctx->work = nullptr;
+        return nullptr;
+    }
+    ctx->work_bytes = bytes;
+    return ctx->work;
+}
+
 extern "C" const char *gb_last_error(void) { return g_last_error.c_str(); }
 
 extern "C" int gb_create(int device, gb_ctx **out) {
@@ -56,6 +77,7 @@ extern "C" void gb_destroy(gb_ctx *ctx) {
     if (ctx->stream) cudaStreamSynchronize(ctx->stream);
     if (ctx->ctl) cudaFree(ctx->ctl);
     if (ctx->scratch_i) cudaFree(ctx->scratch_i);
+    if (ctx->work) cudaFree(ctx->work);
     if (ctx->stream) cudaStreamDestroy(ctx->stream);
     delete ctx;
 }

@@ -47,6 +47,9 @@ class Physics:
             g, R = zoom.g(r), spec.region[r]
             own = zoom.owned(r)
             cols = np.argwhere(own).astype(np.int32)
+            # deepest clouds first: a warp's columns then share their matrices' zero structure
+            top = R["conv"]["cloud_top"]
+            cols = cols[np.argsort(-top[cols[:, 0], cols[:, 1]], kind="stable")]
             ncol = len(cols)
             d = {
                 "conv": {k: up(v, np.int32 if k.startswith("cloud") else np.float64) for k, v in R["conv"].items()},
