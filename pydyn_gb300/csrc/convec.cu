@@ -1,25 +1,26 @@
 // convec: implicit convection with Kzz diffusion folded into one matrix per column, inverted
 // by Crout LU without pivoting, applied to the tracer mass and (by its diagonal) the slopes.
 //
-// Two launches, shaped so that the FP64 pipe -- this GPU's scarcest unit -- issues with its
+// Four launches, shaped so that the FP64 pipe -- this GPU's scarcest unit -- issues with its
 // lanes full:
-//   k_convec_lu     one warp per owned column, the matrix in shared memory: the updraft and
-//                   downdraft chains, the per-level quotients (each division once, lanes across
-//                   levels), f and conv1 = I - dt (f(k-1) - f(k)), Crout LU column by column
-//                   with the rows a term updates packed onto the lanes, and L^-1 by forward
-//                   substitution (row k's terms applied to every later row at once, the
-//                   (row, column) elements packed onto the lanes).  U goes to a work space, L^-1
-//                   to the inverse's place.
-//   k_convec_apply  one thread per (column, column of the inverse): the back substitution
-//                   U X = L^-1 of its column of the inverse; then, whole columns per block, one
-//                   thread per (column, level): the slopes times the inverse's diagonal and
-//                   rm = C rm accumulated in k.
+//   k_convec_chains  one thread per owned column: whether its kept inverse still holds, the
+//                    updraft and downdraft chains, and every division of its matrix, once
+//   k_convec_matrix  one thread per (column, column l of its matrix): conv1(., l) = I - dt
+//                    (f(k-1, l) - f(k, l)), the downdraft chain of f down from the diagonal and
+//                    the updraft chain up from it -- into a work space
+//   k_convec_lu      one warp per column whose inverse is made: Crout LU column by column (the
+//                    rows a term updates packed onto the lanes), then L^-1 by forward
+//                    substitution (row k's terms applied to every later row at once, the
+//                    (row, column) elements packed onto the lanes).  U goes to the work space,
+//                    L^-1 to the inverse's place.
+//   k_convec_apply   one thread per (column, column of the inverse): the back substitution
+//                    U X = L^-1; then, whole columns per block, one thread per (column, level):
+//                    the slopes times the inverse's diagonal and rm = C rm accumulated in k.
 // The reference's operation order is kept element by element -- every element receives its
 // terms in the same k order as in the row-by-row form -- and work is skipped only where a
-// multiplier is exactly zero (the same skips as the reference's own zero tests would leave
-// bitwise: x - w * y with w = +-0 returns x unless x is a zero, and the accumulators of the
-// substitutions are never -0).  Above the cloud the matrix is tridiagonal (diffusion only), so
-// most of the O(n^3) inverse becomes O(n^2).
+// multiplier is exactly zero (x - w * y with w = +-0 returns x unless x is a zero, and the
+// accumulators of the substitutions are never -0).  Above the cloud the matrix is tridiagonal
+// (diffusion only), so most of the O(n^3) inverse becomes O(n^2).
 //
 // The inverse of a column is kept (with the air mass it was made from) and reused by the next
 // call in the same convection epoch when that air mass is bitwise unchanged -- the two `v` of
@@ -33,6 +34,7 @@ namespace {
 
 constexpr int WARPS = 2;
 constexpr int NMAX = 64;
+constexpr int MATRIX_THREADS = 64;
 
 struct CArgs {
     DV m, q[4];
@@ -43,8 +45,9 @@ struct CArgs {
     int ncol, n, nt;
     double dt;
     double *inv;         // ncol * n * n: the inverses (the cache's, or the work space's)
-    double *ubuf;        // ncol * n * n work space: U of the columns factorised in this call
-    int32_t *fresh;      // ncol work space: 1 where this call factorised the column
+    double *abuf;        // ncol * n * n work space: conv1, then U, of the columns made here
+    double *chain;       // ncol * 10 (n+1) work space: the chains and quotients of each column
+    int32_t *fresh;      // ncol work space: 1 where this call makes the column's inverse
     double *cache_m;     // ncol * n, or null (no reuse)
     int32_t *cache_tag;  // ncol
     const int32_t *epoch;
@@ -59,111 +62,105 @@ __device__ __forceinline__ double &AT4(const DV &v, int64_t i, int64_t j, int64_
 }
 __device__ __forceinline__ double max0(double x) { return isnan(x) ? x : (0.0 > x ? 0.0 : x); }
 
-// shared memory of one warp (doubles): A n*n (conv1, then LU), Y (n+1)*n (f, then L^-1), vectors
-// m, amu, amd, zu, zd and the quotients qeu, qed, qamu, qamd, qdk1, qdk2 (n+1 each)
-__host__ __device__ __forceinline__ size_t warp_doubles(int n) {
-    return (size_t)n * n + (size_t)(n + 1) * n + 11 * (size_t)(n + 1);
-}
+// the work space's per-column chains amu, zu, amd, zd and the matrix's quotients qeu, qed, qamu,
+// qamd, qdk1, qdk2 (n+1 each, indexed by level k = 1..n)
+constexpr int NCHAIN = 10;
+__device__ __forceinline__ double *chains(const CArgs &A, int c) { return A.chain + (size_t)c * NCHAIN * (A.n + 1); }
 
-__global__ void __launch_bounds__(WARPS * 32) k_convec_lu(CArgs A) {
-    extern __shared__ double smem[];
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int c = blockIdx.x * WARPS + warp;
+// thread per column: whether the kept inverse still holds; the updraft and downdraft chains; every
+// division of the column's matrix, once
+__global__ void __launch_bounds__(MATRIX_THREADS) k_convec_chains(CArgs A) {
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
     if (c >= A.ncol) return;
     const int n = A.n;
-    double *S = smem + (size_t)warp * warp_doubles(n);
-    double *LU = S;                    // n x n
-    double *Y = LU + (size_t)n * n;    // (n+1) x n
-    double *mc = Y + (size_t)(n + 1) * n;
-    double *amu = mc + (n + 1), *amd = amu + (n + 1), *zu = amd + (n + 1), *zd = zu + (n + 1);
-    double *qeu = zd + (n + 1), *qed = qeu + (n + 1), *qamu = qed + (n + 1), *qamd = qamu + (n + 1);
-    double *qdk1 = qamd + (n + 1), *qdk2 = qdk1 + (n + 1);
     const int i = A.cols[2 * c], j = A.cols[2 * c + 1];
 
-    for (int l = lane; l < n; l += 32) mc[l] = AT(A.m, i, j, l);
-    __syncwarp();
-
-    // ---- the kept inverse, when this column's inputs are bitwise those it was made from
+    // ---- the kept inverse, when this column's air mass is bitwise the one it was made from
     if (A.cache_m) {
-        const double *cm = A.cache_m + (size_t)c * n;
+        double *cm = A.cache_m + (size_t)c * n;
         bool same = A.cache_tag[c] == *A.epoch;
-        for (int l = lane; l < n; l += 32)
-            same = same && (__double_as_longlong(cm[l]) == __double_as_longlong(mc[l]));
-        if (__all_sync(FULL_MASK, same)) {
-            if (lane == 0) A.fresh[c] = 0;
+        for (int l = 0; l < n; ++l) same = same && (__double_as_longlong(cm[l]) == __double_as_longlong(AT(A.m, i, j, l)));
+        if (same) {
+            A.fresh[c] = 0;
             return;
         }
+        for (int l = 0; l < n; ++l) cm[l] = AT(A.m, i, j, l);
+        A.cache_tag[c] = *A.epoch;
     }
+    A.fresh[c] = 1;
 
+    double *amu = chains(A, c), *zu = amu + (n + 1), *amd = zu + (n + 1), *zd = amd + (n + 1);
     const int top = A.top[i * A.ts0 + j * A.ts1], lfs = A.lfs[i * A.ts0 + j * A.ts1];
-    // ---- the scalar chains of the updraft (upward) and downdraft (downward); every lane
-    // computes them alike, lane 0 stores them
-    {
-        double mu = 0.0;
-        if (lane == 0) amu[0] = 0.0;
-        for (int k = 1; k <= n; ++k) {
-            const double eu = AT(A.entu, i, j, k - 1), du = AT(A.detu, i, j, k - 1);
-            const bool act = top >= k;
-            const double a = mu + eu - du;
-            const bool up = a > 0.0;
-            const double z = up ? max0(1.0 - du / (mu + eu)) : 0.0;
-            mu = (act && up) ? a : 0.0;
-            if (lane == 0) {
-                amu[k] = mu;
-                zu[k] = act ? z : -1.0;  // -1 marks an inactive level
-            }
-        }
-        double md = 0.0;
-        if (lane == 0) {
-            amd[n] = 0.0;
-            amd[0] = 0.0;
-            zd[0] = zd[1] = -1.0;
-        }
-        for (int k = n; k >= 2; --k) {
-            const double ed = AT(A.entd, i, j, k - 1), dd = AT(A.detd, i, j, k - 1);
-            const bool act = lfs >= k;
-            const double a = md - ed + dd;
-            const bool dn = a < 0.0;
-            const double z = dn ? max0(1.0 + dd / (md - ed)) : 0.0;
-            md = (act && dn) ? a : 0.0;
-            if (lane == 0) {
-                amd[k - 1] = md;
-                zd[k] = act ? z : -1.0;
-            }
-        }
+    double mu = 0.0;
+    amu[0] = 0.0;
+    for (int k = 1; k <= n; ++k) {
+        const double eu = AT(A.entu, i, j, k - 1), du = AT(A.detu, i, j, k - 1);
+        const bool act = top >= k;
+        const double a = mu + eu - du;
+        const bool up = a > 0.0;
+        const double z = up ? max0(1.0 - du / (mu + eu)) : 0.0;
+        mu = (act && up) ? a : 0.0;
+        amu[k] = mu;
+        zu[k] = act ? z : -1.0;  // -1 marks an inactive level
     }
-    __syncwarp();
-    // ---- every division of the matrix once, lanes across levels k = 1..n
-    for (int k = 1 + lane; k <= n; k += 32) {
-        qeu[k] = AT(A.entu, i, j, k - 1) / mc[k - 1];
-        qed[k] = -AT(A.entd, i, j, k - 1) / mc[k - 1];
+    double md = 0.0;
+    amd[n] = 0.0;
+    amd[0] = 0.0;
+    zd[0] = zd[1] = -1.0;
+    for (int k = n; k >= 2; --k) {
+        const double ed = AT(A.entd, i, j, k - 1), dd = AT(A.detd, i, j, k - 1);
+        const bool act = lfs >= k;
+        const double a = md - ed + dd;
+        const bool dn = a < 0.0;
+        const double z = dn ? max0(1.0 + dd / (md - ed)) : 0.0;
+        md = (act && dn) ? a : 0.0;
+        amd[k - 1] = md;
+        zd[k] = act ? z : -1.0;
+    }
+    double *qeu = zd + (n + 1), *qed = qeu + (n + 1), *qamu = qed + (n + 1), *qamd = qamu + (n + 1);
+    double *qdk1 = qamd + (n + 1), *qdk2 = qdk1 + (n + 1);
+    for (int k = 1; k <= n; ++k) {
+        const double m0 = AT(A.m, i, j, k - 1);
+        qeu[k] = AT(A.entu, i, j, k - 1) / m0;
+        qed[k] = -AT(A.entd, i, j, k - 1) / m0;
         if (k <= n - 1) {
-            qamu[k] = amu[k] / mc[k];
-            qamd[k] = amd[k] / mc[k - 1];
-            qdk1[k] = AT(A.dkg, i, j, k - 1) / mc[k - 1];
-            qdk2[k] = AT(A.dkg, i, j, k - 1) / mc[k];
+            const double m1 = AT(A.m, i, j, k);
+            qamu[k] = amu[k] / m1;
+            qamd[k] = amd[k] / m0;
+            qdk1[k] = AT(A.dkg, i, j, k - 1) / m0;
+            qdk2[k] = AT(A.dkg, i, j, k - 1) / m1;
         }
     }
-    __syncwarp();
-    // ---- f = fd (downward chains per column l), then + fu row by row, then the diagonals
-    for (int l = lane; l < n; l += 32) {
-        for (int k = 0; k <= n; ++k) Y[(size_t)k * n + l] = 0.0;
-        double v = 0.0;  // fd(k-1, l) for k = l+1 down to 2
-        for (int k = n; k >= 2; --k) {
-            const double z = zd[k];
+}
+
+// thread per (column, column l of its matrix): conv1(., l).  f(k, l), k = 0..n: the downdraft
+// chain fd(k, l) for k = l down to 1 (zero elsewhere), plus the updraft chain fu(k, l) for
+// k = l+1 up, plus the diagonal terms; f(0, l) = f(n, l) = 0.  conv1(k-1, l) =
+// -dt (f(k-1, l) - f(k, l)), plus 1 on the diagonal.
+__global__ void __launch_bounds__(MATRIX_THREADS) k_convec_matrix(CArgs A) {
+    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const int n = A.n;
+    if (t >= (int64_t)A.ncol * n) return;
+    const int c = (int)(t / n), l = (int)(t % n);
+    if (!A.fresh[c]) return;
+    const double *zu = chains(A, c) + (n + 1), *zd = zu + 2 * (n + 1);
+    const double *qeu = zd + (n + 1), *qed = qeu + (n + 1), *qamu = qed + (n + 1), *qamd = qamu + (n + 1);
+    const double *qdk1 = qamd + (n + 1), *qdk2 = qdk1 + (n + 1);
+    double fd[NMAX];
+    double *out = A.abuf + (size_t)c * n * n;
+    const double mdt = -A.dt;
+    {
+        double v = 0.0;
+        for (int r = l; r >= 1; --r) {  // fd(r, l), r = k - 1 with k from l + 1 down to 2
+            const double z = zd[r + 1];
             const bool act = z >= 0.0;
-            if (k - 1 == l)
-                v = act ? qed[k] * z : 0.0;
-            else if (k - 1 < l)
-                v = act ? v * z : 0.0;
+            if (r == l)
+                v = act ? qed[r + 1] * z : 0.0;
             else
-                continue;
-            Y[(size_t)(k - 1) * n + l] = v;
+                v = act ? v * z : 0.0;
+            fd[r] = v;
         }
-    }
-    __syncwarp();
-    for (int l = lane; l < n; l += 32) {
-        double u = 0.0;  // fu(k, l) for k = 1..n
+        double u = 0.0, fprev = 0.0;
         for (int k = 1; k <= n; ++k) {
             const double z = zu[k];
             const bool act = z >= 0.0;
@@ -173,27 +170,38 @@ __global__ void __launch_bounds__(WARPS * 32) k_convec_lu(CArgs A) {
                 u = act ? qeu[k] * z : 0.0;
             else
                 u = 0.0;
+            double fk = 0.0;
             if (k <= n - 1) {
-                double f = u + Y[(size_t)k * n + l];
+                double f = u + (k <= l ? fd[k] : 0.0);
                 if (l == k) f = f - qamu[k];
                 if (l == k - 1) {
                     f = f - qamd[k];
                     f = f + qdk1[k];
                 }
                 if (l == k) f = f - qdk2[k];
-                Y[(size_t)k * n + l] = f;
+                fk = f;
             }
+            double e = mdt * (fprev - fk);
+            if (l == k - 1) e = e + 1.0;
+            out[(size_t)(k - 1) * n + l] = e;
+            fprev = fk;
         }
     }
-    __syncwarp();
-    // ---- conv1 = I - dt (f(k-1) - f(k)) into LU
-    const double mdt = -A.dt;
-    for (int l = lane; l < n; l += 32)
-        for (int k = 1; k <= n; ++k) {
-            double v = mdt * (Y[(size_t)(k - 1) * n + l] - Y[(size_t)k * n + l]);
-            if (l == k - 1) v = v + 1.0;
-            LU[(size_t)(k - 1) * n + l] = v;
-        }
+}
+
+// shared memory of one warp (doubles): the matrix (conv1, then LU) and L^-1, n*n each
+__host__ __device__ __forceinline__ size_t warp_doubles(int n) { return 2 * (size_t)n * n; }
+
+__global__ void __launch_bounds__(WARPS * 32) k_convec_lu(CArgs A) {
+    extern __shared__ double smem[];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int c = blockIdx.x * WARPS + warp;
+    if (c >= A.ncol || !A.fresh[c]) return;
+    const int n = A.n;
+    double *LU = smem + (size_t)warp * warp_doubles(n);  // n x n
+    double *Y = LU + (size_t)n * n;                       // n x n
+    double *G = A.abuf + (size_t)c * n * n;
+    for (int e = lane; e < n * n; e += 32) LU[e] = G[e];
     __syncwarp();
     // ---- Crout LU, column by column: column cj receives the terms k = 0..cj-1 in order, each on
     // the rows below k (packed onto the lanes); then its part below the diagonal / the diagonal
@@ -201,7 +209,8 @@ __global__ void __launch_bounds__(WARPS * 32) k_convec_lu(CArgs A) {
         for (int k = 0; k < cj; ++k) {
             const double v = LU[(size_t)k * n + cj];  // U(k, cj), final
             if (v == 0.0) continue;                   // warp-uniform
-            for (int r = k + 1 + lane; r < n; r += 32) LU[(size_t)r * n + cj] = LU[(size_t)r * n + cj] - LU[(size_t)r * n + k] * v;
+            for (int r = k + 1 + lane; r < n; r += 32)
+                LU[(size_t)r * n + cj] = LU[(size_t)r * n + cj] - LU[(size_t)r * n + k] * v;
             __syncwarp();
         }
         const double d = LU[(size_t)cj * n + cj];
@@ -214,41 +223,25 @@ __global__ void __launch_bounds__(WARPS * 32) k_convec_lu(CArgs A) {
     for (int e = lane; e < n * n; e += 32) Y[e] = (e / n == e % n) ? 1.0 : 0.0;
     __syncwarp();
     for (int k = 0; k < n - 1; ++k) {
-        // the rows below k with a non-zero multiplier, in order
-        uint32_t rows0 = __ballot_sync(FULL_MASK, k + 1 + lane < n && LU[(size_t)(k + 1 + lane) * n + k] != 0.0);
-        uint32_t rows1 = __ballot_sync(FULL_MASK, k + 33 + lane < n && LU[(size_t)(k + 33 + lane) * n + k] != 0.0);
-        const int nr = __popc(rows0) + __popc(rows1);
+        const uint32_t rows0 = __ballot_sync(FULL_MASK, k + 1 + lane < n && LU[(size_t)(k + 1 + lane) * n + k] != 0.0);
+        const uint32_t rows1 = __ballot_sync(FULL_MASK, k + 33 + lane < n && LU[(size_t)(k + 33 + lane) * n + k] != 0.0);
+        const int n0 = __popc(rows0), nr = n0 + __popc(rows1);
         if (nr == 0) continue;
         const int w = k + 1;  // the columns 0..k
         for (int e = lane; e < nr * w; e += 32) {
-            int q = e / w;
-            const int col = e % w;
-            // the q-th set bit of (rows1:rows0)
-            int r;
-            const int n0 = __popc(rows0);
-            if (q < n0) {
-                uint32_t b = rows0;
-                for (int s = 0; s < q; ++s) b &= b - 1;
-                r = k + 1 + __ffs(b) - 1;
-            } else {
-                uint32_t b = rows1;
-                for (int s = 0; s < q - n0; ++s) b &= b - 1;
-                r = k + 33 + __ffs(b) - 1;
-            }
+            const int q = e / w, col = e % w;
+            uint32_t b = q < n0 ? rows0 : rows1;  // the q-th row of the set, in order
+            for (int s = q < n0 ? q : q - n0; s > 0; --s) b &= b - 1;
+            const int r = (q < n0 ? k + 1 : k + 33) + __ffs(b) - 1;
             Y[(size_t)r * n + col] = Y[(size_t)r * n + col] - LU[(size_t)r * n + k] * Y[(size_t)k * n + col];
         }
         __syncwarp();
     }
-    // ---- out: U (the upper triangle with the diagonal) and L^-1; the air mass it is made from
-    double *U = A.ubuf + (size_t)c * n * n, *X = A.inv + (size_t)c * n * n;
+    // ---- out: U (the upper triangle with the diagonal) over conv1, L^-1 into the inverse's place
+    double *X = A.inv + (size_t)c * n * n;
     for (int e = lane; e < n * n; e += 32) {
-        U[e] = LU[e];
+        G[e] = LU[e];
         X[e] = Y[e];
-    }
-    if (lane == 0) A.fresh[c] = 1;
-    if (A.cache_m) {
-        for (int l = lane; l < n; l += 32) A.cache_m[(size_t)c * n + l] = mc[l];
-        if (lane == 0) A.cache_tag[c] = *A.epoch;
     }
 }
 
@@ -260,7 +253,7 @@ __global__ void k_convec_apply(CArgs A) {
     double *X = live ? A.inv + (size_t)c * n * n : nullptr;
     // ---- back substitution of inverse column x: rows from the bottom, terms k in order
     if (live && A.fresh[c]) {
-        const double *U = A.ubuf + (size_t)c * n * n;
+        const double *U = A.abuf + (size_t)c * n * n;
         for (int r = n - 1; r >= 0; --r) {
             double a = X[(size_t)r * n + x];
             for (int k = r + 1; k < n; ++k) {
@@ -315,16 +308,24 @@ extern "C" int gb_convec(gb_ctx *ctx, const gb_view *m, const gb_view *rm, const
     A.cols = cols; A.ncol = ncol; A.n = lmax; A.nt = (int)rm->n[3];
     A.dt = dt;
     const size_t nn = (size_t)lmax * lmax;
-    // work space: U of every column, the fresh flags, and the inverses when there is no cache
-    const size_t doubles = nn * ncol + ((size_t)ncol + 1) / 2 + (cache_inv ? 0 : nn * ncol);
+    // work space: conv1 / U of every column, the chains, the fresh flags, and the inverses
+    // without a cache
+    const size_t nchain = (size_t)NCHAIN * (lmax + 1) * ncol, nflag = ((size_t)ncol + 1) / 2;
+    const size_t doubles = nn * ncol + nchain + nflag + (cache_inv ? 0 : nn * ncol);
     double *w = gb_work(ctx, doubles * sizeof(double));
     if (!w) return GB_ECUDA;
-    A.ubuf = w;
-    A.fresh = reinterpret_cast<int32_t *>(w + nn * ncol);
-    A.inv = cache_inv ? cache_inv : w + nn * ncol + ((size_t)ncol + 1) / 2;
+    A.abuf = w;
+    A.chain = w + nn * ncol;
+    A.fresh = reinterpret_cast<int32_t *>(A.chain + nchain);
+    A.inv = cache_inv ? cache_inv : A.chain + nchain + nflag;
     A.cache_m = cache_inv ? cache_m : nullptr;
     A.cache_tag = cache_tag;
     A.epoch = epoch;
+    k_convec_chains<<<(ncol + MATRIX_THREADS - 1) / MATRIX_THREADS, MATRIX_THREADS, 0, ctx->stream>>>(A);
+    if (int rc = gb_after_launch(ctx, "convec_chains")) return rc;
+    const int64_t nel = (int64_t)ncol * lmax;
+    k_convec_matrix<<<(unsigned)((nel + MATRIX_THREADS - 1) / MATRIX_THREADS), MATRIX_THREADS, 0, ctx->stream>>>(A);
+    if (int rc = gb_after_launch(ctx, "convec_matrix")) return rc;
     const size_t smem = (size_t)WARPS * warp_doubles(lmax) * sizeof(double);
     GB_CHECK_CUDA(cudaFuncSetAttribute(k_convec_lu, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     k_convec_lu<<<(ncol + WARPS - 1) / WARPS, WARPS * 32, smem, ctx->stream>>>(A);
