@@ -59,7 +59,7 @@ __device__ int row_search(double *m_s, double *mx_s, double *a_s, int n, bool he
             for (int k = k0 + lane; k <= k1; k += GB_WARP) {
                 double f = a_s[k];
                 int up = (f >= 0.0) ? (k == 0 ? n - 1 : k - 1) : (k == n ? 0 : k);
-                double c = fabs(f / mx_s[up]);
+                double c = gb_abs(f / mx_s[up]);
                 lok = lok && (c < 1.0);
                 cmax = (c > cmax) ? c : cmax;
             }

@@ -48,7 +48,7 @@ __device__ bool z_trial(const ZArgs &A, int i, int j, int n, double *mx, double 
         for (int k = 1 + lane; k < lm; k += GB_WARP) {
             double c = cf[k];
             double mu = (c >= 0.0) ? mx[k - 1] : mx[k];
-            lok = lok && (fabs(c / mu) < 1.0);
+            lok = lok && (gb_abs(c / mu) < 1.0);
         }
         if (!__all_sync(FULL_MASK, lok)) return false;
         if (!scope) continue;  // outside the scope the trial mass is never advanced

@@ -48,6 +48,7 @@ struct CArgs {
     double *abuf;        // ncol * n * n work space: conv1, then U, of the columns made here
     double *chain;       // ncol * 10 (n+1) work space: the chains and quotients of each column
     int32_t *fresh;      // ncol work space: 1 where this call makes the column's inverse
+    int32_t *rend;       // ncol * n work space: per row of U, one past its last non-zero
     double *cache_m;     // ncol * n, or null (no reuse)
     int32_t *cache_tag;  // ncol
     const int32_t *epoch;
@@ -60,7 +61,9 @@ __device__ __forceinline__ double &AT(const DV &v, int64_t i, int64_t j, int64_t
 __device__ __forceinline__ double &AT4(const DV &v, int64_t i, int64_t j, int64_t l, int64_t t) {
     return v.p[i * v.s0 + j * v.s1 + l * v.s2 + t * v.s3];
 }
-__device__ __forceinline__ double max0(double x) { return isnan(x) ? x : (0.0 > x ? 0.0 : x); }
+__device__ __forceinline__ double max0(double x) { return gb_isnan(x) ? x : (0.0 > x ? 0.0 : x); }
+// x == 0.0 (either sign), tested on the integer pipe: the FP64 pipe is kept for arithmetic
+__device__ __forceinline__ bool is_zero(double x) { return (__double_as_longlong(x) << 1) == 0; }
 
 // the work space's per-column chains amu, zu, amd, zd and the matrix's quotients qeu, qed, qamu,
 // qamd, qdk1, qdk2 (n+1 each, indexed by level k = 1..n)
@@ -204,11 +207,17 @@ __global__ void __launch_bounds__(WARPS * 32) k_convec_lu(CArgs A) {
     for (int e = lane; e < n * n; e += 32) LU[e] = G[e];
     __syncwarp();
     // ---- Crout LU, column by column: column cj receives the terms k = 0..cj-1 in order, each on
-    // the rows below k (packed onto the lanes); then its part below the diagonal / the diagonal
+    // the rows below k (packed onto the lanes); then its part below the diagonal / the diagonal.
+    // Above the column's first non-zero the terms' multipliers U(k, cj) are zeros that stay zero
+    // (every term that could change them is itself skipped), so the terms start there.
     for (int cj = 0; cj < n; ++cj) {
-        for (int k = 0; k < cj; ++k) {
+        const uint32_t nz0 = __ballot_sync(FULL_MASK, lane <= cj && lane < n && !is_zero(LU[(size_t)lane * n + cj]));
+        const uint32_t nz1 =
+            __ballot_sync(FULL_MASK, lane + 32 <= cj && lane + 32 < n && !is_zero(LU[(size_t)(lane + 32) * n + cj]));
+        const int first = nz0 ? __ffs(nz0) - 1 : (nz1 ? 32 + __ffs(nz1) - 1 : cj);
+        for (int k = first; k < cj; ++k) {
             const double v = LU[(size_t)k * n + cj];  // U(k, cj), final
-            if (v == 0.0) continue;                   // warp-uniform
+            if (is_zero(v)) continue;                 // warp-uniform
             for (int r = k + 1 + lane; r < n; r += 32)
                 LU[(size_t)r * n + cj] = LU[(size_t)r * n + cj] - LU[(size_t)r * n + k] * v;
             __syncwarp();
@@ -223,8 +232,8 @@ __global__ void __launch_bounds__(WARPS * 32) k_convec_lu(CArgs A) {
     for (int e = lane; e < n * n; e += 32) Y[e] = (e / n == e % n) ? 1.0 : 0.0;
     __syncwarp();
     for (int k = 0; k < n - 1; ++k) {
-        const uint32_t rows0 = __ballot_sync(FULL_MASK, k + 1 + lane < n && LU[(size_t)(k + 1 + lane) * n + k] != 0.0);
-        const uint32_t rows1 = __ballot_sync(FULL_MASK, k + 33 + lane < n && LU[(size_t)(k + 33 + lane) * n + k] != 0.0);
+        const uint32_t rows0 = __ballot_sync(FULL_MASK, k + 1 + lane < n && !is_zero(LU[(size_t)(k + 1 + lane) * n + k]));
+        const uint32_t rows1 = __ballot_sync(FULL_MASK, k + 33 + lane < n && !is_zero(LU[(size_t)(k + 33 + lane) * n + k]));
         const int n0 = __popc(rows0), nr = n0 + __popc(rows1);
         if (nr == 0) continue;
         const int w = k + 1;  // the columns 0..k
@@ -237,11 +246,21 @@ __global__ void __launch_bounds__(WARPS * 32) k_convec_lu(CArgs A) {
         }
         __syncwarp();
     }
-    // ---- out: U (the upper triangle with the diagonal) over conv1, L^-1 into the inverse's place
+    // ---- out: U (the upper triangle with the diagonal) over conv1, L^-1 into the inverse's place,
+    // and for each row r of U one past its last non-zero right of the diagonal (the back
+    // substitution's terms end there: the rest are zeros it would skip)
     double *X = A.inv + (size_t)c * n * n;
     for (int e = lane; e < n * n; e += 32) {
         G[e] = LU[e];
         X[e] = Y[e];
+    }
+    int32_t *rend = A.rend + (size_t)c * n;
+    for (int r = 0; r < n; ++r) {
+        const uint32_t b0 = __ballot_sync(FULL_MASK, lane > r && lane < n && !is_zero(LU[(size_t)r * n + lane]));
+        const uint32_t b1 =
+            __ballot_sync(FULL_MASK, lane + 32 > r && lane + 32 < n && !is_zero(LU[(size_t)r * n + lane + 32]));
+        const int last = b1 ? 63 - __clz(b1) : (b0 ? 31 - __clz(b0) : r);
+        if (lane == 0) rend[r] = last + 1;
     }
 }
 
@@ -254,11 +273,12 @@ __global__ void k_convec_apply(CArgs A) {
     // ---- back substitution of inverse column x: rows from the bottom, terms k in order
     if (live && A.fresh[c]) {
         const double *U = A.abuf + (size_t)c * n * n;
+        const int32_t *rend = A.rend + (size_t)c * n;
         for (int r = n - 1; r >= 0; --r) {
             double a = X[(size_t)r * n + x];
-            for (int k = r + 1; k < n; ++k) {
+            for (int k = r + 1; k < rend[r]; ++k) {
                 const double w = U[(size_t)r * n + k];
-                if (w == 0.0) continue;
+                if (is_zero(w)) continue;
                 a = a - w * X[(size_t)k * n + x];
             }
             X[(size_t)r * n + x] = a / U[(size_t)r * n + r];
@@ -311,13 +331,15 @@ extern "C" int gb_convec(gb_ctx *ctx, const gb_view *m, const gb_view *rm, const
     // work space: conv1 / U of every column, the chains, the fresh flags, and the inverses
     // without a cache
     const size_t nchain = (size_t)NCHAIN * (lmax + 1) * ncol, nflag = ((size_t)ncol + 1) / 2;
-    const size_t doubles = nn * ncol + nchain + nflag + (cache_inv ? 0 : nn * ncol);
+    const size_t nrend = ((size_t)ncol * lmax + 1) / 2;
+    const size_t doubles = nn * ncol + nchain + nflag + nrend + (cache_inv ? 0 : nn * ncol);
     double *w = gb_work(ctx, doubles * sizeof(double));
     if (!w) return GB_ECUDA;
     A.abuf = w;
     A.chain = w + nn * ncol;
     A.fresh = reinterpret_cast<int32_t *>(A.chain + nchain);
-    A.inv = cache_inv ? cache_inv : A.chain + nchain + nflag;
+    A.rend = reinterpret_cast<int32_t *>(A.chain + nchain + nflag);
+    A.inv = cache_inv ? cache_inv : A.chain + nchain + nflag + nrend;
     A.cache_m = cache_inv ? cache_m : nullptr;
     A.cache_tag = cache_tag;
     A.epoch = epoch;

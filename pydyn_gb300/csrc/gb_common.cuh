@@ -64,22 +64,35 @@ static inline DV dv(const gb_view *v) {
     return d;
 }
 
+// ------------------------------------------------------------------ bit tests
+// isnan, |x| and -x on the integer pipe: on this GPU the FP64 pipe is the scarce unit, and a
+// compare or a sign change issued there costs as much as a multiply.  Exact for every input.
+__device__ __forceinline__ bool gb_isnan(double x) {
+    return (unsigned long long)(__double_as_longlong(x) & 0x7fffffffffffffffLL) > 0x7ff0000000000000ULL;
+}
+__device__ __forceinline__ double gb_abs(double x) {
+    return __longlong_as_double(__double_as_longlong(x) & 0x7fffffffffffffffLL);
+}
+__device__ __forceinline__ double gb_neg(double x) {
+    return __longlong_as_double(__double_as_longlong(x) ^ (long long)0x8000000000000000ULL);
+}
+
 // ------------------------------------------------------------------ NumPy's element rules
 // np.clip(s, -|r|, |r|) exactly as NumPy evaluates it: a NaN in s wins, then max with the lower
 // bound ((s > lo) ? s : lo), then a NaN wins again, then min with the upper bound.
 __device__ __forceinline__ double np_limit(double s, double r) {
-    double hi = fabs(r);
-    double lo = -hi;
-    double t = isnan(s) ? s : (s > lo ? s : lo);
-    return isnan(t) ? t : (t < hi ? t : hi);
+    double hi = gb_abs(r);
+    double lo = gb_neg(hi);
+    double t = gb_isnan(s) ? s : (s > lo ? s : lo);
+    return gb_isnan(t) ? t : (t < hi ? t : hi);
 }
 
 // np.maximum(a, b): NaN in a, else NaN in b, else (a > b ? a : b).
 __device__ __forceinline__ double np_max(double a, double b) {
-    return isnan(a) ? a : (isnan(b) ? b : (a > b ? a : b));
+    return gb_isnan(a) ? a : (gb_isnan(b) ? b : (a > b ? a : b));
 }
 __device__ __forceinline__ double np_min(double a, double b) {
-    return isnan(a) ? a : (isnan(b) ? b : (a < b ? a : b));
+    return gb_isnan(a) ? a : (gb_isnan(b) ? b : (a < b ? a : b));
 }
 
 // Tracer fluxes of the slopes scheme through one face (pydyn kernels.py:75-84): the flux,
