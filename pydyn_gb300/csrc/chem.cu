@@ -52,14 +52,38 @@ struct TropEdges {
     __device__ double operator[](int k) const { return k < n ? p[k * s] : 0.0; }
 };
 
-// rebin_levels(ip_mix) of one output layer [top, bot] from the edges ip[0..nip]
+// The input layers that can overlap the output layer [top, bot] of strictly descending edges
+// ip[0..nip] (chem.py:74-75): first = #{k : ip[k+1] >= bot}, last = #{k : ip[k] > top}.  Both
+// conditions hold on a prefix of k, so each count is a binary search (the checked order is what
+// makes them prefixes; a NaN bound fails every test and counts 0 either way).
 template <class Edges>
-__device__ double rebin_layer(const Edges &ip, int nip, const double *data, int64_t stride, double bot, double top) {
-    int first = 0, last = 0;
-    for (int k = 0; k < nip; ++k) {
-        first += ip[k + 1] >= bot;
-        last += ip[k] > top;
+__device__ void rebin_span(const Edges &ip, int nip, double bot, double top, int &first, int &last) {
+    int a = 0, b = nip;
+    while (a < b) {
+        const int mid = (a + b) >> 1;
+        if (ip[mid + 1] >= bot)
+            a = mid + 1;
+        else
+            b = mid;
     }
+    first = a;
+    a = 0;
+    b = nip;
+    while (a < b) {
+        const int mid = (a + b) >> 1;
+        if (ip[mid] > top)
+            a = mid + 1;
+        else
+            b = mid;
+    }
+    last = a;
+}
+
+// rebin_levels(ip_mix) of one output layer [top, bot] from the edges ip[0..nip], its input
+// layers first..last-1 (rebin_span)
+template <class Edges>
+__device__ double rebin_layer(const Edges &ip, int first, int last, const double *data, int64_t stride, double bot,
+                              double top) {
     double overlap = 0.0;
     for (int k = first; k < last; ++k) {
         const double thickness = np_min(bot, ip[k]) - np_max(top, ip[k + 1]);
@@ -117,7 +141,8 @@ __global__ void __launch_bounds__(CELL_THREADS) k_chem(CArgs A) {
     TropEdges tedges{nullptr, 0, 0};
     if (A.has_trop) {
         tedges = TropEdges{&E3(A.pltrop, i, j, 0), A.pltrop.s2, nt};
-        for (int k = 0; k < nt; ++k) ok = ok && (tedges[k + 1] - tedges[k] < 0.0);
+        if (l == 0)  // the column's tropospheric edges, checked once
+            for (int k = 0; k < nt; ++k) ok = ok && (tedges[k + 1] - tedges[k] < 0.0);
     }
     if (!ok) {
         raise_status(A.ctl, GB_ELEVELS);
@@ -128,14 +153,24 @@ __global__ void __launch_bounds__(CELL_THREADS) k_chem(CArgs A) {
 
     {
         const bool below = bot > edges[0];
-        const double s_oh = below ? doh[0] : rebin_layer(edges, ns, doh, A.soh.s1, bot, top);
-        const double s_cl = below ? dcl[0] : rebin_layer(edges, ns, dcl, A.scl.s1, bot, top);
-        const double s_od = below ? dod[0] : rebin_layer(edges, ns, dod, A.sod.s1, bot, top);
+        double s_oh = doh[0], s_cl = dcl[0], s_od = dod[0];
+        if (!below) {  // the three zonal columns share their edges: one overlap search
+            int first, last;
+            rebin_span(edges, ns, bot, top, first, last);
+            s_oh = rebin_layer(edges, first, last, doh, A.soh.s1, bot, top);
+            s_cl = rebin_layer(edges, first, last, dcl, A.scl.s1, bot, top);
+            s_od = rebin_layer(edges, first, last, dod, A.sod.s1, bot, top);
+        }
         const double T = E3(A.temper, i, j, l);
         double trop_cl = 0.0;
         if (A.has_trop) {
             const double *dtr = &E3(A.cltrop, i, j, 0);
-            const double v = bot > tedges[0] ? dtr[0] : rebin_layer(tedges, nt, dtr, A.cltrop.s2, bot, top);
+            double v = dtr[0];
+            if (!(bot > tedges[0])) {
+                int first, last;
+                rebin_span(tedges, nt, bot, top, first, last);
+                v = rebin_layer(tedges, first, last, dtr, A.cltrop.s2, bot, top);
+            }
             const double krate = (2.36e-12 * gbm_pow(T / 298.0, 1.37)) * gbm_exp(-939.0 / T);
             trop_cl = (v * krate) * A.cl_scale;
         }

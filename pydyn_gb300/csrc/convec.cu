@@ -3,11 +3,12 @@
 //
 // Four launches, shaped so that the FP64 pipe -- this GPU's scarcest unit -- issues with its
 // lanes full:
-//   k_convec_chains  one thread per owned column: whether its kept inverse still holds, the
-//                    updraft and downdraft chains, and every division of its matrix, once
-//   k_convec_matrix  one thread per (column, column l of its matrix): conv1(., l) = I - dt
-//                    (f(k-1, l) - f(k, l)), the downdraft chain of f down from the diagonal and
-//                    the updraft chain up from it -- into a work space
+//   k_convec_chains  one thread per owned column: whether its kept inverse still holds, and the
+//                    updraft and downdraft chains
+//   k_convec_matrix  one thread per (column, column l of its matrix): the quotients that column
+//                    uses (each division once), conv1(., l) = I - dt (f(k-1, l) - f(k, l)), the
+//                    downdraft chain of f down from the diagonal and the updraft chain up from
+//                    it -- into a work space
 //   k_convec_lu      one warp per column whose inverse is made: Crout LU column by column (the
 //                    rows a term updates packed onto the lanes), then L^-1 by forward
 //                    substitution (row k's terms applied to every later row at once, the
@@ -46,7 +47,7 @@ struct CArgs {
     double dt;
     double *inv;         // ncol * n * n: the inverses (the cache's, or the work space's)
     double *abuf;        // ncol * n * n work space: conv1, then U, of the columns made here
-    double *chain;       // ncol * 10 (n+1) work space: the chains and quotients of each column
+    double *chain;       // ncol * 4 (n+1) work space: the updraft and downdraft chains
     int32_t *fresh;      // ncol work space: 1 where this call makes the column's inverse
     int32_t *rend;       // ncol * n work space: per row of U, one past its last non-zero
     double *cache_m;     // ncol * n, or null (no reuse)
@@ -65,13 +66,11 @@ __device__ __forceinline__ double max0(double x) { return gb_isnan(x) ? x : (0.0
 // x == 0.0 (either sign), tested on the integer pipe: the FP64 pipe is kept for arithmetic
 __device__ __forceinline__ bool is_zero(double x) { return (__double_as_longlong(x) << 1) == 0; }
 
-// the work space's per-column chains amu, zu, amd, zd and the matrix's quotients qeu, qed, qamu,
-// qamd, qdk1, qdk2 (n+1 each, indexed by level k = 1..n)
-constexpr int NCHAIN = 10;
+// the work space's per-column chains amu, zu, amd, zd (n+1 each, indexed by level k = 0..n)
+constexpr int NCHAIN = 4;
 __device__ __forceinline__ double *chains(const CArgs &A, int c) { return A.chain + (size_t)c * NCHAIN * (A.n + 1); }
 
-// thread per column: whether the kept inverse still holds; the updraft and downdraft chains; every
-// division of the column's matrix, once
+// thread per column: whether the kept inverse still holds; the updraft and downdraft chains
 __global__ void __launch_bounds__(MATRIX_THREADS) k_convec_chains(CArgs A) {
     const int c = blockIdx.x * blockDim.x + threadIdx.x;
     if (c >= A.ncol) return;
@@ -120,20 +119,6 @@ __global__ void __launch_bounds__(MATRIX_THREADS) k_convec_chains(CArgs A) {
         amd[k - 1] = md;
         zd[k] = act ? z : -1.0;
     }
-    double *qeu = zd + (n + 1), *qed = qeu + (n + 1), *qamu = qed + (n + 1), *qamd = qamu + (n + 1);
-    double *qdk1 = qamd + (n + 1), *qdk2 = qdk1 + (n + 1);
-    for (int k = 1; k <= n; ++k) {
-        const double m0 = AT(A.m, i, j, k - 1);
-        qeu[k] = AT(A.entu, i, j, k - 1) / m0;
-        qed[k] = -AT(A.entd, i, j, k - 1) / m0;
-        if (k <= n - 1) {
-            const double m1 = AT(A.m, i, j, k);
-            qamu[k] = amu[k] / m1;
-            qamd[k] = amd[k] / m0;
-            qdk1[k] = AT(A.dkg, i, j, k - 1) / m0;
-            qdk2[k] = AT(A.dkg, i, j, k - 1) / m1;
-        }
-    }
 }
 
 // thread per (column, column l of its matrix): conv1(., l).  f(k, l), k = 0..n: the downdraft
@@ -146,9 +131,16 @@ __global__ void __launch_bounds__(MATRIX_THREADS) k_convec_matrix(CArgs A) {
     if (t >= (int64_t)A.ncol * n) return;
     const int c = (int)(t / n), l = (int)(t % n);
     if (!A.fresh[c]) return;
-    const double *zu = chains(A, c) + (n + 1), *zd = zu + 2 * (n + 1);
-    const double *qeu = zd + (n + 1), *qed = qeu + (n + 1), *qamu = qed + (n + 1), *qamd = qamu + (n + 1);
-    const double *qdk1 = qamd + (n + 1), *qdk2 = qdk1 + (n + 1);
+    const double *amu = chains(A, c), *zu = amu + (n + 1), *amd = zu + (n + 1), *zd = amd + (n + 1);
+    const int i = A.cols[2 * c], j = A.cols[2 * c + 1];
+    // the quotients this column of the matrix uses, each divided once: at level k = l + 1 the
+    // chain starts (qed, qeu) and the sub-diagonal terms (qamd, qdk1); at k = l the diagonal's
+    // (qamu, qdk2)
+    const double ml = AT(A.m, i, j, l);
+    const double qed = -AT(A.entd, i, j, l) / ml, qeu = AT(A.entu, i, j, l) / ml;
+    const bool sub = l + 1 <= n - 1, dia = l >= 1;
+    const double qamd = sub ? amd[l + 1] / ml : 0.0, qdk1 = sub ? AT(A.dkg, i, j, l) / ml : 0.0;
+    const double qamu = dia ? amu[l] / ml : 0.0, qdk2 = dia ? AT(A.dkg, i, j, l - 1) / ml : 0.0;
     double fd[NMAX];
     double *out = A.abuf + (size_t)c * n * n;
     const double mdt = -A.dt;
@@ -158,7 +150,7 @@ __global__ void __launch_bounds__(MATRIX_THREADS) k_convec_matrix(CArgs A) {
             const double z = zd[r + 1];
             const bool act = z >= 0.0;
             if (r == l)
-                v = act ? qed[r + 1] * z : 0.0;
+                v = act ? qed * z : 0.0;
             else
                 v = act ? v * z : 0.0;
             fd[r] = v;
@@ -170,18 +162,18 @@ __global__ void __launch_bounds__(MATRIX_THREADS) k_convec_matrix(CArgs A) {
             if (l < k - 1)
                 u = act ? u * z : 0.0;
             else if (l == k - 1)
-                u = act ? qeu[k] * z : 0.0;
+                u = act ? qeu * z : 0.0;
             else
                 u = 0.0;
             double fk = 0.0;
             if (k <= n - 1) {
                 double f = u + (k <= l ? fd[k] : 0.0);
-                if (l == k) f = f - qamu[k];
+                if (l == k) f = f - qamu;
                 if (l == k - 1) {
-                    f = f - qamd[k];
-                    f = f + qdk1[k];
+                    f = f - qamd;
+                    f = f + qdk1;
                 }
-                if (l == k) f = f - qdk2[k];
+                if (l == k) f = f - qdk2;
                 fk = f;
             }
             double e = mdt * (fprev - fk);
