@@ -141,9 +141,30 @@ __global__ void __launch_bounds__(MATRIX_THREADS) k_convec_matrix(CArgs A) {
     const bool sub = l + 1 <= n - 1, dia = l >= 1;
     const double qamd = sub ? amd[l + 1] / ml : 0.0, qdk1 = sub ? AT(A.dkg, i, j, l) / ml : 0.0;
     const double qamu = dia ? amu[l] / ml : 0.0, qdk2 = dia ? AT(A.dkg, i, j, l - 1) / ml : 0.0;
-    double fd[NMAX];
     double *out = A.abuf + (size_t)c * n * n;
     const double mdt = -A.dt;
+    const int top = A.top[i * A.ts0 + j * A.ts1], lfs = A.lfs[i * A.ts0 + j * A.ts1];
+    if (top <= 0 && lfs <= 1) {
+        // no cloud: every chain level is inactive, so u and fd are +0 throughout and f(k, l) is
+        // +0 except f(l, l) = (+0 - qamu) - qdk2 and f(l+1, l) = (+0 - qamd) + qdk1 -- the
+        // general statements below with their zero operands; conv1(., l) is then the constant
+        // -dt (+0 - +0) off the three bands
+        const double fll = (dia && l <= n - 1) ? (0.0 - qamu) - qdk2 : 0.0;
+        const double fl1 = sub ? (0.0 - qamd) + qdk1 : 0.0;
+        const double off = mdt * (0.0 - 0.0);
+        for (int k = 1; k <= n; ++k) {
+            double e = off;
+            if (k >= l && k <= l + 2) {
+                const double fprev = (k - 1 == l) ? fll : (k - 1 == l + 1 ? fl1 : 0.0);
+                const double fk = (k == l) ? fll : (k == l + 1 && k <= n - 1 ? fl1 : 0.0);
+                e = mdt * (fprev - fk);
+                if (l == k - 1) e = e + 1.0;
+            }
+            out[(size_t)(k - 1) * n + l] = e;
+        }
+        return;
+    }
+    double fd[NMAX];
     {
         double v = 0.0;
         for (int r = l; r >= 1; --r) {  // fd(r, l), r = k - 1 with k from l + 1 down to 2
