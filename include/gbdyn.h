@@ -245,14 +245,22 @@ int gb_loss_rates(gb_ctx *ctx, const gb_view *temper, const gb_view *phlb, const
 /* chemistry_region (zoom/physics.py:67-78 with chem.loss_rates, decay, apply_decay): the same
  * inputs; on the listed columns cols (ncol, 2) int32 0-based (i, j), device, rm, rxm, rym, rzm
  * (im, jm, lm, nt) of every tracer t whose bit t-1 is set in tracer_mask are multiplied by the
- * cell's decay.  The other columns are left as they are (the reference's factor 1.0). */
+ * cell's decay.  The other columns are left as they are (the reference's factor 1.0).  krates:
+ * the rate constants of temper made by gb_chem_krates (the same values), or NULL. */
 int gb_chemistry(gb_ctx *ctx, const gb_view *temper, const gb_view *phlb, const double *lat,
                  const gb_view *strat_press, const gb_view *strat_oh, const gb_view *strat_cl,
                  const gb_view *strat_od, const gb_view *oh_3d, const gb_view *pl_trop,
                  const gb_view *cl_trop, const gb_view *soil, const double *oh_factor,
                  double oh_scale, double cl_scale, double o1d_scale, double soil_rate,
                  double dt_sec, const int32_t *cols, int ncol, uint32_t tracer_mask,
-                 const gb_view *rm, const gb_view *rxm, const gb_view *rym, const gb_view *rzm);
+                 const gb_view *rm, const gb_view *rxm, const gb_view *rym, const gb_view *rzm,
+                 const gb_view *krates);
+/* The temperature's rate constants of chem.loss_rates (chem.py:137-140) into krates
+ * (im, jm, lm, 2): [.., 0] = 2.45e-12 exp(-1775 / T), [.., 1] = (2.36e-12 (T / 298)^1.37)
+ * exp(-939 / T), on the listed columns (cols NULL: every column).  A run whose temperature holds
+ * for a step makes them once per step for all of its chemistry calls. */
+int gb_chem_krates(gb_ctx *ctx, const gb_view *temper, const int32_t *cols, int ncol,
+                   const gb_view *krates);
 /* sources_region (zoom/physics.py:55-64, emission_data do_add_2d): on the listed columns
  * cols (ncol, 2) int32 device, rm(level, tracer) += x and rzm(level, tracer) -= x, level and
  * tracer 1-based, x = (flux(i, j) area(j)) scale with area (jm) device, or x = flux(i, j) when

@@ -33,6 +33,7 @@ struct CArgs {
     uint32_t tracer_mask;       // gb_chemistry: bit t-1 for tracer t
     int apply;
     double *edges, *trop;       // work space: (jm, ns + 1) zonal edges, (jm) tropopause
+    DV krates;                  // (im, jm, lm, 2) the rate constants of the temperature, or absent
     gb_ctl *ctl;
 };
 
@@ -43,6 +44,11 @@ __device__ __forceinline__ double &E3(const DV &v, int64_t a, int64_t b, int64_t
 __device__ __forceinline__ double &E4(const DV &v, int64_t a, int64_t b, int64_t c, int64_t d) {
     return v.p[a * v.s0 + b * v.s1 + c * v.s2 + d * v.s3];
 }
+
+// the rate constants of a cell's temperature (chem.py:137-140): OH, 2.45e-12 exp(-1775 / T), and
+// tropospheric Cl, (2.36e-12 (T / 298)^1.37) exp(-939 / T)
+__device__ __forceinline__ double krate_ohf(double T) { return 2.45e-12 * gbm_exp(-1775.0 / T); }
+__device__ __forceinline__ double krate_cl(double T) { return (2.36e-12 * gbm_pow(T / 298.0, 1.37)) * gbm_exp(-939.0 / T); }
 
 // the tropospheric Cl column's edges: pl_trop(i, j, 0 .. ntrop-1), then 0 (chem.py:135)
 struct TropEdges {
@@ -171,12 +177,12 @@ __global__ void __launch_bounds__(CELL_THREADS) k_chem(CArgs A) {
                 rebin_span(tedges, nt, bot, top, first, last);
                 v = rebin_layer(tedges, first, last, dtr, A.cltrop.s2, bot, top);
             }
-            const double krate = (2.36e-12 * gbm_pow(T / 298.0, 1.37)) * gbm_exp(-939.0 / T);
+            const double krate = A.krates.p ? E4(A.krates, i, j, l, 1) : krate_cl(T);
             trop_cl = (v * krate) * A.cl_scale;
         }
         double oh = E3(A.oh3d, i, j, l);
         if (A.oh_factor) oh = oh * A.oh_factor[i];
-        const double krate_oh = 2.45e-12 * gbm_exp(-1775.0 / T);
+        const double krate_oh = A.krates.p ? E4(A.krates, i, j, l, 0) : krate_ohf(T);
         const double spiv = (krate_oh * oh) * A.oh_scale;
         const bool strat = bot < trop;
         const double L0 = strat ? s_oh : spiv;
@@ -293,12 +299,13 @@ extern "C" int gb_chemistry(gb_ctx *ctx, const gb_view *temper, const gb_view *p
                             const gb_view *cl_trop, const gb_view *soil, const double *oh_factor, double oh_scale,
                             double cl_scale, double o1d_scale, double soil_rate, double dt_sec, const int32_t *cols,
                             int ncol, uint32_t tracer_mask, const gb_view *rm, const gb_view *rxm,
-                            const gb_view *rym, const gb_view *rzm) {
+                            const gb_view *rym, const gb_view *rzm, const gb_view *krates) {
     if (!ctx || !rm || !rxm || !rym || !rzm || (ncol > 0 && !cols) || ncol < 0) return GB_EARG;
     CArgs A{};
     if (int rc = setup_chem(A, temper, phlb, lat, strat_press, strat_oh, strat_cl, strat_od, oh_3d, pl_trop, cl_trop,
                             soil, oh_factor, oh_scale, cl_scale, o1d_scale, soil_rate, dt_sec))
         return rc;
+    A.krates = krates ? dv(krates) : DV{};
     if (rm->n[3] < 32 && (tracer_mask >> rm->n[3]) != 0) {
         gb_set_error("gb_chemistry: a tracer of the mask is beyond the arrays' nt");
         return GB_EARG;
@@ -309,6 +316,35 @@ extern "C" int gb_chemistry(gb_ctx *ctx, const gb_view *temper, const gb_view *p
     A.cols = cols;
     A.ncol = ncol;
     return launch_chem(ctx, A);
+}
+
+namespace {
+__global__ void k_chem_krates(DV temper, DV krates, const int32_t *cols, int64_t ncol, int jm, int lm) {
+    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= ncol * lm) return;
+    const int64_t c = t / lm;
+    const int l = (int)(t % lm);
+    const int i = cols ? cols[2 * c] : (int)(c / jm), j = cols ? cols[2 * c + 1] : (int)(c % jm);
+    const double T = E3(temper, i, j, l);
+    E4(krates, i, j, l, 0) = krate_ohf(T);
+    E4(krates, i, j, l, 1) = krate_cl(T);
+}
+}  // namespace
+
+extern "C" int gb_chem_krates(gb_ctx *ctx, const gb_view *temper, const int32_t *cols, int ncol,
+                              const gb_view *krates) {
+    if (!ctx || !temper || !krates || ncol < 0) return GB_EARG;
+    if (krates->n[0] != temper->n[0] || krates->n[1] != temper->n[1] || krates->n[2] != temper->n[2] ||
+        krates->n[3] != 2) {
+        gb_set_error("gb_chem_krates: krates must be (im, jm, lm, 2) over temper's (im, jm, lm)");
+        return GB_EARG;
+    }
+    const int64_t n = cols ? (int64_t)ncol : temper->n[0] * temper->n[1];
+    const int lm = (int)temper->n[2];
+    if (n == 0) return GB_OK;
+    k_chem_krates<<<(unsigned)((n * lm + CELL_THREADS - 1) / CELL_THREADS), CELL_THREADS, 0, ctx->stream>>>(
+        dv(temper), dv(krates), cols, n, (int)temper->n[1], lm);
+    return gb_after_launch(ctx, "chem_krates");
 }
 
 extern "C" int gb_sources(gb_ctx *ctx, const gb_view *rm, const gb_view *rzm, const gb_view *flux,

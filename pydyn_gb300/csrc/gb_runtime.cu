@@ -253,15 +253,19 @@ __device__ __forceinline__ int64_t off4(const DV &v, int64_t i0, int64_t i1, int
     return i0 * v.s0 + i1 * v.s1 + i2 * v.s2 + i3 * v.s3;
 }
 
-__global__ void k_box(int op, DV d, DV a, DV b, double x, double y, int64_t total) {
-    int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-    int64_t stride = (int64_t)gridDim.x * blockDim.x;
+// IDX: the flat index type -- 32-bit whenever the box has fewer than 2^31 elements, so that its
+// decomposition into (i0, i1, i2, i3) takes three 32-bit divisions, not 64-bit ones
+template <typename IDX>
+__global__ void k_box(int op, DV d, DV a, DV b, double x, double y, IDX total) {
+    IDX k = (IDX)(blockIdx.x * (int64_t)blockDim.x + threadIdx.x);
+    const IDX stride = (IDX)((int64_t)gridDim.x * blockDim.x);
+    const IDX n1 = (IDX)d.n1, n2 = (IDX)d.n2, n3 = (IDX)d.n3;
     for (; k < total; k += stride) {
-        int64_t r = k;
-        int64_t i3 = r % d.n3; r /= d.n3;
-        int64_t i2 = r % d.n2; r /= d.n2;
-        int64_t i1 = r % d.n1; r /= d.n1;
-        int64_t i0 = r;
+        IDX r = k;
+        const IDX i3 = r % n3; r /= n3;
+        const IDX i2 = r % n2; r /= n2;
+        const IDX i1 = r % n1; r /= n1;
+        const IDX i0 = r;
         double va = (op != 3) ? a.p[off4(a, i0, i1, i2, i3)] : 0.0;
         double vb = (op >= 4 && op <= 7) || op == 9 ? b.p[off4(b, i0, i1, i2, i3)] : 0.0;
         double out;
@@ -298,7 +302,10 @@ extern "C" int gb_box(gb_ctx *ctx, int op, const gb_view *dst, const gb_view *a,
     DV vb = b ? dv(b) : d;
     int64_t total = d.n0 * d.n1 * d.n2 * d.n3;
     if (total <= 0) return GB_OK;
-    k_box<<<launch_grid(total), 256, 0, ctx->stream>>>(op, d, va, vb, x, y, total);
+    if (total < (int64_t)1 << 31)
+        k_box<uint32_t><<<launch_grid(total), 256, 0, ctx->stream>>>(op, d, va, vb, x, y, (uint32_t)total);
+    else
+        k_box<int64_t><<<launch_grid(total), 256, 0, ctx->stream>>>(op, d, va, vb, x, y, total);
     return gb_after_launch(ctx, "box");
 }
 

@@ -258,8 +258,16 @@ class DevArray:
                                   None if vb is None else ctypes.byref(vb), float(x), float(y)), "gb_box")  # fmt: skip
 
     def assign(self, src):
-        """self[...] = src (same extents)."""
+        """self[...] = src (same extents).  Two contiguous arrays of one layout are one device copy
+        (stream-ordered, capturable); other sections go through the box kernel."""
         _same(self, src)
+        nbytes = self.size * self.dtype.itemsize
+        if self.contiguous() and src.contiguous() and self.dtype == src.dtype:
+            if self.ptr == src.ptr:
+                return
+            if self.ptr + nbytes <= src.ptr or src.ptr + nbytes <= self.ptr:  # disjoint
+                N.check(self.dev.L.gb_copy_d2d(self.dev.h, self.ptr, src.ptr, nbytes), "gb_copy_d2d")
+                return
         self._box(0, src)
 
     def fill(self, x):

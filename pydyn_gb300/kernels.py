@@ -175,9 +175,9 @@ def loss_rates(temper, phlb, lat, fields, dt, loss=None, decay=None, oh_factor=N
 
 
 def chemistry(temper, phlb, lat, fields, dt, cols, tracers, rm, rxm, rym, rzm, oh_factor=None, oh_scale=1.0,
-              cl_scale=1.0, o1d_scale=1.0, soil_rate=0.0):
+              cl_scale=1.0, o1d_scale=1.0, soil_rate=0.0, krates=None):
     """chemistry_region (zoom/physics.py:67): the decay of each listed column's cells applied to
-    the mass and slopes of the (1-based) `tracers`."""
+    the mass and slopes of the (1-based) `tracers`.  krates: chem_krates(temper)'s, or None."""
     _tracer_strides(rm, rxm, rym, rzm)
     mask = 0
     for t in tracers:
@@ -185,7 +185,15 @@ def chemistry(temper, phlb, lat, fields, dt, cols, tracers, rm, rxm, rym, rzm, o
     L, h = _lib(temper)
     N.check(L.gb_chemistry(h, *_chem_args(temper, phlb, lat, fields, oh_factor, oh_scale, cl_scale, o1d_scale,
                                           soil_rate, dt), cols.ptr, cols.shape[0], mask,
-                           *views(rm, rxm, rym, rzm)), "chemistry")  # fmt: skip
+                           *views(rm, rxm, rym, rzm, krates)), "chemistry")  # fmt: skip
+
+
+def chem_krates(temper, krates, cols=None):
+    """The rate constants of the temperature (chem.py:137-140) into krates (im, jm, lm, 2) on the
+    listed columns (cols a DevArray (ncol, 2) int32, or None: every column)."""
+    L, h = _lib(temper)
+    N.check(L.gb_chem_krates(h, *views(temper), None if cols is None else cols.ptr,
+                             0 if cols is None else cols.shape[0], *views(krates)), "chem_krates")  # fmt: skip
 
 
 def sources(rm, rzm, flux, cols, level, tracer, area=None, scale=1.0):

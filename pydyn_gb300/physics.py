@@ -58,6 +58,7 @@ class Physics:
                 "spm": [up(s) for s in R["kzz"]["spm"]],
                 "spm_now": DevArray.zeros(dev, (0, g.im - 1), (0, g.jm - 1)),
                 "dkg": DevArray.zeros(dev, (0, g.im - 1), (0, g.jm - 1), (0, self.lmax - 1)),
+                "krates": DevArray.zeros(dev, (0, g.im - 1), (0, g.jm - 1), (0, zoom.lm - 1), (0, 1)),
                 "chem": {k: up(v) for k, v in R["chem"].items()},
                 "flux": up(R["flux"]),
                 "factors": DevArray.zeros(dev, (0, 2 * g.tref - 1), (0, g.im - 1)),
@@ -90,8 +91,9 @@ class Physics:
 
     # -------------------------------------------------------------- enqueued (capturable)
     def prepare(self, fwd, ndyn):
-        """After Setup_MassFlow: the step counter, spm, Calc_Kzz of every region.  Returns the
-        driver's (conv, kwargs)."""
+        """After Setup_MassFlow: the step counter, spm, Calc_Kzz of every region, and the rate
+        constants of the step's temperature on the owned columns (every chemistry call of the
+        step uses them).  Returns the driver's (conv, kwargs)."""
         self.ndyn = ndyn
         N.check(self.dev.L.gb_iadd(self.dev.h, self.epoch.ptr, 1), "gb_iadd")
         st = fwd.st
@@ -101,6 +103,8 @@ class Physics:
             dx, dy, ybeg = d["grid"]
             K.calc_kzz(d["spm_now"], f["sp"][1 : g.im, 1 : g.jm, 1], f["pu"], f["pv"], d["t"], d["q"],
                        d["surface"], self.at, self.bt, d["dxyp"], self.lmax, dx, dy, ybeg, d["dkg"])  # fmt: skip
+            if d["ncol"]:
+                K.chem_krates(d["t"], d["krates"], d["cols"])
         conv = {r: self for r in self.r}
         return conv, {"sources": self.sources, "chemistry": self.chemistry}
 
@@ -134,7 +138,7 @@ class Physics:
         c = d["chem"]
         K.chemistry(d["t"], f["phlb"][1 : g.im, 1 : g.jm, 1 : zoom.lm + 1], c["lat"], c, self.spec.half_step(region,
                     self.ndyn), d["cols"], CH4_TRACERS, *_interior(st, region)[1:], oh_factor=d["factors"][h],
-                    **self.spec.settings)  # fmt: skip
+                    krates=d["krates"], **self.spec.settings)  # fmt: skip
 
     def free(self):
         seen = set()

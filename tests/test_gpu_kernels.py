@@ -190,10 +190,13 @@ def test_chemistry_and_sources_on_owned_columns_at_size(dev, shape, ns, ntrop):
         want[q][..., 0][own] = want[q][..., 0][own] * decay[own]
     d = {k: DevArray.from_host(dev, v) for k, v in {**st, **ins, "fac": fac, "flux": flux, "area": area}.items()}
     dcols = DevArray.from_host(dev, cols)
+    krates = DevArray.zeros(dev, (0, im - 1), (0, jm - 1), (0, lm - 1), (0, 1))
+    K.chem_krates(d["temper"], krates, dcols)  # the step's rate constants, made once
     K.sources(d["rm"], d["rzm"], d["flux"], dcols, 1, 1, area=d["area"], scale=1800.0)
     K.chemistry(d["temper"], d["phlb"], d["lat"], d, 1800.0, dcols, (1,), *(d[q] for q in TRACERS),
-                oh_factor=d["fac"], **kw)  # fmt: skip
+                oh_factor=d["fac"], krates=krates, **kw)  # fmt: skip
     dev.sync()
+    krates.free()
     for k in ("m", *TRACERS):
         assert_bitwise(d[k].host(), want[k], f"chem.{k}")
     assert (decay < 1.0).mean() > 0.5
