@@ -1,7 +1,7 @@
 // convec: implicit convection with Kzz diffusion folded into one matrix per column, inverted
 // by Crout LU without pivoting, applied to the tracer mass and (by its diagonal) the slopes.
 //
-// Four launches, shaped so that the FP64 pipe -- this GPU's scarcest unit -- issues with its
+// Five launches, shaped so that the FP64 pipe -- this GPU's scarcest unit -- issues with its
 // lanes full:
 //   k_convec_chains  one thread per owned column: whether its kept inverse still holds, and the
 //                    updraft and downdraft chains
@@ -9,7 +9,9 @@
 //                    uses (each division once), conv1(., l) = I - dt (f(k-1, l) - f(k, l)), the
 //                    downdraft chain of f down from the diagonal and the updraft chain up from
 //                    it -- into a work space
-//   k_convec_lu      one warp per column whose inverse is made: Crout LU column by column (the
+//   k_convec_tri     one thread per cloudless column (tridiagonal conv1): the same LU and L^-1
+//                    by the recurrence their non-zero elements follow
+//   k_convec_lu      one warp per other column whose inverse is made: Crout LU column by column (the
 //                    rows a term updates packed onto the lanes), then L^-1 by forward
 //                    substitution (row k's terms applied to every later row at once, the
 //                    (row, column) elements packed onto the lanes).  U goes to the work space,
@@ -205,6 +207,51 @@ __global__ void __launch_bounds__(MATRIX_THREADS) k_convec_matrix(CArgs A) {
     }
 }
 
+// thread per cloudless column: conv1 is tridiagonal.  When its three bands are finite and
+// non-zero, the general Crout LU does, in its non-zero elements, exactly the recurrence
+//   L(c, c-1) = A(c, c-1) / U(c-1, c-1),   U(c, c) = A(c, c) - L(c, c-1) A(c-1, c),
+// U(c-1, c) = A(c-1, c): every other term it applies has a zero multiplier or multiplicand and
+// only changes zeros, which are never used but as zero-tested multipliers.  Likewise L^-1 row by
+// row: Y(r, col) = +0 - L(r, r-1) Y(r-1, col) for col < r, Y(r, r) = 1.  Written here: the
+// diagonal of U over conv1's (the bands above stay), L^-1 into the inverse's place, and the
+// rows' term ends; fresh = 2 tells the warp kernel the column is done.  A column with a zero or
+// non-finite band entry is left to the warp kernel.
+__global__ void __launch_bounds__(MATRIX_THREADS) k_convec_tri(CArgs A) {
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= A.ncol || A.fresh[c] != 1) return;
+    const int i = A.cols[2 * c], j = A.cols[2 * c + 1];
+    if (!(A.top[i * A.ts0 + j * A.ts1] <= 0 && A.lfs[i * A.ts0 + j * A.ts1] <= 1)) return;
+    const int n = A.n;
+    double *G = A.abuf + (size_t)c * n * n;
+    for (int r = 0; r < n; ++r) {
+        const int64_t bits[3] = {__double_as_longlong(G[(size_t)r * n + r]),
+                                 r + 1 < n ? __double_as_longlong(G[(size_t)r * n + r + 1]) : 0x3ff0000000000000LL,
+                                 r + 1 < n ? __double_as_longlong(G[(size_t)(r + 1) * n + r]) : 0x3ff0000000000000LL};
+        for (int b = 0; b < 3; ++b) {
+            const int64_t mag = bits[b] & 0x7fffffffffffffffLL;
+            if (mag == 0 || mag >= 0x7ff0000000000000LL) return;  // zero, infinite or NaN
+        }
+    }
+    double *X = A.inv + (size_t)c * n * n;
+    int32_t *rend = A.rend + (size_t)c * n;
+    double uprev = G[0];  // U(r-1, r-1)
+    for (int r = 1; r < n; ++r) {
+        const double l = G[(size_t)r * n + r - 1] / uprev;
+        const double u = G[(size_t)r * n + r] - l * G[(size_t)(r - 1) * n + r];
+        G[(size_t)r * n + r] = u;
+        // row r of L^-1 from row r-1's (written just before, cached)
+        for (int col = 0; col < r - 1; ++col) X[(size_t)r * n + col] = 0.0 - l * X[(size_t)(r - 1) * n + col];
+        X[(size_t)r * n + r - 1] = 0.0 - l * 1.0;
+        X[(size_t)r * n + r] = 1.0;
+        for (int col = r + 1; col < n; ++col) X[(size_t)r * n + col] = 0.0;
+        uprev = u;
+    }
+    X[0] = 1.0;
+    for (int col = 1; col < n; ++col) X[col] = 0.0;
+    for (int r = 0; r < n; ++r) rend[r] = r + 1 < n ? r + 2 : r + 1;
+    A.fresh[c] = 2;
+}
+
 // shared memory of one warp (doubles): the matrix (conv1, then LU) and L^-1, n*n each
 __host__ __device__ __forceinline__ size_t warp_doubles(int n) { return 2 * (size_t)n * n; }
 
@@ -212,7 +259,7 @@ __global__ void __launch_bounds__(WARPS * 32) k_convec_lu(CArgs A) {
     extern __shared__ double smem[];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int c = blockIdx.x * WARPS + warp;
-    if (c >= A.ncol || !A.fresh[c]) return;
+    if (c >= A.ncol || A.fresh[c] != 1) return;
     const int n = A.n;
     double *LU = smem + (size_t)warp * warp_doubles(n);  // n x n
     double *Y = LU + (size_t)n * n;                       // n x n
@@ -361,6 +408,8 @@ extern "C" int gb_convec(gb_ctx *ctx, const gb_view *m, const gb_view *rm, const
     const int64_t nel = (int64_t)ncol * lmax;
     k_convec_matrix<<<(unsigned)((nel + MATRIX_THREADS - 1) / MATRIX_THREADS), MATRIX_THREADS, 0, ctx->stream>>>(A);
     if (int rc = gb_after_launch(ctx, "convec_matrix")) return rc;
+    k_convec_tri<<<(ncol + MATRIX_THREADS - 1) / MATRIX_THREADS, MATRIX_THREADS, 0, ctx->stream>>>(A);
+    if (int rc = gb_after_launch(ctx, "convec_tri")) return rc;
     const size_t smem = (size_t)WARPS * warp_doubles(lmax) * sizeof(double);
     GB_CHECK_CUDA(cudaFuncSetAttribute(k_convec_lu, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     k_convec_lu<<<(ncol + WARPS - 1) / WARPS, WARPS * 32, smem, ctx->stream>>>(A);
