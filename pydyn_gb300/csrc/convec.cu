@@ -211,11 +211,10 @@ __global__ void __launch_bounds__(MATRIX_THREADS) k_convec_matrix(CArgs A) {
 // non-zero, the general Crout LU does, in its non-zero elements, exactly the recurrence
 //   L(c, c-1) = A(c, c-1) / U(c-1, c-1),   U(c, c) = A(c, c) - L(c, c-1) A(c-1, c),
 // U(c-1, c) = A(c-1, c): every other term it applies has a zero multiplier or multiplicand and
-// only changes zeros, which are never used but as zero-tested multipliers.  Likewise L^-1 row by
-// row: Y(r, col) = +0 - L(r, r-1) Y(r-1, col) for col < r, Y(r, r) = 1.  Written here: the
-// diagonal of U over conv1's (the bands above stay), L^-1 into the inverse's place, and the
-// rows' term ends; fresh = 2 tells the warp kernel the column is done.  A column with a zero or
-// non-finite band entry is left to the warp kernel.
+// only changes zeros, which are never used but as zero-tested multipliers.  Written here over
+// conv1: U's diagonal (its band above stays) and L's band below; and the rows' term ends.
+// fresh = 2 tells the warp kernel the column is done and k_convec_apply that L^-1 is still to be
+// made from that band.  A column with a zero or non-finite band entry is left to the warp kernel.
 __global__ void __launch_bounds__(MATRIX_THREADS) k_convec_tri(CArgs A) {
     const int c = blockIdx.x * blockDim.x + threadIdx.x;
     if (c >= A.ncol || A.fresh[c] != 1) return;
@@ -232,22 +231,15 @@ __global__ void __launch_bounds__(MATRIX_THREADS) k_convec_tri(CArgs A) {
             if (mag == 0 || mag >= 0x7ff0000000000000LL) return;  // zero, infinite or NaN
         }
     }
-    double *X = A.inv + (size_t)c * n * n;
     int32_t *rend = A.rend + (size_t)c * n;
     double uprev = G[0];  // U(r-1, r-1)
     for (int r = 1; r < n; ++r) {
         const double l = G[(size_t)r * n + r - 1] / uprev;
         const double u = G[(size_t)r * n + r] - l * G[(size_t)(r - 1) * n + r];
         G[(size_t)r * n + r] = u;
-        // row r of L^-1 from row r-1's (written just before, cached)
-        for (int col = 0; col < r - 1; ++col) X[(size_t)r * n + col] = 0.0 - l * X[(size_t)(r - 1) * n + col];
-        X[(size_t)r * n + r - 1] = 0.0 - l * 1.0;
-        X[(size_t)r * n + r] = 1.0;
-        for (int col = r + 1; col < n; ++col) X[(size_t)r * n + col] = 0.0;
+        G[(size_t)r * n + r - 1] = l;  // L(r, r-1) over A(r, r-1): k_convec_apply builds L^-1 from it
         uprev = u;
     }
-    X[0] = 1.0;
-    for (int col = 1; col < n; ++col) X[col] = 0.0;
     for (int r = 0; r < n; ++r) rend[r] = r + 1 < n ? r + 2 : r + 1;
     A.fresh[c] = 2;
 }
@@ -330,6 +322,19 @@ __global__ void k_convec_apply(CArgs A) {
     const int c = blockIdx.x * A.cols_per_block + cl;
     const bool live = cl < A.cols_per_block && c < A.ncol;
     double *X = live ? A.inv + (size_t)c * n * n : nullptr;
+    // ---- a cloudless column's L^-1, column x: the forward substitution of the identity with L's
+    // single band, Y(r, x) = +0 - L(r, r-1) Y(r-1, x) below the diagonal (the terms of a zero
+    // L(r, r-1) it skips leave the +0 that this writes), 1 on it, +0 above
+    if (live && A.fresh[c] == 2) {
+        const double *L = A.abuf + (size_t)c * n * n;
+        for (int r = 0; r < x; ++r) X[(size_t)r * n + x] = 0.0;
+        X[(size_t)x * n + x] = 1.0;
+        double y = 1.0;
+        for (int r = x + 1; r < n; ++r) {
+            y = 0.0 - L[(size_t)r * n + r - 1] * y;
+            X[(size_t)r * n + x] = y;
+        }
+    }
     // ---- back substitution of inverse column x: rows from the bottom, terms k in order
     if (live && A.fresh[c]) {
         const double *U = A.abuf + (size_t)c * n * n;
