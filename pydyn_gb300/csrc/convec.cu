@@ -68,8 +68,8 @@ __device__ __forceinline__ double max0(double x) { return gb_isnan(x) ? x : (0.0
 // x == 0.0 (either sign), tested on the integer pipe: the FP64 pipe is kept for arithmetic
 __device__ __forceinline__ bool is_zero(double x) { return (__double_as_longlong(x) << 1) == 0; }
 
-// the work space's per-column chains amu, amd (n+1 each, indexed by level k = 0..n)
-constexpr int NCHAIN = 2;
+// the work space's per-column chains amu, zu, amd, zd (n+1 each, indexed by level k = 0..n)
+constexpr int NCHAIN = 4;
 __device__ __forceinline__ double *chains(const CArgs &A, int c) { return A.chain + (size_t)c * NCHAIN * (A.n + 1); }
 
 // thread per column: whether the kept inverse still holds; the updraft and downdraft chains
@@ -93,67 +93,48 @@ __global__ void __launch_bounds__(MATRIX_THREADS) k_convec_chains(CArgs A) {
     }
     A.fresh[c] = 1;
 
-    // the mass fluxes of the chains (their ratios z, divisions each, are made per level by
-    // k_convec_matrix from these): amu(k) after level k upward, amd(k-1) after level k downward
-    double *amu = chains(A, c), *amd = amu + (n + 1);
+    double *amu = chains(A, c), *zu = amu + (n + 1), *amd = zu + (n + 1), *zd = amd + (n + 1);
     const int top = A.top[i * A.ts0 + j * A.ts1], lfs = A.lfs[i * A.ts0 + j * A.ts1];
     double mu = 0.0;
     amu[0] = 0.0;
     for (int k = 1; k <= n; ++k) {
         const double eu = AT(A.entu, i, j, k - 1), du = AT(A.detu, i, j, k - 1);
+        const bool act = top >= k;
         const double a = mu + eu - du;
-        mu = (top >= k && a > 0.0) ? a : 0.0;
+        const bool up = a > 0.0;
+        const double z = up ? max0(1.0 - du / (mu + eu)) : 0.0;
+        mu = (act && up) ? a : 0.0;
         amu[k] = mu;
+        zu[k] = act ? z : -1.0;  // -1 marks an inactive level
     }
     double md = 0.0;
     amd[n] = 0.0;
     amd[0] = 0.0;
+    zd[0] = zd[1] = -1.0;
     for (int k = n; k >= 2; --k) {
         const double ed = AT(A.entd, i, j, k - 1), dd = AT(A.detd, i, j, k - 1);
+        const bool act = lfs >= k;
         const double a = md - ed + dd;
-        md = (lfs >= k && a < 0.0) ? a : 0.0;
+        const bool dn = a < 0.0;
+        const double z = dn ? max0(1.0 + dd / (md - ed)) : 0.0;
+        md = (act && dn) ? a : 0.0;
         amd[k - 1] = md;
+        zd[k] = act ? z : -1.0;
     }
 }
 
-// whole columns per block (cols_per_block of n threads), thread (column, column l of its
-// matrix).  First every thread makes the chains' ratios of level k = l + 1 (upward: z =
-// max0(1 - du / (mu + eu)) where the updraft grows, downward: z = max0(1 + dd / (md - ed)) where
-// the downdraft grows, -1 at an inactive level) into shared memory.  Then conv1(., l): f(k, l),
-// k = 0..n, is the downdraft chain fd(k, l) for k = l down to 1 (zero elsewhere), plus the
-// updraft chain fu(k, l) for k = l+1 up, plus the diagonal terms; f(0, l) = f(n, l) = 0;
-// conv1(k-1, l) = -dt (f(k-1, l) - f(k, l)), plus 1 on the diagonal.
-__global__ void k_convec_matrix(CArgs A) {
-    extern __shared__ double zsm[];
+// thread per (column, column l of its matrix): conv1(., l).  f(k, l), k = 0..n: the downdraft
+// chain fd(k, l) for k = l down to 1 (zero elsewhere), plus the updraft chain fu(k, l) for
+// k = l+1 up, plus the diagonal terms; f(0, l) = f(n, l) = 0.  conv1(k-1, l) =
+// -dt (f(k-1, l) - f(k, l)), plus 1 on the diagonal.
+__global__ void __launch_bounds__(MATRIX_THREADS) k_convec_matrix(CArgs A) {
+    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     const int n = A.n;
-    const int cl = threadIdx.x / n, l = threadIdx.x % n;
-    const int c = blockIdx.x * A.cols_per_block + cl;
-    const bool live = cl < A.cols_per_block && c < A.ncol && A.fresh[c];
-    double *zu = zsm + (size_t)cl * 2 * (n + 1), *zd = zu + (n + 1);
-    const int i = live ? A.cols[2 * c] : 0, j = live ? A.cols[2 * c + 1] : 0;
-    const double *amu = live ? chains(A, c) : nullptr, *amd = live ? amu + (n + 1) : nullptr;
-    if (live) {
-        const int top = A.top[i * A.ts0 + j * A.ts1], lfs = A.lfs[i * A.ts0 + j * A.ts1];
-        const int k = l + 1;
-        {
-            const double mu = amu[k - 1];  // the updraft below level k
-            const double eu = AT(A.entu, i, j, k - 1), du = AT(A.detu, i, j, k - 1);
-            const double a = mu + eu - du;
-            const double z = a > 0.0 ? max0(1.0 - du / (mu + eu)) : 0.0;
-            zu[k] = top >= k ? z : -1.0;
-        }
-        if (k >= 2) {
-            const double md = amd[k];  // the downdraft above level k
-            const double ed = AT(A.entd, i, j, k - 1), dd = AT(A.detd, i, j, k - 1);
-            const double a = md - ed + dd;
-            const double z = a < 0.0 ? max0(1.0 + dd / (md - ed)) : 0.0;
-            zd[k] = lfs >= k ? z : -1.0;
-        } else {
-            zd[0] = zd[1] = -1.0;
-        }
-    }
-    __syncthreads();
-    if (!live) return;
+    if (t >= (int64_t)A.ncol * n) return;
+    const int c = (int)(t / n), l = (int)(t % n);
+    if (!A.fresh[c]) return;
+    const double *amu = chains(A, c), *zu = amu + (n + 1), *amd = zu + (n + 1), *zd = amd + (n + 1);
+    const int i = A.cols[2 * c], j = A.cols[2 * c + 1];
     // the quotients this column of the matrix uses, each divided once: at level k = l + 1 the
     // chain starts (qed, qeu) and the sub-diagonal terms (qamd, qdk1); at k = l the diagonal's
     // (qamu, qdk2)
@@ -427,16 +408,10 @@ extern "C" int gb_convec(gb_ctx *ctx, const gb_view *m, const gb_view *rm, const
     A.cache_m = cache_inv ? cache_m : nullptr;
     A.cache_tag = cache_tag;
     A.epoch = epoch;
-    // whole columns per block, as many as make the block a whole number of warps (<= 1024 threads)
-    int per = 32 / gcd(lmax, 32);
-    while (per > 1 && per * lmax > 1024) per /= 2;
-    if (per * lmax < 128) per = (128 + lmax - 1) / lmax;
-    A.cols_per_block = per;
-    const int threads = ((per * lmax + 31) / 32) * 32;
-    const unsigned col_blocks = (unsigned)((ncol + per - 1) / per);
     k_convec_chains<<<(ncol + MATRIX_THREADS - 1) / MATRIX_THREADS, MATRIX_THREADS, 0, ctx->stream>>>(A);
     if (int rc = gb_after_launch(ctx, "convec_chains")) return rc;
-    k_convec_matrix<<<col_blocks, threads, (size_t)per * 2 * (lmax + 1) * sizeof(double), ctx->stream>>>(A);
+    const int64_t nel = (int64_t)ncol * lmax;
+    k_convec_matrix<<<(unsigned)((nel + MATRIX_THREADS - 1) / MATRIX_THREADS), MATRIX_THREADS, 0, ctx->stream>>>(A);
     if (int rc = gb_after_launch(ctx, "convec_matrix")) return rc;
     k_convec_tri<<<(ncol + MATRIX_THREADS - 1) / MATRIX_THREADS, MATRIX_THREADS, 0, ctx->stream>>>(A);
     if (int rc = gb_after_launch(ctx, "convec_tri")) return rc;
@@ -444,6 +419,12 @@ extern "C" int gb_convec(gb_ctx *ctx, const gb_view *m, const gb_view *rm, const
     GB_CHECK_CUDA(cudaFuncSetAttribute(k_convec_lu, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     k_convec_lu<<<(ncol + WARPS - 1) / WARPS, WARPS * 32, smem, ctx->stream>>>(A);
     if (int rc = gb_after_launch(ctx, "convec_lu")) return rc;
-    k_convec_apply<<<col_blocks, threads, 0, ctx->stream>>>(A);
+    // whole columns per block, as many as make the block a whole number of warps (<= 1024 threads)
+    int per = 32 / gcd(lmax, 32);
+    while (per > 1 && per * lmax > 1024) per /= 2;
+    if (per * lmax < 128) per = (128 + lmax - 1) / lmax;
+    A.cols_per_block = per;
+    const int threads = ((per * lmax + 31) / 32) * 32;
+    k_convec_apply<<<(ncol + per - 1) / per, threads, 0, ctx->stream>>>(A);
     return gb_after_launch(ctx, "convec_apply");
 }
