@@ -190,7 +190,7 @@ def run_reference(args, ws, rank):
 def main():
     ap = argparse.ArgumentParser(description=__doc__.split("\n")[0])
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--steps", type=int, default=100)  # ~1 s timed: several clock samples
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--config", default=DEFAULT, choices=sorted(WORKLOADS))
     ap.add_argument("--impl", default="gbdyn", choices=("gbdyn", "reference"))
@@ -292,15 +292,15 @@ def main():
             "bytes_per_launch": per_call_bytes, "ms_per_launch": total_ms / calls,
             "note": "float64 with no contraction: the FP64 pipe (500 G DMUL/DADD/s measured) bounds the step"}  # fmt: skip
     if body == "convec_region" and fw.physics is not None:
-        # the explicit Crout inverse: (8/3) lmax^3 flops per column on its first call of a step (the
-        # second call of the same air mass reuses it: 2 lmax^2 nt for the tracer product only)
-        ncol = fw.physics.r[int(region) if region else 1]["ncol"]
-        pairs = calls // 2  # each pair of calls on one air mass computes one inverse per column
-        flops = pairs * ncol * ((8.0 / 3.0) * lmax**3 + 2.0 * 2.0 * lmax * lmax)
+        # the reference's dense explicit inverse, (8/3) lmax^3 flops per column and inverse, plus
+        # 2 lmax^2 per call's tracer product; the kernels skip its exact zeros (most columns are
+        # tridiagonal), so this is an effective rate, not the pipe's
+        d = fw.physics.r[int(region) if region else 1]
+        inverses = calls - 1  # one call a step reuses the inverses (the `v` after `c s` on the same air mass)
+        flops = d["ncol"] * (inverses * (8.0 / 3.0) * lmax**3 + calls * 2.0 * lmax * lmax)
         gflops = flops / (total_ms / 1e3) / 1e9
-        roof["fp64"] = {"achieved_gflops": gflops, "peak_gflops": FP64_PEAK, "frac": gflops / FP64_PEAK,
-                        "flops_per_interval": flops,
-                        "note": "(8/3) lmax^3 per column inverse, 2 lmax^2 per call's product; peak = the "
+        roof["fp64"] = {"effective_gflops": gflops, "peak_gflops": FP64_PEAK, "flops_per_interval": flops,
+                        "note": "dense-equivalent flops of the reference's inverse per second; peak = the "
                                 "measured DMUL/DADD issue rate"}  # fmt: skip
 
     b_half = (496 if physics else 296)  # bytes per cell per half step at nt = 1
