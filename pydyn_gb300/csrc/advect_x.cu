@@ -42,9 +42,10 @@ __device__ __forceinline__ double &AT4(const DV &v, int64_t i, int64_t j, int64_
 // The per-row CFL search (kernels.py:169-199): the smallest nloop for which nloop trial
 // sub-steps of the mass stay under |Courant| < 1 on every face (division form,
 // ops.py:267-270), the faces rescaled by (n-1)/n per retry.  Faces k0..k1, cells i0..i1 move.
-// Returns nloop, or nmax + 1.
+// Returns nloop, or nmax + 1.  want_amax: also the largest |Courant| of the passing trial (the
+// division on every face); without it the test is cfl_pass's.
 __device__ int row_search(double *m_s, double *mx_s, double *a_s, int n, bool held, int nmax, int lane,
-                          double &amax_out) {
+                          double &amax_out, bool want_amax) {
     const int k0 = held ? 1 : 0, k1 = held ? n - 1 : n;
     const int i0 = held ? 1 : 0, i1 = held ? n - 1 : n;  // cells [i0, i1)
     int nloop = 1;
@@ -59,17 +60,23 @@ __device__ int row_search(double *m_s, double *mx_s, double *a_s, int n, bool he
             for (int k = k0 + lane; k <= k1; k += GB_WARP) {
                 double f = a_s[k];
                 int up = (f >= 0.0) ? (k == 0 ? n - 1 : k - 1) : (k == n ? 0 : k);
-                double c = gb_abs(f / mx_s[up]);
-                lok = lok && (c < 1.0);
-                cmax = (c > cmax) ? c : cmax;
+                if (want_amax) {
+                    double c = gb_abs(f / mx_s[up]);
+                    lok = lok && (c < 1.0);
+                    cmax = (c > cmax) ? c : cmax;
+                } else {
+                    lok = lok && cfl_pass(f, mx_s[up]);
+                }
             }
             ok = __all_sync(FULL_MASK, lok);
             if (!ok) break;
-            for (int o = 16; o > 0; o >>= 1) {
-                double other = __shfl_xor_sync(FULL_MASK, cmax, o);
-                cmax = (other > cmax) ? other : cmax;
+            if (want_amax) {
+                for (int o = 16; o > 0; o >>= 1) {
+                    double other = __shfl_xor_sync(FULL_MASK, cmax, o);
+                    cmax = (other > cmax) ? other : cmax;
+                }
+                amax = (amax > cmax) ? amax : cmax;
             }
-            amax = (amax > cmax) ? amax : cmax;
             __syncwarp();
             for (int k = i0 + lane; k < i1; k += GB_WARP) mx_s[k] = (mx_s[k] + a_s[k]) - a_s[k + 1];
             __syncwarp();
@@ -140,7 +147,7 @@ __global__ void __launch_bounds__(WARPS * 32) k_advect_x(XArgs A) {
             for (int k = lane; k < n; k += GB_WARP) Q(1, t)[k] = np_limit(Q(1, t)[k], Q(0, t)[k]);
 
     double amax = 0.0;
-    const int nloop = row_search(m_s, mx_s, a_s, n, held, A.nmax, lane, amax);
+    const int nloop = row_search(m_s, mx_s, a_s, n, held, A.nmax, lane, amax, A.amax_out != nullptr);
     if (nloop > A.nmax) {
         if (lane == 0) {
             if (MASS_ONLY)

@@ -66,7 +66,7 @@ __device__ bool column_trial(const YArgs &A, int i, int l, int n, double *mx, do
         for (int k = k0 + lane; k <= k1 - (A.held ? 0 : 0) && k < nc; k += GB_WARP) {
             double f = bf[k];
             double mu = (f >= 0.0) ? mx[k - 1] : mx[k];
-            lok = lok && (gb_abs(f / mu) < 1.0);
+            lok = lok && cfl_pass(f, mu);
         }
         if (!__all_sync(FULL_MASK, lok)) return false;
         for (int k = c0 + lane; k < c1; k += GB_WARP) mx[k] = (mx[k] + bf[k]) - bf[k + 1];

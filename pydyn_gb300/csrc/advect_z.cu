@@ -27,6 +27,7 @@ struct ZArgs {
     int ncell;               // lm + 2
     gb_ctl *ctl;
     int mass_only;
+    int32_t *coln;           // work space (im * jm): the n each column's last trial passed at
 };
 
 __device__ __forceinline__ double &AT(const DV &v, int64_t i, int64_t j, int64_t l) {
@@ -48,7 +49,7 @@ __device__ bool z_trial(const ZArgs &A, int i, int j, int n, double *mx, double 
         for (int k = 1 + lane; k < lm; k += GB_WARP) {
             double c = cf[k];
             double mu = (c >= 0.0) ? mx[k - 1] : mx[k];
-            lok = lok && (gb_abs(c / mu) < 1.0);
+            lok = lok && cfl_pass(c, mu);
         }
         if (!__all_sync(FULL_MASK, lok)) return false;
         if (!scope) continue;  // outside the scope the trial mass is never advanced
@@ -74,15 +75,23 @@ __global__ void __launch_bounds__(WARPS * 32) k_z_search(ZArgs A, int round) {
             raise_status(A.ctl, GB_EHALO);
         int n = 1;
         while (n <= A.nmax && !z_trial(A, i, j, n, mx, cf, lane)) ++n;
-        if (lane == 0) atomicMax(&A.ctl->zsearch_n[1], n);
+        if (lane == 0) {
+            A.coln[col] = n;
+            atomicMax(&A.ctl->zsearch_n[1], n);
+        }
         return;
     }
     const int cand = A.ctl->zsearch_n[round];
     if (cand > A.nmax) return;  // some column never passes: the steps raise the error
-    if (z_trial(A, i, j, cand, mx, cf, lane)) return;
+    if (A.coln[col] == cand) return;  // its own trial passed at the candidate already
+    if (z_trial(A, i, j, cand, mx, cf, lane)) {
+        if (lane == 0) A.coln[col] = cand;
+        return;
+    }
     int n = cand + 1;
     while (n <= A.nmax && !z_trial(A, i, j, n, mx, cf, lane)) ++n;
     if (lane == 0) {
+        A.coln[col] = n;
         atomicMax(&A.ctl->zsearch_n[round + 1], n);
         atomicExch(&A.ctl->zsearch_changed[round], 1);
     }
@@ -189,6 +198,8 @@ int launch_z(gb_ctx *ctx, ZArgs &A) {
     int64_t cols = (int64_t)A.im * A.jm;
     int blocks = (int)((cols + WARPS - 1) / WARPS);
     if (blocks == 0) return GB_OK;
+    A.coln = reinterpret_cast<int32_t *>(gb_work(ctx, (size_t)cols * sizeof(int32_t)));
+    if (!A.coln) return GB_ECUDA;
     for (int r = 0; r < ROUNDS; ++r) {
         k_z_search<<<blocks, WARPS * 32, smem_s, ctx->stream>>>(A, r);
         int rc = gb_after_launch(ctx, "z_search");

@@ -77,6 +77,17 @@ __device__ __forceinline__ double gb_neg(double x) {
     return __longlong_as_double(__double_as_longlong(x) ^ (long long)0x8000000000000000ULL);
 }
 
+// abs(c / mu) < 1.0 (the sub-cycle searches' Courant test, ops.py:330-341) without the division
+// where the answer is certain: |c| < fl(0.9999 |mu|) puts the quotient below 0.9999 (1 + 2^-53)
+// < 1 - 2^-54, so it rounds below 1 (for subnormal |mu| too); |c| > |mu| puts it above 1.  The
+// band between, zeros, NaNs and infinities take the division itself.
+__device__ __forceinline__ bool cfl_pass(double c, double mu) {
+    const double ac = gb_abs(c), am = gb_abs(mu);
+    if (ac < am * 0.9999) return true;
+    if (ac > am) return false;
+    return gb_abs(c / mu) < 1.0;
+}
+
 // ------------------------------------------------------------------ NumPy's element rules
 // np.clip(s, -|r|, |r|) exactly as NumPy evaluates it: a NaN in s wins, then max with the lower
 // bound ((s > lo) ? s : lo), then a NaN wins again, then min with the upper bound.
