@@ -155,6 +155,110 @@ __global__ void __launch_bounds__(SEARCH_THREADS) k_y_search(YArgs A) {
     }
 }
 
+// ------------------------------------------------------------------ the search, column-parallel
+// The same smallest n every column of a layer passes, found with every (i, l) column working at
+// once: round 0, each column its own smallest passing n (into coln) and the layer's candidate
+// their maximum (integer atomic); round r >= 1, the columns below the layer's candidate try it,
+// and one that fails pushes the next candidate to its own next passing n.  A layer's count is
+// the first candidate no column moved.  No assumption that passing is monotone in n.
+constexpr int YROUNDS = 3;
+
+struct YSearch {
+    int32_t *cand;     // [YROUNDS + 1][nl], zeroed
+    int32_t *changed;  // [YROUNDS][nl], zeroed
+    int32_t *coln;     // [ni][nl]
+};
+
+__global__ void __launch_bounds__(STEP_WARPS * 32) k_y_search_cols(YArgs A, YSearch S, int round) {
+    extern __shared__ double smem[];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int64_t col = (int64_t)blockIdx.x * STEP_WARPS + warp;
+    if (col >= (int64_t)A.ni * A.nl) return;
+    if (A.mass_only && __shfl_sync(FULL_MASK, *(volatile int *)&A.ctl->cfl_failed, 0)) return;
+    const int i = (int)(col / A.nl), l = (int)(col % A.nl);
+    if (round >= 2 && !S.changed[(round - 1) * A.nl + l]) return;  // the layer has settled
+    double *mx = smem + (size_t)warp * 2 * A.ncell;
+    double *bf = mx + A.ncell;
+    int n;
+    if (round == 0) {
+        n = 1;
+        while (n <= A.nmax && !column_trial(A, i, l, n, mx, bf, lane)) ++n;
+        if (lane == 0) {
+            S.coln[col] = n;
+            atomicMax(&S.cand[1 * A.nl + l], n);
+        }
+        return;
+    }
+    const int cand = S.cand[round * A.nl + l];
+    if (cand > A.nmax || S.coln[col] == cand) return;
+    if (column_trial(A, i, l, cand, mx, bf, lane)) {
+        if (lane == 0) S.coln[col] = cand;
+        return;
+    }
+    n = cand + 1;
+    while (n <= A.nmax && !column_trial(A, i, l, n, mx, bf, lane)) ++n;
+    if (lane == 0) {
+        S.coln[col] = n;
+        atomicMax(&S.cand[(round + 1) * A.nl + l], n);
+        atomicExch(&S.changed[round * A.nl + l], 1);
+    }
+}
+
+// one CTA per layer: the layer's settled count (or the errors), then the faces of the halo'd
+// layer outside the columns' own, rescaled and restored alike (as k_y_search does)
+__global__ void __launch_bounds__(SEARCH_THREADS) k_y_search_done(YArgs A, YSearch S) {
+    __shared__ int s_nloop;
+    __shared__ int s_halo;
+    const int l = blockIdx.x;
+    if (threadIdx.x == 0) s_halo = 0;
+    __syncthreads();
+    // region 1's polar outer faces must carry nothing (kernels.py:233-234), checked before the
+    // count as the reference does; dynamvm does not check
+    if (!A.mass_only && !A.held)
+        for (int i = threadIdx.x; i < A.ni; i += SEARCH_THREADS)
+            if (AT(A.bm, i, 0, l) != 0.0 || AT(A.bm, i, A.nc, l) != 0.0) s_halo = 1;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        int nloop = -1;
+        if (s_halo) {
+            nloop = A.nmax + 1;
+            raise_status(A.ctl, GB_EHALO);
+        } else if (A.mass_only && *(volatile int *)&A.ctl->cfl_failed) {
+            nloop = A.nmax + 1;
+        } else {
+            for (int r = 1; r < YROUNDS; ++r)
+                if (!S.changed[r * A.nl + l]) {
+                    nloop = S.cand[r * A.nl + l];
+                    break;
+                }
+            if (nloop < 0) {  // did not settle in its rounds
+                nloop = A.nmax + 1;
+                raise_status(A.ctl, GB_ESEARCH);
+            } else if (nloop > A.nmax) {
+                if (A.mass_only)
+                    atomicExch(&A.ctl->cfl_failed, 1);
+                else
+                    raise_status(A.ctl, GB_ECFL);
+            }
+            if (A.nloop_out) A.nloop_out[l] = nloop;
+        }
+        A.nloop[l] = nloop;
+        s_nloop = nloop;
+    }
+    __syncthreads();
+    const int nloop = s_nloop;
+    if (nloop > A.nmax || nloop == 1 || !A.full.p) return;
+    const int64_t ni = A.full.n0, nj = A.full.n1;
+    const int lf = l + A.full_l0;
+    for (int64_t k = threadIdx.x; k < ni * nj; k += SEARCH_THREADS) {
+        int64_t fi = k / nj, fj = k % nj;
+        bool inside = fi >= A.own_i0 && fi <= A.own_i1 && fj >= A.own_j0 && fj <= A.own_j1;
+        if (inside) continue;
+        double &b = AT(A.full, fi, fj, lf);
+        b = (A.full_mode == 0 ? progressive_chain(b, nloop) : b) * (double)nloop;
+    }
+}
+
 template <bool MASS_ONLY>
 __global__ void __launch_bounds__(STEP_WARPS * 32) k_y_steps(YArgs A) {
     extern __shared__ double smem[];
@@ -274,20 +378,40 @@ __global__ void __launch_bounds__(STEP_WARPS * 32) k_y_steps(YArgs A) {
 
 int launch_y(gb_ctx *ctx, YArgs &A, int32_t *scratch = nullptr) {
     A.ncell = A.nc + 2;
-    A.nloop = scratch ? scratch : gb_scratch_i(ctx, A.nl);
+    const int64_t cols = (int64_t)A.ni * A.nl;
+    const int blocks = (int)((cols + STEP_WARPS - 1) / STEP_WARPS);
+    // the column-parallel search needs the per-layer candidates and a count per column: in the
+    // context's scratch when it holds them; the fixed scratch of gb_advect_y_noalloc (and a
+    // scratch too small) take the CTA-per-layer search, which needs the layer counts only
+    const size_t need = (size_t)A.nl * (1 + (YROUNDS + 1) + YROUNDS) + (size_t)cols;
+    int32_t *wide = scratch ? nullptr : gb_scratch_i(ctx, need);
+    A.nloop = scratch ? scratch : (wide ? wide : gb_scratch_i(ctx, A.nl));
     if (!A.nloop) {
         gb_set_error("gb_advect_y: too many levels for the scratch");
         return GB_EARG;
     }
-    size_t smem_s = (size_t)(SEARCH_THREADS / 32) * 2 * A.ncell * sizeof(double);
-    GB_CHECK_CUDA(cudaFuncSetAttribute(k_y_search, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_s));
-    k_y_search<<<A.nl, SEARCH_THREADS, smem_s, ctx->stream>>>(A);
-    int rc = gb_after_launch(ctx, "y_search");
-    if (rc) return rc;
+    if (wide) {
+        YSearch S;
+        S.cand = wide + A.nl;
+        S.changed = S.cand + (YROUNDS + 1) * A.nl;
+        S.coln = S.changed + YROUNDS * A.nl;
+        GB_CHECK_CUDA(cudaMemsetAsync(S.cand, 0, (size_t)(2 * YROUNDS + 1) * A.nl * sizeof(int32_t), ctx->stream));
+        const size_t smem_c = (size_t)STEP_WARPS * 2 * A.ncell * sizeof(double);
+        GB_CHECK_CUDA(cudaFuncSetAttribute(k_y_search_cols, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_c));
+        for (int r = 0; r < YROUNDS; ++r) {
+            k_y_search_cols<<<blocks, STEP_WARPS * 32, smem_c, ctx->stream>>>(A, S, r);
+            if (int rc = gb_after_launch(ctx, "y_search_cols")) return rc;
+        }
+        k_y_search_done<<<A.nl, SEARCH_THREADS, 0, ctx->stream>>>(A, S);
+        if (int rc = gb_after_launch(ctx, "y_search_done")) return rc;
+    } else {
+        size_t smem_s = (size_t)(SEARCH_THREADS / 32) * 2 * A.ncell * sizeof(double);
+        GB_CHECK_CUDA(cudaFuncSetAttribute(k_y_search, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_s));
+        k_y_search<<<A.nl, SEARCH_THREADS, smem_s, ctx->stream>>>(A);
+        if (int rc = gb_after_launch(ctx, "y_search")) return rc;
+    }
     const int nt = A.mass_only ? 0 : A.nt;
     size_t smem = (size_t)STEP_WARPS * A.ncell * (2 + 8 * nt) * sizeof(double);
-    int64_t cols = (int64_t)A.ni * A.nl;
-    int blocks = (int)((cols + STEP_WARPS - 1) / STEP_WARPS);
     if (A.mass_only) {
         GB_CHECK_CUDA(cudaFuncSetAttribute(k_y_steps<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
         k_y_steps<true><<<blocks, STEP_WARPS * 32, smem, ctx->stream>>>(A);
