@@ -52,7 +52,6 @@ BYTES_PER_CELL = {"_dynamu_region1": 12, "_dynamv_region1": 12, "_dynamw_region1
                   "_dynamv_child": 12, "_dynamw_child": 11, "convec_region": 14, "chemistry_region": 11,
                   "sources_region": 4, "calc_kzz": 5, "m2phlb1": 2, "m2phlb": 2,
                   "dynam0": 5}  # fmt: skip  (values of 8 bytes per cell and application at nt = 1)
-FP64_PEAK = 500.0  # G DMUL or DADD per second, measured on this GB300 (profiles/fp64_throughput_gb300.md)
 
 
 def metric_name(workload):
@@ -282,6 +281,7 @@ def main():
 
     # roofline of the dominant body
     hbm, how = peaks()
+    fp64 = dev.fp64_rates()  # measured here, after the timed region: the FP64 pipe's issue rates
     name, (calls, total_ms, nlaunch) = max(bodies.items(), key=lambda kv: kv[1][1])
     cells = {r: fw.zoom.g(r).im * fw.zoom.g(r).jm * lm for r in fw.zoom.regions()}
     body, _, region = name.partition("@")
@@ -290,7 +290,8 @@ def main():
     roof = {"bound": "hbm", "kernel": name, "achieved": achieved, "peak": hbm, "unit": "GB/s",
             "frac": achieved / hbm if achieved else None, "traffic": None, "peak_source": how,
             "bytes_per_launch": per_call_bytes, "ms_per_launch": total_ms / calls,
-            "note": "float64 with no contraction: the FP64 pipe (500 G DMUL/DADD/s measured) bounds the step"}  # fmt: skip
+            "fp64_rates_g_per_s": fp64,
+            "note": "float64 with no contraction: the FP64 pipe (fp64_rates, measured in this run) bounds the step"}  # fmt: skip
     if body == "convec_region" and fw.physics is not None:
         # the reference's dense explicit inverse, (8/3) lmax^3 flops per column and inverse, plus
         # 2 lmax^2 per call's tracer product; the kernels skip its exact zeros (most columns are
@@ -299,7 +300,7 @@ def main():
         inverses = calls - 1  # one call a step reuses the inverses (the `v` after `c s` on the same air mass)
         flops = d["ncol"] * (inverses * (8.0 / 3.0) * lmax**3 + calls * 2.0 * lmax * lmax)
         gflops = flops / (total_ms / 1e3) / 1e9
-        roof["fp64"] = {"effective_gflops": gflops, "peak_gflops": FP64_PEAK, "flops_per_interval": flops,
+        roof["fp64"] = {"effective_gflops": gflops, "peak_gflops": fp64["dmul_dadd"], "flops_per_interval": flops,
                         "note": "dense-equivalent flops of the reference's inverse per second; peak = the "
                                 "measured DMUL/DADD issue rate"}  # fmt: skip
 

@@ -287,6 +287,11 @@ int gb_m2phlb(gb_ctx *ctx, const gb_view *m, const gb_view *sp, const gb_view *p
  * check that it equals the host build (libgbmath.so) bit for bit.  No reference counterpart. */
 int gb_math_eval(gb_ctx *ctx, int op, const double *x, const double *y, double *out, int64_t n);
 
+/* Measured FP64 issue rate of this GPU, instructions per second over all SMs: kind 0 a multiply
+ * and an add (what -fmad=false emits), 1 a fused multiply-add, 2 a correctly rounded division.
+ * The compute ceiling of the float64 step; not capturable.  No reference counterpart. */
+int gb_fp64_rate(gb_ctx *ctx, int kind, double *rate);
+
 #ifdef __cplusplus
 }
 #endif

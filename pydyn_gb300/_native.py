@@ -91,6 +91,7 @@ SIGNATURES = {
     "gb_chem_krates": (_I, [_VP, _P, _VP, _I, _P]),
     "gb_sources": (_I, [_VP, _P, _P, _P, _VP, _D, _I, _I, _VP, _I]),
     "gb_math_eval":(_I, [_VP, _I, _VP, _VP, _VP, ctypes.c_int64]),
+    "gb_fp64_rate": (_I, [_VP, _I, ctypes.POINTER(_D)]),
     "gb_fluxes_from_meteo": (_I, [_VP, _P, _P, _VP, _D, _P, _P, _P]),
     "gb_m2phlb": (_I, [_VP, _P, _P, _P, _VP, _VP, _VP, _I, _I, _I, _VP]),
 }

@@ -97,6 +97,17 @@ class Device:
         N.check(self.L.gb_cfl_failed(self.h, ctypes.byref(f)), "gb_cfl_failed")
         return bool(f.value)
 
+    # -------------------------------------------------------------- FP64 ceiling
+    def fp64_rates(self):
+        """Measured FP64 issue rates of this GPU in G instructions/s: multiply + add pairs,
+        fused multiply-adds, correctly rounded divisions."""
+        out = {}
+        for kind, name in enumerate(("dmul_dadd", "dfma", "ddiv")):
+            r = ctypes.c_double()
+            N.check(self.L.gb_fp64_rate(self.h, kind, ctypes.byref(r)), "gb_fp64_rate")
+            out[name] = r.value / 1e9
+        return out
+
 
 class Graph:
     def __init__(self, dev):

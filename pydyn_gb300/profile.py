@@ -81,6 +81,8 @@ def main(argv=None):
     no pinned copies -- for a launch list under a profiler:
 
         python -m pydyn_gb300.profile --config glb3x2+nam1x1 --levels 34 --intervals 1
+
+    With --fp64-rates it measures the GPU's FP64 issue rates instead (the step's compute ceiling).
     """
     import argparse
     import sys
@@ -94,6 +96,7 @@ def main(argv=None):
     ap.add_argument("--intervals", type=int, default=1)
     ap.add_argument("--physics", type=int, default=1, help="1: convection, Kzz, emission, chemistry; 0: advection")
     ap.add_argument("--lmax", type=int, default=None)
+    ap.add_argument("--fp64-rates", action="store_true", help="measure the FP64 issue rates and exit")
     a = ap.parse_args(argv)
     from __graft_entry__ import build
 
@@ -102,6 +105,11 @@ def main(argv=None):
     from .forward import Forward
 
     dev = Device(0)
+    if a.fp64_rates:
+        for name, rate in dev.fp64_rates().items():
+            print(f"{name}: {rate:.1f} G instructions/s")
+        dev.close()
+        return
     fw = Forward(dev, a.config, a.levels, a.seed, physics=bool(a.physics), lmax=a.lmax)
     n0 = dev.launches()
     for _ in range(a.intervals):
