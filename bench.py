@@ -23,6 +23,7 @@ With N > 1 (torchrun), every rank runs an independent replica of the workload (t
 data-parallel split; the runs are independent members) and rank 0 reports the whole-job rate."""
 
 import argparse
+import hashlib
 import json
 import os
 import statistics
@@ -155,6 +156,38 @@ def cpu_baseline(workload, seconds=15.0):
             "sample": f"{n} whole intervals of {workload} on one host thread ({per:.3f} s each)"}  # fmt: skip
 
 
+def run_reference_ensemble(args):
+    """The reference arm of the ensemble: the oracle port looped over the members, timed on a
+    bounded sample -- one interval of one member of each class -- and scaled by the mix."""
+    from oracle.forward import OracleRun
+    from pydyn_gb300.ensemble import CLASSES, MIX
+
+    mix = MIX if not args.mix else tuple((c, int(n)) for c, n in (x.split(":") for x in args.mix.split(",")))
+    per_step, sample = 0.0, []
+    for cls, count in mix:
+        tree, lm, lmax, seed = CLASSES[cls]
+        orc = OracleRun(tree, lm, seed, physics=True, lmax=lmax)
+        t0 = time.perf_counter()
+        orc.interval()
+        sec = time.perf_counter() - t0
+        per_step += count * sec
+        sample.append(f"{cls} {sec:.2f} s")
+    n = sum(c for _, c in mix)
+    v = n * sim_years_per_hour(per_step)
+    line = {
+        "impl": "reference", "metric": "member-years/hour, 256-member ensemble (128 glb6×4, 96 glb3×2, "
+        "32 glb3×2+nam1×1) FP64-bitwise", "value": v, "unit": "member-years/hour", "n_gpus": args.gpus,
+        "steps": 1, "warmup": 0, "ms_per_step": per_step * 1e3, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": "ensemble", "members": n, "mix": [list(m) for m in mix]},
+        "cpu_baseline": {"value": v, "unit": "member-years/hour", "cores": 1, "kind": "port",
+                         "sample": "one interval of one member per class (oracle, one host thread): "
+                                   + ", ".join(sample) + "; scaled by the member counts"},
+        "e2e": {"value": v, "unit": "member-years/hour", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }  # fmt: skip
+    print(json.dumps(line), flush=True)
+
+
 def run_reference(args, ws, rank):
     """--impl reference: the CPU reference arm on rank 0 (the oracle port of pydyn)."""
     if rank != 0:
@@ -164,6 +197,9 @@ def run_reference(args, ws, rank):
     build()
     from oracle.forward import OracleRun
 
+    if args.config == "ensemble":
+        run_reference_ensemble(args)
+        return
     tree, lm, physics, seed, lmax = WORKLOADS[args.config]
     orc = OracleRun(tree, lm, seed, physics=physics, lmax=lmax)
     for _ in range(args.warmup):
@@ -186,16 +222,167 @@ def run_reference(args, ws, rank):
     print(json.dumps(line), flush=True)
 
 
+def _ensemble_timed(ens, steps, fn):
+    """Device time (s per step) of `steps` calls of fn(ens): an event on the first member's
+    stream that every member's stream waits on opens the region, each member's own event after
+    the last step closes it; the slowest member's span counts."""
+    d0 = ens.devs[0]
+    start = d0.event()
+    start.record()
+    for d in ens.devs[1:]:
+        d.wait(start)
+    for _ in range(steps):
+        fn(ens)
+    ends = []
+    for d in ens.devs:
+        e = d.event()
+        e.record()
+        ends.append(e)
+    ens.sync()
+    return max(start.elapsed_ms(e) for e in ends) / 1e3 / steps
+
+
+def run_ensemble(args, ws, rank):
+    """--config ensemble: the batched ensemble (pydyn_gb300.ensemble) against the plain step
+    looped over the same members, member-years per hour; every rank runs its own ensemble."""
+    from __graft_entry__ import build
+
+    build()
+    from pydyn_gb300.ensemble import MIX, Ensemble, member_specs
+    from pydyn_gb300.hostbuf import PinnedArray
+    from pydyn_gb300.tune import tune_classes, tune_width
+
+    def log(msg):
+        if rank == 0:
+            print(msg, file=sys.stderr, flush=True)
+
+    mix = MIX if not args.mix else tuple((c, int(n)) for c, n in (x.split(":") for x in args.mix.split(",")))
+    specs = member_specs(mix, seed=2024 + rank)
+    t_setup = time.perf_counter()
+    tuned = tune_classes(specs, log=log)
+    shapes = {c: s for c, (s, _) in tuned.items()}
+    costs = {c: ms for c, (_, ms) in tuned.items()}
+    ens = Ensemble(specs, shapes=shapes, costs=costs)
+    ens.step()  # every member's first interval, uncaptured, and its capture
+    width, _ = tune_width(ens, log=log)
+    setup_s = time.perf_counter() - t_setup
+    for _ in range(args.warmup):
+        ens.step()
+    barrier(ws)
+    n0 = sum(d.launches() for d in ens.devs)
+    with Clocks(int(os.environ.get("LOCAL_RANK", "0"))) as clk:
+        batched = max_over_ranks(_ensemble_timed(ens, args.steps, lambda e: e.step()), ws)
+    launches = sum(d.launches() for d in ens.devs) - n0
+    looped = max_over_ranks(_ensemble_timed(ens, args.steps, lambda e: e.step_looped()), ws)
+
+    # end to end: every member's new meteo instant in from pinned host memory, its tracer mass
+    # out, on its own stream around its graph
+    pin_in, pin_out, h2d, d2h = {}, {}, 0, 0
+    for k, fw in enumerate(ens.runs):
+        pin_in[k] = {r: [PinnedArray.copy_of(x) for x in fw.met.fluxes(r, 1)] for r in fw.zoom.regions()}
+        pin_out[k] = {r: PinnedArray.empty((fw.zoom.g(r).im, fw.zoom.g(r).jm, fw.zoom.lm, 1)) for r in fw.zoom.regions()}
+        h2d += sum(p.nbytes for v in pin_in[k].values() for p in v)
+        d2h += sum(p.nbytes for p in pin_out[k].values())
+
+    def before(k):
+        fw = ens.runs[k]
+        for r in fw.zoom.regions():
+            pu1, pv1 = fw.meteo[r][1]
+            pin_in[k][r][0].to_device(ens.devs[k], pu1)
+            pin_in[k][r][1].to_device(ens.devs[k], pv1)
+
+    def after(k):
+        fw = ens.runs[k]
+        for r in fw.zoom.regions():
+            g = fw.zoom.g(r)
+            pin_out[k][r].from_device(ens.devs[k], fw.st[r]["rm"][1 : g.im, 1 : g.jm, 1 : fw.zoom.lm])
+
+    ens.step(before, after)  # the staging arrays of the strided reads are made outside the timing
+    barrier(ws)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        ens.step(before, after)
+    e2e = max_over_ranks((time.perf_counter() - t0) / args.steps, ws)
+
+    # every class's first member against its solo run over the same intervals
+    from pydyn_gb300.device import Device
+
+    def digest(fw):
+        h = hashlib.sha1()
+        for r in fw.zoom.regions():
+            for name in sorted(fw.st[r]):
+                h.update(np.ascontiguousarray(fw.st[r][name].host()).tobytes())
+        return h.hexdigest()
+
+    checked = []
+    for cls, _ in mix:
+        k = next(i for i, s in enumerate(specs) if s.cls == cls)
+        fw = ens.runs[k]
+        got = digest(fw)
+        intervals = round(fw.t / fw.nread)
+        solo_dev = Device(0)
+        solo = specs[k].forward(solo_dev)
+        for _ in range(intervals):
+            solo.interval(graph=True)
+        want = digest(solo)
+        solo.close()
+        solo_dev.close()
+        checked.append({"member": k, "class": cls, "intervals": intervals, "bitwise": got == want})
+    n = len(specs)
+    step_bytes = 0
+    hbm, how = peaks()
+    for fw in ens.runs:
+        b_half = 496
+        for r in fw.zoom.regions():
+            g = fw.zoom.g(r)
+            step_bytes += g.im * g.jm * fw.zoom.lm * (2 * g.tref * b_half + 40 + 40 + 248)
+    line = {
+        "metric": "member-years/hour, 256-member ensemble (128 glb6×4, 96 glb3×2, 32 glb3×2+nam1×1) FP64-bitwise",
+        "value": n * sim_years_per_hour(batched) * ws,
+        "unit": "member-years/hour",
+        "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": batched * 1e3,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (seeded meteo per class, per-member wind scale and physics inputs; pydyn_gb300.synth)",
+        "config": {"workload": "ensemble", "members": n, "mix": [list(m) for m in mix], "width": width,
+                   "shapes": shapes, "physics": True,
+                   "step": "every member's captured interval (Check_CFL rehearsal + step), members in flight together",
+                   "l2": f"inputs larger than L2 (the members' state: {step_bytes / 1e9:.1f} GB of step traffic)",
+                   "parallelism": f"ensemble x{ws}"},
+        "plain_looped": {"value": n * sim_years_per_hour(looped) * ws, "unit": "member-years/hour",
+                         "ms_per_step": looped * 1e3},
+        "batched_vs_plain": looped / batched,
+        "roofline": {"bound": "hbm", "achieved": step_bytes / batched / 1e9, "peak": hbm, "unit": "GB/s",
+                     "frac": step_bytes / batched / 1e9 / hbm, "traffic": None, "peak_source": how,
+                     "note": "algorithmic step bytes of all members over the batched step; the float64 "
+                             "kernels are bound by the FP64 pipe, not HBM"},
+        "e2e": {"value": n * sim_years_per_hour(e2e) * ws, "unit": "member-years/hour", "h2d_bytes_per_step": h2d,
+                "d2h_bytes_per_step": d2h},
+        "gpu_launches": launches,
+        "clocks": clk.summary(),
+        "bitwise_vs_solo": checked,
+        "redone_intervals": ens.redone,
+        "setup_s": setup_s,
+        "cpu_baseline": None,
+    }  # fmt: skip
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    ens.close()
+
+
 def main():
     ap = argparse.ArgumentParser(description=__doc__.split("\n")[0])
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=100)  # ~1 s timed: several clock samples
     ap.add_argument("--warmup", type=int, default=3)
-    ap.add_argument("--config", default=DEFAULT, choices=sorted(WORKLOADS))
+    ap.add_argument("--config", default=DEFAULT, choices=sorted(WORKLOADS) + ["ensemble"])
+    ap.add_argument("--mix", default=None, help="ensemble members, e.g. glb6x4:128,glb3x2:96,glb3x2+nam1x1:32")
     ap.add_argument("--impl", default="gbdyn", choices=("gbdyn", "reference"))
     ap.add_argument("--no-cpu-baseline", action="store_true")
     args = ap.parse_args()
     ws, rank, local = dist_env()
+    if args.config == "ensemble":  # before the first CUDA call: one hardware queue per lane
+        os.environ.setdefault("CUDA_DEVICE_MAX_CONNECTIONS", "32")
     if ws > 1:
         import torch
         import torch.distributed as dist
@@ -206,6 +393,11 @@ def main():
         run_reference(args, ws, rank)
         return
     args.warmup = max(args.warmup, 3)
+    if args.config == "ensemble":
+        if args.steps == 100:  # the plain step's default; an ensemble step is ~0.5 s
+            args.steps = 5
+        run_ensemble(args, ws, rank)
+        return
 
     from __graft_entry__ import build
 

@@ -67,9 +67,24 @@ int gb_capture_end(gb_ctx *ctx, void **graph);
 int gb_graph_launch(gb_ctx *ctx, void *graph);
 int gb_graph_destroy(void *graph);
 
+/* Launch shapes the autotuner sets per context (pydyn_gb300.tune).  They choose how work is
+ * laid onto threads and blocks, never what any element computes: results are bitwise the same
+ * for every accepted value.  No reference counterpart (pydyn has no device launch shapes). */
+#define GB_TUNE_COLUMN_THREADS 0 /* thread-per-column kernels (convection chains, Kzz columns): 32..256 */
+#define GB_TUNE_CELL_THREADS 1   /* thread-per-cell kernels (convection matrix, Kzz, chemistry): 32..512 */
+#define GB_TUNE_LU_WARPS 2       /* columns (one warp each) per block of the convection LU: 1, 2, 4 */
+#define GB_TUNE_APPLY_THREADS 3  /* the convection apply's smallest block (whole columns): 32..1024 */
+#define GB_TUNE_N 4
+int gb_device_name(gb_ctx *ctx, char *buf, int len); /* "<name> sm_<cc> x<SMs>": the tuning cache's key */
+int gb_tune_set(gb_ctx *ctx, int key, int value); /* GB_EARG for a value outside the key's range */
+int gb_tune_get(gb_ctx *ctx, int key, int *value);
+
 /* Timing: events recorded on the context's stream. */
 int gb_event_create(void **ev);
 int gb_event_record(gb_ctx *ctx, void *ev);
+/* Work enqueued on the context's stream after this call waits for the event (recorded on
+ * another context's stream): how an ensemble bounds how many members run at once. */
+int gb_stream_wait(gb_ctx *ctx, void *ev);
 int gb_event_elapsed_ms(void *start, void *stop, float *ms);
 int gb_event_destroy(void *ev);
 

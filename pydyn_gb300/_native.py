@@ -9,6 +9,8 @@ import numpy as np
 from .build import LIBGBDYN, LIBGBMATH
 
 GB_OK, GB_ECFL, GB_EHALO, GB_ELEVELS, GB_ESEARCH, GB_EARG, GB_ECUDA, GB_ETIMEOUT = 0, 1, 2, 4, 8, 16, 32, 64
+# launch-shape keys of gb_tune_set / gb_tune_get
+TUNE_KEYS = {"column_threads": 0, "cell_threads": 1, "lu_warps": 2, "apply_threads": 3}
 
 
 class GBView(ctypes.Structure):
@@ -54,6 +56,10 @@ SIGNATURES = {
     "gb_graph_destroy": (_I, [_VP]),
     "gb_event_create": (_I, [ctypes.POINTER(_VP)]),
     "gb_event_record": (_I, [_VP, _VP]),
+    "gb_stream_wait": (_I, [_VP, _VP]),
+    "gb_device_name": (_I, [_VP, ctypes.c_char_p, _I]),
+    "gb_tune_set": (_I, [_VP, _I, _I]),
+    "gb_tune_get": (_I, [_VP, _I, ctypes.POINTER(_I)]),
     "gb_event_elapsed_ms": (_I, [_VP, _VP, ctypes.POINTER(ctypes.c_float)]),
     "gb_event_destroy": (_I, [_VP]),
     "gb_cfl_reset": (_I, [_VP]),

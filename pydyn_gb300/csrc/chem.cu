@@ -19,7 +19,6 @@
 
 namespace {
 
-constexpr int CELL_THREADS = 128;
 
 struct CArgs {
     DV temper, phlb, soil, oh3d, pltrop, cltrop, sp, soh, scl, sod;
@@ -126,7 +125,7 @@ __global__ void k_chem_rows(CArgs A) {
 }
 
 // thread per (column, level): the four rates, the decay, and its use
-__global__ void __launch_bounds__(CELL_THREADS) k_chem(CArgs A) {
+__global__ void __launch_bounds__(GB_TUNE_MAX_CELL) k_chem(CArgs A) {
     const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     const int lm = A.lm;
     if (t >= A.ncol * lm) return;
@@ -270,7 +269,8 @@ int launch_chem(gb_ctx *ctx, CArgs &A) {
     k_chem_rows<<<(unsigned)((A.jm + 127) / 128), 128, 0, ctx->stream>>>(A);
     if (int rc = gb_after_launch(ctx, "chem_rows")) return rc;
     const int64_t cells = A.ncol * A.lm;
-    k_chem<<<(unsigned)((cells + CELL_THREADS - 1) / CELL_THREADS), CELL_THREADS, 0, ctx->stream>>>(A);
+    const int tcell = ctx->tune[GB_TUNE_CELL_THREADS];
+    k_chem<<<gb_blocks(cells, tcell), tcell, 0, ctx->stream>>>(A);
     return gb_after_launch(ctx, A.apply ? "chemistry" : "loss_rates");
 }
 
@@ -342,7 +342,8 @@ extern "C" int gb_chem_krates(gb_ctx *ctx, const gb_view *temper, const int32_t 
     const int64_t n = cols ? (int64_t)ncol : temper->n[0] * temper->n[1];
     const int lm = (int)temper->n[2];
     if (n == 0) return GB_OK;
-    k_chem_krates<<<(unsigned)((n * lm + CELL_THREADS - 1) / CELL_THREADS), CELL_THREADS, 0, ctx->stream>>>(
+    const int tcell = ctx->tune[GB_TUNE_CELL_THREADS];
+    k_chem_krates<<<gb_blocks(n * lm, tcell), tcell, 0, ctx->stream>>>(
         dv(temper), dv(krates), cols, n, (int)temper->n[1], lm);
     return gb_after_launch(ctx, "chem_krates");
 }

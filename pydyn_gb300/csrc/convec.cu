@@ -35,9 +35,7 @@
 
 namespace {
 
-constexpr int WARPS = 2;
 constexpr int NMAX = 64;
-constexpr int MATRIX_THREADS = 64;
 
 struct CArgs {
     DV m, q[4];
@@ -73,7 +71,7 @@ constexpr int NCHAIN = 4;
 __device__ __forceinline__ double *chains(const CArgs &A, int c) { return A.chain + (size_t)c * NCHAIN * (A.n + 1); }
 
 // thread per column: whether the kept inverse still holds; the updraft and downdraft chains
-__global__ void __launch_bounds__(MATRIX_THREADS) k_convec_chains(CArgs A) {
+__global__ void __launch_bounds__(GB_TUNE_MAX_COLUMN) k_convec_chains(CArgs A) {
     const int c = blockIdx.x * blockDim.x + threadIdx.x;
     if (c >= A.ncol) return;
     const int n = A.n;
@@ -127,7 +125,7 @@ __global__ void __launch_bounds__(MATRIX_THREADS) k_convec_chains(CArgs A) {
 // chain fd(k, l) for k = l down to 1 (zero elsewhere), plus the updraft chain fu(k, l) for
 // k = l+1 up, plus the diagonal terms; f(0, l) = f(n, l) = 0.  conv1(k-1, l) =
 // -dt (f(k-1, l) - f(k, l)), plus 1 on the diagonal.
-__global__ void __launch_bounds__(MATRIX_THREADS) k_convec_matrix(CArgs A) {
+__global__ void __launch_bounds__(GB_TUNE_MAX_CELL) k_convec_matrix(CArgs A) {
     const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     const int n = A.n;
     if (t >= (int64_t)A.ncol * n) return;
@@ -215,7 +213,7 @@ __global__ void __launch_bounds__(MATRIX_THREADS) k_convec_matrix(CArgs A) {
 // conv1: U's diagonal (its band above stays) and L's band below; and the rows' term ends.
 // fresh = 2 tells the warp kernel the column is done and k_convec_apply that L^-1 is still to be
 // made from that band.  A column with a zero or non-finite band entry is left to the warp kernel.
-__global__ void __launch_bounds__(MATRIX_THREADS) k_convec_tri(CArgs A) {
+__global__ void __launch_bounds__(GB_TUNE_MAX_COLUMN) k_convec_tri(CArgs A) {
     const int c = blockIdx.x * blockDim.x + threadIdx.x;
     if (c >= A.ncol || A.fresh[c] != 1) return;
     const int i = A.cols[2 * c], j = A.cols[2 * c + 1];
@@ -247,10 +245,10 @@ __global__ void __launch_bounds__(MATRIX_THREADS) k_convec_tri(CArgs A) {
 // shared memory of one warp (doubles): the matrix (conv1, then LU) and L^-1, n*n each
 __host__ __device__ __forceinline__ size_t warp_doubles(int n) { return 2 * (size_t)n * n; }
 
-__global__ void __launch_bounds__(WARPS * 32) k_convec_lu(CArgs A) {
+__global__ void __launch_bounds__(GB_TUNE_MAX_LU_WARPS * 32) k_convec_lu(CArgs A) {
     extern __shared__ double smem[];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int c = blockIdx.x * WARPS + warp;
+    const int c = blockIdx.x * (blockDim.x >> 5) + warp;
     if (c >= A.ncol || A.fresh[c] != 1) return;
     const int n = A.n;
     double *LU = smem + (size_t)warp * warp_doubles(n);  // n x n
@@ -408,21 +406,27 @@ extern "C" int gb_convec(gb_ctx *ctx, const gb_view *m, const gb_view *rm, const
     A.cache_m = cache_inv ? cache_m : nullptr;
     A.cache_tag = cache_tag;
     A.epoch = epoch;
-    k_convec_chains<<<(ncol + MATRIX_THREADS - 1) / MATRIX_THREADS, MATRIX_THREADS, 0, ctx->stream>>>(A);
+    const int tcol = ctx->tune[GB_TUNE_COLUMN_THREADS], tcell = ctx->tune[GB_TUNE_CELL_THREADS];
+    k_convec_chains<<<gb_blocks(ncol, tcol), tcol, 0, ctx->stream>>>(A);
     if (int rc = gb_after_launch(ctx, "convec_chains")) return rc;
-    const int64_t nel = (int64_t)ncol * lmax;
-    k_convec_matrix<<<(unsigned)((nel + MATRIX_THREADS - 1) / MATRIX_THREADS), MATRIX_THREADS, 0, ctx->stream>>>(A);
+    k_convec_matrix<<<gb_blocks((int64_t)ncol * lmax, tcell), tcell, 0, ctx->stream>>>(A);
     if (int rc = gb_after_launch(ctx, "convec_matrix")) return rc;
-    k_convec_tri<<<(ncol + MATRIX_THREADS - 1) / MATRIX_THREADS, MATRIX_THREADS, 0, ctx->stream>>>(A);
+    k_convec_tri<<<gb_blocks(ncol, tcol), tcol, 0, ctx->stream>>>(A);
     if (int rc = gb_after_launch(ctx, "convec_tri")) return rc;
-    const size_t smem = (size_t)WARPS * warp_doubles(lmax) * sizeof(double);
+    // warps (columns) per LU block: the tuned count, fewer where their shared memory would not fit
+    int warps = ctx->tune[GB_TUNE_LU_WARPS];
+    while (warps > 1 && (size_t)warps * warp_doubles(lmax) * sizeof(double) > 227 * 1024) warps /= 2;
+    const size_t smem = (size_t)warps * warp_doubles(lmax) * sizeof(double);
     GB_CHECK_CUDA(cudaFuncSetAttribute(k_convec_lu, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    k_convec_lu<<<(ncol + WARPS - 1) / WARPS, WARPS * 32, smem, ctx->stream>>>(A);
+    k_convec_lu<<<gb_blocks(ncol, warps), warps * 32, smem, ctx->stream>>>(A);
     if (int rc = gb_after_launch(ctx, "convec_lu")) return rc;
-    // whole columns per block, as many as make the block a whole number of warps (<= 1024 threads)
+    // whole columns per block, as many as make the block a whole number of warps (<= 1024
+    // threads), and at least the tuned block size
     int per = 32 / gcd(lmax, 32);
     while (per > 1 && per * lmax > 1024) per /= 2;
-    if (per * lmax < 128) per = (128 + lmax - 1) / lmax;
+    const int least = ctx->tune[GB_TUNE_APPLY_THREADS];
+    if (per * lmax < least) per = (least + lmax - 1) / lmax;
+    while (per > 1 && ((per * lmax + 31) / 32) * 32 > 1024) --per;
     A.cols_per_block = per;
     const int threads = ((per * lmax + 31) / 32) * 32;
     k_convec_apply<<<(ncol + per - 1) / per, threads, 0, ctx->stream>>>(A);

@@ -33,6 +33,7 @@ struct gb_ctx {
     double *work = nullptr;        // per-op float64 work space, grown outside capture (gb_work)
     size_t work_bytes = 0;
     int64_t launches = 0;
+    int tune[GB_TUNE_N] = {64, 128, 2, 128};  // launch shapes (GB_TUNE_*)
     bool capturing = false;
     int64_t capture_launches = 0;
 };
@@ -144,6 +145,10 @@ __device__ __forceinline__ void raise_status(gb_ctl *ctl, int bits) { atomicOr(&
 __device__ __forceinline__ void atomic_max_nonneg(double *addr, double v) {
     atomicMax((unsigned long long *)addr, (unsigned long long)__double_as_longlong(v));
 }
+
+// the largest block a tunable kernel is compiled for (its __launch_bounds__)
+constexpr int GB_TUNE_MAX_COLUMN = 256, GB_TUNE_MAX_CELL = 512, GB_TUNE_MAX_LU_WARPS = 4;
+static inline unsigned gb_blocks(int64_t n, int threads) { return (unsigned)((n + threads - 1) / threads); }
 
 #define GB_WARP 32
 #define FULL_MASK 0xffffffffu

@@ -71,6 +71,38 @@ extern "C" int gb_create(int device, gb_ctx **out) {
     return GB_OK;
 }
 
+extern "C" int gb_device_name(gb_ctx *ctx, char *buf, int len) {
+    if (!ctx || !buf || len <= 0) return GB_EARG;
+    cudaDeviceProp prop;
+    GB_CHECK_CUDA(cudaGetDeviceProperties(&prop, ctx->device));
+    snprintf(buf, (size_t)len, "%s sm_%d%d x%d", prop.name, prop.major, prop.minor, prop.multiProcessorCount);
+    return GB_OK;
+}
+
+extern "C" int gb_tune_set(gb_ctx *ctx, int key, int value) {
+    if (!ctx || key < 0 || key >= GB_TUNE_N) return GB_EARG;
+    const bool pow2 = value > 0 && (value & (value - 1)) == 0;
+    bool ok = false;
+    switch (key) {
+        case GB_TUNE_COLUMN_THREADS: ok = pow2 && value >= 32 && value <= GB_TUNE_MAX_COLUMN; break;
+        case GB_TUNE_CELL_THREADS: ok = pow2 && value >= 32 && value <= GB_TUNE_MAX_CELL; break;
+        case GB_TUNE_LU_WARPS: ok = pow2 && value <= GB_TUNE_MAX_LU_WARPS; break;
+        case GB_TUNE_APPLY_THREADS: ok = value >= 32 && value <= 1024; break;
+    }
+    if (!ok) {
+        gb_set_error("gb_tune_set: value " + std::to_string(value) + " outside the range of key " + std::to_string(key));
+        return GB_EARG;
+    }
+    ctx->tune[key] = value;
+    return GB_OK;
+}
+
+extern "C" int gb_tune_get(gb_ctx *ctx, int key, int *value) {
+    if (!ctx || !value || key < 0 || key >= GB_TUNE_N) return GB_EARG;
+    *value = ctx->tune[key];
+    return GB_OK;
+}
+
 extern "C" void gb_destroy(gb_ctx *ctx) {
     if (!ctx) return;
     cudaSetDevice(ctx->device);
@@ -220,6 +252,11 @@ extern "C" int gb_event_create(void **ev) {
 }
 extern "C" int gb_event_record(gb_ctx *ctx, void *ev) {
     GB_CHECK_CUDA(cudaEventRecord((cudaEvent_t)ev, ctx->stream));
+    return GB_OK;
+}
+extern "C" int gb_stream_wait(gb_ctx *ctx, void *ev) {
+    if (!ctx || !ev) return GB_EARG;
+    GB_CHECK_CUDA(cudaStreamWaitEvent(ctx->stream, (cudaEvent_t)ev, 0));
     return GB_OK;
 }
 extern "C" int gb_event_elapsed_ms(void *start, void *stop, float *ms) {

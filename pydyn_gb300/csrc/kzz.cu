@@ -23,7 +23,6 @@ constexpr double LVAP = 2.5e6, RGAS = 8.3144, XMAIR = 28.94, RHO_AIR = 1.2, CKMI
 constexpr double APZERO = 100000.0, BETAH = 15.0, FAK = 8.5, FAKN = 7.2, TINY = 1.0e-9, ZACB = 100.0;
 constexpr double RICR = 0.3, SSFRAC = 0.1, KVHMIN = 0.1;
 constexpr int NCOLVAL = 10;  // z0, pblh, wobkl, wheatv, ustr, zwstr, t1a, t2a, t1b, t2b
-constexpr int THREADS = 128;
 
 struct KArgs {
     DV spm, sp, pu, pv, t, q, surf[10], dkg, pblh;
@@ -53,7 +52,7 @@ __global__ void k_kzz_rows(KArgs A) {
     A.dxx[j] = AE * A.dx * GTOR * gbm_cos(lat * GTOR);
 }
 
-__global__ void __launch_bounds__(THREADS) k_kzz_levels(KArgs A) {
+__global__ void __launch_bounds__(GB_TUNE_MAX_CELL) k_kzz_levels(KArgs A) {
     const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     const int lm = A.lm;
     if (t >= (int64_t)A.im * A.jm * lm) return;
@@ -105,7 +104,7 @@ __device__ double pbl_sweep(double pblh, const double *whm, const double *uw, co
     return first ? (1.0 - jwork) * pblh + whm[lm - 1] * jwork : (1.0 - jwork) * pblh + jwork * whm[lm - 1];
 }
 
-__global__ void __launch_bounds__(THREADS) k_kzz_columns(KArgs A) {
+__global__ void __launch_bounds__(GB_TUNE_MAX_COLUMN) k_kzz_columns(KArgs A) {
     const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (c >= (int64_t)A.im * A.jm) return;
     const int i = (int)(c / A.jm), j = (int)(c % A.jm);
@@ -182,7 +181,7 @@ __global__ void __launch_bounds__(THREADS) k_kzz_columns(KArgs A) {
     cv[9] = sqrt(stab1);
 }
 
-__global__ void __launch_bounds__(THREADS) k_kzz_interfaces(KArgs A) {
+__global__ void __launch_bounds__(GB_TUNE_MAX_CELL) k_kzz_interfaces(KArgs A) {
     const int lm = A.lm, ni = lm - 1;
     const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= (int64_t)A.im * A.jm * ni) return;
@@ -259,8 +258,6 @@ __global__ void __launch_bounds__(THREADS) k_kzz_interfaces(KArgs A) {
     if (k == 1) S3(A.dkg, i, j, A.lmax - 1) = 0.0;
 }
 
-unsigned blocks(int64_t n) { return (unsigned)((n + THREADS - 1) / THREADS); }
-
 }  // namespace
 
 extern "C" int gb_calc_kzz(gb_ctx *ctx, const gb_view *spm, const gb_view *sp, const gb_view *pu, const gb_view *pv,
@@ -295,12 +292,13 @@ extern "C" int gb_calc_kzz(gb_ctx *ctx, const gb_view *spm, const gb_view *sp, c
     A.whm = w; w += ncell;
     A.gph = w; w += ncol * (A.lm + 1);
     A.col = w;
-    k_kzz_rows<<<blocks(A.jm), THREADS, 0, ctx->stream>>>(A);
+    const int tcol = ctx->tune[GB_TUNE_COLUMN_THREADS], tcell = ctx->tune[GB_TUNE_CELL_THREADS];
+    k_kzz_rows<<<gb_blocks(A.jm, 128), 128, 0, ctx->stream>>>(A);
     if (int rc = gb_after_launch(ctx, "kzz_rows")) return rc;
-    k_kzz_levels<<<blocks(ncell), THREADS, 0, ctx->stream>>>(A);
+    k_kzz_levels<<<gb_blocks(ncell, tcell), tcell, 0, ctx->stream>>>(A);
     if (int rc = gb_after_launch(ctx, "kzz_levels")) return rc;
-    k_kzz_columns<<<blocks(ncol), THREADS, 0, ctx->stream>>>(A);
+    k_kzz_columns<<<gb_blocks(ncol, tcol), tcol, 0, ctx->stream>>>(A);
     if (int rc = gb_after_launch(ctx, "kzz_columns")) return rc;
-    k_kzz_interfaces<<<blocks(ncol * (A.lm - 1)), THREADS, 0, ctx->stream>>>(A);
+    k_kzz_interfaces<<<gb_blocks(ncol * (A.lm - 1), tcell), tcell, 0, ctx->stream>>>(A);
     return gb_after_launch(ctx, "kzz_interfaces");
 }

@@ -88,6 +88,10 @@ class Device:
     def event(self):
         return Event(self)
 
+    def wait(self, event):
+        """Work enqueued here from now on waits for `event` (recorded on any context's stream)."""
+        N.check(self.L.gb_stream_wait(self.h, event.p), "gb_stream_wait")
+
     # -------------------------------------------------------------- Check_CFL flag
     def cfl_reset(self):
         N.check(self.L.gb_cfl_reset(self.h), "gb_cfl_reset")
@@ -96,6 +100,27 @@ class Device:
         f = ctypes.c_int()
         N.check(self.L.gb_cfl_failed(self.h, ctypes.byref(f)), "gb_cfl_failed")
         return bool(f.value)
+
+    # -------------------------------------------------------------- launch shapes
+    def name(self):
+        """The GPU's name, compute capability and SM count."""
+        buf = ctypes.create_string_buffer(256)
+        N.check(self.L.gb_device_name(self.h, buf, 256), "gb_device_name")
+        return buf.value.decode()
+
+    def tuning(self):
+        """{name: value} of the context's launch shapes (gb_tune_get)."""
+        out = {}
+        for name, key in N.TUNE_KEYS.items():
+            v = ctypes.c_int()
+            N.check(self.L.gb_tune_get(self.h, key, ctypes.byref(v)), "gb_tune_get")
+            out[name] = v.value
+        return out
+
+    def tune(self, **shapes):
+        """Set launch shapes by name (gb_tune_set); results do not depend on them."""
+        for name, value in shapes.items():
+            N.check(self.L.gb_tune_set(self.h, N.TUNE_KEYS[name], int(value)), f"gb_tune_set({name}={value})")
 
     # -------------------------------------------------------------- FP64 ceiling
     def fp64_rates(self):

@@ -37,11 +37,12 @@ class Forward:
     """A configuration's run on one device: the state, the Check_CFL copy, the meteo instants."""
 
     def __init__(self, dev, config="glb6x4", lm=25, seed=0, nt=1, ndyn=3600, nread=3600, limits=True, physics=False,
-                 umax=40.0, lmax=None):  # fmt: skip
+                 umax=40.0, lmax=None, wind_scale=1.0, physics_seed=None):  # fmt: skip
         """physics: with convection (Kzz folded in), emission and CH4 chemistry over lmax levels
-        (default lm), on the inputs of pydyn_gb300.synth.Physics; without, advection only."""
+        (default lm), on the inputs of pydyn_gb300.synth.Physics drawn from physics_seed (default
+        seed); without, advection only.  wind_scale multiplies the meteo's winds."""
         self.dev = dev
-        self.zoom, self.met, fields = synth.case(config, lm, seed, nt, umax=umax)
+        self.zoom, self.met, fields = synth.case(config, lm, seed, nt, umax=umax, wind_scale=wind_scale)
         self.st = ZoomState.from_host(dev, self.zoom, fields)
         self.cfl_st = ZoomState.zeros(dev, self.zoom, nt)
         for r in self.zoom.regions():
@@ -57,7 +58,8 @@ class Forward:
         if physics:
             from .physics import Physics
 
-            spec = synth.Physics(self.zoom, self.met, seed, lm if lmax is None else lmax)
+            pseed = seed if physics_seed is None else physics_seed
+            spec = synth.Physics(self.zoom, self.met, pseed, lm if lmax is None else lmax)
             self.physics = Physics(dev, self.zoom, spec, {r: self.st[r]["dxyp"] for r in self.zoom.regions()})
             self.physics.init_state(self.st)
         self.graphs = {}
@@ -157,21 +159,33 @@ class Forward:
             # the first interval runs uncaptured: every device constant and scratch array the
             # bodies create lazily exists before capture (allocation is not capturable)
             out = self.interval(graph=False)
+            self.capture_interval()
+            return out
+        self.enqueue_interval_async(t0)
+        return self.settle_interval(t0)
+
+    def capture_interval(self):
+        """(Re)capture the interval graph with the context's current launch shapes; the run has
+        made one uncaptured interval before (its lazily made device arrays exist)."""
+        if not hasattr(self, "_spec"):
             self._spec = {(r, k): DevArray.zeros(self.dev, *((lo, lo + n - 1) for lo, n in
                                                          zip(a.lower, a.shape, strict=True)))
                           for r in self.zoom.regions() for k, a in self.st[r].items() if k in SPECULATED}  # fmt: skip
-            self.st.lib.save(self.cfl_st, "check_cfl", ("m", "am", "bm", "cm"))
-            self.dev.sync()
-            with self.dev.capture() as g:
-                self._enqueue_interval()
-            self.graphs["interval"] = g
-            return out
-        self.put_step_inputs(t0, self.nread)
-        self.graphs["interval"].launch()
+        self.st.lib.save(self.cfl_st, "check_cfl", ("m", "am", "bm", "cm"))
+        self.dev.sync()
+        self.graphs.pop("interval", None)
+        with self.dev.capture() as g:
+            self._enqueue_interval()
+        self.graphs["interval"] = g
+
+    def settle_interval(self, t0):
+        """After a launched interval: read the rehearsal's flag; if Check_CFL rejected ndyn =
+        nread, put the state back and redo the interval uncaptured.  Returns (ndyn, n)."""
         if self.dev.cfl_failed():  # the speculation was wrong: back to the interval's start
             for (r, k), a in self._spec.items():
                 self.st[r][k].assign(a)
             self.dev.discard_status()  # the speculative step's own errors are not the run's
+            self.t = t0
             return self.interval(graph=False)
         self.dev.sync()
         self.t = t0 + self.nread

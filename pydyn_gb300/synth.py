@@ -400,14 +400,15 @@ class Physics:
         return np.stack([self.oh_factor(r, t0 + h * dt) for h in range(2 * self.zoom.g(r).tref)])
 
 
-def case(name, lm, seed=0, nt=1, umax=40.0):
+def case(name, lm, seed=0, nt=1, umax=40.0, wind_scale=1.0):
     """(zoom, meteo, {r: {field: host array}}): the initial state of every region in the
     declared (halo'd) shapes: m and rm from the meteo's surface pressure, slopes zero, dxyp.
-    pu / pv are set per step by the run (interpolated between the meteo instants)."""
+    pu / pv are set per step by the run (interpolated between the meteo instants); wind_scale
+    multiplies the winds (an ensemble member's perturbation)."""
     from .state import bounds
 
     zoom = tree(name, lm)
-    met = Meteo(zoom, seed, umax=umax)
+    met = Meteo(zoom, seed, umax=umax, wind_scale=wind_scale)
     fields = {}
     for r in zoom.regions():
         g = zoom.g(r)
