@@ -370,12 +370,102 @@ def run_ensemble(args, ws, rank):
     ens.close()
 
 
+def run_adjoint(args, ws, rank):
+    """--config adjoint: the CH4 surface-flux gradient on glb3x2 (34 levels, physics, unlimited
+    slopes) through `--hours` one-hour intervals (default 168: 7 days), 500 seeded samples,
+    checkpoints every 6 intervals: the forward J, the checkpointed adjoint, their ratio; the
+    dot-product test on one interval; central differences on `--fd` flux elements."""
+    from __graft_entry__ import build
+
+    build()
+    from pydyn_gb300.adjoint import FluxGradient, make_samples
+    from pydyn_gb300.device import DevArray, Device
+    from pydyn_gb300.forward import Forward
+
+    dev = Device(int(os.environ.get("LOCAL_RANK", "0")))
+    hours = args.hours
+    fw = Forward(dev, "glb3x2", 34, seed=41, physics=True, lmax=34, limits=False)
+    im, jm = fw.zoom.g(1).im, fw.zoom.g(1).jm
+    samples = make_samples(fw.zoom, hours, 500, seed=7)
+
+    # the dot-product test on the first interval: tracers x, adjoints y (the state put back after)
+    prob = FluxGradient(fw, hours, samples, np.zeros(len(samples)), every=6)
+    flux = fw.physics.r[1]["flux"].host()
+    rng = np.random.default_rng(9)
+    names = ("rm", "rxm", "rym", "rzm")
+    shape = (4, im, jm, 34)
+    scale = np.array([1.0, 0.3, 0.3, 0.3])[:, None, None, None]
+    x, y = rng.random(shape) * scale, (rng.random(shape) + 0.5) * scale
+    prob.set_flux(np.zeros((im, jm)))
+    for w, name in enumerate(names):
+        fw.st[1][name][1:im, 1:jm, 1:34, 1:1].upload(x[w][..., None])
+    tape = prob._taped_interval()
+    ax = np.stack([fw.st[1][name][1:im, 1:jm, 1:34, 1].host() for name in names])
+    qb = [DevArray.from_host(dev, y[w][..., None], lower=(1, 1, 1, 1)) for w in range(4)]
+    g0 = DevArray.zeros(dev, (0, im - 1), (0, jm - 1))
+    for op in reversed(tape):
+        prob._adjoint_op(op, qb, g0)
+    aty = np.stack([q.host()[..., 0] for q in qb])
+    lhs, rhs = float(np.dot(ax.ravel(), y.ravel())), float(np.dot(x.ravel(), aty.ravel()))
+    dot_rel = abs(lhs - rhs) / abs(lhs)
+    prob._restore(prob.start)
+    prob.set_flux(flux)
+
+    # observations: the first guess's sampled values perturbed by 2 %
+    prob.cost(flux)
+    rows = np.concatenate([prob.rm_at[h][0] for h in range(1, hours + 1)])
+    vals = np.concatenate([prob.rm_at[h][1] for h in range(1, hours + 1)])
+    obs = np.empty(len(samples))
+    obs[rows] = vals * (1.0 + 0.02 * np.random.default_rng(4).standard_normal(len(vals)))
+    prob.obs = obs
+    prob.cost(flux)  # warm: every lazily made array exists
+    prob.gradient().free()
+    dev.sync()
+    t0 = time.perf_counter()
+    J = prob.cost(flux)
+    t_fwd = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    grad = prob.gradient().host()
+    t_adj = time.perf_counter() - t0
+
+    # central differences (step 1e-6 relative) on seeded flux elements
+    fd_err, picks = [], np.random.default_rng(11).choice(im * jm, args.fd, replace=False)
+    for k in picks:
+        i, j = np.unravel_index(int(k), (im, jm))
+        h = 1e-6 * abs(flux[i, j])
+        fp, fm = flux.copy(), flux.copy()
+        fp[i, j] += h
+        fm[i, j] -= h
+        fd = (prob.cost(fp) - prob.cost(fm)) / (2.0 * h)
+        fd_err.append(abs(fd - grad[i, j]) / np.abs(grad).max())
+    line = {
+        "metric": "adjoint cost / forward cost, CH4 surface-flux gradient, glb3×2 7 days",
+        "value": t_adj / t_fwd, "unit": "x forward", "higher_is_better": False,
+        "n_gpus": ws, "steps": hours, "warmup": 1, "ms_per_step": t_adj / hours * 1e3,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (glb3x2 case of pydyn_gb300.synth, 500 seeded samples, 2 % perturbed observations)",
+        "config": {"workload": "adjoint", "tree": "glb3x2", "levels": 34, "lmax": 34, "hours": hours,
+                   "checkpoint_every": 6, "samples": len(samples), "limits": False},
+        "forward_s": t_fwd, "adjoint_s": t_adj, "J": J,
+        "dot_product_rel_err": dot_rel,
+        "fd": {"elements": int(args.fd), "step": "1e-6 relative", "max_err_rel_to_max_grad": max(fd_err) if fd_err else None},
+        "gpu_launches": None, "e2e": None, "cpu_baseline": None,
+    }  # fmt: skip
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    prob.close()
+    fw.close()
+    dev.close()
+
+
 def main():
     ap = argparse.ArgumentParser(description=__doc__.split("\n")[0])
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=100)  # ~1 s timed: several clock samples
     ap.add_argument("--warmup", type=int, default=3)
-    ap.add_argument("--config", default=DEFAULT, choices=sorted(WORKLOADS) + ["ensemble"])
+    ap.add_argument("--config", default=DEFAULT, choices=sorted(WORKLOADS) + ["ensemble", "adjoint"])
+    ap.add_argument("--hours", type=int, default=168, help="adjoint: one-hour intervals")
+    ap.add_argument("--fd", type=int, default=50, help="adjoint: flux elements checked by central differences")
     ap.add_argument("--mix", default=None, help="ensemble members, e.g. glb6x4:128,glb3x2:96,glb3x2+nam1x1:32")
     ap.add_argument("--impl", default="gbdyn", choices=("gbdyn", "reference"))
     ap.add_argument("--no-cpu-baseline", action="store_true")
@@ -393,6 +483,9 @@ def main():
         run_reference(args, ws, rank)
         return
     args.warmup = max(args.warmup, 3)
+    if args.config == "adjoint":
+        run_adjoint(args, ws, rank)
+        return
     if args.config == "ensemble":
         if args.steps == 100:  # the plain step's default; an ensemble step is ~0.5 s
             args.steps = 5

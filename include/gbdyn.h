@@ -302,6 +302,33 @@ int gb_m2phlb(gb_ctx *ctx, const gb_view *m, const gb_view *sp, const gb_view *p
  * check that it equals the host build (libgbmath.so) bit for bit.  No reference counterpart. */
 int gb_math_eval(gb_ctx *ctx, int op, const double *x, const double *y, double *out, int64_t n);
 
+/* ------------------------------------------------------------------ the adjoint
+ * The transposes of a region-1 step's tracer operators with unlimited slopes (limits = 0), for
+ * the CH4 surface-flux gradient (one tracer: the adjoint views have nt = 1).  Each call reads
+ * the air mass and fluxes the forward operator was given -- taped by the host -- and overwrites
+ * the tracer adjoints (rm_b .. rzm_b, the interior (im, jm, lm, 1)) with the adjoints before the
+ * operator.  pydyn has no adjoint: these are the transposes of kernels.py:129-346 (dynamu,
+ * dynamv, dynamw) and :423-457 (convec), zoom/physics.py:55 (sources_region).
+ * gb_adjoint_x: m, am as gb_advect_x got them (am (im+1, jm, lm)), the sub-cycle search redone
+ *   as the forward did it; clust as gb_advect_x's.
+ * gb_adjoint_y: bm (im, jm+1, lm) before the call, nloop the device int32 per level the forward
+ *   returned through its nloop_out.
+ * gb_adjoint_z: cm (im, jm, lm+1), n_advz a device int32 (gb_advect_z_last after the forward).
+ * gb_adjoint_convec: inv the ncol (lmax x lmax) inverses the forward applied (the cache's).
+ * gb_adjoint_sources: grad (im, jm) += area(j) scale (rm_b - rzm_b)(level) on the columns. */
+int gb_advect_z_last(gb_ctx *ctx, int32_t *n_out);
+int gb_adjoint_x(gb_ctx *ctx, const gb_view *m, const gb_view *rm_b, const gb_view *rxm_b,
+                 const gb_view *rym_b, const gb_view *rzm_b, const gb_view *am, const int32_t *clust,
+                 int max_nloop);
+int gb_adjoint_y(gb_ctx *ctx, const gb_view *m, const gb_view *rm_b, const gb_view *rxm_b,
+                 const gb_view *rym_b, const gb_view *rzm_b, const gb_view *bm, const int32_t *nloop);
+int gb_adjoint_z(gb_ctx *ctx, const gb_view *m, const gb_view *rm_b, const gb_view *rxm_b,
+                 const gb_view *rym_b, const gb_view *rzm_b, const gb_view *cm, const int32_t *n_advz);
+int gb_adjoint_convec(gb_ctx *ctx, const gb_view *rm_b, const gb_view *rxm_b, const gb_view *rym_b,
+                      const gb_view *rzm_b, const double *inv, const int32_t *cols, int ncol, int lmax);
+int gb_adjoint_sources(gb_ctx *ctx, const gb_view *rm_b, const gb_view *rzm_b, const gb_view *grad,
+                       const double *area, double scale, int level, const int32_t *cols, int ncol);
+
 /* Measured FP64 issue rate of this GPU, instructions per second over all SMs: kind 0 a multiply
  * and an add (what -fmad=false emits), 1 a fused multiply-add, 2 a correctly rounded division.
  * The compute ceiling of the float64 step; not capturable.  No reference counterpart. */

@@ -97,6 +97,12 @@ SIGNATURES = {
     "gb_chem_krates": (_I, [_VP, _P, _VP, _I, _P]),
     "gb_sources": (_I, [_VP, _P, _P, _P, _VP, _D, _I, _I, _VP, _I]),
     "gb_math_eval":(_I, [_VP, _I, _VP, _VP, _VP, ctypes.c_int64]),
+    "gb_advect_z_last": (_I, [_VP, _VP]),
+    "gb_adjoint_x": (_I, [_VP, _P, _P, _P, _P, _P, _P, _VP, _I]),
+    "gb_adjoint_y": (_I, [_VP, _P, _P, _P, _P, _P, _P, _VP]),
+    "gb_adjoint_z": (_I, [_VP, _P, _P, _P, _P, _P, _P, _VP]),
+    "gb_adjoint_convec": (_I, [_VP, _P, _P, _P, _P, _VP, _VP, _I, _I]),
+    "gb_adjoint_sources": (_I, [_VP, _P, _P, _P, _VP, _D, _I, _VP, _I]),
     "gb_fp64_rate": (_I, [_VP, _I, ctypes.POINTER(_D)]),
     "gb_fluxes_from_meteo": (_I, [_VP, _P, _P, _VP, _D, _P, _P, _P]),
     "gb_m2phlb": (_I, [_VP, _P, _P, _P, _VP, _VP, _VP, _I, _I, _I, _VP]),

@@ -12,6 +12,7 @@
 // redgrid.py:56-110 (uni2red, uni2red_mf, red2uni), zoom/advect.py:237-345 (_dynamu_region1's
 // halos, _dynamu_child, _rows_child, _substeps_child), cfl.py:140-167 (dynamum) and
 // zoom/check_cfl.py:113-137 (_dynamum_child).
+#include "gb_adjoint.cuh"
 #include "gb_common.cuh"
 
 namespace {
@@ -270,6 +271,66 @@ int launch_x(gb_ctx *ctx, XArgs &A, bool mass_only) {
     return gb_after_launch(ctx, mass_only ? "cfl_x" : "advect_x");
 }
 
+// The adjoint of dynamu on region 1's rows (unlimited slopes): one warp per (j, l) row.  The
+// row is staged and searched exactly as k_advect_x does it (the same sub-cycle count and rescaled
+// faces), then the transposes run in reverse: red2uni's (a reduced row's cells gather their
+// cluster's adjoints with the shares m_uni'(i) / m(cluster)), the sub-steps', uni2red's (every
+// cell of a cluster receives the cluster's adjoint).  A.m / A.am: the mass and faces before the
+// forward operator; A.q: the tracer adjoints, overwritten with the adjoints before it.
+__global__ void __launch_bounds__(WARPS * 32) k_adj_x(XArgs A) {
+    extern __shared__ double smem[];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int64_t row = (int64_t)blockIdx.x * WARPS + warp;
+    if (row >= (int64_t)A.nj * A.nl) return;
+    const int j = (int)(row / A.nl), l = (int)(row % A.nl);
+    const int NC = A.ncell;
+    double *base = smem + (size_t)warp * adj_doubles_per_line(NC);
+    const AdjLine L = adj_line(base, NC);
+    double *mx = base + 14 * NC;
+    const int c = (A.clust && A.clust[j] > 1) ? A.clust[j] : 1;
+    const int n = A.n0 / c;
+    const bool reduced = c > 1;
+
+    for (int k = lane; k < n; k += GB_WARP) {
+        double acc = AT(A.m, (int64_t)k * c, j, l);
+        for (int cc = 1; cc < c; ++cc) acc = acc + AT(A.m, (int64_t)k * c + cc, j, l);
+        L.m0[k] = acc;
+    }
+    for (int k = lane; k <= n; k += GB_WARP) L.a[k] = AT(A.am, k == 0 ? (reduced ? n * c : 0) : k * c, j, l);
+    __syncwarp();
+    double amax = 0.0;
+    const int nloop = row_search(L.m0, mx, L.a, n, false, A.nmax, lane, amax, false);
+    if (nloop > A.nmax) {
+        if (lane == 0) raise_status(A.ctl, GB_ECFL);
+        return;
+    }
+    if (reduced) {  // red2uni's transpose: the reduced mass after the sub-steps first
+        for (int k = lane; k < n; k += GB_WARP) L.mw[k] = L.m0[k];
+        __syncwarp();
+        for (int s = 0; s < nloop; ++s) {
+            for (int k = lane; k < n; k += GB_WARP) L.mw[k] = (L.mw[k] + L.a[k]) - L.a[k + 1];
+            __syncwarp();
+        }
+        for (int k = lane; k < n; k += GB_WARP)
+            for (int w = 0; w < 4; ++w) {
+                double acc = 0.0;
+                for (int p = 0; p < c; ++p) {
+                    const int64_t i = (int64_t)k * c + p;
+                    const double mun = (AT(A.m, i, j, l) + AT(A.am, i, j, l)) - AT(A.am, i + 1, j, l);
+                    acc = acc + (mun / L.mw[k]) * AT4(A.q[w], i, j, l, 0);
+                }
+                L.q[w][k] = acc;
+            }
+    } else {
+        for (int k = lane; k < n; k += GB_WARP)
+            for (int w = 0; w < 4; ++w) L.q[w][k] = AT4(A.q[w], k, j, l, 0);
+    }
+    __syncwarp();
+    adj_line_substeps(L, n, nloop, LINE_PERIODIC, true, lane);
+    for (int i = lane; i < A.n0; i += GB_WARP)  // uni2red's transpose
+        for (int w = 0; w < 4; ++w) AT4(A.q[w], i, j, l, 0) = L.q[w][i / c];
+}
+
 int setup(XArgs &A, const gb_view *m, const gb_view *am, int held) {
     A.m = dv(m);
     A.am = dv(am);
@@ -347,4 +408,28 @@ extern "C" int gb_cfl_x_held(gb_ctx *ctx, const gb_view *m, const gb_view *am, i
     A.js = 1; A.je = 0;
     A.ctl = ctx->ctl;
     return launch_x(ctx, A, true);
+}
+
+extern "C" int gb_adjoint_x(gb_ctx *ctx, const gb_view *m, const gb_view *rm_b, const gb_view *rxm_b,
+                            const gb_view *rym_b, const gb_view *rzm_b, const gb_view *am, const int32_t *clust,
+                            int max_nloop) {
+    if (!ctx || !m || !rm_b || !rxm_b || !rym_b || !rzm_b || !am) return GB_EARG;
+    XArgs A{};
+    if (int rc = setup(A, m, am, 0)) return rc;
+    A.q[0] = dv(rm_b); A.q[1] = dv(rxm_b); A.q[2] = dv(rym_b); A.q[3] = dv(rzm_b);
+    if (rm_b->n[3] != 1) {
+        gb_set_error("gb_adjoint_x: one tracer");
+        return GB_EARG;
+    }
+    A.clust = clust;
+    A.nt = 1;
+    A.nmax = max_nloop - 1;
+    A.ctl = ctx->ctl;
+    A.ncell = A.n0 + 2;
+    const size_t smem = (size_t)WARPS * 15 * A.ncell * sizeof(double);
+    const int64_t rows = (int64_t)A.nj * A.nl;
+    if (rows == 0) return GB_OK;
+    GB_CHECK_CUDA(cudaFuncSetAttribute(k_adj_x, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    k_adj_x<<<(unsigned)((rows + WARPS - 1) / WARPS), WARPS * 32, smem, ctx->stream>>>(A);
+    return gb_after_launch(ctx, "adjoint_x");
 }

@@ -104,6 +104,8 @@ __device__ int z_settled(const ZArgs &A) {
     return -1;
 }
 
+__global__ void k_z_last(ZArgs A, int32_t *n_out) { *n_out = z_settled(A); }
+
 template <bool MASS_ONLY>
 __global__ void __launch_bounds__(WARPS * 32) k_z_steps(ZArgs A) {
     extern __shared__ double smem[];
@@ -262,4 +264,14 @@ extern "C" int gb_cfl_z(gb_ctx *ctx, const gb_view *m, const gb_view *cm, int si
     A.ctl = ctx->ctl;
     A.mass_only = 1;
     return launch_z(ctx, A);
+}
+
+// n_advz of the context's last dynamw (or dynamwm) into a device int32, -1 if its search did not
+// settle: what the adjoint of that call divides cm by
+extern "C" int gb_advect_z_last(gb_ctx *ctx, int32_t *n_out) {
+    if (!ctx || !n_out) return GB_EARG;
+    ZArgs A{};
+    A.ctl = ctx->ctl;
+    k_z_last<<<1, 1, 0, ctx->stream>>>(A, n_out);
+    return gb_after_launch(ctx, "advect_z_last");
 }

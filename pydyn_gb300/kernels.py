@@ -205,6 +205,53 @@ def sources(rm, rzm, flux, cols, level, tracer, area=None, scale=1.0):
                          int(tracer), cols.ptr, cols.shape[0]), "sources")  # fmt: skip
 
 
+# ------------------------------------------------------------------ the adjoint (one tracer)
+def advect_z_last(m, n_out):
+    """The n_advz of the context's last dynamw into n_out (a DevArray (1,) int32)."""
+    L, h = _lib(m)
+    N.check(L.gb_advect_z_last(h, n_out.ptr), "advect_z_last")
+
+
+def adjoint_x(m, rm_b, rxm_b, rym_b, rzm_b, am, clust=None, max_nloop=MAX_NLOOP_X):
+    """The transpose of advect_x (unlimited slopes) on the tracer adjoints, in place: m and am as
+    the forward call got them."""
+    _tracer_strides(rm_b, rxm_b, rym_b, rzm_b)
+    L, h = _lib(m)
+    N.check(L.gb_adjoint_x(h, *views(m, rm_b, rxm_b, rym_b, rzm_b, am), None if clust is None else clust.ptr,
+                           max_nloop), "adjoint_x")  # fmt: skip
+
+
+def adjoint_y(m, rm_b, rxm_b, rym_b, rzm_b, bm, nloop):
+    """The transpose of advect_y (unlimited slopes): m and bm (im, jm+1, lm) as the forward call
+    got them, nloop the per-level counts it returned."""
+    _tracer_strides(rm_b, rxm_b, rym_b, rzm_b)
+    L, h = _lib(m)
+    N.check(L.gb_adjoint_y(h, *views(m, rm_b, rxm_b, rym_b, rzm_b, bm), nloop.ptr), "adjoint_y")
+
+
+def adjoint_z(m, rm_b, rxm_b, rym_b, rzm_b, cm, n_advz):
+    """The transpose of advect_z (unlimited slopes): m and cm as the forward call got them."""
+    _tracer_strides(rm_b, rxm_b, rym_b, rzm_b)
+    L, h = _lib(m)
+    N.check(L.gb_adjoint_z(h, *views(m, rm_b, rxm_b, rym_b, rzm_b, cm), n_advz.ptr), "adjoint_z")
+
+
+def adjoint_convec(rm_b, rxm_b, rym_b, rzm_b, inv, cols, lmax):
+    """The transpose of convec on the listed columns with the inverses it applied."""
+    _tracer_strides(rm_b, rxm_b, rym_b, rzm_b)
+    L, h = _lib(rm_b)
+    N.check(L.gb_adjoint_convec(h, *views(rm_b, rxm_b, rym_b, rzm_b), inv.ptr, cols.ptr, cols.shape[0], int(lmax)),
+            "adjoint_convec")  # fmt: skip
+
+
+def adjoint_sources(rm_b, rzm_b, grad, cols, level, area, scale):
+    """grad (im, jm) += area scale (rm_b - rzm_b)(level) on the listed columns: the flux gradient
+    of one sources call."""
+    L, h = _lib(rm_b)
+    N.check(L.gb_adjoint_sources(h, *views(rm_b, rzm_b, grad), area.ptr, float(scale), int(level), cols.ptr,
+                                 cols.shape[0]), "adjoint_sources")  # fmt: skip
+
+
 def to_device(dev, arr, dtype=np.float64):
     """A DevArray copy of a host array (0-based bounds)."""
     return DevArray.from_host(dev, np.asarray(arr, dtype=dtype))

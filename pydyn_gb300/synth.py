@@ -124,6 +124,14 @@ def two():
     return [glb, child]
 
 
+def one():
+    """A 24 x 18 global region alone (15 x 10 degrees) with a reduced grid on its two outer rows
+    at each pole: the adjoint's small case, where the reference's forward can be applied to
+    basis vectors."""
+    g = Region("one", 24, 18, xcyc=1, touch_sp=1, touch_np=1, redgrid=RedGrid(24, 18, (1, 2, 17, 18), (24, 6, 6, 24)))
+    return [g]
+
+
 def three():
     """A grandchild: region 2 at 2 x 2 / tref 2, region 3 at 3 x 2 / tref 2 relative to it."""
     glb = Region("glb", 24, 18, xcyc=1, touch_sp=1, touch_np=1)
@@ -134,7 +142,7 @@ def three():
 
 def tree(name, lm):
     regions = {"glb6x4": glb6x4, "glb3x2": glb3x2, "glb3x2+nam1x1": lambda: [*glb3x2(), nam1x1()], "two": two,
-               "three": three}[name]()  # fmt: skip
+               "three": three, "one": one}[name]()  # fmt: skip
     at, bt = levels(lm)
     return Zoom(regions, lm, at, bt)
 

@@ -5,6 +5,7 @@ Run where the pydyn reference is importable (its checkout is on PYDYN_REFERENCE,
 against on machines that do not have the reference:
 
     python tests/golden/make_golden.py kernels     -> tests/golden/kernels.npz
+    python tests/golden/make_golden.py adjoint     -> tests/golden/adjoint.npz
 
 kernels.npz holds, per case, the inputs pydyn.synth makes and the outputs of the reference
 function on them (pydyn.kernels, pydyn.redgrid, pydyn.cfl, pydyn.balance): keys
@@ -257,6 +258,104 @@ class _RefPhysics:
         return conv, {"sources": sources, "chemistry": chemistry}
 
 
+def _reference_case(config, lm, seed, nt=1, physics=False, umax=40.0, lmax=None):
+    """pydyn's Zoom, states and meteo for the synthetic case of pydyn_gb300.synth, and an
+    interval runner: (zref, st, cst, phys, run_interval(t0, limits) -> (ndyn, n))."""
+    _reference()
+    sys.path.insert(0, str(HERE.parents[1]))
+    from pydyn import redgrid as RG
+    from pydyn import zoom as Z
+
+    from pydyn_gb300 import forward, synth
+
+    zoom, met, fields = synth.case(config, lm, seed, nt, umax=umax)
+    regions = []
+    for g in zoom.region[1:]:
+        kw = {k: getattr(g, k) for k in g.__dataclass_fields__ if k != "redgrid"}
+        rg = None
+        if g.redgrid is not None:
+            rg = RG.RedGrid(g.im, g.jm, [b[0] + 1 for b in g.redgrid.bands], [b[1] for b in g.redgrid.bands])
+        regions.append(Z.Region(**kw, redgrid=rg))
+    zref = Z.Zoom(regions, lm, zoom.at, zoom.bt)
+    st, cst = Z.ZoomState.zeros(zref, nt), Z.ZoomState.zeros(zref, nt)
+    for r, f in fields.items():
+        for name, a in f.items():
+            st[r][name].data[...] = a
+        cst[r]["dxyp"].data[...] = f["dxyp"]
+    meteo = {r: [met.fluxes(r, k) for k in (0, 1)] for r in zref.regions()}
+
+    def interp(s, t):
+        a1, a2 = forward.weights(t)
+        for r in zref.regions():
+            (pu0, pv0), (pu1, pv1) = meteo[r]
+            s[r]["pu"].data[...] = a1 * pu0 + a2 * pu1
+            s[r]["pv"].data[...] = a1 * pv0 + a2 * pv1
+
+    phys = None
+    if physics:
+        phys = _RefPhysics(zref, synth.Physics(zoom, met, seed, lm if lmax is None else lmax), fields)
+        phys.init(st)
+
+    def run_interval(t0, limits=True):
+        for r in zref.regions():
+            for name in ("m", "sp"):
+                cst[r][name].data[...] = st[r][name].data
+        ndyn, n, _ = Z.check_cfl_zoom(zref, cst, 3600, 1, 3600, lambda z, s, i, nd: interp(s, t0 + (i - 0.5) * nd))
+        for k in range(n):
+            interp(st, t0 + k * ndyn + ndyn / 2.0)
+            Z.setup_massflow(zref, st, ndyn)
+            kw = {}
+            if phys is not None:
+                conv, kw = phys.step(st, t0 + k * ndyn, ndyn)
+            else:
+                conv = {r: _no_convection(zref, r) for r in zref.regions()}
+            Z.step(zref, st, conv, ndyn, limits=limits, inverse="crout", **kw)
+        return ndyn, n
+
+    return zref, st, cst, phys, run_interval
+
+
+ADJOINT_CASE = {"config": "one", "lm": 4, "seed": 23, "lmax": 4}
+
+
+def adjoint_goldens(nbasis=None, ny=2, seed=5):
+    """The transposed reference operator on the `one` tree: pydyn's own interval (Check_CFL,
+    Setup_MassFlow, Calc_Kzz, xyzvsc|csvzyx with convection, emission at zero flux and chemistry,
+    limits off) is linear in the tracer moments; it is applied to every basis vector e_j of the
+    interior (rm, rxm, rym, rzm) (or `nbasis` sampled ones) and dotted with `ny` seeded vectors
+    y_k, which gives (A^T y_k)_j.  Also A delta for one seeded delta (the forward's own check)."""
+    c = ADJOINT_CASE
+    zref, st, _, phys, run_interval = _reference_case(c["config"], c["lm"], c["seed"], physics=True, lmax=c["lmax"])
+    for r in zref.regions():
+        phys.spec.region[r]["flux"][...] = 0.0
+    g, lm = zref.g(1), c["lm"]
+    names = ("rm", "rxm", "rym", "rzm")
+    start = {k: v.data.copy() for k, v in st[1].items()}
+
+    def apply(vec):
+        for k, v in start.items():
+            st[1][k].data[...] = v
+        for w, name in enumerate(names):
+            st[1][name].data[2 : g.im + 2, 2 : g.jm + 2, :, 0] = vec[w]
+        run_interval(0.0, limits=False)
+        return np.stack([st[1][name].data[2 : g.im + 2, 2 : g.jm + 2, :, 0].copy() for name in names])
+
+    rng = np.random.default_rng([seed, 31337])
+    shape = (4, g.im, g.jm, lm)
+    ys = rng.random((ny, *shape)) + 0.5
+    delta = rng.random(shape) * np.array([1.0, 0.3, 0.3, 0.3])[:, None, None, None]
+    a_delta = apply(delta)
+    size = int(np.prod(shape))
+    idx = np.arange(size) if nbasis is None else np.sort(rng.choice(size, size=nbasis, replace=False))
+    vals = np.zeros((ny, idx.size))
+    for n, j in enumerate(idx):
+        e = np.zeros(shape)
+        e.flat[j] = 1.0
+        out = apply(e)
+        vals[:, n] = [float(np.dot(out.ravel(), y.ravel())) for y in ys]
+    return {"adjoint": ({"y": ys, "delta": delta, "index": idx}, {"ATy": vals, "A_delta": a_delta}, dict(c))}
+
+
 def reference_run(config, lm, seed, nsteps, nt=1, physics=False, keep=None, umax=40.0, lmax=None):
     """pydyn's own driver (zoom.check_cfl_zoom on a copy of m and sp, then setup_massflow and
     zoom.step, as pydyn forward.py:388-451 runs an interval of one step) on the synthetic case
@@ -391,6 +490,9 @@ if __name__ == "__main__":
     if "kernels" in what:
         save(kernel_cases(), HERE / "kernels.npz")
         print("wrote", HERE / "kernels.npz")
+    if "adjoint" in what:
+        save(adjoint_goldens(), HERE / "adjoint.npz")
+        print("wrote", HERE / "adjoint.npz")
     if "steps" in what:  # `steps [name ...]`: those runs only, the others kept
         path = HERE / "steps.json"
         old = json.loads(path.read_text()) if path.exists() else {}
