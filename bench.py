@@ -379,7 +379,7 @@ def run_adjoint(args, ws, rank):
 
     build()
     from pydyn_gb300.adjoint import FluxGradient, make_samples
-    from pydyn_gb300.device import DevArray, Device
+    from pydyn_gb300.device import Device
     from pydyn_gb300.forward import Forward
 
     dev = Device(int(os.environ.get("LOCAL_RANK", "0")))
@@ -392,20 +392,10 @@ def run_adjoint(args, ws, rank):
     prob = FluxGradient(fw, hours, samples, np.zeros(len(samples)), every=6)
     flux = fw.physics.r[1]["flux"].host()
     rng = np.random.default_rng(9)
-    names = ("rm", "rxm", "rym", "rzm")
     shape = (4, im, jm, 34)
     scale = np.array([1.0, 0.3, 0.3, 0.3])[:, None, None, None]
     x, y = rng.random(shape) * scale, (rng.random(shape) + 0.5) * scale
-    prob.set_flux(np.zeros((im, jm)))
-    for w, name in enumerate(names):
-        fw.st[1][name][1:im, 1:jm, 1:34, 1:1].upload(x[w][..., None])
-    tape = prob._taped_interval()
-    ax = np.stack([fw.st[1][name][1:im, 1:jm, 1:34, 1].host() for name in names])
-    qb = [DevArray.from_host(dev, y[w][..., None], lower=(1, 1, 1, 1)) for w in range(4)]
-    g0 = DevArray.zeros(dev, (0, im - 1), (0, jm - 1))
-    for op in reversed(tape):
-        prob._adjoint_op(op, qb, g0)
-    aty = np.stack([q.host()[..., 0] for q in qb])
+    ax, (aty,) = prob.interval_pair(x, [y])
     lhs, rhs = float(np.dot(ax.ravel(), y.ravel())), float(np.dot(x.ravel(), aty.ravel()))
     dot_rel = abs(lhs - rhs) / abs(lhs)
     prob._restore(prob.start)

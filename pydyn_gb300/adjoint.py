@@ -216,6 +216,33 @@ class FluxGradient:
                 if isinstance(a, DevArray) and a is not d["cols"]:
                     a.free()
 
+    def interval_pair(self, x, ys):
+        """A x and A^T y for the linear map A of one interval from the present state at zero
+        flux: x and every y of ys are (4, im, jm, lm) host arrays of (rm, rxm, rym, rzm) on the
+        interior.  The run is left after the interval, the flux at zero."""
+        fw = self.fw
+        g, lm = fw.zoom.g(1), fw.zoom.lm
+        self.set_flux(np.zeros((g.im, g.jm)))
+        for w, name in enumerate(TRACERS):
+            fw.st[1][name][1 : g.im, 1 : g.jm, 1:lm, 1:1].upload(np.asarray(x[w])[..., None])
+        tape = self._taped_interval()
+        ax = np.stack([fw.st[1][name][1 : g.im, 1 : g.jm, 1:lm, 1].host() for name in TRACERS])
+        grad = DevArray.zeros(fw.dev, (0, g.im - 1), (0, g.jm - 1))
+        out = []
+        for y in ys:
+            qb = [DevArray.from_host(fw.dev, np.asarray(y[w])[..., None], lower=(1, 1, 1, 1)) for w in range(4)]
+            for op in reversed(tape):
+                self._adjoint_op(op, qb, grad, free=False)
+            out.append(np.stack([q.host()[..., 0] for q in qb]))
+            for q in qb:
+                q.free()
+        for op in tape:
+            for a in op[1:]:
+                if isinstance(a, DevArray) and a is not self.d["cols"]:
+                    a.free()
+        grad.free()
+        return ax, out
+
     def gradient(self):
         """dJ / dflux (a DevArray (im, jm)) of the last cost() evaluation."""
         if not self.checkpoints:

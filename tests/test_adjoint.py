@@ -17,7 +17,6 @@ from pydyn_gb300 import synth
 from pydyn_gb300.adjoint import make_samples
 
 FIX = load(Path(__file__).parent / "golden" / "adjoint.npz")["adjoint"]
-NAMES = ("rm", "rxm", "rym", "rzm")
 
 
 def test_fixture_is_a_transpose():
@@ -48,44 +47,14 @@ def _run(dev, config, lm, seed, lmax):
     return fw, prob
 
 
-def _set_tracers(fw, vec):
-    g, lm = fw.zoom.g(1), fw.zoom.lm
-    for w, name in enumerate(NAMES):
-        fw.st[1][name][1 : g.im, 1 : g.jm, 1:lm, 1:1].upload(vec[w][..., None])
-
-
-def _tracers(fw):
-    g, lm = fw.zoom.g(1), fw.zoom.lm
-    return np.stack([fw.st[1][name][1 : g.im, 1 : g.jm, 1:lm, 1].host() for name in NAMES])
-
-
-def _transpose(fw, prob, tape, y):
-    """A^T y through the taped interval's transposed operators."""
-    from pydyn_gb300.device import DevArray
-
-    g, lm = fw.zoom.g(1), fw.zoom.lm
-    qb = [DevArray.from_host(fw.dev, y[w][..., None], lower=(1, 1, 1, 1)) for w in range(4)]
-    grad = DevArray.zeros(fw.dev, (0, g.im - 1), (0, g.jm - 1))
-    for op in reversed(tape):
-        prob._adjoint_op(op, qb, grad, free=False)
-    fw.dev.sync()
-    out = np.stack([q.host()[..., 0] for q in qb])
-    for q in qb:
-        q.free()
-    grad.free()
-    return out
-
-
 @pytest.mark.gpu
 def test_adjoint_is_the_reference_transpose(dev):
     ins, outs, meta = FIX
     fw, prob = _run(dev, meta["config"], meta["lm"], meta["seed"], meta["lmax"])
-    _set_tracers(fw, ins["delta"])
-    tape = prob._taped_interval()
-    got = _tracers(fw)
+    got, atys = prob.interval_pair(ins["delta"], ins["y"])
     np.testing.assert_allclose(got, outs["A_delta"], rtol=1e-13, atol=1e-13 * np.abs(outs["A_delta"]).max())
-    for k, y in enumerate(ins["y"]):
-        aty = _transpose(fw, prob, tape, y).ravel()[ins["index"]]
+    for k, aty in enumerate(atys):
+        aty = aty.ravel()[ins["index"]]
         want = outs["ATy"][k]
         err = np.abs(aty - want).max() / np.abs(want).max()
         assert err <= 1e-12, f"y_{k}: A^T y differs from the reference's transpose by {err:.2e} (relative)"
@@ -103,10 +72,7 @@ def test_dot_product(dev, config, lm, seed):
     scale = np.array([1.0, 0.3, 0.3, 0.3])[:, None, None, None]
     x = rng.random(shape) * scale
     y = (rng.random(shape) + 0.5) * scale
-    _set_tracers(fw, x)
-    tape = prob._taped_interval()
-    ax = _tracers(fw)
-    aty = _transpose(fw, prob, tape, y)
+    ax, (aty,) = prob.interval_pair(x, [y])
     lhs, rhs = float(np.dot(ax.ravel(), y.ravel())), float(np.dot(x.ravel(), aty.ravel()))
     assert abs(lhs - rhs) <= 1e-12 * abs(lhs), f"<Ax, y> = {lhs!r}, <x, A^T y> = {rhs!r}"
     prob.close()
