@@ -55,6 +55,11 @@ BYTES_PER_CELL = {"_dynamu_region1": 12, "_dynamv_region1": 12, "_dynamw_region1
                   "dynam0": 5}  # fmt: skip  (values of 8 bytes per cell and application at nt = 1)
 
 
+# DRAM bytes (read + write) per call of a body, from one ncu capture of an eager interval of
+# glb3x2+nam1x1 with physics (profiles/interval_dram_fp64_glb3x2+nam1x1.md): the roofline's traffic
+TRAFFIC_PER_CALL = {"glb3x2+nam1x1": {"convec_region@2": 119.0e6, "convec_region@1": 231.9e6}}
+
+
 def metric_name(workload):
     """The headline metric's name for the full-physics glb3x2 + nam1x1 tree, else the workload's."""
     if workload == "glb3x2+nam1x1":
@@ -563,7 +568,8 @@ def main():
     per_call_bytes = 8 * BYTES_PER_CELL.get(body, 0) * cells[int(region) if region else 1]
     achieved = per_call_bytes / (total_ms / calls / 1e3) / 1e9 if per_call_bytes else None
     roof = {"bound": "hbm", "kernel": name, "achieved": achieved, "peak": hbm, "unit": "GB/s",
-            "frac": achieved / hbm if achieved else None, "traffic": None, "peak_source": how,
+            "frac": achieved / hbm if achieved else None,
+            "traffic": TRAFFIC_PER_CALL.get(args.config, {}).get(name), "peak_source": how,
             "bytes_per_launch": per_call_bytes, "ms_per_launch": total_ms / calls,
             "fp64_rates_g_per_s": fp64,
             "note": "float64 with no contraction: the FP64 pipe (fp64_rates, measured in this run) bounds the step"}  # fmt: skip
