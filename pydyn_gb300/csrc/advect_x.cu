@@ -28,6 +28,7 @@ struct XArgs {
     int restore_am;      // 1: am = a * nloop written back; 0: am untouched (reduced grid)
     int held;            // child rows
     int ncell;           // smem cells per array (n0 + 2)
+    int tc;              // tracers staged at once (launch_x)
     int32_t *nloop_out;
     double *amax_out;
     gb_ctl *ctl;
@@ -105,33 +106,28 @@ __global__ void __launch_bounds__(WARPS * 32) k_advect_x(XArgs A) {
     if (MASS_ONLY && __shfl_sync(FULL_MASK, *(volatile int *)&A.ctl->cfl_failed, 0)) return;
     const int j = (int)(row / A.nl), l = (int)(row % A.nl);
     const int nt = MASS_ONLY ? 0 : A.nt;
+    const int tc = MASS_ONLY ? 0 : A.tc;  // tracers staged at once (a chunk)
     const int NC = A.ncell;
-    const int per_warp = NC * (4 + 8 * nt);
+    const int per_warp = NC * (4 + 8 * tc);
     const bool held = A.held != 0;
     double *m_s = smem + (size_t)warp * per_warp;
     double *mx_s = m_s + NC;
     double *minv_s = mx_s + NC;
     double *a_s = minv_s + NC;
-    double *q_s = a_s + NC;          // [4][nt][NC]: rm, rxm, rym, rzm
-    double *f_s = q_s + 4 * nt * NC; // [4][nt][NC]: f, pf, fy, fz
-    auto Q = [&](int w, int t) { return q_s + (size_t)(w * nt + t) * NC; };
-    auto F = [&](int w, int t) { return f_s + (size_t)(w * nt + t) * NC; };
+    double *q_s = a_s + NC;          // [4][tc][NC]: rm, rxm, rym, rzm
+    double *f_s = q_s + 4 * tc * NC; // [4][tc][NC]: f, pf, fy, fz
+    auto Q = [&](int w, int t) { return q_s + (size_t)(w * tc + t) * NC; };
+    auto F = [&](int w, int t) { return f_s + (size_t)(w * tc + t) * NC; };
 
     const int c = (!held && A.clust && A.clust[j] > 1) ? A.clust[j] : 1;
     const int n = A.n0 / c;
     const bool reduced = c > 1;
 
-    // ---- stage the row: cluster sums onto the reduced cells (uni2red, seqsum in order)
+    // ---- stage the row's mass: cluster sums onto the reduced cells (uni2red, seqsum in order)
     for (int k = lane; k < n; k += GB_WARP) {
         double acc = AT(A.m, (int64_t)k * c, j, l);
         for (int cc = 1; cc < c; ++cc) acc = acc + AT(A.m, (int64_t)k * c + cc, j, l);
         m_s[k] = acc;
-        for (int w = 0; w < 4; ++w)
-            for (int t = 0; t < nt; ++t) {
-                double s = AT4(A.q[w], (int64_t)k * c, j, l, t);
-                for (int cc = 1; cc < c; ++cc) s = s + AT4(A.q[w], (int64_t)k * c + cc, j, l, t);
-                Q(w, t)[k] = s;
-            }
     }
     if (held) {  // n-1 interior faces, face k between cells k-1 and k
         for (int k = 1 + lane; k < n; k += GB_WARP) a_s[k] = AT(A.am, k - 1, j, l);
@@ -142,10 +138,6 @@ __global__ void __launch_bounds__(WARPS * 32) k_advect_x(XArgs A) {
         }
     }
     __syncwarp();
-
-    if (!MASS_ONLY && A.limits)  // every cell of the row, a child's held ends included
-        for (int t = 0; t < nt; ++t)
-            for (int k = lane; k < n; k += GB_WARP) Q(1, t)[k] = np_limit(Q(1, t)[k], Q(0, t)[k]);
 
     double amax = 0.0;
     const int nloop = row_search(m_s, mx_s, a_s, n, held, A.nmax, lane, amax, A.amax_out != nullptr);
@@ -161,45 +153,97 @@ __global__ void __launch_bounds__(WARPS * 32) k_advect_x(XArgs A) {
     }
 
     const int i0 = held ? 1 : 0, i1 = held ? n - 1 : n;  // the cells that move
+    const bool in_scope = (j + 1 >= A.js) && (j + 1 <= A.je);
+    const int im = A.n0;
     if (MASS_ONLY) {
         for (int s = 0; s < nloop; ++s) {
             for (int k = i0 + lane; k < i1; k += GB_WARP) m_s[k] = (m_s[k] + a_s[k]) - a_s[k + 1];
             __syncwarp();
         }
     } else {
-        for (int k = lane; k < n; k += GB_WARP) minv_s[k] = 1.0 / m_s[k];
+        // the tracers, tc at a time: every chunk restarts from the staged mass (kept in mx_s) and
+        // repeats the same mass updates; tracers never mix, so each sees exactly what it would
+        // with all of them staged together
+        for (int k = lane; k < n; k += GB_WARP) mx_s[k] = m_s[k];
         __syncwarp();
-        const int k0 = 1, k1 = held ? n - 1 : n;  // periodic: face 0 is the seam copy of face n
-        for (int s = 0; s < nloop; ++s) {
-            for (int k = k0 + lane; k <= k1; k += GB_WARP) {
-                double f = a_s[k];
-                int up = (f >= 0.0) ? k - 1 : (k == n ? 0 : k);
-                double alpha = f * minv_s[up];  // the reciprocal form of production dynamu
-                for (int t = 0; t < nt; ++t) {
-                    double ff, pf, fy, fz;
-                    slopes_flux(f, alpha, Q(0, t)[up], Q(1, t)[up], Q(2, t)[up], Q(3, t)[up], ff, pf, fy, fz);
-                    F(0, t)[k] = ff; F(1, t)[k] = pf; F(2, t)[k] = fy; F(3, t)[k] = fz;
-                }
+        for (int t0 = 0; t0 < nt; t0 += tc) {
+            const int ntc = min(tc, nt - t0);
+            for (int k = lane; k < n; k += GB_WARP) {
+                m_s[k] = mx_s[k];
+                minv_s[k] = 1.0 / mx_s[k];
+                for (int w = 0; w < 4; ++w)
+                    for (int t = 0; t < ntc; ++t) {
+                        double v = AT4(A.q[w], (int64_t)k * c, j, l, t0 + t);
+                        for (int cc = 1; cc < c; ++cc) v = v + AT4(A.q[w], (int64_t)k * c + cc, j, l, t0 + t);
+                        Q(w, t)[k] = v;
+                    }
+                if (A.limits)  // every cell of the row, a child's held ends included
+                    for (int t = 0; t < ntc; ++t) Q(1, t)[k] = np_limit(Q(1, t)[k], Q(0, t)[k]);
             }
             __syncwarp();
-            for (int i = i0 + lane; i < i1; i += GB_WARP) {
-                const int lo = (i == 0) ? n : i;
-                const double mo = m_s[i], alo = a_s[i], ahi = a_s[i + 1];
-                const double mn = (mo + alo) - ahi;
-                for (int t = 0; t < nt; ++t) {
-                    double *f = F(0, t), *pf = F(1, t), *fy = F(2, t), *fz = F(3, t);
-                    double rmn = Q(0, t)[i] - (f[i + 1] - f[lo]);
-                    double rxn = along_slope(Q(1, t)[i], pf[lo], pf[i + 1], alo, ahi, rmn, f[lo], f[i + 1], mo, mn);
-                    if (A.limits) rxn = np_limit(rxn, rmn);
-                    Q(0, t)[i] = rmn;
-                    Q(1, t)[i] = rxn;
-                    Q(2, t)[i] = Q(2, t)[i] - (fy[i + 1] - fy[lo]);
-                    Q(3, t)[i] = Q(3, t)[i] - (fz[i + 1] - fz[lo]);
+            const int k0 = 1, k1 = held ? n - 1 : n;  // periodic: face 0 is the seam copy of face n
+            for (int s = 0; s < nloop; ++s) {
+                for (int k = k0 + lane; k <= k1; k += GB_WARP) {
+                    double f = a_s[k];
+                    int up = (f >= 0.0) ? k - 1 : (k == n ? 0 : k);
+                    double alpha = f * minv_s[up];  // the reciprocal form of production dynamu
+                    for (int t = 0; t < ntc; ++t) {
+                        double ff, pf, fy, fz;
+                        slopes_flux(f, alpha, Q(0, t)[up], Q(1, t)[up], Q(2, t)[up], Q(3, t)[up], ff, pf, fy, fz);
+                        F(0, t)[k] = ff; F(1, t)[k] = pf; F(2, t)[k] = fy; F(3, t)[k] = fz;
+                    }
                 }
-                m_s[i] = mn;
-                minv_s[i] = 1.0 / mn;
+                __syncwarp();
+                for (int i = i0 + lane; i < i1; i += GB_WARP) {
+                    const int lo = (i == 0) ? n : i;
+                    const double mo = m_s[i], alo = a_s[i], ahi = a_s[i + 1];
+                    const double mn = (mo + alo) - ahi;
+                    for (int t = 0; t < ntc; ++t) {
+                        double *f = F(0, t), *pf = F(1, t), *fy = F(2, t), *fz = F(3, t);
+                        double rmn = Q(0, t)[i] - (f[i + 1] - f[lo]);
+                        double rxn = along_slope(Q(1, t)[i], pf[lo], pf[i + 1], alo, ahi, rmn, f[lo], f[i + 1], mo, mn);
+                        if (A.limits) rxn = np_limit(rxn, rmn);
+                        Q(0, t)[i] = rmn;
+                        Q(1, t)[i] = rxn;
+                        Q(2, t)[i] = Q(2, t)[i] - (fy[i + 1] - fy[lo]);
+                        Q(3, t)[i] = Q(3, t)[i] - (fz[i + 1] - fz[lo]);
+                    }
+                    m_s[i] = mn;
+                    minv_s[i] = 1.0 / mn;
+                }
+                __syncwarp();
             }
-            __syncwarp();
+            // ---- the chunk's tracers out
+            if (!reduced) {
+                for (int i = i0 + lane; i < i1; i += GB_WARP)
+                    for (int w = 0; w < 4; ++w)
+                        for (int t = 0; t < ntc; ++t) AT4(A.q[w], i, j, l, t0 + t) = Q(w, t)[i];
+                if (held && A.limits && lane == 0)  // the held ends keep their limited rxm
+                    for (int t = 0; t < ntc; ++t) {
+                        AT4(A.q[1], 0, j, l, t0 + t) = Q(1, t)[0];
+                        AT4(A.q[1], n - 1, j, l, t0 + t) = Q(1, t)[n - 1];
+                    }
+                if (A.halo && in_scope && lane == 0)  // q(0) = q(im), q(im+1) = q(1)
+                    for (int w = 0; w < 4; ++w)
+                        for (int t = 0; t < ntc; ++t) {
+                            AT4(A.q[w], -1, j, l, t0 + t) = Q(w, t)[n - 1];
+                            AT4(A.q[w], n, j, l, t0 + t) = Q(w, t)[0];
+                        }
+            } else {
+                // red2uni: every cell of a cluster given its share m_uni(i) / m(cluster) of the
+                // cluster's tracers, m_uni the uniform mass updated with the untouched am
+                for (int i = lane; i < im; i += GB_WARP) {
+                    const int k = i / c;
+                    const double mun = (AT(A.m, i, j, l) + AT(A.am, i, j, l)) - AT(A.am, i + 1, j, l);
+                    const double sc = mun / m_s[k];
+                    for (int w = 0; w < 4; ++w)
+                        for (int t = 0; t < ntc; ++t) AT4(A.q[w], i, j, l, t0 + t) = sc * Q(w, t)[k];
+                    if (A.halo && i == im - 1)  // q(0) = q(im) after red2uni
+                        for (int w = 0; w < 4; ++w)
+                            for (int t = 0; t < ntc; ++t) AT4(A.q[w], -1, j, l, t0 + t) = sc * Q(w, t)[k];
+                }
+            }
+            __syncwarp();  // the next chunk overwrites the staged tracers
         }
     }
 
@@ -213,51 +257,34 @@ __global__ void __launch_bounds__(WARPS * 32) k_advect_x(XArgs A) {
             for (int k = lane; k <= n; k += GB_WARP) AT(A.am, k, j, l) = a_s[k] * (double)nloop;
     }
 
-    const bool in_scope = (j + 1 >= A.js) && (j + 1 <= A.je);
+    // ---- the mass out, after every chunk (red2uni's shares read the uniform mass)
     if (!reduced) {
-        for (int i = i0 + lane; i < i1; i += GB_WARP) {
-            AT(A.m, i, j, l) = m_s[i];
-            for (int w = 0; w < 4; ++w)
-                for (int t = 0; t < nt; ++t) AT4(A.q[w], i, j, l, t) = Q(w, t)[i];
-        }
-        if (held && A.limits && !MASS_ONLY && lane == 0)  // the held ends keep their limited rxm
-            for (int t = 0; t < nt; ++t) {
-                AT4(A.q[1], 0, j, l, t) = Q(1, t)[0];
-                AT4(A.q[1], n - 1, j, l, t) = Q(1, t)[n - 1];
-            }
-        if (A.halo && in_scope && lane == 0) {  // q(0) = q(im), q(im+1) = q(1)
+        for (int i = i0 + lane; i < i1; i += GB_WARP) AT(A.m, i, j, l) = m_s[i];
+        if (A.halo && in_scope && lane == 0) {
             AT(A.m, -1, j, l) = m_s[n - 1];
             AT(A.m, n, j, l) = m_s[0];
-            for (int w = 0; w < 4; ++w)
-                for (int t = 0; t < nt; ++t) {
-                    AT4(A.q[w], -1, j, l, t) = Q(w, t)[n - 1];
-                    AT4(A.q[w], n, j, l, t) = Q(w, t)[0];
-                }
         }
     } else {
-        // red2uni: the uniform mass update with the untouched am, and every cell of a cluster
-        // given its share m_uni(i) / m(cluster) of the cluster's tracers
-        const int im = A.n0;
         for (int i = lane; i < im; i += GB_WARP) {
-            const int k = i / c;
-            double mun = (AT(A.m, i, j, l) + AT(A.am, i, j, l)) - AT(A.am, i + 1, j, l);
-            double sc = mun / m_s[k];
-            for (int w = 0; w < 4; ++w)
-                for (int t = 0; t < nt; ++t) AT4(A.q[w], i, j, l, t) = sc * Q(w, t)[k];
+            const double mun = (AT(A.m, i, j, l) + AT(A.am, i, j, l)) - AT(A.am, i + 1, j, l);
             AT(A.m, i, j, l) = mun;
-            if (A.halo && i == im - 1 && (MASS_ONLY ? in_scope : true)) {  // q(0) = q(im) after red2uni
-                AT(A.m, -1, j, l) = mun;
-                for (int w = 0; w < 4; ++w)
-                    for (int t = 0; t < nt; ++t) AT4(A.q[w], -1, j, l, t) = sc * Q(w, t)[k];
-            }
+            if (A.halo && i == im - 1 && (MASS_ONLY ? in_scope : true)) AT(A.m, -1, j, l) = mun;
         }
     }
 }
 
+// tracers a warp stages at once: as many as fit in the block's shared memory (all when they do)
+int tracer_chunk(int warps, int ncell, int fixed, int per_tracer, int nt) {
+    const size_t cap = 227 * 1024;
+    int tc = nt;
+    while (tc > 1 && (size_t)warps * ncell * (fixed + per_tracer * tc) * sizeof(double) > cap) --tc;
+    return tc;
+}
+
 int launch_x(gb_ctx *ctx, XArgs &A, bool mass_only) {
     A.ncell = A.n0 + 2;
-    const int nt = mass_only ? 0 : A.nt;
-    size_t smem = (size_t)WARPS * A.ncell * (4 + 8 * nt) * sizeof(double);
+    A.tc = mass_only ? 0 : tracer_chunk(WARPS, A.ncell, 4, 8, A.nt);
+    size_t smem = (size_t)WARPS * A.ncell * (4 + 8 * A.tc) * sizeof(double);
     int64_t rows = (int64_t)A.nj * A.nl;
     int blocks = (int)((rows + WARPS - 1) / WARPS);
     if (blocks == 0) return GB_OK;

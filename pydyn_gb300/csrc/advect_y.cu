@@ -32,6 +32,7 @@ struct YArgs {
     int full_mode;            // 0: chain * nloop outside; 1: * nloop only (a child's dynamvm)
     int limits, nmax;
     int ncell;                // nc + 2
+    int tc;                   // tracers staged at once (launch_y)
     int held;
     int32_t *nloop;           // nl, written by the search
     int32_t *nloop_out;
@@ -271,20 +272,21 @@ __global__ void __launch_bounds__(STEP_WARPS * 32) k_y_steps(YArgs A) {
     if (nloop > A.nmax) return;
     const bool held = A.held != 0;
     const int nc = A.nc, nt = MASS_ONLY ? 0 : A.nt, NC = A.ncell;
+    const int tc = MASS_ONLY ? 0 : A.tc;  // tracers staged at once (a chunk)
     const int kf0 = held ? 1 : 0, kf1 = held ? nc - 1 : nc;  // faces held in smem (inclusive)
     const int c0 = held ? 1 : 0, c1 = held ? nc - 1 : nc;    // cells that move
-    double *m_s = smem + (size_t)warp * NC * (2 + 8 * nt);
+    double *m_s = smem + (size_t)warp * NC * (3 + 8 * tc);
     double *b_s = m_s + NC;
-    double *q_s = b_s + NC;            // [4][nt]: rm, rxm, rym, rzm
-    double *f_s = q_s + 4 * nt * NC;   // [4][nt]: f, pf, fx, fz
-    auto Q = [&](int w, int t) { return q_s + (size_t)(w * nt + t) * NC; };
-    auto F = [&](int w, int t) { return f_s + (size_t)(w * nt + t) * NC; };
+    double *m0_s = b_s + NC;           // the staged mass, each chunk's start
+    double *q_s = m0_s + NC;           // [4][tc]: rm, rxm, rym, rzm
+    double *f_s = q_s + 4 * tc * NC;   // [4][tc]: f, pf, fx, fz
+    auto Q = [&](int w, int t) { return q_s + (size_t)(w * tc + t) * NC; };
+    auto F = [&](int w, int t) { return f_s + (size_t)(w * tc + t) * NC; };
 
     for (int k = kf0 + lane; k <= kf1; k += GB_WARP) b_s[k] = progressive_chain(BF(A, i, k, l), nloop);
     for (int k = lane; k < nc; k += GB_WARP) {
         m_s[k] = AT(A.m, i, k, l);
-        for (int w = 0; w < 4; ++w)
-            for (int t = 0; t < nt; ++t) Q(w, t)[k] = AT4(A.q[w], i, k, l, t);
+        m0_s[k] = m_s[k];
     }
     __syncwarp();
 
@@ -299,81 +301,98 @@ __global__ void __launch_bounds__(STEP_WARPS * 32) k_y_steps(YArgs A) {
         return;
     }
 
-    if (A.limits)  // every cell of the column, the poles / held ends included
-        for (int t = 0; t < nt; ++t)
-            for (int k = lane; k < nc; k += GB_WARP) Q(2, t)[k] = np_limit(Q(2, t)[k], Q(0, t)[k]);
-    if (!held && lane == 0)  // closed polar faces
-        for (int w = 0; w < 4; ++w)
-            for (int t = 0; t < nt; ++t) F(w, t)[0] = F(w, t)[nc] = 0.0;
-    __syncwarp();
-
-    for (int s = 0; s < nloop; ++s) {
-        for (int k = 1 + lane; k < nc; k += GB_WARP) {
-            const double bk = b_s[k];
-            const int up = (bk >= 0.0) ? k - 1 : k;
-            const double beta = bk / m_s[up];
-            for (int t = 0; t < nt; ++t) {
-                double f, pf, fx, fz;
-                // the along slope is rym, the cross slopes rxm, rzm
-                slopes_flux(bk, beta, Q(0, t)[up], Q(2, t)[up], Q(1, t)[up], Q(3, t)[up], f, pf, fx, fz);
-                if (!held) {  // flow out of a pole cell carries no slope (Fortran faces 2 and jmr)
-                    if (k == 1 && bk >= 0.0) {
-                        f = beta * Q(0, t)[0];
-                        pf = (-3.0 * bk) * f;
-                        fx = 0.0;
-                        fz = beta * Q(3, t)[0];
-                    }
-                    if (k == nc - 1 && bk < 0.0) {
-                        f = beta * Q(0, t)[nc - 1];
-                        pf = (-3.0 * bk) * f;
-                        fx = 0.0;
-                        fz = beta * Q(3, t)[nc - 1];
-                    }
-                }
-                F(0, t)[k] = f; F(1, t)[k] = pf; F(2, t)[k] = fx; F(3, t)[k] = fz;
-            }
+    // the tracers, tc at a time: each chunk restarts from the staged mass and repeats the same
+    // mass updates; tracers never mix, so the chunking changes no value
+    for (int t0 = 0; t0 < nt; t0 += tc) {
+        const int ntc = min(tc, nt - t0);
+        for (int k = lane; k < nc; k += GB_WARP) {
+            m_s[k] = m0_s[k];
+            for (int w = 0; w < 4; ++w)
+                for (int t = 0; t < ntc; ++t) Q(w, t)[k] = AT4(A.q[w], i, k, l, t0 + t);
+            if (A.limits)  // every cell of the column, the poles / held ends included
+                for (int t = 0; t < ntc; ++t) Q(2, t)[k] = np_limit(Q(2, t)[k], Q(0, t)[k]);
         }
+        if (!held && lane == 0)  // closed polar faces
+            for (int w = 0; w < 4; ++w)
+                for (int t = 0; t < ntc; ++t) F(w, t)[0] = F(w, t)[nc] = 0.0;
         __syncwarp();
-        for (int j = c0 + lane; j < c1; j += GB_WARP) {
-            const double mo = m_s[j], blo = b_s[j], bhi = b_s[j + 1];
-            const double mn = (mo + blo) - bhi;
-            const double inv = 1.0 / mn;  // production dynamv hoists the reciprocal
-            const double fc = blo - bhi;
-            const double fm = 3.0 * (blo + bhi);
-            const double mx3 = 3.0 * mo;
-            const bool pole = !held && ((j == 0) || (j == nc - 1));
-            for (int t = 0; t < nt; ++t) {
-                const double *f = F(0, t), *pf = F(1, t), *fx = F(2, t), *fz = F(3, t);
-                // region 1: rm - (f(j+1) - f(j)); a child: rm + (f(j) - f(j+1))
-                const double rmn = held ? Q(0, t)[j] + (f[j] - f[j + 1]) : Q(0, t)[j] - (f[j + 1] - f[j]);
-                const double ry = Q(2, t)[j];
-                double ryn = ry + ((((pf[j] - pf[j + 1]) - fc * ry) + fm * rmn) - mx3 * (f[j] + f[j + 1])) * inv;
-                if (A.limits) ryn = np_limit(ryn, rmn);
-                const double rx = Q(1, t)[j], rz = Q(3, t)[j];
-                const double rxn = held ? rx + (fx[j] - fx[j + 1]) : rx - (fx[j + 1] - fx[j]);
-                Q(3, t)[j] = held ? rz + (fz[j] - fz[j + 1]) : rz - (fz[j + 1] - fz[j]);
-                Q(0, t)[j] = rmn;
-                if (!pole) {  // the poles keep rxm, rym (only rm, rzm are updated there)
-                    Q(2, t)[j] = ryn;
-                    Q(1, t)[j] = rxn;
+
+        for (int s = 0; s < nloop; ++s) {
+            for (int k = 1 + lane; k < nc; k += GB_WARP) {
+                const double bk = b_s[k];
+                const int up = (bk >= 0.0) ? k - 1 : k;
+                const double beta = bk / m_s[up];
+                for (int t = 0; t < ntc; ++t) {
+                    double f, pf, fx, fz;
+                    // the along slope is rym, the cross slopes rxm, rzm
+                    slopes_flux(bk, beta, Q(0, t)[up], Q(2, t)[up], Q(1, t)[up], Q(3, t)[up], f, pf, fx, fz);
+                    if (!held) {  // flow out of a pole cell carries no slope (Fortran faces 2 and jmr)
+                        if (k == 1 && bk >= 0.0) {
+                            f = beta * Q(0, t)[0];
+                            pf = (-3.0 * bk) * f;
+                            fx = 0.0;
+                            fz = beta * Q(3, t)[0];
+                        }
+                        if (k == nc - 1 && bk < 0.0) {
+                            f = beta * Q(0, t)[nc - 1];
+                            pf = (-3.0 * bk) * f;
+                            fx = 0.0;
+                            fz = beta * Q(3, t)[nc - 1];
+                        }
+                    }
+                    F(0, t)[k] = f; F(1, t)[k] = pf; F(2, t)[k] = fx; F(3, t)[k] = fz;
                 }
             }
-            m_s[j] = mn;
+            __syncwarp();
+            for (int j = c0 + lane; j < c1; j += GB_WARP) {
+                const double mo = m_s[j], blo = b_s[j], bhi = b_s[j + 1];
+                const double mn = (mo + blo) - bhi;
+                const double inv = 1.0 / mn;  // production dynamv hoists the reciprocal
+                const double fc = blo - bhi;
+                const double fm = 3.0 * (blo + bhi);
+                const double mx3 = 3.0 * mo;
+                const bool pole = !held && ((j == 0) || (j == nc - 1));
+                for (int t = 0; t < ntc; ++t) {
+                    const double *f = F(0, t), *pf = F(1, t), *fx = F(2, t), *fz = F(3, t);
+                    // region 1: rm - (f(j+1) - f(j)); a child: rm + (f(j) - f(j+1))
+                    const double rmn = held ? Q(0, t)[j] + (f[j] - f[j + 1]) : Q(0, t)[j] - (f[j + 1] - f[j]);
+                    const double ry = Q(2, t)[j];
+                    double ryn = ry + ((((pf[j] - pf[j + 1]) - fc * ry) + fm * rmn) - mx3 * (f[j] + f[j + 1])) * inv;
+                    if (A.limits) ryn = np_limit(ryn, rmn);
+                    const double rx = Q(1, t)[j], rz = Q(3, t)[j];
+                    const double rxn = held ? rx + (fx[j] - fx[j + 1]) : rx - (fx[j + 1] - fx[j]);
+                    Q(3, t)[j] = held ? rz + (fz[j] - fz[j + 1]) : rz - (fz[j + 1] - fz[j]);
+                    Q(0, t)[j] = rmn;
+                    if (!pole) {  // the poles keep rxm, rym (only rm, rzm are updated there)
+                        Q(2, t)[j] = ryn;
+                        Q(1, t)[j] = rxn;
+                    }
+                }
+                m_s[j] = mn;
+            }
+            __syncwarp();
         }
-        __syncwarp();
+        for (int k = c0 + lane; k < c1; k += GB_WARP)
+            for (int w = 0; w < 4; ++w)
+                for (int t = 0; t < ntc; ++t) AT4(A.q[w], i, k, l, t0 + t) = Q(w, t)[k];
+        if (held && A.limits && lane == 0)  // the held ends keep their limited rym
+            for (int t = 0; t < ntc; ++t) {
+                AT4(A.q[2], i, 0, l, t0 + t) = Q(2, t)[0];
+                AT4(A.q[2], i, nc - 1, l, t0 + t) = Q(2, t)[nc - 1];
+            }
+        __syncwarp();  // the next chunk overwrites the staged tracers
     }
 
-    for (int k = c0 + lane; k < c1; k += GB_WARP) {
-        AT(A.m, i, k, l) = m_s[k];
-        for (int w = 0; w < 4; ++w)
-            for (int t = 0; t < nt; ++t) AT4(A.q[w], i, k, l, t) = Q(w, t)[k];
-    }
-    if (held && A.limits && lane == 0)  // the held ends keep their limited rym
-        for (int t = 0; t < nt; ++t) {
-            AT4(A.q[2], i, 0, l, t) = Q(2, t)[0];
-            AT4(A.q[2], i, nc - 1, l, t) = Q(2, t)[nc - 1];
-        }
+    for (int k = c0 + lane; k < c1; k += GB_WARP) AT(A.m, i, k, l) = m_s[k];
     for (int k = kf0 + lane; k <= kf1; k += GB_WARP) BF(A, i, k, l) = b_s[k] * (double)nloop;
+}
+
+// tracers a warp stages at once: as many as fit in the block's shared memory (all when they do)
+int tracer_chunk(int warps, int ncell, int fixed, int per_tracer, int nt) {
+    const size_t cap = 227 * 1024;
+    int tc = nt;
+    while (tc > 1 && (size_t)warps * ncell * (fixed + per_tracer * tc) * sizeof(double) > cap) --tc;
+    return tc;
 }
 
 int launch_y(gb_ctx *ctx, YArgs &A, int32_t *scratch = nullptr) {
@@ -410,8 +429,8 @@ int launch_y(gb_ctx *ctx, YArgs &A, int32_t *scratch = nullptr) {
         k_y_search<<<A.nl, SEARCH_THREADS, smem_s, ctx->stream>>>(A);
         if (int rc = gb_after_launch(ctx, "y_search")) return rc;
     }
-    const int nt = A.mass_only ? 0 : A.nt;
-    size_t smem = (size_t)STEP_WARPS * A.ncell * (2 + 8 * nt) * sizeof(double);
+    A.tc = A.mass_only ? 0 : tracer_chunk(STEP_WARPS, A.ncell, 3, 8, A.nt);
+    size_t smem = (size_t)STEP_WARPS * A.ncell * (3 + 8 * A.tc) * sizeof(double);
     if (A.mass_only) {
         GB_CHECK_CUDA(cudaFuncSetAttribute(k_y_steps<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
         k_y_steps<true><<<blocks, STEP_WARPS * 32, smem, ctx->stream>>>(A);

@@ -25,6 +25,7 @@ struct ZArgs {
     int si0, si1, sj0, sj1;  // scope (0-based, half-open): the columns the trial mass advances on
     int limits, nmax;
     int ncell;               // lm + 2
+    int tc;                  // tracers staged at once (launch_z)
     gb_ctl *ctl;
     int mass_only;
     int32_t *coln;           // work space (im * jm): the n each column's last trial passed at
@@ -126,18 +127,19 @@ __global__ void __launch_bounds__(WARPS * 32) k_z_steps(ZArgs A) {
     const int ns = A.sj1 - A.sj0;
     const int i = A.si0 + (int)(col / ns), j = A.sj0 + (int)(col % ns);
     const int lm = A.lm, nt = MASS_ONLY ? 0 : A.nt, NC = A.ncell;
-    double *m_s = smem + (size_t)warp * NC * (2 + 8 * nt);
+    const int tc = MASS_ONLY ? 0 : A.tc;  // tracers staged at once (a chunk)
+    double *m_s = smem + (size_t)warp * NC * (3 + 8 * tc);
     double *c_s = m_s + NC;
-    double *q_s = c_s + NC;
-    double *f_s = q_s + 4 * nt * NC;
-    auto Q = [&](int w, int t) { return q_s + (size_t)(w * nt + t) * NC; };
-    auto F = [&](int w, int t) { return f_s + (size_t)(w * nt + t) * NC; };
+    double *m0_s = c_s + NC;           // the staged mass, each chunk's start
+    double *q_s = m0_s + NC;
+    double *f_s = q_s + 4 * tc * NC;
+    auto Q = [&](int w, int t) { return q_s + (size_t)(w * tc + t) * NC; };
+    auto F = [&](int w, int t) { return f_s + (size_t)(w * tc + t) * NC; };
 
     for (int k = lane; k <= lm; k += GB_WARP) c_s[k] = AT(A.cm, i, j, k) / (double)n;
     for (int k = lane; k < lm; k += GB_WARP) {
         m_s[k] = AT(A.m, i, j, k);
-        for (int w = 0; w < 4; ++w)
-            for (int t = 0; t < nt; ++t) Q(w, t)[k] = AT4(A.q[w], i, j, k, t);
+        m0_s[k] = m_s[k];
     }
     __syncwarp();
 
@@ -146,50 +148,67 @@ __global__ void __launch_bounds__(WARPS * 32) k_z_steps(ZArgs A) {
         return;
     }
 
-    if (A.limits)
-        for (int t = 0; t < nt; ++t)
-            for (int k = lane; k < lm; k += GB_WARP) Q(3, t)[k] = np_limit(Q(3, t)[k], Q(0, t)[k]);
-    if (lane == 0)
-        for (int w = 0; w < 4; ++w)
-            for (int t = 0; t < nt; ++t) F(w, t)[0] = F(w, t)[lm] = 0.0;
-    __syncwarp();
-
-    for (int s = 0; s < n; ++s) {
-        for (int k = 1 + lane; k < lm; k += GB_WARP) {
-            const double ck = c_s[k];
-            const int up = (ck >= 0.0) ? k - 1 : k;
-            const double gamma = ck / m_s[up];
-            for (int t = 0; t < nt; ++t) {
-                double f, pf, fx, fy;
-                // the along slope is rzm, the cross slopes rxm, rym
-                slopes_flux(ck, gamma, Q(0, t)[up], Q(3, t)[up], Q(1, t)[up], Q(2, t)[up], f, pf, fx, fy);
-                F(0, t)[k] = f; F(1, t)[k] = pf; F(2, t)[k] = fx; F(3, t)[k] = fy;
-            }
-        }
-        __syncwarp();
+    // the tracers, tc at a time: each chunk restarts from the staged mass and repeats the same
+    // mass updates; tracers never mix, so the chunking changes no value
+    for (int t0 = 0; t0 < nt; t0 += tc) {
+        const int ntc = min(tc, nt - t0);
         for (int k = lane; k < lm; k += GB_WARP) {
-            const double mo = m_s[k], clo = c_s[k], chi = c_s[k + 1];
-            const double mn = (mo + clo) - chi;
-            for (int t = 0; t < nt; ++t) {
-                const double *f = F(0, t), *pf = F(1, t), *fx = F(2, t), *fy = F(3, t);
-                // advectz: rm + f(l-1) - f(l), no parentheses
-                const double rmn = (Q(0, t)[k] + f[k]) - f[k + 1];
-                double rzn = along_slope(Q(3, t)[k], pf[k], pf[k + 1], clo, chi, rmn, f[k], f[k + 1], mo, mn);
-                if (A.limits) rzn = np_limit(rzn, rmn);
-                Q(0, t)[k] = rmn;
-                Q(3, t)[k] = rzn;
-                Q(1, t)[k] = (Q(1, t)[k] + fx[k]) - fx[k + 1];
-                Q(2, t)[k] = (Q(2, t)[k] + fy[k]) - fy[k + 1];
-            }
-            m_s[k] = mn;
+            m_s[k] = m0_s[k];
+            for (int w = 0; w < 4; ++w)
+                for (int t = 0; t < ntc; ++t) Q(w, t)[k] = AT4(A.q[w], i, j, k, t0 + t);
+            if (A.limits)
+                for (int t = 0; t < ntc; ++t) Q(3, t)[k] = np_limit(Q(3, t)[k], Q(0, t)[k]);
         }
+        if (lane == 0)
+            for (int w = 0; w < 4; ++w)
+                for (int t = 0; t < ntc; ++t) F(w, t)[0] = F(w, t)[lm] = 0.0;
         __syncwarp();
+
+        for (int s = 0; s < n; ++s) {
+            for (int k = 1 + lane; k < lm; k += GB_WARP) {
+                const double ck = c_s[k];
+                const int up = (ck >= 0.0) ? k - 1 : k;
+                const double gamma = ck / m_s[up];
+                for (int t = 0; t < ntc; ++t) {
+                    double f, pf, fx, fy;
+                    // the along slope is rzm, the cross slopes rxm, rym
+                    slopes_flux(ck, gamma, Q(0, t)[up], Q(3, t)[up], Q(1, t)[up], Q(2, t)[up], f, pf, fx, fy);
+                    F(0, t)[k] = f; F(1, t)[k] = pf; F(2, t)[k] = fx; F(3, t)[k] = fy;
+                }
+            }
+            __syncwarp();
+            for (int k = lane; k < lm; k += GB_WARP) {
+                const double mo = m_s[k], clo = c_s[k], chi = c_s[k + 1];
+                const double mn = (mo + clo) - chi;
+                for (int t = 0; t < ntc; ++t) {
+                    const double *f = F(0, t), *pf = F(1, t), *fx = F(2, t), *fy = F(3, t);
+                    // advectz: rm + f(l-1) - f(l), no parentheses
+                    const double rmn = (Q(0, t)[k] + f[k]) - f[k + 1];
+                    double rzn = along_slope(Q(3, t)[k], pf[k], pf[k + 1], clo, chi, rmn, f[k], f[k + 1], mo, mn);
+                    if (A.limits) rzn = np_limit(rzn, rmn);
+                    Q(0, t)[k] = rmn;
+                    Q(3, t)[k] = rzn;
+                    Q(1, t)[k] = (Q(1, t)[k] + fx[k]) - fx[k + 1];
+                    Q(2, t)[k] = (Q(2, t)[k] + fy[k]) - fy[k + 1];
+                }
+                m_s[k] = mn;
+            }
+            __syncwarp();
+        }
+        for (int k = lane; k < lm; k += GB_WARP)
+            for (int w = 0; w < 4; ++w)
+                for (int t = 0; t < ntc; ++t) AT4(A.q[w], i, j, k, t0 + t) = Q(w, t)[k];
+        __syncwarp();  // the next chunk overwrites the staged tracers
     }
-    for (int k = lane; k < lm; k += GB_WARP) {
-        AT(A.m, i, j, k) = m_s[k];
-        for (int w = 0; w < 4; ++w)
-            for (int t = 0; t < nt; ++t) AT4(A.q[w], i, j, k, t) = Q(w, t)[k];
-    }
+    for (int k = lane; k < lm; k += GB_WARP) AT(A.m, i, j, k) = m_s[k];
+}
+
+// tracers a warp stages at once: as many as fit in the block's shared memory (all when they do)
+int tracer_chunk(int warps, int ncell, int fixed, int per_tracer, int nt) {
+    const size_t cap = 227 * 1024;
+    int tc = nt;
+    while (tc > 1 && (size_t)warps * ncell * (fixed + per_tracer * tc) * sizeof(double) > cap) --tc;
+    return tc;
 }
 
 int launch_z(gb_ctx *ctx, ZArgs &A) {
@@ -207,8 +226,8 @@ int launch_z(gb_ctx *ctx, ZArgs &A) {
         int rc = gb_after_launch(ctx, "z_search");
         if (rc) return rc;
     }
-    const int nt = A.mass_only ? 0 : A.nt;
-    size_t smem = (size_t)WARPS * A.ncell * (2 + 8 * nt) * sizeof(double);
+    A.tc = A.mass_only ? 0 : tracer_chunk(WARPS, A.ncell, 3, 8, A.nt);
+    size_t smem = (size_t)WARPS * A.ncell * (3 + 8 * A.tc) * sizeof(double);
     int64_t scols = (int64_t)(A.si1 - A.si0) * (A.sj1 - A.sj0);
     int sblocks = (int)((scols + WARPS - 1) / WARPS);
     if (sblocks < 1) sblocks = 1;

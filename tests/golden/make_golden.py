@@ -427,7 +427,7 @@ def _no_convection(zoom, r):
     return {"entu": z, "detu": z, "entd": z, "detd": z, "dkg": z, "cloud_top": c, "cloud_lfs": c, "lmax": 0}
 
 
-STEP_RUNS = {  # name: (tree, lm, seed, intervals, umax[, physics lmax, intervals the CPU tests run])
+STEP_RUNS = {  # name: (tree, lm, seed, intervals, umax[, physics lmax, intervals the CPU tests run][, options])
     "config0": ("glb6x4", 25, 11, 24, 40.0),
     "config0-strong": ("glb6x4", 25, 12, 6, 160.0),
     "two": ("two", 5, 13, 6, 40.0),
@@ -438,6 +438,9 @@ STEP_RUNS = {  # name: (tree, lm, seed, intervals, umax[, physics lmax, interval
     "three-phys": ("three", 6, 22, 4, 40.0, 6, 4),
     "config1": ("glb3x2", 34, 41, 3, 40.0, 34, 1),
     "config2": ("glb3x2+nam1x1", 34, 42, 2, 40.0, 34, 1),
+    "two-phys-nt3": ("two", 8, 24, 4, 40.0, 8, 2, {"nt": 3}),
+    "config0-nt8": ("glb6x4", 25, 16, 3, 40.0, {"nt": 8}),
+    "config1-nt12": ("glb3x2", 34, 43, 2, 40.0, 34, 1, {"nt": 12}),
 }
 
 
@@ -448,12 +451,17 @@ def step_goldens(names=None):
     for name, spec in STEP_RUNS.items():
         if names and name not in names:
             continue
+        opts = spec[-1] if isinstance(spec[-1], dict) else {}
+        spec = spec[:-1] if opts else spec
         config, lm, seed, nsteps, umax = spec[:5]
         lmax = spec[5] if len(spec) > 5 else None
+        nt = opts.get("nt", 1)
         t = time.perf_counter()
-        runs = reference_run(config, lm, seed, nsteps, umax=umax, physics=lmax is not None, lmax=lmax)
+        runs = reference_run(config, lm, seed, nsteps, nt=nt, umax=umax, physics=lmax is not None, lmax=lmax)
         res[name] = {"config": config, "lm": lm, "seed": seed, "umax": umax, "steps": [list(x) for x in runs],
                      "reference_seconds_per_interval": (time.perf_counter() - t) / nsteps}  # fmt: skip
+        if nt != 1:
+            res[name]["nt"] = nt
         if lmax is not None:
             res[name].update(physics=True, lmax=lmax, cpu_prefix=spec[6])
         print(name, runs[-1], res[name]["reference_seconds_per_interval"])

@@ -25,7 +25,7 @@ def test_intervals_match_reference(dev, name, graph):
     from pydyn_gb300.forward import Forward
 
     run = GOLDEN[name]
-    fw = Forward(dev, run["config"], run["lm"], run["seed"], umax=run.get("umax", 40.0),
+    fw = Forward(dev, run["config"], run["lm"], run["seed"], nt=run.get("nt", 1), umax=run.get("umax", 40.0),
                  physics=run.get("physics", False), lmax=run.get("lmax"))  # fmt: skip
     for k, (ndyn, n, want) in enumerate(run["steps"]):
         got_ndyn, got_n = fw.interval(graph=graph)

@@ -15,8 +15,8 @@ def test_oracle_intervals_match_reference(built, name):
 
     run = GOLDEN[name]
     steps = run["steps"][: run.get("cpu_prefix", 8)]
-    orc = OracleRun(run["config"], run["lm"], run["seed"], umax=run.get("umax", 40.0), physics=run.get("physics", False),
-                    lmax=run.get("lmax"))  # fmt: skip
+    orc = OracleRun(run["config"], run["lm"], run["seed"], nt=run.get("nt", 1), umax=run.get("umax", 40.0),
+                    physics=run.get("physics", False), lmax=run.get("lmax"))  # fmt: skip
     for k, (ndyn, n, want) in enumerate(steps):
         assert orc.interval() == (ndyn, n), f"interval {k}"
         assert digest(orc.st) == want, f"{name}: interval {k} differs from the reference"
