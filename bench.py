@@ -275,10 +275,10 @@ def run_ensemble(args, ws, rank):
     for _ in range(args.warmup):
         ens.step()
     barrier(ws)
-    n0 = sum(d.launches() for d in ens.devs)
+    n0 = sum(fw.launches() for fw in ens.runs)
     with Clocks(int(os.environ.get("LOCAL_RANK", "0"))) as clk:
         batched = max_over_ranks(_ensemble_timed(ens, args.steps, lambda e: e.step()), ws)
-    launches = sum(d.launches() for d in ens.devs) - n0
+    launches = sum(fw.launches() for fw in ens.runs) - n0
     looped = max_over_ranks(_ensemble_timed(ens, args.steps, lambda e: e.step_looped()), ws)
 
     # end to end: every member's new meteo instant in from pinned host memory, its tracer mass
@@ -508,7 +508,7 @@ def main():
         fw.interval(graph=True)
     flush = DevArray.zeros(dev, (0, 32 * 1024 * 1024 - 1))  # 256 MiB > the 129 MB L2
     evs = [(dev.event(), dev.event()) for _ in range(args.steps)]
-    n0 = dev.launches()
+    n0 = fw.launches()
     barrier(ws)
     dev.sync()
     t_wall = time.perf_counter()
@@ -523,8 +523,8 @@ def main():
             t += fw.nread
         dev.sync()
     wall = time.perf_counter() - t_wall
-    launches = dev.launches() - n0 - args.steps  # the flushes are not the step's
-    if dev.cfl_failed():
+    launches = fw.launches() - n0 - args.steps  # the flushes are not the step's
+    if fw.rehearsal_failed():
         raise RuntimeError("bench: Check_CFL rejected ndyn = nread inside the timed region")
     fw.t = t
     ms = [a.elapsed_ms(b) for a, b in evs]
@@ -557,7 +557,7 @@ def main():
             pinned_out[r].from_device(dev, fw.st[r]["rm"][1 : g.im, 1 : g.jm, 1:lm])
         dev.sync()
     e2e_sec = max_over_ranks((time.perf_counter() - t0) / args.steps, ws)
-    if dev.cfl_failed():
+    if fw.rehearsal_failed():
         raise RuntimeError("bench: Check_CFL rejected ndyn = nread in the e2e loop")
 
     # roofline of the dominant body

@@ -1,13 +1,19 @@
 // Calc_Kzz: the vertical diffusion exchange rate dkg of every column of a region.
 //
-// Four launches, each with every lane on its own cell, column or interface (FP64 issue slots are
-// this GPU's scarcest resource, so no lane idles through another's serial work):
+// Eight launches, each with every lane on its own cell, column or interface (FP64 issue slots
+// are this GPU's scarcest resource, so no lane idles through another's serial work), the
+// column-serial parts reduced to the recurrences that carry from level to level:
 //   k_kzz_rows        thread per latitude: the zonal wind factor dxx (a cosine per row)
 //   k_kzz_levels      thread per (column, level): potential temperature, the logarithms, the
 //                     geopotential increments, the level winds -- into a work space
-//   k_kzz_columns     thread per column: the geopotential's running sum, the level heights,
-//                     ustar, the surface fluxes and both bulk-Richardson sweeps (pblh), and the
-//                     column constants of the diffusivity (w*, the Prandtl stability terms)
+//   k_kzz_surface     thread per column: the geopotential's running sum, ustar, the surface
+//                     fluxes and the Obukhov length
+//   k_kzz_heights     thread per (column, level): the level height and the first
+//                     bulk-Richardson sweep's level terms
+//   k_kzz_sweep1      thread per column: the first sweep's running mask (pblh), the parcel excess
+//   k_kzz_raw2        thread per (column, level): the second sweep's level terms
+//   k_kzz_sweep2      thread per column: the second sweep (pblh) and the column constants of
+//                     the diffusivity (w*, the Prandtl stability terms)
 //   k_kzz_interfaces  thread per (column, interface): the free-troposphere and boundary-layer
 //                     diffusivities, then dkg of the interface (zero at lmax_conv - 1)
 // Every value is the per-element statement of the reference in its order; exp / log / pow / cos
@@ -22,7 +28,7 @@ constexpr double GRAV = 9.80665, PI_ = 3.14159265358979, AE = 6.371e6, VKARMAN =
 constexpr double LVAP = 2.5e6, RGAS = 8.3144, XMAIR = 28.94, RHO_AIR = 1.2, CKMIN = 1.0e-15, SFFRAC = 0.1;
 constexpr double APZERO = 100000.0, BETAH = 15.0, FAK = 8.5, FAKN = 7.2, TINY = 1.0e-9, ZACB = 100.0;
 constexpr double RICR = 0.3, SSFRAC = 0.1, KVHMIN = 0.1;
-constexpr int NCOLVAL = 10;  // z0, pblh, wobkl, wheatv, ustr, zwstr, t1a, t2a, t1b, t2b
+constexpr int NCOLVAL = 12;  // z0, pblh, wobkl, wheatv, ustr, zwstr, t1a, t2a, t1b, t2b, wtseff, thvparc
 
 struct KArgs {
     DV spm, sp, pu, pv, t, q, surf[10], dkg, pblh;
@@ -31,6 +37,7 @@ struct KArgs {
     double dx, dy, ybeg;
     // work space
     double *dxx, *wthm, *zthvk, *lpf, *lphlb, *dzg, *uw, *vw, *whm, *gph, *col;
+    double *sw_vvk, *sw_dz, *sw_raw;  // the sweeps' level terms
 };
 
 __device__ __forceinline__ double S2(const DV &v, int i, int j) { return v.p[(int64_t)i * v.s0 + (int64_t)j * v.s1]; }
@@ -81,19 +88,17 @@ __global__ void __launch_bounds__(GB_TUNE_MAX_CELL) k_kzz_levels(KArgs A) {
     A.vw[t] = dyy * (S3(A.pv, i, j + 1, l) + S3(A.pv, i, j, l)) * 0.5 / m;
 }
 
-// one sweep of the bulk Richardson number up the column (diffusion.py:123-152)
-__device__ double pbl_sweep(double pblh, const double *whm, const double *uw, const double *vw, const double *wthm,
-                            const DV &q, int i, int j, double ustr, double wtseff, double ref, bool first, int lm,
-                            double zcrdq_) {
+// The bulk-Richardson sweep up a column (diffusion.py:123-152), split where its terms allow:
+// each level's Richardson number before the running mask,
+//   zrino(k) = GRAV (tkv(k) - ref) dz(k) / (wtseff vvk(k)) + copysign(1e-10, .)
+// (first pass: ref = wtseff; second: ref = the parcel's thvparc, the product vvk wtseff), needs
+// only the column's constants, so it is computed a thread per (column, level) (k_kzz_heights,
+// k_kzz_raw2); the carried part -- the mask jwork, the last Richardson number, pblh -- runs a
+// thread per column (sweep_carry).
+__device__ double sweep_carry(double pblh, const double *whm, const double *raw, int k0, int lm) {
     double jwork = 1.0, wrino = 0.0;
-    for (int k = first ? 0 : 1; k < lm; ++k) {
-        const double du = uw[k] - uw[0], dv = vw[k] - vw[0];
-        const double vvk = np_max(du * du + dv * dv + ZACB * ustr * ustr, TINY);
-        const double tkv = wthm[k] * (1.0 + zcrdq_ * S3(q, i, j, k));
-        const double dz = whm[k] - whm[0];
-        double zrino = first ? GRAV * (tkv - wtseff) * dz / (wtseff * vvk) : GRAV * (tkv - ref) * dz / (vvk * wtseff);
-        zrino = zrino + copysign(1.0e-10, zrino);
-        zrino = jwork * zrino;
+    for (int k = k0; k < lm; ++k) {
+        const double zrino = jwork * raw[k];
         const double jq = jqif(RICR, zrino);
         const double frac = (RICR - wrino) / (zrino - wrino);
         const double at_ricr = (k == 0) ? frac * whm[k] : whm[k - 1] + frac * (whm[k] - whm[k - 1]);
@@ -101,37 +106,31 @@ __device__ double pbl_sweep(double pblh, const double *whm, const double *uw, co
         jwork = jq * jwork;
         wrino = zrino + (1.0 - jwork) * 0.1;
     }
-    return first ? (1.0 - jwork) * pblh + whm[lm - 1] * jwork : (1.0 - jwork) * pblh + jwork * whm[lm - 1];
+    return k0 == 0 ? (1.0 - jwork) * pblh + whm[lm - 1] * jwork : (1.0 - jwork) * pblh + jwork * whm[lm - 1];
 }
 
-__global__ void __launch_bounds__(GB_TUNE_MAX_COLUMN) k_kzz_columns(KArgs A) {
+// thread per column: the geopotential's running sum, ustar (diffusion.py:76-89), the surface
+// fluxes and the Obukhov length (diffusion.py:155-170) into the column values
+__global__ void __launch_bounds__(GB_TUNE_MAX_COLUMN) k_kzz_surface(KArgs A) {
     const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (c >= (int64_t)A.im * A.jm) return;
     const int i = (int)(c / A.jm), j = (int)(c % A.jm);
     const int lm = A.lm;
-    const double ZCRDQ = zcrdq(), ONET = 1.0 / 3.0, BINM = 15.0 * SFFRAC;
+    const double ZCRDQ = zcrdq();
     double *gph = A.gph + c * (lm + 1);
-    double *whm = A.whm + c * lm;
-    const double *dzg = A.dzg + c * lm, *wthm = A.wthm + c * lm, *uw = A.uw + c * lm, *vw = A.vw + c * lm;
+    const double *dzg = A.dzg + c * lm, *wthm = A.wthm + c * lm;
     const double sm = S2(A.spm, i, j);
 
-    // the geopotential's running sum and the level heights
-    gph[0] = S2(A.surf[0], i, j) / GRAV;
-    double g = gph[0];
+    const double g0 = S2(A.surf[0], i, j) / GRAV;
+    gph[0] = g0;
+    double g = g0, g1 = g0;
     for (int k = 0; k < lm - 1; ++k) {
         g = g + dzg[k];
         gph[k + 1] = g;
+        if (k == 0) g1 = g;
     }
     gph[lm] = 200000.0;
-    const double z0 = gph[0];
-    for (int l = 0; l < lm; ++l) {
-        const double ph0 = A.at[l] + A.bt[l] * sm, ph1 = A.at[l + 1] + A.bt[l + 1] * sm;
-        const double pf = (ph0 + ph1) * 0.5;
-        const double intfac = (ph0 - pf) / (ph0 - ph1);
-        whm[l] = (gph[l] - z0) * (1.0 - intfac) + (gph[l + 1] - z0) * intfac;
-    }
 
-    // ustar (diffusion.py:76-89)
     const double xland = S2(A.surf[1], i, j) / 100.0;
     const double ew = S2(A.surf[8], i, j), ns = S2(A.surf[9], i, j);
     const double tau = sqrt(ew * ew + ns * ns);
@@ -145,33 +144,99 @@ __global__ void __launch_bounds__(GB_TUNE_MAX_COLUMN) k_kzz_columns(KArgs A) {
     const double ustar_land = xland > 0.0 ? land : 0.0;
     const double ustar_loc = xland * ustar_land + (1.0 - xland) * ustar_sea;
 
-    // the surface fluxes, Obukhov length and the two sweeps (diffusion.py:155-200)
     const double ph0 = A.at[0] + A.bt[0] * sm, ph1 = A.at[1] + A.bt[1] * sm;
-    const double dz1 = gph[1] - gph[0], dp1 = ph0 - ph1;
+    const double dz1 = (lm > 1 ? g1 : gph[1]) - g0, dp1 = ph0 - ph1;
     const double wheat = -S2(A.surf[6], i, j) * dz1 * GRAV / dp1 / CP_AIR;
     const double wqflx = -S2(A.surf[7], i, j) * dz1 * GRAV / dp1 / LVAP;
     const double ustr = np_max(ustar_loc, 0.01);
     const double wtseff = wthm[0] * (1.0 + ZCRDQ * S3(A.q, i, j, 0));
     const double wheatv = wheat + ZCRDQ * wthm[0] * wqflx;
     const double wobkl = -wtseff * cube(ustr) / (GRAV * VKARMAN * (wheatv + copysign(1.0e-10, wheatv)));
-    double pblh = pbl_sweep(0.0, whm, uw, vw, wthm, A.q, i, j, ustr, wtseff, 0.0, true, lm, ZCRDQ);
+    double *cv = A.col + c * NCOLVAL;
+    cv[0] = g0;
+    cv[2] = wobkl;
+    cv[3] = wheatv;
+    cv[4] = ustr;
+    cv[10] = wtseff;
+}
+
+// the height of level l above the surface (mass_t, diffusion.py:107-120)
+__device__ __forceinline__ double level_height(const KArgs &A, const double *gph, double z0, double sm, int l) {
+    const double ph0 = A.at[l] + A.bt[l] * sm, ph1 = A.at[l + 1] + A.bt[l + 1] * sm;
+    const double pf = (ph0 + ph1) * 0.5;
+    const double intfac = (ph0 - pf) / (ph0 - ph1);
+    return (gph[l] - z0) * (1.0 - intfac) + (gph[l + 1] - z0) * intfac;
+}
+
+// thread per (column, level): the level height, and the first sweep's level terms
+__global__ void __launch_bounds__(GB_TUNE_MAX_CELL) k_kzz_heights(KArgs A) {
+    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const int lm = A.lm;
+    if (t >= (int64_t)A.im * A.jm * lm) return;
+    const int64_t c = t / lm;
+    const int k = (int)(t % lm);
+    const int i = (int)(c / A.jm), j = (int)(c % A.jm);
+    const double *gph = A.gph + c * (lm + 1), *cv = A.col + c * NCOLVAL;
+    const double z0 = cv[0], ustr = cv[4], wtseff = cv[10];
+    const double sm = S2(A.spm, i, j);
+    const double whk = level_height(A, gph, z0, sm, k), wh0 = level_height(A, gph, z0, sm, 0);
+    A.whm[t] = whk;
+    const double *uw = A.uw + c * lm, *vw = A.vw + c * lm;
+    const double du = uw[k] - uw[0], dv = vw[k] - vw[0];
+    const double vvk = np_max(du * du + dv * dv + ZACB * ustr * ustr, TINY);
+    const double dz = whk - wh0;
+    double zrino = GRAV * (A.zthvk[t] - wtseff) * dz / (wtseff * vvk);
+    zrino = zrino + copysign(1.0e-10, zrino);
+    A.sw_vvk[t] = vvk;
+    A.sw_dz[t] = dz;
+    A.sw_raw[t] = zrino;
+}
+
+// thread per column: the first sweep (pblh from 0), the parcel's excess (diffusion.py:171-178)
+__global__ void __launch_bounds__(GB_TUNE_MAX_COLUMN) k_kzz_sweep1(KArgs A) {
+    const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= (int64_t)A.im * A.jm) return;
+    const int lm = A.lm;
+    const double ONET = 1.0 / 3.0, BINM = 15.0 * SFFRAC;
+    double *cv = A.col + c * NCOLVAL;
+    const double wobkl = cv[2], wheatv = cv[3], ustr = cv[4], wtseff = cv[10];
+    const double pblh = sweep_carry(0.0, A.whm + c * lm, A.sw_raw + c * lm, 0, lm);
     const double jq = jqif(wheatv, 0.0);
     const double fmt = gbm_pow(jq * (1.0 - BINM * pblh / wobkl) + (1.0 - jq), ONET);
     const double wsc = ustr * fmt;
     const double zexcess = wheatv * FAK / wsc;
-    const double thvparc = wtseff + jq * zexcess;
-    pblh = pbl_sweep(pblh, whm, uw, vw, wthm, A.q, i, j, ustr, wtseff, thvparc, false, lm, ZCRDQ);
+    cv[1] = pblh;
+    cv[11] = wtseff + jq * zexcess;  // thvparc
+}
+
+// thread per (column, level >= 1): the second sweep's level terms
+__global__ void __launch_bounds__(GB_TUNE_MAX_CELL) k_kzz_raw2(KArgs A) {
+    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const int lm = A.lm;
+    if (t >= (int64_t)A.im * A.jm * lm) return;
+    const int64_t c = t / lm;
+    if (t % lm == 0) return;
+    const double *cv = A.col + c * NCOLVAL;
+    const double wtseff = cv[10], thvparc = cv[11];
+    double zrino = GRAV * (A.zthvk[t] - thvparc) * A.sw_dz[t] / (A.sw_vvk[t] * wtseff);
+    zrino = zrino + copysign(1.0e-10, zrino);
+    A.sw_raw[t] = zrino;
+}
+
+// thread per column: the second sweep, pblh, and the interfaces' column constants: w* and the
+// Prandtl term's stability for jq3 = 0 (obukov = 0 * wobkl - 1) and jq3 = 1 (obukov = 1 * wobkl - 0)
+__global__ void __launch_bounds__(GB_TUNE_MAX_COLUMN) k_kzz_sweep2(KArgs A) {
+    const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= (int64_t)A.im * A.jm) return;
+    const int i = (int)(c / A.jm), j = (int)(c % A.jm);
+    const int lm = A.lm;
+    const double ONET = 1.0 / 3.0;
+    double *cv = A.col + c * NCOLVAL;
+    const double wobkl = cv[2], wheatv = cv[3], wtseff = cv[10];
+    double pblh = sweep_carry(cv[1], A.whm + c * lm, A.sw_raw + c * lm, 1, lm);
     pblh = np_max(pblh, 100.0);
     if (A.pblh.p) A.pblh.p[(int64_t)i * A.pblh.s0 + (int64_t)j * A.pblh.s1] = pblh;
-
-    // the interfaces' column constants: w* and the Prandtl term's stability for jq3 = 0
-    // (obukov = 0 * wobkl - 1) and jq3 = 1 (obukov = 1 * wobkl - 0)
-    double *cv = A.col + c * NCOLVAL;
-    cv[0] = z0;
     cv[1] = pblh;
-    cv[2] = wobkl;
-    cv[3] = wheatv;
-    cv[4] = ustr;
     cv[5] = gbm_pow(fabs(wheatv) * GRAV * pblh / wtseff, ONET);
     const double stab0 = 1.0 - SSFRAC * BETAH * pblh / (0.0 * wobkl - 1.0);
     const double stab1 = 1.0 - SSFRAC * BETAH * pblh / (1.0 * wobkl - 0.0);
@@ -278,7 +343,7 @@ extern "C" int gb_calc_kzz(gb_ctx *ctx, const gb_view *spm, const gb_view *sp, c
         return GB_EARG;
     }
     const int64_t ncol = (int64_t)A.im * A.jm, ncell = ncol * A.lm;
-    const size_t doubles = (size_t)A.jm + 8 * (size_t)ncell + (size_t)ncol * (A.lm + 1) + (size_t)ncol * NCOLVAL;
+    const size_t doubles = (size_t)A.jm + 11 * (size_t)ncell + (size_t)ncol * (A.lm + 1) + (size_t)ncol * NCOLVAL;
     double *w = gb_work(ctx, doubles * sizeof(double));
     if (!w) return GB_ECUDA;
     A.dxx = w; w += A.jm;
@@ -290,6 +355,9 @@ extern "C" int gb_calc_kzz(gb_ctx *ctx, const gb_view *spm, const gb_view *sp, c
     A.uw = w; w += ncell;
     A.vw = w; w += ncell;
     A.whm = w; w += ncell;
+    A.sw_vvk = w; w += ncell;
+    A.sw_dz = w; w += ncell;
+    A.sw_raw = w; w += ncell;
     A.gph = w; w += ncol * (A.lm + 1);
     A.col = w;
     const int tcol = ctx->tune[GB_TUNE_COLUMN_THREADS], tcell = ctx->tune[GB_TUNE_CELL_THREADS];
@@ -297,8 +365,16 @@ extern "C" int gb_calc_kzz(gb_ctx *ctx, const gb_view *spm, const gb_view *sp, c
     if (int rc = gb_after_launch(ctx, "kzz_rows")) return rc;
     k_kzz_levels<<<gb_blocks(ncell, tcell), tcell, 0, ctx->stream>>>(A);
     if (int rc = gb_after_launch(ctx, "kzz_levels")) return rc;
-    k_kzz_columns<<<gb_blocks(ncol, tcol), tcol, 0, ctx->stream>>>(A);
-    if (int rc = gb_after_launch(ctx, "kzz_columns")) return rc;
+    k_kzz_surface<<<gb_blocks(ncol, tcol), tcol, 0, ctx->stream>>>(A);
+    if (int rc = gb_after_launch(ctx, "kzz_surface")) return rc;
+    k_kzz_heights<<<gb_blocks(ncell, tcell), tcell, 0, ctx->stream>>>(A);
+    if (int rc = gb_after_launch(ctx, "kzz_heights")) return rc;
+    k_kzz_sweep1<<<gb_blocks(ncol, tcol), tcol, 0, ctx->stream>>>(A);
+    if (int rc = gb_after_launch(ctx, "kzz_sweep1")) return rc;
+    k_kzz_raw2<<<gb_blocks(ncell, tcell), tcell, 0, ctx->stream>>>(A);
+    if (int rc = gb_after_launch(ctx, "kzz_raw2")) return rc;
+    k_kzz_sweep2<<<gb_blocks(ncol, tcol), tcol, 0, ctx->stream>>>(A);
+    if (int rc = gb_after_launch(ctx, "kzz_sweep2")) return rc;
     k_kzz_interfaces<<<gb_blocks(ncol * (A.lm - 1), tcell), tcell, 0, ctx->stream>>>(A);
     return gb_after_launch(ctx, "kzz_interfaces");
 }

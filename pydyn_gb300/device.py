@@ -92,6 +92,17 @@ class Device:
         """Work enqueued here from now on waits for `event` (recorded on any context's stream)."""
         N.check(self.L.gb_stream_wait(self.h, event.p), "gb_stream_wait")
 
+    @contextmanager
+    def redirect(self, other):
+        """Inside the block, work enqueued through this device (its arrays' operators) goes to
+        `other`'s context instead: its stream, work space and status word."""
+        h = self.h
+        self.h = other.h
+        try:
+            yield other
+        finally:
+            self.h = h
+
     # -------------------------------------------------------------- Check_CFL flag
     def cfl_reset(self):
         N.check(self.L.gb_cfl_reset(self.h), "gb_cfl_reset")

@@ -145,6 +145,7 @@ class Ensemble:
                 if before is not None:
                     before(k)
                 fw.graphs["interval"].launch()
+                fw._replays += 1
                 if after is not None:
                     after(k)
                 self.events[k].record()

@@ -18,7 +18,7 @@ import numpy as np
 
 from . import driver as D
 from . import synth
-from .device import DevArray
+from .device import DevArray, Device
 from .state import TRACERS, ZoomState
 
 WINDOW = 6 * 3600.0
@@ -64,6 +64,9 @@ class Forward:
             self.physics.init_state(self.st)
         self.graphs = {}
         self.last = {}
+        self.aux = None  # the captured interval's side contexts, one per region (with physics)
+        self.aux_cfl = None  # the captured interval's rehearsal context
+        self._replays, self._side_per_replay = 0, 0
 
     # -------------------------------------------------------------- meteo
     def put_weights(self, t):
@@ -137,7 +140,13 @@ class Forward:
 
     # -------------------------------------------------------------- the captured interval
     def _enqueue_interval(self):
-        """Check_CFL's rehearsal of one step at ndyn = nread and that step, speculatively."""
+        """Check_CFL's rehearsal of one step at ndyn = nread and that step, speculatively: the
+        step never reads the rehearsal's outcome (the host reads its flag after the replay), so
+        the rehearsal runs on its own context -- its own Check_CFL flag, search counters and
+        scratch -- beside the step, on the copies of m and sp taken at the interval's start.
+        With physics each region's Calc_Kzz and rate constants also run on a side context from
+        after Setup_MassFlow to the region's first convection, which is the first to read them.
+        Every kernel gets the inputs of the sequential order; only the overlap is new."""
         zoom, cst, st = self.zoom, self.cfl_st, self.st
         lib = st.lib
         for r in zoom.regions():
@@ -145,12 +154,51 @@ class Forward:
                 self._spec[(r, name)].assign(st[r][name])
             for name in ("m", "sp"):
                 cst[r][name].assign(st[r][name])
+        fork = self.dev.event()
+        fork.record()
+        self.aux_cfl.wait(fork)
+        with self.dev.redirect(self.aux_cfl):
+            self._enqueue_rehearsal()
+        rehearsed = self.aux_cfl.event()
+        rehearsed.record()
+        self.interpolate(st)
+        D.setup_massflow(zoom, st, self.nread)
+        kw = {"limits": self.limits}
+        conv = None
+        joins = []
+        if self.physics is not None:
+            forked = self.dev.event()
+            forked.record()
+            self.physics.prepare_step(self.nread)
+            for r, aux in zip(zoom.regions(), self.aux, strict=True):  # each region on its own stream
+                aux.wait(forked)
+                with self.dev.redirect(aux):
+                    self.physics.prepare_region(self, r)
+                joins.append(aux.event())
+                joins[-1].record()
+            # a region's side stream joins at the region's first convection (dkg; the rate
+            # constants follow in chemistry).  Until then the step's advection and exchange run
+            # beside it: they read and write none of Calc_Kzz's arrays (sp, pu, pv, t, q in; dkg,
+            # krates out) -- sp changes only in m2phlb after the region's first v
+            self.physics.pending = {r: (self.dev, j) for r, j in zip(zoom.regions(), joins, strict=True)}
+            conv, kw2 = self.physics.driver_args()
+            kw.update(kw2)
+            joins.insert(0, forked)
+        D.step(zoom, st, conv, self.nread, **kw)
+        if self.physics is not None:
+            self.physics.join_all()
+        self.dev.wait(rehearsed)
+        self._fork_events = (fork, rehearsed, joins)  # alive until the capture ends
+
+    def _enqueue_rehearsal(self):
+        """Check_CFL's rehearsal of one step on the copy (save, reset the flag, meteo, the
+        mass-only operators, restore), enqueued on whatever context the device points to."""
+        cst, lib = self.cfl_st, self.st.lib
         lib.save(cst, "check_cfl", ("m", "am", "bm", "cm"))
         lib.cfl_begin(cst)
         self.interpolate(cst)
         self._rehearse(cst, 1, 1, self.nread)
         lib.restore(cst, "check_cfl")
-        self.enqueue_step(self.nread)
 
     def _interval_graph(self, t0):
         if self.nread // self.ndyn_max != 1:
@@ -172,16 +220,43 @@ class Forward:
                                                          zip(a.lower, a.shape, strict=True)))
                           for r in self.zoom.regions() for k, a in self.st[r].items() if k in SPECULATED}  # fmt: skip
         self.st.lib.save(self.cfl_st, "check_cfl", ("m", "am", "bm", "cm"))
+        if self.aux_cfl is None:
+            # the captured interval's side contexts, their work spaces and scratch sized by one
+            # uncaptured run of what they will run (harmless: the rehearsal's copy is refilled at
+            # every interval's start, and every step recomputes what Calc_Kzz writes)
+            self.dev.sync()
+            self.aux_cfl = Device(self.dev.ordinal)
+            with self.dev.redirect(self.aux_cfl):
+                self._enqueue_rehearsal()
+            self.aux_cfl.sync()
+            if self.physics is not None:
+                self.aux = [Device(self.dev.ordinal) for _ in self.zoom.regions()]
+                for r, aux in zip(self.zoom.regions(), self.aux, strict=True):
+                    with self.dev.redirect(aux):
+                        self.physics.prepare_region(self, r)
+                    aux.sync()
         self.dev.sync()
         self.graphs.pop("interval", None)
+        side0 = self._side_launches()
         with self.dev.capture() as g:
             self._enqueue_interval()
         self.graphs["interval"] = g
+        self._side_per_replay = self._side_launches() - side0  # the side branches' kernels
+
+    def rehearsal_failed(self):
+        """Whether the last captured interval's rehearsal rejected ndyn = nread (waits for the
+        replay)."""
+        self.dev.sync_stream()
+        return (self.aux_cfl or self.dev).cfl_failed()
 
     def settle_interval(self, t0):
         """After a launched interval: read the rehearsal's flag; if Check_CFL rejected ndyn =
         nread, put the state back and redo the interval uncaptured.  Returns (ndyn, n)."""
-        if self.dev.cfl_failed():  # the speculation was wrong: back to the interval's start
+        self.dev.sync_stream()  # the replay, the side contexts' branches included
+        failed = self.aux_cfl.cfl_failed()  # the rehearsal's flag, on its context
+        for aux in self.aux or ():
+            aux.sync()  # errors of the side contexts' kernels (Calc_Kzz) are raised here
+        if failed:  # the speculation was wrong: back to the interval's start
             for (r, k), a in self._spec.items():
                 self.st[r][k].assign(a)
             self.dev.discard_status()  # the speculative step's own errors are not the run's
@@ -205,12 +280,25 @@ class Forward:
         if self.physics is not None:
             self.physics.free()
         self.w.free()
+        for aux in (self.aux or []) + ([self.aux_cfl] if self.aux_cfl is not None else []):
+            aux.close()
+        self.aux, self.aux_cfl = None, None
+
+    def _side_launches(self):
+        side = (self.aux or []) + ([self.aux_cfl] if self.aux_cfl is not None else [])
+        return sum(aux.launches() for aux in side)
+
+    def launches(self):
+        """Kernels launched so far by the run's contexts, the captured side branches' included
+        (a replay counts the main context's captured kernels there, the side ones here)."""
+        return self.dev.launches() + self._side_launches() + self._replays * self._side_per_replay
 
     def enqueue_interval_async(self, t0):
         """The captured interval, launched without any host read (the benchmark's timed loop;
         the rehearsal flag is read once after the loop)."""
         self.put_step_inputs(t0, self.nread)
         self.graphs["interval"].launch()
+        self._replays += 1
 
 
 def _interp(dst, a, b, w):

@@ -74,6 +74,8 @@ class Physics:
         self.ndyn = None
 
     # -------------------------------------------------------------- host side, outside capture
+    pending = {}  # region -> (device, event): a forked preparation not yet joined
+
     def init_state(self, st):
         """sp and phlb of every region from its initial air mass (m2phlb1 / m2phlb), so that the
         first step's Calc_Kzz and chemistry see the pressures of the state they start from."""
@@ -94,23 +96,45 @@ class Physics:
         """After Setup_MassFlow: the step counter, spm, Calc_Kzz of every region, and the rate
         constants of the step's temperature on the owned columns (every chemistry call of the
         step uses them).  Returns the driver's (conv, kwargs)."""
+        self.prepare_step(ndyn)
+        for r in self.r:
+            self.prepare_region(fwd, r)
+        return self.driver_args()
+
+    def join(self, region):
+        """A forked preparation of the region (pending) joins the step's stream here."""
+        dev_event = self.pending.pop(region, None)
+        if dev_event is not None:
+            dev, event = dev_event
+            dev.wait(event)
+
+    def join_all(self):
+        for r in list(self.pending):
+            self.join(r)
+
+    def prepare_step(self, ndyn):
+        """The step's half-step length and the step counter (convection's kept inverses)."""
         self.ndyn = ndyn
         N.check(self.dev.L.gb_iadd(self.dev.h, self.epoch.ptr, 1), "gb_iadd")
-        st = fwd.st
-        for r, d in self.r.items():
-            g, f = self.zoom.g(r), st[r]
-            fwd.interp_into(d["spm_now"], d["spm"][0], d["spm"][1])
-            dx, dy, ybeg = d["grid"]
-            K.calc_kzz(d["spm_now"], f["sp"][1 : g.im, 1 : g.jm, 1], f["pu"], f["pv"], d["t"], d["q"],
-                       d["surface"], self.at, self.bt, d["dxyp"], self.lmax, dx, dy, ybeg, d["dkg"])  # fmt: skip
-            if d["ncol"]:
-                K.chem_krates(d["t"], d["krates"], d["cols"])
-        conv = {r: self for r in self.r}
-        return conv, {"sources": self.sources, "chemistry": self.chemistry}
+
+    def prepare_region(self, fwd, r):
+        """Region r's spm at the step's middle, Calc_Kzz and the rate constants."""
+        d, g, f = self.r[r], self.zoom.g(r), fwd.st[r]
+        fwd.interp_into(d["spm_now"], d["spm"][0], d["spm"][1])
+        dx, dy, ybeg = d["grid"]
+        K.calc_kzz(d["spm_now"], f["sp"][1 : g.im, 1 : g.jm, 1], f["pu"], f["pv"], d["t"], d["q"],
+                   d["surface"], self.at, self.bt, d["dxyp"], self.lmax, dx, dy, ybeg, d["dkg"])  # fmt: skip
+        if d["ncol"]:
+            K.chem_krates(d["t"], d["krates"], d["cols"])
+
+    def driver_args(self):
+        """The driver's (conv, kwargs) of a prepared step."""
+        return {r: self for r in self.r}, {"sources": self.sources, "chemistry": self.chemistry}
 
     def convec_region(self, zoom, st, region, ndyn, inverse="crout"):
         if inverse != "crout":
             raise NotImplementedError("convec_region: the device solves with the Crout inverse only")
+        self.join(region)
         d = self.r[region]
         if d["ncol"] == 0:
             return
@@ -130,6 +154,7 @@ class Physics:
                   scale=self.spec.half_step(region, self.ndyn))  # fmt: skip
 
     def chemistry(self, zoom, st, region):
+        self.join(region)
         d = self.r[region]
         if d["ncol"] == 0:
             return
