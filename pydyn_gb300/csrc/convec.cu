@@ -11,8 +11,8 @@
 //                    it -- into a work space
 //   k_convec_tri     one thread per cloudless column (tridiagonal conv1): the same LU and L^-1
 //                    by the recurrence their non-zero elements follow
-//   k_convec_lu      one warp per other column whose inverse is made: Crout LU column by column (the
-//                    rows a term updates packed onto the lanes), then L^-1 by forward
+//   k_convec_lu      one warp per other column whose inverse is made: LU right-looking (each
+//                    step's trailing (row, column) elements packed onto the lanes), then L^-1 by forward
 //                    substitution (row k's terms applied to every later row at once, the
 //                    (row, column) elements packed onto the lanes).  U goes to the work space,
 //                    L^-1 to the inverse's place.
@@ -256,24 +256,26 @@ __global__ void __launch_bounds__(GB_TUNE_MAX_LU_WARPS * 32) k_convec_lu(CArgs A
     double *G = A.abuf + (size_t)c * n * n;
     for (int e = lane; e < n * n; e += 32) LU[e] = G[e];
     __syncwarp();
-    // ---- Crout LU, column by column: column cj receives the terms k = 0..cj-1 in order, each on
-    // the rows below k (packed onto the lanes); then its part below the diagonal / the diagonal.
-    // Above the column's first non-zero the terms' multipliers U(k, cj) are zeros that stay zero
-    // (every term that could change them is itself skipped), so the terms start there.
-    for (int cj = 0; cj < n; ++cj) {
-        const uint32_t nz0 = __ballot_sync(FULL_MASK, lane <= cj && lane < n && !is_zero(LU[(size_t)lane * n + cj]));
-        const uint32_t nz1 =
-            __ballot_sync(FULL_MASK, lane + 32 <= cj && lane + 32 < n && !is_zero(LU[(size_t)(lane + 32) * n + cj]));
-        const int first = nz0 ? __ffs(nz0) - 1 : (nz1 ? 32 + __ffs(nz1) - 1 : cj);
-        for (int k = first; k < cj; ++k) {
-            const double v = LU[(size_t)k * n + cj];  // U(k, cj), final
-            if (is_zero(v)) continue;                 // warp-uniform
-            for (int r = k + 1 + lane; r < n; r += 32)
-                LU[(size_t)r * n + cj] = LU[(size_t)r * n + cj] - LU[(size_t)r * n + k] * v;
-            __syncwarp();
+    // ---- LU, right-looking: at step k, L's column k (its rows below k divided by U(k, k), final
+    // after the steps before k), then every later element (r, c) receives its term k,
+    // A(r, c) - L(r, k) U(k, c) -- the (row, column) elements packed onto the lanes.  Each element
+    // receives its terms in k order, each skipped exactly where Crout's column-by-column form
+    // skips it (the multiplier U(k, c) a zero: above a column's first non-zero such zeros stay
+    // zero), and L's column is divided after all its terms: the same operations on every
+    // element, the same bits.
+    for (int k = 0; k < n; ++k) {
+        const double d = LU[(size_t)k * n + k];
+        for (int r = k + 1 + lane; r < n; r += 32) LU[(size_t)r * n + k] = LU[(size_t)r * n + k] / d;
+        const uint32_t m0 = __ballot_sync(FULL_MASK, lane > k && lane < n && !is_zero(LU[(size_t)k * n + lane]));
+        const uint32_t m1 =
+            __ballot_sync(FULL_MASK, lane + 32 > k && lane + 32 < n && !is_zero(LU[(size_t)k * n + lane + 32]));
+        __syncwarp();
+        const int nrow = n - k - 1, n0 = __popc(m0), ncols = n0 + __popc(m1);
+        for (int e = lane; e < nrow * ncols; e += 32) {
+            const int q = e / nrow, r = k + 1 + e % nrow;
+            const int c = q < n0 ? (int)__fns(m0, 0, q + 1) : 32 + (int)__fns(m1, 0, q - n0 + 1);
+            LU[(size_t)r * n + c] = LU[(size_t)r * n + c] - LU[(size_t)r * n + k] * LU[(size_t)k * n + c];
         }
-        const double d = LU[(size_t)cj * n + cj];
-        for (int r = cj + 1 + lane; r < n; r += 32) LU[(size_t)r * n + cj] = LU[(size_t)r * n + cj] / d;
         __syncwarp();
     }
     // ---- forward substitution of the identity: Y = L^-1.  Row k is final once the terms of
