@@ -11,7 +11,8 @@
 //                    it -- into a work space
 //   k_convec_tri     one thread per cloudless column (tridiagonal conv1): the same LU and L^-1
 //                    by the recurrence their non-zero elements follow
-//   k_convec_lu      one warp per other column whose inverse is made: LU right-looking (each
+//   k_convec_lu      one warp per other column whose inverse is made (beside k_convec_tri, on the
+//                    context's side stream): LU right-looking (each
 //                    step's trailing (row, column) elements packed onto the lanes), then L^-1 by forward
 //                    substitution (row k's terms applied to every later row at once, the
 //                    (row, column) elements packed onto the lanes).  U goes to the work space,
@@ -50,6 +51,7 @@ struct CArgs {
     double *chain;       // ncol * 4 (n+1) work space: the updraft and downdraft chains
     int32_t *fresh;      // ncol work space: 1 where this call makes the column's inverse
     int32_t *rend;       // ncol * n work space: per row of U, one past its last non-zero
+    double *tband;       // ncol * 2n work space: a tridiagonal column's U diagonal, then L's band
     double *cache_m;     // ncol * n, or null (no reuse)
     int32_t *cache_tag;  // ncol
     const int32_t *epoch;
@@ -210,32 +212,43 @@ __global__ void __launch_bounds__(GB_TUNE_MAX_CELL) k_convec_matrix(CArgs A) {
 //   L(c, c-1) = A(c, c-1) / U(c-1, c-1),   U(c, c) = A(c, c) - L(c, c-1) A(c-1, c),
 // U(c-1, c) = A(c-1, c): every other term it applies has a zero multiplier or multiplicand and
 // only changes zeros, which are never used but as zero-tested multipliers.  Written here over
-// conv1: U's diagonal (its band above stays) and L's band below; and the rows' term ends.
-// fresh = 2 tells the warp kernel the column is done and k_convec_apply that L^-1 is still to be
-// made from that band.  A column with a zero or non-finite band entry is left to the warp kernel.
+// its own band buffer (conv1 is left as it is, so that k_convec_lu, running beside it, reads the
+// bands it tests unchanged): U's diagonal and L's band below (U's band above is conv1's); and the
+// rows' term ends.  fresh = 2 tells k_convec_apply to take them from there and that L^-1 is still
+// to be made from that band.  A column with a zero or non-finite band entry is left to the warp
+// kernel, which makes the same test.
+
+// whether k_convec_tri takes column c: a cloudless column made fresh whose three bands are all
+// finite and non-zero (k_convec_lu takes the other fresh columns; the two run side by side)
+__device__ __forceinline__ bool band_ok(double v) {
+    const int64_t mag = __double_as_longlong(v) & 0x7fffffffffffffffLL;
+    return mag != 0 && mag < 0x7ff0000000000000LL;  // neither zero, infinite nor NaN
+}
+__device__ __forceinline__ bool cloudless(const CArgs &A, int c) {
+    const int i = A.cols[2 * c], j = A.cols[2 * c + 1];
+    return A.top[i * A.ts0 + j * A.ts1] <= 0 && A.lfs[i * A.ts0 + j * A.ts1] <= 1;
+}
+__device__ __forceinline__ bool band_row_ok(const double *G, int n, int r) {
+    return band_ok(G[(size_t)r * n + r]) &&
+           (r + 1 >= n || (band_ok(G[(size_t)r * n + r + 1]) && band_ok(G[(size_t)(r + 1) * n + r])));
+}
+
 __global__ void __launch_bounds__(GB_TUNE_MAX_COLUMN) k_convec_tri(CArgs A) {
     const int c = blockIdx.x * blockDim.x + threadIdx.x;
-    if (c >= A.ncol || A.fresh[c] != 1) return;
-    const int i = A.cols[2 * c], j = A.cols[2 * c + 1];
-    if (!(A.top[i * A.ts0 + j * A.ts1] <= 0 && A.lfs[i * A.ts0 + j * A.ts1] <= 1)) return;
+    if (c >= A.ncol || A.fresh[c] != 1 || !cloudless(A, c)) return;
     const int n = A.n;
     double *G = A.abuf + (size_t)c * n * n;
-    for (int r = 0; r < n; ++r) {
-        const int64_t bits[3] = {__double_as_longlong(G[(size_t)r * n + r]),
-                                 r + 1 < n ? __double_as_longlong(G[(size_t)r * n + r + 1]) : 0x3ff0000000000000LL,
-                                 r + 1 < n ? __double_as_longlong(G[(size_t)(r + 1) * n + r]) : 0x3ff0000000000000LL};
-        for (int b = 0; b < 3; ++b) {
-            const int64_t mag = bits[b] & 0x7fffffffffffffffLL;
-            if (mag == 0 || mag >= 0x7ff0000000000000LL) return;  // zero, infinite or NaN
-        }
-    }
+    for (int r = 0; r < n; ++r)
+        if (!band_row_ok(G, n, r)) return;
     int32_t *rend = A.rend + (size_t)c * n;
+    double *ud = A.tband + (size_t)c * 2 * n, *lb = ud + n;
     double uprev = G[0];  // U(r-1, r-1)
+    ud[0] = uprev;
     for (int r = 1; r < n; ++r) {
         const double l = G[(size_t)r * n + r - 1] / uprev;
         const double u = G[(size_t)r * n + r] - l * G[(size_t)(r - 1) * n + r];
-        G[(size_t)r * n + r] = u;
-        G[(size_t)r * n + r - 1] = l;  // L(r, r-1) over A(r, r-1): k_convec_apply builds L^-1 from it
+        ud[r] = u;
+        lb[r] = l;  // L(r, r-1): k_convec_apply builds L^-1 from it
         uprev = u;
     }
     for (int r = 0; r < n; ++r) rend[r] = r + 1 < n ? r + 2 : r + 1;
@@ -249,8 +262,16 @@ __global__ void __launch_bounds__(GB_TUNE_MAX_LU_WARPS * 32) k_convec_lu(CArgs A
     extern __shared__ double smem[];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int c = blockIdx.x * (blockDim.x >> 5) + warp;
-    if (c >= A.ncol || A.fresh[c] != 1) return;
+    // made in this call (k_convec_tri, beside this kernel, turns its columns' 1 into 2: the test
+    // reads 0 or not, which that write does not change)
+    if (c >= A.ncol || A.fresh[c] == 0) return;
     const int n = A.n;
+    if (cloudless(A, c)) {  // k_convec_tri's column unless a band entry is zero or not finite
+        const double *G0 = A.abuf + (size_t)c * n * n;
+        bool ok = true;
+        for (int r = lane; r < n; r += 32) ok = ok && band_row_ok(G0, n, r);
+        if (__all_sync(FULL_MASK, ok)) return;
+    }
     double *LU = smem + (size_t)warp * warp_doubles(n);  // n x n
     double *Y = LU + (size_t)n * n;                       // n x n
     double *G = A.abuf + (size_t)c * n * n;
@@ -326,12 +347,12 @@ __global__ void k_convec_apply(CArgs A) {
     // single band, Y(r, x) = +0 - L(r, r-1) Y(r-1, x) below the diagonal (the terms of a zero
     // L(r, r-1) it skips leave the +0 that this writes), 1 on it, +0 above
     if (live && A.fresh[c] == 2) {
-        const double *L = A.abuf + (size_t)c * n * n;
+        const double *lb = A.tband + (size_t)c * 2 * n + n;
         for (int r = 0; r < x; ++r) X[(size_t)r * n + x] = 0.0;
         X[(size_t)x * n + x] = 1.0;
         double y = 1.0;
         for (int r = x + 1; r < n; ++r) {
-            y = 0.0 - L[(size_t)r * n + r - 1] * y;
+            y = 0.0 - lb[r] * y;
             X[(size_t)r * n + x] = y;
         }
     }
@@ -339,6 +360,7 @@ __global__ void k_convec_apply(CArgs A) {
     if (live && A.fresh[c]) {
         const double *U = A.abuf + (size_t)c * n * n;
         const int32_t *rend = A.rend + (size_t)c * n;
+        const double *ud = A.fresh[c] == 2 ? A.tband + (size_t)c * 2 * n : nullptr;  // tri's diagonal
         for (int r = n - 1; r >= 0; --r) {
             double a = X[(size_t)r * n + x];
             for (int k = r + 1; k < rend[r]; ++k) {
@@ -346,7 +368,7 @@ __global__ void k_convec_apply(CArgs A) {
                 if (is_zero(w)) continue;
                 a = a - w * X[(size_t)k * n + x];
             }
-            X[(size_t)r * n + x] = a / U[(size_t)r * n + r];
+            X[(size_t)r * n + x] = a / (ud ? ud[r] : U[(size_t)r * n + r]);
         }
     }
     __syncthreads();
@@ -397,14 +419,16 @@ extern "C" int gb_convec(gb_ctx *ctx, const gb_view *m, const gb_view *rm, const
     // without a cache
     const size_t nchain = (size_t)NCHAIN * (lmax + 1) * ncol, nflag = ((size_t)ncol + 1) / 2;
     const size_t nrend = ((size_t)ncol * lmax + 1) / 2;
-    const size_t doubles = nn * ncol + nchain + nflag + nrend + (cache_inv ? 0 : nn * ncol);
+    const size_t ntband = (size_t)ncol * 2 * lmax;
+    const size_t doubles = nn * ncol + nchain + nflag + nrend + ntband + (cache_inv ? 0 : nn * ncol);
     double *w = gb_work(ctx, doubles * sizeof(double));
     if (!w) return GB_ECUDA;
     A.abuf = w;
     A.chain = w + nn * ncol;
     A.fresh = reinterpret_cast<int32_t *>(A.chain + nchain);
     A.rend = reinterpret_cast<int32_t *>(A.chain + nchain + nflag);
-    A.inv = cache_inv ? cache_inv : A.chain + nchain + nflag + nrend;
+    A.tband = A.chain + nchain + nflag + nrend;
+    A.inv = cache_inv ? cache_inv : A.tband + ntband;
     A.cache_m = cache_inv ? cache_m : nullptr;
     A.cache_tag = cache_tag;
     A.epoch = epoch;
@@ -413,7 +437,11 @@ extern "C" int gb_convec(gb_ctx *ctx, const gb_view *m, const gb_view *rm, const
     if (int rc = gb_after_launch(ctx, "convec_chains")) return rc;
     k_convec_matrix<<<gb_blocks((int64_t)ncol * lmax, tcell), tcell, 0, ctx->stream>>>(A);
     if (int rc = gb_after_launch(ctx, "convec_matrix")) return rc;
-    k_convec_tri<<<gb_blocks(ncol, tcol), tcol, 0, ctx->stream>>>(A);
+    // the cloudless columns' recurrence on the side stream, beside the LU of the others: each
+    // kernel decides the same split (cloudless with regular bands: tri's), so they share nothing
+    GB_CHECK_CUDA(cudaEventRecord(ctx->fork, ctx->stream));
+    GB_CHECK_CUDA(cudaStreamWaitEvent(ctx->side, ctx->fork, 0));
+    k_convec_tri<<<gb_blocks(ncol, tcol), tcol, 0, ctx->side>>>(A);
     if (int rc = gb_after_launch(ctx, "convec_tri")) return rc;
     // warps (columns) per LU block: the tuned count, fewer where their shared memory would not fit
     int warps = ctx->tune[GB_TUNE_LU_WARPS];
@@ -422,6 +450,8 @@ extern "C" int gb_convec(gb_ctx *ctx, const gb_view *m, const gb_view *rm, const
     GB_CHECK_CUDA(cudaFuncSetAttribute(k_convec_lu, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     k_convec_lu<<<gb_blocks(ncol, warps), warps * 32, smem, ctx->stream>>>(A);
     if (int rc = gb_after_launch(ctx, "convec_lu")) return rc;
+    GB_CHECK_CUDA(cudaEventRecord(ctx->join, ctx->side));
+    GB_CHECK_CUDA(cudaStreamWaitEvent(ctx->stream, ctx->join, 0));
     // whole columns per block, as many as make the block a whole number of warps (<= 1024
     // threads), and at least the tuned block size
     int per = 32 / gcd(lmax, 32);

@@ -27,6 +27,8 @@ struct gb_ctl {         // device-resident control block, one per context
 struct gb_ctx {
     int device = 0;
     cudaStream_t stream = nullptr;
+    cudaStream_t side = nullptr;   // a second stream an operator forks independent work onto
+    cudaEvent_t fork = nullptr, join = nullptr;  // (timing disabled) its fork and join
     gb_ctl *ctl = nullptr;         // device
     int32_t *scratch_i = nullptr;  // per-op integer scratch (layer nloops, ...)
     size_t scratch_i_n = 0;

@@ -58,6 +58,9 @@ extern "C" int gb_create(int device, gb_ctx **out) {
     if (!ctx) return GB_EARG;
     ctx->device = device;
     cudaError_t e = cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&ctx->side, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ctx->fork, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ctx->join, cudaEventDisableTiming);
     if (e == cudaSuccess) e = cudaMalloc(&ctx->ctl, sizeof(gb_ctl));
     if (e == cudaSuccess) e = cudaMemset(ctx->ctl, 0, sizeof(gb_ctl));
     ctx->scratch_i_n = 1 << 16;
@@ -110,6 +113,10 @@ extern "C" void gb_destroy(gb_ctx *ctx) {
     if (ctx->ctl) cudaFree(ctx->ctl);
     if (ctx->scratch_i) cudaFree(ctx->scratch_i);
     if (ctx->work) cudaFree(ctx->work);
+    if (ctx->side) cudaStreamSynchronize(ctx->side);
+    if (ctx->fork) cudaEventDestroy(ctx->fork);
+    if (ctx->join) cudaEventDestroy(ctx->join);
+    if (ctx->side) cudaStreamDestroy(ctx->side);
     if (ctx->stream) cudaStreamDestroy(ctx->stream);
     delete ctx;
 }
