@@ -261,7 +261,12 @@ int gb_loss_rates(gb_ctx *ctx, const gb_view *temper, const gb_view *phlb, const
  * inputs; on the listed columns cols (ncol, 2) int32 0-based (i, j), device, rm, rxm, rym, rzm
  * (im, jm, lm, nt) of every tracer t whose bit t-1 is set in tracer_mask are multiplied by the
  * cell's decay.  The other columns are left as they are (the reference's factor 1.0).  krates:
- * the rate constants of temper made by gb_chem_krates (the same values), or NULL. */
+ * the rate constants of temper made by gb_chem_krates (the same values), or NULL.  cache: NULL,
+ * or 8 doubles per (listed column, level) kept between calls, with epoch (a device int32 step
+ * counter, changed whenever temper, the rate constants or dt may change): a call that finds a
+ * cell's bot and top pressures and the counter as the last call left them takes the rates that
+ * do not depend on oh_factor from there (and, above the tropopause, the decay) -- the same values
+ * it would compute.  No reference counterpart for the cache (pydyn recomputes). */
 int gb_chemistry(gb_ctx *ctx, const gb_view *temper, const gb_view *phlb, const double *lat,
                  const gb_view *strat_press, const gb_view *strat_oh, const gb_view *strat_cl,
                  const gb_view *strat_od, const gb_view *oh_3d, const gb_view *pl_trop,
@@ -269,7 +274,7 @@ int gb_chemistry(gb_ctx *ctx, const gb_view *temper, const gb_view *phlb, const 
                  double oh_scale, double cl_scale, double o1d_scale, double soil_rate,
                  double dt_sec, const int32_t *cols, int ncol, uint32_t tracer_mask,
                  const gb_view *rm, const gb_view *rxm, const gb_view *rym, const gb_view *rzm,
-                 const gb_view *krates);
+                 const gb_view *krates, double *cache, const int32_t *epoch);
 /* The temperature's rate constants of chem.loss_rates (chem.py:137-140) into krates
  * (im, jm, lm, 2): [.., 0] = 2.45e-12 exp(-1775 / T), [.., 1] = (2.36e-12 (T / 298)^1.37)
  * exp(-939 / T), on the listed columns (cols NULL: every column).  A run whose temperature holds

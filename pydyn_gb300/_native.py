@@ -93,7 +93,7 @@ SIGNATURES = {
     "gb_calc_kzz": (_I, [_VP, _P, _P, _P, _P, _P, _P, _P, _VP, _VP, _VP, _I, _D, _D, _D, _P, _P]),
     "gb_loss_rates": (_I, [_VP, _P, _P, _VP, _P, _P, _P, _P, _P, _P, _P, _P, _VP, _D, _D, _D, _D, _D, _P, _P]),
     "gb_chemistry": (_I, [_VP, _P, _P, _VP, _P, _P, _P, _P, _P, _P, _P, _P, _VP, _D, _D, _D, _D, _D, _VP, _I,
-                          ctypes.c_uint32, _P, _P, _P, _P, _P]),
+                          ctypes.c_uint32, _P, _P, _P, _P, _P, _VP, _VP]),
     "gb_chem_krates": (_I, [_VP, _P, _VP, _I, _P]),
     "gb_sources": (_I, [_VP, _P, _P, _P, _VP, _D, _I, _I, _VP, _I]),
     "gb_math_eval":(_I, [_VP, _I, _VP, _VP, _VP, ctypes.c_int64]),

@@ -33,6 +33,8 @@ struct CArgs {
     int apply;
     double *edges, *trop;       // work space: (jm, ns + 1) zonal edges, (jm) tropopause
     DV krates;                  // (im, jm, lm, 2) the rate constants of the temperature, or absent
+    double *cache;              // gb_chemistry: CACHE_VALUES per (column, level), or null
+    const int32_t *epoch;       // the step counter the cache is keyed by
     gb_ctl *ctl;
 };
 
@@ -124,6 +126,15 @@ __global__ void k_chem_rows(CArgs A) {
     A.trop[j] = 30000.0 - 21500.0 * (cl * cl);
 }
 
+// The cache of gb_chemistry, per (column, level): the cell's bot and top pressures and the step
+// counter it was filled at, then the rates that do not depend on the OH factor -- the zonal OH
+// column's rate, L1 (Cl) and L2 (O(1D)) -- and, for a cell above the tropopause (where OH's rate
+// is the zonal column's), the decay itself.  A step calls chemistry in pairs on one air mass (the
+// end of a half step and the start of the next, nothing in between moves mass): the second call
+// of a pair finds the same pressures and step counter and takes these instead of remaking them --
+// the same inputs, so the same bits; only the OH factor (the half step's diurnal factor) differs.
+constexpr int CACHE_VALUES = 8;
+
 // thread per (column, level): the four rates, the decay, and its use
 __global__ void __launch_bounds__(GB_TUNE_MAX_CELL) k_chem(CArgs A) {
     const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -157,38 +168,61 @@ __global__ void __launch_bounds__(GB_TUNE_MAX_CELL) k_chem(CArgs A) {
     const double *doh = &E2(A.soh, j, 0), *dcl = &E2(A.scl, j, 0), *dod = &E2(A.sod, j, 0);
 
     {
-        const bool below = bot > edges[0];
-        double s_oh = doh[0], s_cl = dcl[0], s_od = dod[0];
-        if (!below) {  // the three zonal columns share their edges: one overlap search
-            int first, last;
-            rebin_span(edges, ns, bot, top, first, last);
-            s_oh = rebin_layer(edges, first, last, doh, A.soh.s1, bot, top);
-            s_cl = rebin_layer(edges, first, last, dcl, A.scl.s1, bot, top);
-            s_od = rebin_layer(edges, first, last, dod, A.sod.s1, bot, top);
-        }
-        const double T = E3(A.temper, i, j, l);
-        double trop_cl = 0.0;
-        if (A.has_trop) {
-            const double *dtr = &E3(A.cltrop, i, j, 0);
-            double v = dtr[0];
-            if (!(bot > tedges[0])) {
-                int first, last;
-                rebin_span(tedges, nt, bot, top, first, last);
-                v = rebin_layer(tedges, first, last, dtr, A.cltrop.s2, bot, top);
-            }
-            const double krate = A.krates.p ? E4(A.krates, i, j, l, 1) : krate_cl(T);
-            trop_cl = (v * krate) * A.cl_scale;
-        }
-        double oh = E3(A.oh3d, i, j, l);
-        if (A.oh_factor) oh = oh * A.oh_factor[i];
-        const double krate_oh = A.krates.p ? E4(A.krates, i, j, l, 0) : krate_ohf(T);
-        const double spiv = (krate_oh * oh) * A.oh_scale;
         const bool strat = bot < trop;
-        const double L0 = strat ? s_oh : spiv;
-        const double L1 = strat ? s_cl : s_cl + trop_cl;
-        const double L2 = s_od * A.o1d_scale;
+        const double T = E3(A.temper, i, j, l);
+        double *cc = A.cache ? A.cache + (size_t)t * CACHE_VALUES : nullptr;
+        const bool hit = cc && __double_as_longlong(cc[0]) == __double_as_longlong(bot) &&
+                         __double_as_longlong(cc[1]) == __double_as_longlong(top) &&
+                         __double_as_longlong(cc[2]) == (long long)*A.epoch;
+        double s_oh, L1, L2;
+        if (hit) {
+            s_oh = cc[3];
+            L1 = cc[4];
+            L2 = cc[5];
+        } else {
+            const bool below = bot > edges[0];
+            double s_cl = dcl[0], s_od = dod[0];
+            s_oh = doh[0];
+            if (!below) {  // the three zonal columns share their edges: one overlap search
+                int first, last;
+                rebin_span(edges, ns, bot, top, first, last);
+                s_oh = rebin_layer(edges, first, last, doh, A.soh.s1, bot, top);
+                s_cl = rebin_layer(edges, first, last, dcl, A.scl.s1, bot, top);
+                s_od = rebin_layer(edges, first, last, dod, A.sod.s1, bot, top);
+            }
+            double trop_cl = 0.0;
+            if (A.has_trop) {
+                const double *dtr = &E3(A.cltrop, i, j, 0);
+                double v = dtr[0];
+                if (!(bot > tedges[0])) {
+                    int first, last;
+                    rebin_span(tedges, nt, bot, top, first, last);
+                    v = rebin_layer(tedges, first, last, dtr, A.cltrop.s2, bot, top);
+                }
+                const double krate = A.krates.p ? E4(A.krates, i, j, l, 1) : krate_cl(T);
+                trop_cl = (v * krate) * A.cl_scale;
+            }
+            L1 = strat ? s_cl : s_cl + trop_cl;
+            L2 = s_od * A.o1d_scale;
+        }
+        double L0 = s_oh;
+        if (!strat) {  // below the tropopause: OH's own rate, with the half step's factor
+            double oh = E3(A.oh3d, i, j, l);
+            if (A.oh_factor) oh = oh * A.oh_factor[i];
+            const double krate_oh = A.krates.p ? E4(A.krates, i, j, l, 0) : krate_ohf(T);
+            L0 = (krate_oh * oh) * A.oh_scale;
+        }
         const double L3 = (A.has_soil && l == 0) ? -(A.soil_rate * E2(A.soil, i, j)) : 0.0;
-        const double d = gbm_exp(-((((L0 + L1) + L2) + L3) * A.dt));
+        const double d = (hit && strat) ? cc[6] : gbm_exp(-((((L0 + L1) + L2) + L3) * A.dt));
+        if (cc && !hit) {
+            cc[0] = bot;
+            cc[1] = top;
+            cc[2] = __longlong_as_double((long long)*A.epoch);
+            cc[3] = s_oh;
+            cc[4] = L1;
+            cc[5] = L2;
+            cc[6] = d;  // taken again only above the tropopause, where no input differs
+        }
         if (A.apply) {
             for (uint32_t mask = A.tracer_mask; mask; mask &= mask - 1) {
                 const int t = __ffs(mask) - 1;
@@ -299,8 +333,10 @@ extern "C" int gb_chemistry(gb_ctx *ctx, const gb_view *temper, const gb_view *p
                             const gb_view *cl_trop, const gb_view *soil, const double *oh_factor, double oh_scale,
                             double cl_scale, double o1d_scale, double soil_rate, double dt_sec, const int32_t *cols,
                             int ncol, uint32_t tracer_mask, const gb_view *rm, const gb_view *rxm,
-                            const gb_view *rym, const gb_view *rzm, const gb_view *krates) {
+                            const gb_view *rym, const gb_view *rzm, const gb_view *krates, double *cache,
+                            const int32_t *epoch) {
     if (!ctx || !rm || !rxm || !rym || !rzm || (ncol > 0 && !cols) || ncol < 0) return GB_EARG;
+    if (cache && !epoch) return GB_EARG;
     CArgs A{};
     if (int rc = setup_chem(A, temper, phlb, lat, strat_press, strat_oh, strat_cl, strat_od, oh_3d, pl_trop, cl_trop,
                             soil, oh_factor, oh_scale, cl_scale, o1d_scale, soil_rate, dt_sec))
@@ -311,6 +347,8 @@ extern "C" int gb_chemistry(gb_ctx *ctx, const gb_view *temper, const gb_view *p
         return GB_EARG;
     }
     A.q[0] = dv(rm); A.q[1] = dv(rxm); A.q[2] = dv(rym); A.q[3] = dv(rzm);
+    A.cache = cache;
+    A.epoch = epoch;
     A.tracer_mask = tracer_mask;
     A.apply = 1;
     A.cols = cols;

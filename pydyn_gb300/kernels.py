@@ -175,9 +175,11 @@ def loss_rates(temper, phlb, lat, fields, dt, loss=None, decay=None, oh_factor=N
 
 
 def chemistry(temper, phlb, lat, fields, dt, cols, tracers, rm, rxm, rym, rzm, oh_factor=None, oh_scale=1.0,
-              cl_scale=1.0, o1d_scale=1.0, soil_rate=0.0, krates=None):
+              cl_scale=1.0, o1d_scale=1.0, soil_rate=0.0, krates=None, cache=None):
     """chemistry_region (zoom/physics.py:67): the decay of each listed column's cells applied to
-    the mass and slopes of the (1-based) `tracers`.  krates: chem_krates(temper)'s, or None."""
+    the mass and slopes of the (1-based) `tracers`.  krates: chem_krates(temper)'s, or None.
+    cache: None or (array of 8 doubles per listed cell, step counter int32 DevArray): the
+    rates a later call on the same pressures in the same step takes again."""
     _tracer_strides(rm, rxm, rym, rzm)
     mask = 0
     for t in tracers:
@@ -185,7 +187,8 @@ def chemistry(temper, phlb, lat, fields, dt, cols, tracers, rm, rxm, rym, rzm, o
     L, h = _lib(temper)
     N.check(L.gb_chemistry(h, *_chem_args(temper, phlb, lat, fields, oh_factor, oh_scale, cl_scale, o1d_scale,
                                           soil_rate, dt), cols.ptr, cols.shape[0], mask,
-                           *views(rm, rxm, rym, rzm, krates)), "chemistry")  # fmt: skip
+                           *views(rm, rxm, rym, rzm, krates), None if cache is None else cache[0].ptr,
+                           None if cache is None else cache[1].ptr), "chemistry")  # fmt: skip
 
 
 def chem_krates(temper, krates, cols=None):

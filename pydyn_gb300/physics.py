@@ -67,6 +67,8 @@ class Physics:
                 "cache": (DevArray.zeros(dev, (0, max(ncol, 1) * self.lmax * self.lmax - 1)),
                           DevArray.zeros(dev, (0, max(ncol, 1) * self.lmax - 1)),
                           DevArray.from_host(dev, np.full(max(ncol, 1), -1, dtype=np.int32)), self.epoch),
+                # chemistry's paired-call cache: 8 doubles per owned cell, keyed by the step counter
+                "chem_cache": DevArray.zeros(dev, (0, max(ncol, 1) * zoom.lm * 8 - 1)),
                 "dxyp": dxyp[r],
                 "grid": ((g.xend - g.xbeg) / g.im, (g.yend - g.ybeg) / g.jm, float(g.ybeg)),
             }  # fmt: skip
@@ -163,7 +165,7 @@ class Physics:
         c = d["chem"]
         K.chemistry(d["t"], f["phlb"][1 : g.im, 1 : g.jm, 1 : zoom.lm + 1], c["lat"], c, self.spec.half_step(region,
                     self.ndyn), d["cols"], CH4_TRACERS, *_interior(st, region)[1:], oh_factor=d["factors"][h],
-                    krates=d["krates"], **self.spec.settings)  # fmt: skip
+                    krates=d["krates"], cache=(d["chem_cache"], self.epoch), **self.spec.settings)  # fmt: skip
 
     def free(self):
         seen = set()
