@@ -76,6 +76,11 @@ int gb_graph_destroy(void *graph);
 #define GB_TUNE_APPLY_THREADS 3  /* the convection apply's smallest block (whole columns): 32..1024 */
 #define GB_TUNE_N 4
 int gb_device_name(gb_ctx *ctx, char *buf, int len); /* "<name> sm_<cc> x<SMs>": the tuning cache's key */
+/* The context's work space (what operators allocate lazily outside a capture): at least bytes
+ * from now on, and its present size -- a context that will run captured work first takes the
+ * size another context's uncaptured run grew to. */
+int gb_work_reserve(gb_ctx *ctx, size_t bytes);
+size_t gb_work_size(gb_ctx *ctx);
 int gb_tune_set(gb_ctx *ctx, int key, int value); /* GB_EARG for a value outside the key's range */
 int gb_tune_get(gb_ctx *ctx, int key, int *value);
 

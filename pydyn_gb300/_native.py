@@ -57,6 +57,8 @@ SIGNATURES = {
     "gb_event_create": (_I, [ctypes.POINTER(_VP)]),
     "gb_event_record": (_I, [_VP, _VP]),
     "gb_stream_wait": (_I, [_VP, _VP]),
+    "gb_work_reserve": (_I, [_VP, ctypes.c_size_t]),
+    "gb_work_size": (ctypes.c_size_t, [_VP]),
     "gb_device_name": (_I, [_VP, ctypes.c_char_p, _I]),
     "gb_tune_set": (_I, [_VP, _I, _I]),
     "gb_tune_get": (_I, [_VP, _I, ctypes.POINTER(_I)]),

@@ -74,6 +74,13 @@ extern "C" int gb_create(int device, gb_ctx **out) {
     return GB_OK;
 }
 
+extern "C" int gb_work_reserve(gb_ctx *ctx, size_t bytes) {
+    if (!ctx) return GB_EARG;
+    return gb_work(ctx, bytes) ? GB_OK : GB_ECUDA;
+}
+
+extern "C" size_t gb_work_size(gb_ctx *ctx) { return ctx ? ctx->work_bytes : 0; }
+
 extern "C" int gb_device_name(gb_ctx *ctx, char *buf, int len) {
     if (!ctx || !buf || len <= 0) return GB_EARG;
     cudaDeviceProp prop;

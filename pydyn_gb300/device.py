@@ -112,6 +112,14 @@ class Device:
         N.check(self.L.gb_cfl_failed(self.h, ctypes.byref(f)), "gb_cfl_failed")
         return bool(f.value)
 
+    # -------------------------------------------------------------- work space
+    def work_size(self):
+        return int(self.L.gb_work_size(self.h))
+
+    def reserve_work(self, nbytes):
+        """At least nbytes of work space (outside a capture)."""
+        N.check(self.L.gb_work_reserve(self.h, int(nbytes)), "gb_work_reserve")
+
     # -------------------------------------------------------------- launch shapes
     def name(self):
         """The GPU's name, compute capability and SM count."""

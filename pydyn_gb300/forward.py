@@ -19,6 +19,7 @@ import numpy as np
 from . import driver as D
 from . import synth
 from .device import DevArray, Device
+from .schedule import ScheduledLib, Scheduler, scheduled_physics, spreadable
 from .state import TRACERS, ZoomState
 
 WINDOW = 6 * 3600.0
@@ -166,12 +167,16 @@ class Forward:
         kw = {"limits": self.limits}
         conv = None
         joins = []
-        if self.physics is not None:
+        forked = None
+        if self.aux is not None:  # the side contexts start from the step's own setup
+            if self.physics is not None:
+                self.physics.prepare_step(self.nread)
             forked = self.dev.event()
             forked.record()
-            self.physics.prepare_step(self.nread)
-            for r, aux in zip(zoom.regions(), self.aux, strict=True):  # each region on its own stream
+            for aux in self.aux:
                 aux.wait(forked)
+        if self.physics is not None:
+            for r, aux in zip(zoom.regions(), self.aux, strict=True):  # each region on its own stream
                 with self.dev.redirect(aux):
                     self.physics.prepare_region(self, r)
                 joins.append(aux.event())
@@ -183,12 +188,29 @@ class Forward:
             self.physics.pending = {r: (self.dev, j) for r, j in zip(zoom.regions(), joins, strict=True)}
             conv, kw2 = self.physics.driver_args()
             kw.update(kw2)
-            joins.insert(0, forked)
-        D.step(zoom, st, conv, self.nread, **kw)
+        sched = None
+        if self.aux is not None and zoom.nregions > 1 and spreadable(zoom):
+            # the step's bodies spread over one stream per region (pydyn_gb300.schedule)
+            sched = Scheduler(self.dev, {r: aux for r, aux in zip(zoom.regions(), self.aux, strict=True) if r != 1})
+            for name in ("sources", "chemistry"):
+                if name in kw:
+                    kw[name] = scheduled_physics(sched, kw[name], name)
+            st.lib = ScheduledLib(lib, sched)
+        try:
+            D.step(zoom, st, conv, self.nread, **kw)
+        finally:
+            st.lib = lib
+        if sched is not None:
+            sched.join()
         if self.physics is not None:
             self.physics.join_all()
+        for aux in self.aux or ():  # every side stream is joined before the capture ends
+            done = aux.event()
+            done.record()
+            self.dev.wait(done)
+            joins.append(done)
         self.dev.wait(rehearsed)
-        self._fork_events = (fork, rehearsed, joins)  # alive until the capture ends
+        self._fork_events = (fork, rehearsed, forked, joins, sched.keep if sched else None)  # alive until the capture ends
 
     def _enqueue_rehearsal(self):
         """Check_CFL's rehearsal of one step on the copy (save, reset the flag, meteo, the
@@ -229,11 +251,15 @@ class Forward:
             with self.dev.redirect(self.aux_cfl):
                 self._enqueue_rehearsal()
             self.aux_cfl.sync()
-            if self.physics is not None:
+            if self.physics is not None or (self.zoom.nregions > 1 and spreadable(self.zoom)):
+                # one per region: Calc_Kzz, and a child's share of the step; their work spaces
+                # as large as the run's own grew in its uncaptured interval
                 self.aux = [Device(self.dev.ordinal) for _ in self.zoom.regions()]
                 for r, aux in zip(self.zoom.regions(), self.aux, strict=True):
-                    with self.dev.redirect(aux):
-                        self.physics.prepare_region(self, r)
+                    if self.physics is not None:
+                        with self.dev.redirect(aux):
+                            self.physics.prepare_region(self, r)
+                    aux.reserve_work(self.dev.work_size())
                     aux.sync()
         self.dev.sync()
         self.graphs.pop("interval", None)

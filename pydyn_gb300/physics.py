@@ -15,6 +15,8 @@ region tree as pydyn forward.py:411-451 runs them for one region:
 Everything a step enqueues reads its time-dependent inputs (weights, OH factors, the step
 counter) from device memory, so one captured graph serves every step."""
 
+from contextlib import contextmanager
+
 import numpy as np
 
 from . import _native as N
@@ -46,10 +48,18 @@ class Physics:
         for r in zoom.regions():
             g, R = zoom.g(r), spec.region[r]
             own = zoom.owned(r)
-            cols = np.argwhere(own).astype(np.int32)
-            # deepest clouds first: a warp's columns then share their matrices' zero structure
             top = R["conv"]["cloud_top"]
-            cols = cols[np.argsort(-top[cols[:, 0], cols[:, 1]], kind="stable")]
+
+            def listed(mask, top=top):  # deepest clouds first: a warp's columns share their matrices' zeros
+                c = np.argwhere(mask).astype(np.int32)
+                return c[np.argsort(-top[c[:, 0], c[:, 1]], kind="stable")]
+
+            # the owned columns in two segments: outside every child's footprint, and inside one
+            # (the footprint's edge under a child's ring, which update_parent writes first)
+            inside = np.zeros_like(own)
+            for ch in zoom.children[r]:
+                inside[zoom.ibeg[ch] - 1 : zoom.iend[ch], zoom.jbeg[ch] - 1 : zoom.jend[ch]] = True
+            cols = listed(own)
             ncol = len(cols)
             d = {
                 "conv": {k: up(v, np.int32 if k.startswith("cloud") else np.float64) for k, v in R["conv"].items()},
@@ -72,11 +82,40 @@ class Physics:
                 "dxyp": dxyp[r],
                 "grid": ((g.xend - g.xbeg) / g.im, (g.yend - g.ybeg) / g.jm, float(g.ybeg)),
             }  # fmt: skip
+            segs = [("far", listed(own & ~inside)), ("edge", listed(own & inside))] if inside.any() else []
+            d["segments"] = [{"name": "all", "cols": d["cols"], "ncol": ncol, "cache": d["cache"],
+                              "chem_cache": d["chem_cache"]}] if not segs else [
+                {"name": name, "cols": up(c if len(c) else np.zeros((0, 2)), np.int32), "ncol": len(c),
+                 "cache": (DevArray.zeros(dev, (0, max(len(c), 1) * self.lmax * self.lmax - 1)),
+                           DevArray.zeros(dev, (0, max(len(c), 1) * self.lmax - 1)),
+                           DevArray.from_host(dev, np.full(max(len(c), 1), -1, dtype=np.int32)), self.epoch),
+                 "chem_cache": DevArray.zeros(dev, (0, max(len(c), 1) * zoom.lm * 8 - 1))}
+                for name, c in segs]  # fmt: skip
+            if segs:  # the whole list's caches are the segments' now
+                for a in (*d["cache"][:3], d["chem_cache"]):
+                    a.free()
+                d["cache"], d["chem_cache"] = None, None
             self.r[r] = d
         self.ndyn = None
 
     # -------------------------------------------------------------- host side, outside capture
     pending = {}  # region -> (device, event): a forked preparation not yet joined
+    only = None  # a segment name: the physics bodies act on that segment's columns alone
+
+    def segment_names(self, region):
+        return [s["name"] for s in self.r[region]["segments"]]
+
+    @contextmanager
+    def only_segment(self, name):
+        """Inside the block the physics bodies act on one segment of the owned columns."""
+        self.only = name
+        try:
+            yield
+        finally:
+            self.only = None
+
+    def _segments(self, region):
+        return [s for s in self.r[region]["segments"] if s["ncol"] and self.only in (None, s["name"])]
 
     def init_state(self, st):
         """sp and phlb of every region from its initial air mass (m2phlb1 / m2phlb), so that the
@@ -138,34 +177,32 @@ class Physics:
             raise NotImplementedError("convec_region: the device solves with the Crout inverse only")
         self.join(region)
         d = self.r[region]
-        if d["ncol"] == 0:
-            return
         c = d["conv"]
         dt = ndyn / (2.0 * zoom.g(region).tref)
-        K.convec(*_interior(st, region), c["entu"], c["detu"], c["entd"], c["detd"], d["dkg"], c["cloud_top"],
-                 c["cloud_lfs"], d["cols"], dt, self.lmax, cache=d["cache"])  # fmt: skip
+        for s in self._segments(region):  # column by column: the segments' order changes nothing
+            K.convec(*_interior(st, region), c["entu"], c["detu"], c["entd"], c["detd"], d["dkg"], c["cloud_top"],
+                     c["cloud_lfs"], s["cols"], dt, self.lmax, cache=s["cache"])  # fmt: skip
 
     def sources(self, zoom, st, region):
         d = self.r[region]
-        if d["ncol"] == 0:
-            return
         g, f = zoom.g(region), st[region]
         rm = f["rm"][1 : g.im, 1 : g.jm, 1 : zoom.lm]
         rzm = f["rzm"][1 : g.im, 1 : g.jm, 1 : zoom.lm]
-        K.sources(rm, rzm, d["flux"], d["cols"], LEVEL, TRACER, area=d["dxyp"],
-                  scale=self.spec.half_step(region, self.ndyn))  # fmt: skip
+        for s in self._segments(region):
+            K.sources(rm, rzm, d["flux"], s["cols"], LEVEL, TRACER, area=d["dxyp"],
+                      scale=self.spec.half_step(region, self.ndyn))  # fmt: skip
 
     def chemistry(self, zoom, st, region):
         self.join(region)
         d = self.r[region]
-        if d["ncol"] == 0:
-            return
         g, f = zoom.g(region), st[region]
         h = zoom.status[region] // N_OPERATORS
         c = d["chem"]
-        K.chemistry(d["t"], f["phlb"][1 : g.im, 1 : g.jm, 1 : zoom.lm + 1], c["lat"], c, self.spec.half_step(region,
-                    self.ndyn), d["cols"], CH4_TRACERS, *_interior(st, region)[1:], oh_factor=d["factors"][h],
-                    krates=d["krates"], cache=(d["chem_cache"], self.epoch), **self.spec.settings)  # fmt: skip
+        for s in self._segments(region):
+            K.chemistry(d["t"], f["phlb"][1 : g.im, 1 : g.jm, 1 : zoom.lm + 1], c["lat"], c,
+                        self.spec.half_step(region, self.ndyn), s["cols"], CH4_TRACERS, *_interior(st, region)[1:],
+                        oh_factor=d["factors"][h], krates=d["krates"], cache=(s["chem_cache"], self.epoch),
+                        **self.spec.settings)  # fmt: skip
 
     def free(self):
         seen = set()
@@ -175,12 +212,20 @@ class Physics:
                 seen.add(id(a))
                 a.free()
 
+        def walk(v):
+            if isinstance(v, dict):
+                for x in v.values():
+                    walk(x)
+            elif isinstance(v, (list, tuple)):
+                for x in v:
+                    walk(x)
+            else:
+                rel(v)
+
         for d in self.r.values():
             for k, v in d.items():
-                if k == "dxyp":  # the state's
-                    continue
-                for a in v.values() if isinstance(v, dict) else v if isinstance(v, (list, tuple)) else [v]:
-                    rel(a)
+                if k != "dxyp":  # the state's
+                    walk(v)
         for a in (self.at, self.bt, self.epoch):
             rel(a)
 
