@@ -66,8 +66,9 @@ class Scheduler:
 
     def __init__(self, dev, streams):
         self.dev, self.streams = dev, streams
-        self.writer = {}  # part -> (stream key, event)
-        self.readers = {}  # part -> [(stream key, event)]
+        self.writer = {}  # part -> (stream key, sequence number, event)
+        self.readers = {}  # part -> [(stream key, sequence number, event)]
+        self.seq = 0
         self.last = {}  # stream key -> its last event
         self.keep = []  # the events, alive until the capture ends
 
@@ -86,24 +87,27 @@ class Scheduler:
                 waits.append(w)
         for p in writes:
             waits.extend(self.readers.get(p, []))
+        latest = {}  # another stream -> its latest event to wait for (a stream's events are ordered)
+        for k, n, ev in waits:
+            if k != key and (k not in latest or n > latest[k][0]):
+                latest[k] = (n, ev)
         side = self.streams.get(region) if key != 1 else None
         ctx = self.dev.redirect(side) if side is not None else _nothing()
         with ctx:
-            seen = set()
-            for k, ev in waits:
-                if k != key and id(ev) not in seen:
-                    seen.add(id(ev))
-                    self.dev.wait(ev)
+            for _, ev in latest.values():
+                self.dev.wait(ev)
             yield
             ev = self.dev.event()
             ev.record()
+        self.seq += 1
+        entry = (key, self.seq, ev)
         self.keep.append(ev)
         self.last[key] = ev
         for p in writes:
-            self.writer[p] = (key, ev)
+            self.writer[p] = entry
             self.readers[p] = []
         for p in reads - writes:
-            self.readers.setdefault(p, []).append((key, ev))
+            self.readers.setdefault(p, []).append(entry)
 
     def join(self):
         """The run's own stream waits for every other stream's last body."""

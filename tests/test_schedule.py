@@ -1,0 +1,96 @@
+"""The region scheduler's dependency tracking (pydyn_gb300.schedule), on the host with a fake
+device that records which stream each event is recorded on and which stream waits for it."""
+
+from contextlib import contextmanager
+
+from pydyn_gb300 import schedule as S
+
+
+class FakeEvent:
+    def __init__(self, dev):
+        self.dev, self.stream = dev, None
+
+    def record(self):
+        self.stream = self.dev.current
+        self.dev.log.append(("record", self.stream, id(self)))
+
+
+class FakeDev:
+    def __init__(self):
+        self.current, self.log = "main", []
+
+    def event(self):
+        return FakeEvent(self)
+
+    def wait(self, ev):
+        self.log.append(("wait", self.current, ev.stream))
+
+    @contextmanager
+    def redirect(self, other):
+        old, self.current = self.current, other
+        try:
+            yield other
+        finally:
+            self.current = old
+
+
+def _run(bodies):
+    dev = FakeDev()
+    sched = S.Scheduler(dev, {2: "child"})
+    waits = []
+    for name, region in bodies:
+        n0 = len(dev.log)
+        with sched.body(name, region):
+            pass
+        waits.append([e for e in dev.log[n0:] if e[0] == "wait"])
+    return waits
+
+
+def test_parts_follow_the_kernels():
+    assert S.parts("put_xedges", 1) == (S.PARENT_ALL, {"c_halo", "c_ring"})
+    assert S.parts("update_parent", 2) == (S.CHILD_ALL, {"p_edge", "p_core"})
+    assert S.parts("convec_region:far", 1) == ({"p_far"}, {"p_far"})
+    assert S.parts("chemistry:edge", 1) == ({"p_edge"}, {"p_edge"})
+    assert S.parts("chemistry", 2) == ({"c_in"}, {"c_in"})
+    assert S.parts("outer_x_faces_zeroed", 1) == (set(), set())
+
+
+def test_far_physics_beside_the_child_edge_after_it():
+    waits = _run([
+        ("_dynamu_region1", 1),       # 0: the parent's advection
+        ("put_xedges", 1),            # 1: the parent -> the child's halo and ring
+        ("_dynamu_child", 2),         # 2: the child waits for the edges
+        ("update_parent", 2),         # 3: the child's sums -> the footprint
+        ("convec_region:far", 1),     # 4: beside the child
+        ("convec_region:edge", 1),    # 5: after update_parent
+        ("put_xedges", 1),            # 6: after the child's last use of its halo and ring
+        ("m2phlb1", 1),               # 7: the whole parent, after update_parent
+    ])  # fmt: skip
+    assert waits[2] == [("wait", "child", "main")]
+    assert waits[3] == [("wait", "child", "main")]  # the parent's advection and edges, one wait
+    assert waits[4] == []
+    assert waits[5] == [("wait", "main", "child")]
+    assert waits[6] == [("wait", "main", "child")]
+    assert waits[7] == [("wait", "main", "child")]
+
+
+def test_child_physics_beside_the_parent_advection():
+    waits = _run([
+        ("update_parent", 2),
+        ("_dynamw_region1", 1),       # the parent's z: waits for update_parent
+        ("put_yedges", 1),            # writes the child's halo and ring
+        ("chemistry", 2),             # the child's scope: nothing to wait for
+        ("convec_region", 2),
+        ("_dynamw_child", 2),         # the child's advection: waits for put_yedges
+    ])  # fmt: skip
+    assert waits[1] == [("wait", "main", "child")]
+    assert waits[3] == [] and waits[4] == []
+    assert waits[5] == [("wait", "child", "main")]
+
+
+def test_spreadable_trees():
+    from pydyn_gb300 import synth
+
+    assert S.spreadable(synth.tree("two", 4))
+    assert S.spreadable(synth.tree("glb3x2+nam1x1", 4))
+    assert not S.spreadable(synth.tree("three", 4))
