@@ -69,6 +69,7 @@ class Scheduler:
         self.writer = {}  # part -> (stream key, sequence number, event)
         self.readers = {}  # part -> [(stream key, sequence number, event)]
         self.seq = 0
+        self.waited = {}  # (stream key, other stream key) -> the latest sequence number waited for
         self.last = {}  # stream key -> its last event
         self.keep = []  # the events, alive until the capture ends
 
@@ -89,8 +90,10 @@ class Scheduler:
             waits.extend(self.readers.get(p, []))
         latest = {}  # another stream -> its latest event to wait for (a stream's events are ordered)
         for k, n, ev in waits:
-            if k != key and (k not in latest or n > latest[k][0]):
+            if k != key and n > self.waited.get((key, k), 0) and (k not in latest or n > latest[k][0]):
                 latest[k] = (n, ev)
+        for k, (n, _) in latest.items():
+            self.waited[(key, k)] = n
         side = self.streams.get(region) if key != 1 else None
         ctx = self.dev.redirect(side) if side is not None else _nothing()
         with ctx:

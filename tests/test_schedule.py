@@ -71,7 +71,7 @@ def test_far_physics_beside_the_child_edge_after_it():
     assert waits[4] == []
     assert waits[5] == [("wait", "main", "child")]
     assert waits[6] == [("wait", "main", "child")]
-    assert waits[7] == [("wait", "main", "child")]
+    assert waits[7] == []  # the main stream waited for the child's update_parent already
 
 
 def test_child_physics_beside_the_parent_advection():
