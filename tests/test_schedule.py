@@ -66,12 +66,12 @@ def test_far_physics_beside_the_child_edge_after_it():
         ("put_xedges", 1),            # 6: after the child's last use of its halo and ring
         ("m2phlb1", 1),               # 7: the whole parent, after update_parent
     ])  # fmt: skip
-    assert waits[2] == [("wait", "child", "main")]
-    assert waits[3] == [("wait", "child", "main")]  # the parent's advection and edges, one wait
+    assert waits[2] == [("wait", "child", "main")]  # after the parent's advection and edges
+    assert waits[3] == []  # the child's stream waited for those already (at 2)
     assert waits[4] == []
-    assert waits[5] == [("wait", "main", "child")]
-    assert waits[6] == [("wait", "main", "child")]
-    assert waits[7] == []  # the main stream waited for the child's update_parent already
+    assert waits[5] == [("wait", "main", "child")]  # after update_parent, the child's last body
+    assert waits[6] == []  # implied by 5
+    assert waits[7] == []
 
 
 def test_child_physics_beside_the_parent_advection():
