@@ -1,7 +1,10 @@
 // The CH4 `c` and `s` operators on a region's columns.
 //
 // k_chem_rows: thread per latitude -- the zonal loss-rate columns' edges (strat_edges), checked
-// strictly descending, and the tropopause pressure.  k_chem: thread per (column, level) -- the
+// strictly descending, and the tropopause pressure.  k_chem: thread per (column, level), a warp
+// holding one level of 32 columns (cells at one level take the same branches -- above or below
+// the tropopause, inside the zonal columns or under them -- so the FP64 pipe issues with its
+// lanes full) and a block that warp's neighbouring levels -- the
 // cell's half levels and tropospheric Cl edges checked, the four loss rates, decay =
 // exp(-(((L1 + L2) + L3) + L4) dt), and either the rates and decay written out (gb_loss_rates,
 // every column of the region) or the decay applied to the listed tracers' mass and slopes
@@ -33,7 +36,8 @@ struct CArgs {
     int apply;
     double *edges, *trop;       // work space: (jm, ns + 1) zonal edges, (jm) tropopause
     DV krates;                  // (im, jm, lm, 2) the rate constants of the temperature, or absent
-    double *cache;              // gb_chemistry: CACHE_VALUES per (column, level), or null
+    double *cache;              // gb_chemistry: CACHE_VALUES per (column, level), or null: value v
+                                // of the cell (c, l) at v * ncol * lm + l * ncol + c
     const int32_t *epoch;       // the step counter the cache is keyed by
     gb_ctl *ctl;
 };
@@ -126,7 +130,8 @@ __global__ void k_chem_rows(CArgs A) {
     A.trop[j] = 30000.0 - 21500.0 * (cl * cl);
 }
 
-// The cache of gb_chemistry, per (column, level): the cell's bot and top pressures and the step
+// The cache of gb_chemistry, per (column, level) (value-major, then level, then column: a warp's
+// reads are contiguous): the cell's bot and top pressures and the step
 // counter it was filled at, then the rates that do not depend on the OH factor -- the zonal OH
 // column's rate, L1 (Cl) and L2 (O(1D)) -- and, for a cell above the tropopause (where OH's rate
 // is the zonal column's), the decay itself.  A step calls chemistry in pairs on one air mass (the
@@ -135,13 +140,15 @@ __global__ void k_chem_rows(CArgs A) {
 // the same inputs, so the same bits; only the OH factor (the half step's diurnal factor) differs.
 constexpr int CACHE_VALUES = 8;
 
-// thread per (column, level): the four rates, the decay, and its use
+// thread per (column, level): the four rates, the decay, and its use.  Lanes run along the
+// columns, warps along the levels: a block is 32 columns at blockDim / 32 consecutive levels.
 __global__ void __launch_bounds__(GB_TUNE_MAX_CELL) k_chem(CArgs A) {
-    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    const int lm = A.lm;
-    if (t >= A.ncol * lm) return;
-    const int64_t c = t / lm;
-    const int l = (int)(t % lm);
+    const int lm = A.lm, lv = blockDim.x >> 5;
+    const int nlg = (lm + lv - 1) / lv;
+    const int64_t c = (int64_t)(blockIdx.x / nlg) * 32 + (threadIdx.x & 31);
+    const int l = (int)(blockIdx.x % nlg) * lv + (int)(threadIdx.x >> 5);
+    if (c >= A.ncol || l >= lm) return;
+    const int64_t ncell = A.ncol * lm, u = (int64_t)l * A.ncol + c;  // u: the cell's place in the cache
     int i, j;
     if (A.cols) {
         i = A.cols[2 * c];
@@ -170,15 +177,15 @@ __global__ void __launch_bounds__(GB_TUNE_MAX_CELL) k_chem(CArgs A) {
     {
         const bool strat = bot < trop;
         const double T = E3(A.temper, i, j, l);
-        double *cc = A.cache ? A.cache + (size_t)t * CACHE_VALUES : nullptr;
+        double *cc = A.cache ? A.cache + u : nullptr;  // value v at cc[v * ncell]
         const bool hit = cc && __double_as_longlong(cc[0]) == __double_as_longlong(bot) &&
-                         __double_as_longlong(cc[1]) == __double_as_longlong(top) &&
-                         __double_as_longlong(cc[2]) == (long long)*A.epoch;
+                         __double_as_longlong(cc[ncell]) == __double_as_longlong(top) &&
+                         __double_as_longlong(cc[2 * ncell]) == (long long)*A.epoch;
         double s_oh, L1, L2;
         if (hit) {
-            s_oh = cc[3];
-            L1 = cc[4];
-            L2 = cc[5];
+            s_oh = cc[3 * ncell];
+            L1 = cc[4 * ncell];
+            L2 = cc[5 * ncell];
         } else {
             const bool below = bot > edges[0];
             double s_cl = dcl[0], s_od = dod[0];
@@ -213,15 +220,15 @@ __global__ void __launch_bounds__(GB_TUNE_MAX_CELL) k_chem(CArgs A) {
             L0 = (krate_oh * oh) * A.oh_scale;
         }
         const double L3 = (A.has_soil && l == 0) ? -(A.soil_rate * E2(A.soil, i, j)) : 0.0;
-        const double d = (hit && strat) ? cc[6] : gbm_exp(-((((L0 + L1) + L2) + L3) * A.dt));
+        const double d = (hit && strat) ? cc[6 * ncell] : gbm_exp(-((((L0 + L1) + L2) + L3) * A.dt));
         if (cc && !hit) {
             cc[0] = bot;
-            cc[1] = top;
-            cc[2] = __longlong_as_double((long long)*A.epoch);
-            cc[3] = s_oh;
-            cc[4] = L1;
-            cc[5] = L2;
-            cc[6] = d;  // taken again only above the tropopause, where no input differs
+            cc[ncell] = top;
+            cc[2 * ncell] = __longlong_as_double((long long)*A.epoch);
+            cc[3 * ncell] = s_oh;
+            cc[4 * ncell] = L1;
+            cc[5 * ncell] = L2;
+            cc[6 * ncell] = d;  // taken again only above the tropopause, where no input differs
         }
         if (A.apply) {
             for (uint32_t mask = A.tracer_mask; mask; mask &= mask - 1) {
@@ -302,9 +309,10 @@ int launch_chem(gb_ctx *ctx, CArgs &A) {
     A.trop = w + (size_t)A.jm * (A.ns + 1);
     k_chem_rows<<<(unsigned)((A.jm + 127) / 128), 128, 0, ctx->stream>>>(A);
     if (int rc = gb_after_launch(ctx, "chem_rows")) return rc;
-    const int64_t cells = A.ncol * A.lm;
-    const int tcell = ctx->tune[GB_TUNE_CELL_THREADS];
-    k_chem<<<gb_blocks(cells, tcell), tcell, 0, ctx->stream>>>(A);
+    // blocks of 32 columns x (tcell / 32) levels
+    const int tcell = ctx->tune[GB_TUNE_CELL_THREADS], lv = tcell / 32;
+    const int64_t blocks = (A.ncol + 31) / 32 * ((A.lm + lv - 1) / lv);
+    k_chem<<<(unsigned)blocks, tcell, 0, ctx->stream>>>(A);
     return gb_after_launch(ctx, A.apply ? "chemistry" : "loss_rates");
 }
 
