@@ -67,6 +67,11 @@ __device__ __forceinline__ double &AT4(const DV &v, int64_t i, int64_t j, int64_
 __device__ __forceinline__ double max0(double x) { return gb_isnan(x) ? x : (0.0 > x ? 0.0 : x); }
 // x == 0.0 (either sign), tested on the integer pipe: the FP64 pipe is kept for arithmetic
 __device__ __forceinline__ bool is_zero(double x) { return (__double_as_longlong(x) << 1) == 0; }
+// x >= 0.0 on the integer pipe: +0 up to +inf, or -0 (a NaN compares false)
+__device__ __forceinline__ bool ge_zero(double x) {
+    const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+    return b <= 0x7ff0000000000000ULL || b == 0x8000000000000000ULL;
+}
 
 // the work space's per-column chains amu, zu, amd, zd (n+1 each, indexed by level k = 0..n)
 constexpr int NCHAIN = 4;
@@ -171,7 +176,7 @@ __global__ void __launch_bounds__(GB_TUNE_MAX_CELL) k_convec_matrix(CArgs A) {
         double v = 0.0;
         for (int r = l; r >= 1; --r) {  // fd(r, l), r = k - 1 with k from l + 1 down to 2
             const double z = zd[r + 1];
-            const bool act = z >= 0.0;
+            const bool act = ge_zero(z);
             if (r == l)
                 v = act ? qed * z : 0.0;
             else
@@ -181,7 +186,7 @@ __global__ void __launch_bounds__(GB_TUNE_MAX_CELL) k_convec_matrix(CArgs A) {
         double u = 0.0, fprev = 0.0;
         for (int k = 1; k <= n; ++k) {
             const double z = zu[k];
-            const bool act = z >= 0.0;
+            const bool act = ge_zero(z);
             if (l < k - 1)
                 u = act ? u * z : 0.0;
             else if (l == k - 1)
@@ -255,8 +260,9 @@ __global__ void __launch_bounds__(GB_TUNE_MAX_COLUMN) k_convec_tri(CArgs A) {
     A.fresh[c] = 2;
 }
 
-// shared memory of one warp (doubles): the matrix (conv1, then LU) and L^-1, n*n each
-__host__ __device__ __forceinline__ size_t warp_doubles(int n) { return 2 * (size_t)n * n; }
+// shared memory of one warp (doubles): the matrix (conv1, then LU, then U over L^-1's strict
+// lower triangle), and one step's multipliers (n)
+__host__ __device__ __forceinline__ size_t warp_doubles(int n) { return (size_t)n * n + n; }
 
 __global__ void __launch_bounds__(GB_TUNE_MAX_LU_WARPS * 32) k_convec_lu(CArgs A) {
     extern __shared__ double smem[];
@@ -273,7 +279,7 @@ __global__ void __launch_bounds__(GB_TUNE_MAX_LU_WARPS * 32) k_convec_lu(CArgs A
         if (__all_sync(FULL_MASK, ok)) return;
     }
     double *LU = smem + (size_t)warp * warp_doubles(n);  // n x n
-    double *Y = LU + (size_t)n * n;                       // n x n
+    double *mult = LU + (size_t)n * n;                    // n: step k's multipliers L(r, k)
     double *G = A.abuf + (size_t)c * n * n;
     for (int e = lane; e < n * n; e += 32) LU[e] = G[e];
     __syncwarp();
@@ -299,23 +305,30 @@ __global__ void __launch_bounds__(GB_TUNE_MAX_LU_WARPS * 32) k_convec_lu(CArgs A
         }
         __syncwarp();
     }
-    // ---- forward substitution of the identity: Y = L^-1.  Row k is final once the terms of
-    // rows < k are in; its term then goes to every later row r with L(r, k) != 0 at once, the
-    // (r, column <= k) elements packed onto the lanes -- each element still in k order.
-    for (int e = lane; e < n * n; e += 32) Y[e] = (e / n == e % n) ? 1.0 : 0.0;
-    __syncwarp();
+    // ---- forward substitution of the identity: Y = L^-1, in place of L's strict lower triangle
+    // (Y's diagonal is 1 and its upper triangle +0, U stays where it is).  Row k of Y is final
+    // once the terms of rows < k are in; its term then goes to every later row r with
+    // L(r, k) != 0 at once, Y(r, c) = Y(r, c) - L(r, k) Y(k, c) for the columns c <= k, the
+    // (r, c) elements packed onto the lanes -- each element still in k order.  Step k is the
+    // first to touch column k of Y: its elements start as the identity's +0 (Y(k, k) is the
+    // identity's 1), and L(r, k) is taken into `mult` first, since the step overwrites it.
     for (int k = 0; k < n - 1; ++k) {
         const uint32_t rows0 = __ballot_sync(FULL_MASK, k + 1 + lane < n && !is_zero(LU[(size_t)(k + 1 + lane) * n + k]));
         const uint32_t rows1 = __ballot_sync(FULL_MASK, k + 33 + lane < n && !is_zero(LU[(size_t)(k + 33 + lane) * n + k]));
+        for (int r = k + 1 + lane; r < n; r += 32) {
+            mult[r] = LU[(size_t)r * n + k];
+            LU[(size_t)r * n + k] = 0.0;  // Y(r, k) before its terms: the identity's +0
+        }
+        __syncwarp();
         const int n0 = __popc(rows0), nr = n0 + __popc(rows1);
-        if (nr == 0) continue;
         const int w = k + 1;  // the columns 0..k
         for (int e = lane; e < nr * w; e += 32) {
             const int q = e / w, col = e % w;
             uint32_t b = q < n0 ? rows0 : rows1;  // the q-th row of the set, in order
             for (int s = q < n0 ? q : q - n0; s > 0; --s) b &= b - 1;
             const int r = (q < n0 ? k + 1 : k + 33) + __ffs(b) - 1;
-            Y[(size_t)r * n + col] = Y[(size_t)r * n + col] - LU[(size_t)r * n + k] * Y[(size_t)k * n + col];
+            const double ykc = col == k ? 1.0 : LU[(size_t)k * n + col];  // Y(k, col)
+            LU[(size_t)r * n + col] = LU[(size_t)r * n + col] - mult[r] * ykc;
         }
         __syncwarp();
     }
@@ -324,8 +337,9 @@ __global__ void __launch_bounds__(GB_TUNE_MAX_LU_WARPS * 32) k_convec_lu(CArgs A
     // substitution's terms end there: the rest are zeros it would skip)
     double *X = A.inv + (size_t)c * n * n;
     for (int e = lane; e < n * n; e += 32) {
-        G[e] = LU[e];
-        X[e] = Y[e];
+        const int r = e / n, col = e % n;
+        G[e] = LU[e];  // the back substitution reads U only (the diagonal and right of it)
+        X[e] = r > col ? LU[e] : (r == col ? 1.0 : 0.0);
     }
     int32_t *rend = A.rend + (size_t)c * n;
     for (int r = 0; r < n; ++r) {
