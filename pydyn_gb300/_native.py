@@ -10,7 +10,7 @@ from .build import LIBGBDYN, LIBGBMATH
 
 GB_OK, GB_ECFL, GB_EHALO, GB_ELEVELS, GB_ESEARCH, GB_EARG, GB_ECUDA, GB_ETIMEOUT = 0, 1, 2, 4, 8, 16, 32, 64
 # launch-shape keys of gb_tune_set / gb_tune_get
-TUNE_KEYS = {"column_threads": 0, "cell_threads": 1, "lu_warps": 2, "apply_threads": 3}
+TUNE_KEYS = {"column_threads": 0, "cell_threads": 1, "lu_warps": 2, "apply_threads": 3, "lu_lanes": 4}
 
 
 class GBView(ctypes.Structure):

@@ -84,16 +84,32 @@ __global__ void __launch_bounds__(GB_TUNE_MAX_COLUMN) k_convec_chains(CArgs A) {
     const int n = A.n;
     const int i = A.cols[2 * c], j = A.cols[2 * c + 1];
 
+    // The loops read their inputs B levels at a time into registers before using them, so that a
+    // batch's loads are in flight together (one column a thread: few warps hide little latency).
+    constexpr int B = 8;
     // ---- the kept inverse, when this column's air mass is bitwise the one it was made from
     if (A.cache_m) {
         double *cm = A.cache_m + (size_t)c * n;
         bool same = A.cache_tag[c] == *A.epoch;
-        for (int l = 0; l < n; ++l) same = same && (__double_as_longlong(cm[l]) == __double_as_longlong(AT(A.m, i, j, l)));
+        for (int l0 = 0; l0 < n; l0 += B) {
+            double mb[B], cb[B];
+#pragma unroll
+            for (int u = 0; u < B; ++u)
+                if (l0 + u < n) {
+                    mb[u] = AT(A.m, i, j, l0 + u);
+                    cb[u] = cm[l0 + u];
+                }
+#pragma unroll
+            for (int u = 0; u < B; ++u)
+                if (l0 + u < n) {
+                    same = same && (__double_as_longlong(cb[u]) == __double_as_longlong(mb[u]));
+                    cm[l0 + u] = mb[u];  // unchanged bits where the column's mass is the kept one
+                }
+        }
         if (same) {
             A.fresh[c] = 0;
             return;
         }
-        for (int l = 0; l < n; ++l) cm[l] = AT(A.m, i, j, l);
         A.cache_tag[c] = *A.epoch;
     }
     A.fresh[c] = 1;
@@ -102,29 +118,53 @@ __global__ void __launch_bounds__(GB_TUNE_MAX_COLUMN) k_convec_chains(CArgs A) {
     const int top = A.top[i * A.ts0 + j * A.ts1], lfs = A.lfs[i * A.ts0 + j * A.ts1];
     double mu = 0.0;
     amu[0] = 0.0;
-    for (int k = 1; k <= n; ++k) {
-        const double eu = AT(A.entu, i, j, k - 1), du = AT(A.detu, i, j, k - 1);
-        const bool act = top >= k;
-        const double a = mu + eu - du;
-        const bool up = a > 0.0;
-        const double z = up ? max0(1.0 - du / (mu + eu)) : 0.0;
-        mu = (act && up) ? a : 0.0;
-        amu[k] = mu;
-        zu[k] = act ? z : -1.0;  // -1 marks an inactive level
+    for (int k0 = 1; k0 <= n; k0 += B) {
+        double eb[B], db[B];
+#pragma unroll
+        for (int u = 0; u < B; ++u)
+            if (k0 + u <= n) {
+                eb[u] = AT(A.entu, i, j, k0 + u - 1);
+                db[u] = AT(A.detu, i, j, k0 + u - 1);
+            }
+#pragma unroll
+        for (int u = 0; u < B; ++u) {
+            const int k = k0 + u;
+            if (k > n) break;
+            const double eu = eb[u], du = db[u];
+            const bool act = top >= k;
+            const double a = mu + eu - du;
+            const bool up = a > 0.0;
+            const double z = up ? max0(1.0 - du / (mu + eu)) : 0.0;
+            mu = (act && up) ? a : 0.0;
+            amu[k] = mu;
+            zu[k] = act ? z : -1.0;  // -1 marks an inactive level
+        }
     }
     double md = 0.0;
     amd[n] = 0.0;
     amd[0] = 0.0;
     zd[0] = zd[1] = -1.0;
-    for (int k = n; k >= 2; --k) {
-        const double ed = AT(A.entd, i, j, k - 1), dd = AT(A.detd, i, j, k - 1);
-        const bool act = lfs >= k;
-        const double a = md - ed + dd;
-        const bool dn = a < 0.0;
-        const double z = dn ? max0(1.0 + dd / (md - ed)) : 0.0;
-        md = (act && dn) ? a : 0.0;
-        amd[k - 1] = md;
-        zd[k] = act ? z : -1.0;
+    for (int k0 = n; k0 >= 2; k0 -= B) {
+        double eb[B], db[B];
+#pragma unroll
+        for (int u = 0; u < B; ++u)
+            if (k0 - u >= 2) {
+                eb[u] = AT(A.entd, i, j, k0 - u - 1);
+                db[u] = AT(A.detd, i, j, k0 - u - 1);
+            }
+#pragma unroll
+        for (int u = 0; u < B; ++u) {
+            const int k = k0 - u;
+            if (k < 2) break;
+            const double ed = eb[u], dd = db[u];
+            const bool act = lfs >= k;
+            const double a = md - ed + dd;
+            const bool dn = a < 0.0;
+            const double z = dn ? max0(1.0 + dd / (md - ed)) : 0.0;
+            md = (act && dn) ? a : 0.0;
+            amd[k - 1] = md;
+            zd[k] = act ? z : -1.0;
+        }
     }
 }
 
@@ -243,111 +283,177 @@ __global__ void __launch_bounds__(GB_TUNE_MAX_COLUMN) k_convec_tri(CArgs A) {
     if (c >= A.ncol || A.fresh[c] != 1 || !cloudless(A, c)) return;
     const int n = A.n;
     double *G = A.abuf + (size_t)c * n * n;
-    for (int r = 0; r < n; ++r)
-        if (!band_row_ok(G, n, r)) return;
     int32_t *rend = A.rend + (size_t)c * n;
     double *ud = A.tband + (size_t)c * 2 * n, *lb = ud + n;
+    // The bands are tested as the recurrence reads them (band_row_ok of every row): the band
+    // buffer is this kernel's alone, so what it writes for a column that fails the test is never
+    // read (fresh stays 1 and k_convec_lu makes that column); rend and fresh are written after.
     double uprev = G[0];  // U(r-1, r-1)
+    bool ok = band_ok(uprev);
     ud[0] = uprev;
-    for (int r = 1; r < n; ++r) {
-        const double l = G[(size_t)r * n + r - 1] / uprev;
-        const double u = G[(size_t)r * n + r] - l * G[(size_t)(r - 1) * n + r];
-        ud[r] = u;
-        lb[r] = l;  // L(r, r-1): k_convec_apply builds L^-1 from it
-        uprev = u;
+    constexpr int B = 8;  // rows whose bands are read into registers at once (loads in flight together)
+    for (int r0 = 1; r0 < n; r0 += B) {
+        double sub[B], dia[B], sup[B];
+#pragma unroll
+        for (int u = 0; u < B; ++u)
+            if (r0 + u < n) {
+                const int r = r0 + u;
+                sub[u] = G[(size_t)r * n + r - 1];
+                dia[u] = G[(size_t)r * n + r];
+                sup[u] = G[(size_t)(r - 1) * n + r];
+            }
+#pragma unroll
+        for (int u = 0; u < B; ++u) {
+            const int r = r0 + u;
+            if (r >= n) break;
+            ok = ok && band_ok(sub[u]) && band_ok(dia[u]) && band_ok(sup[u]);
+            const double l = sub[u] / uprev;
+            const double v = dia[u] - l * sup[u];
+            ud[r] = v;
+            lb[r] = l;  // L(r, r-1): k_convec_apply builds L^-1 from it
+            uprev = v;
+        }
     }
+    if (!ok) return;
     for (int r = 0; r < n; ++r) rend[r] = r + 1 < n ? r + 2 : r + 1;
     A.fresh[c] = 2;
 }
 
-// shared memory of one warp (doubles): the matrix (conv1, then LU, then U over L^-1's strict
-// lower triangle), and one step's multipliers (n)
-__host__ __device__ __forceinline__ size_t warp_doubles(int n) { return (size_t)n * n + n; }
+// shared memory of one column of the LU (doubles): the matrix (conv1, then LU, then U over L^-1's
+// strict lower triangle), one step's multipliers (n), and one step's list of the columns (or
+// rows) it updates (NMAX int32)
+__host__ __device__ __forceinline__ size_t warp_doubles(int n) { return (size_t)n * n + n + NMAX / 2; }
 
+// e / d for 0 <= e < 2^16 and 1 <= d <= NMAX: the high word of e * (floor((2^32 - 1) / d) + 1),
+// exact in that range (the multiplier exceeds 2^32 / d by less than 1, which moves e / d by
+// less than 2^-16, below the 1 / d that separates it from the next integer)
+__device__ __forceinline__ unsigned div_magic(int d) { return d > 1 ? 0xffffffffu / (unsigned)d + 1u : 0u; }
+__device__ __forceinline__ int div_by(int e, int d, unsigned magic) {
+    return d > 1 ? (int)__umulhi((unsigned)e, magic) : e;
+}
+
+// G lanes per column (32 / G columns a warp): every step's divisions and ballots serve the warp's
+// columns at once.  Lanes of a group whose column is not made here (reused, k_convec_tri's, or past
+// the list) take part in the warp's ballots with false predicates and do nothing else.
+template <int G>
 __global__ void __launch_bounds__(GB_TUNE_MAX_LU_WARPS * 32) k_convec_lu(CArgs A) {
     extern __shared__ double smem[];
+    constexpr int MPW = 32 / G, NCH = NMAX / G;
+    constexpr unsigned GMASK = G == 32 ? 0xffffffffu : ((1u << (G % 32)) - 1u);
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int c = blockIdx.x * (blockDim.x >> 5) + warp;
-    // made in this call (k_convec_tri, beside this kernel, turns its columns' 1 into 2: the test
-    // reads 0 or not, which that write does not change)
-    if (c >= A.ncol || A.fresh[c] == 0) return;
+    const int h = lane / G, gl = lane % G;  // the group (column) in the warp, the lane in the group
+    const int c = (blockIdx.x * (blockDim.x >> 5) + warp) * MPW + h;
     const int n = A.n;
-    if (cloudless(A, c)) {  // k_convec_tri's column unless a band entry is zero or not finite
+    // made in this call (k_convec_tri, beside this kernel, turns its columns' 1 into 2: the test
+    // reads 0 or not, which that write does not change), and not k_convec_tri's: a cloudless
+    // column is its unless a band entry is zero or not finite
+    bool mine = c < A.ncol && A.fresh[c] != 0;
+    const bool cand = mine && cloudless(A, c);
+    bool ok = true;
+    if (cand) {
         const double *G0 = A.abuf + (size_t)c * n * n;
-        bool ok = true;
-        for (int r = lane; r < n; r += 32) ok = ok && band_row_ok(G0, n, r);
-        if (__all_sync(FULL_MASK, ok)) return;
+        for (int r = gl; r < n; r += G) ok = ok && band_row_ok(G0, n, r);
     }
-    double *LU = smem + (size_t)warp * warp_doubles(n);  // n x n
-    double *mult = LU + (size_t)n * n;                    // n: step k's multipliers L(r, k)
-    double *G = A.abuf + (size_t)c * n * n;
-    for (int e = lane; e < n * n; e += 32) LU[e] = G[e];
+    const unsigned bad = (__ballot_sync(FULL_MASK, cand && !ok) >> (h * G)) & GMASK;
+    mine = mine && !(cand && bad == 0);
+    if (__ballot_sync(FULL_MASK, mine) == 0) return;  // the whole warp
+    double *LU = smem + ((size_t)warp * MPW + h) * warp_doubles(n);  // n x n
+    double *mult = LU + (size_t)n * n;                                 // n: step k's multipliers L(r, k)
+    int32_t *list = reinterpret_cast<int32_t *>(mult + n);             // NMAX: a step's columns or rows
+    double *Gm = A.abuf + (size_t)c * n * n;
+    if (mine)
+        for (int e = gl; e < n * n; e += G) LU[e] = Gm[e];
     __syncwarp();
     // ---- LU, right-looking: at step k, L's column k (its rows below k divided by U(k, k), final
     // after the steps before k), then every later element (r, c) receives its term k,
-    // A(r, c) - L(r, k) U(k, c) -- the (row, column) elements packed onto the lanes.  Each element
-    // receives its terms in k order, each skipped exactly where Crout's column-by-column form
-    // skips it (the multiplier U(k, c) a zero: above a column's first non-zero such zeros stay
-    // zero), and L's column is divided after all its terms: the same operations on every
+    // A(r, c) - L(r, k) U(k, c) -- the (row, column) elements packed onto the group's lanes.  Each
+    // element receives its terms in k order, each skipped exactly where Crout's column-by-column
+    // form skips it (the multiplier U(k, c) a zero: above a column's first non-zero such zeros
+    // stay zero), and L's column is divided after all its terms: the same operations on every
     // element, the same bits.
     for (int k = 0; k < n; ++k) {
-        const double d = LU[(size_t)k * n + k];
-        for (int r = k + 1 + lane; r < n; r += 32) LU[(size_t)r * n + k] = LU[(size_t)r * n + k] / d;
-        const uint32_t m0 = __ballot_sync(FULL_MASK, lane > k && lane < n && !is_zero(LU[(size_t)k * n + lane]));
-        const uint32_t m1 =
-            __ballot_sync(FULL_MASK, lane + 32 > k && lane + 32 < n && !is_zero(LU[(size_t)k * n + lane + 32]));
-        __syncwarp();
-        const int nrow = n - k - 1, n0 = __popc(m0), ncols = n0 + __popc(m1);
-        for (int e = lane; e < nrow * ncols; e += 32) {
-            const int q = e / nrow, r = k + 1 + e % nrow;
-            const int c = q < n0 ? (int)__fns(m0, 0, q + 1) : 32 + (int)__fns(m1, 0, q - n0 + 1);
-            LU[(size_t)r * n + c] = LU[(size_t)r * n + c] - LU[(size_t)r * n + k] * LU[(size_t)k * n + c];
+        if (mine) {
+            const double d = LU[(size_t)k * n + k];
+            for (int r = k + 1 + gl; r < n; r += G) LU[(size_t)r * n + k] = LU[(size_t)r * n + k] / d;
         }
+        // row k's non-zeros right of the diagonal, listed in order: the columns step k updates
+        int ncols = 0;
+#pragma unroll
+        for (int s = 0; s < NCH; ++s) {
+            const int col = s * G + gl;
+            const bool p = mine && col > k && col < n && !is_zero(LU[(size_t)k * n + col]);
+            const unsigned b = (__ballot_sync(FULL_MASK, p) >> (h * G)) & GMASK;
+            if (p) list[ncols + __popc(b & ((1u << gl) - 1u))] = col;
+            ncols += __popc(b);
+        }
+        __syncwarp();
+        const int nrow = n - k - 1;
+        const unsigned magic = div_magic(nrow);
+        if (mine)
+            for (int e = gl; e < nrow * ncols; e += G) {
+                const int q = div_by(e, nrow, magic), r = k + 1 + (e - q * nrow);
+                const int col = list[q];
+                LU[(size_t)r * n + col] = LU[(size_t)r * n + col] - LU[(size_t)r * n + k] * LU[(size_t)k * n + col];
+            }
         __syncwarp();
     }
     // ---- forward substitution of the identity: Y = L^-1, in place of L's strict lower triangle
     // (Y's diagonal is 1 and its upper triangle +0, U stays where it is).  Row k of Y is final
     // once the terms of rows < k are in; its term then goes to every later row r with
     // L(r, k) != 0 at once, Y(r, c) = Y(r, c) - L(r, k) Y(k, c) for the columns c <= k, the
-    // (r, c) elements packed onto the lanes -- each element still in k order.  Step k is the
-    // first to touch column k of Y: its elements start as the identity's +0 (Y(k, k) is the
+    // (r, c) elements packed onto the group's lanes -- each element still in k order.  Step k is
+    // the first to touch column k of Y: its elements start as the identity's +0 (Y(k, k) is the
     // identity's 1), and L(r, k) is taken into `mult` first, since the step overwrites it.
     for (int k = 0; k < n - 1; ++k) {
-        const uint32_t rows0 = __ballot_sync(FULL_MASK, k + 1 + lane < n && !is_zero(LU[(size_t)(k + 1 + lane) * n + k]));
-        const uint32_t rows1 = __ballot_sync(FULL_MASK, k + 33 + lane < n && !is_zero(LU[(size_t)(k + 33 + lane) * n + k]));
-        for (int r = k + 1 + lane; r < n; r += 32) {
-            mult[r] = LU[(size_t)r * n + k];
-            LU[(size_t)r * n + k] = 0.0;  // Y(r, k) before its terms: the identity's +0
+        // the rows below k with L(r, k) != 0, listed in order
+        int nr = 0;
+#pragma unroll
+        for (int s = 0; s < NCH; ++s) {
+            const int r = k + 1 + s * G + gl;
+            const bool p = mine && r < n && !is_zero(LU[(size_t)r * n + k]);
+            const unsigned b = (__ballot_sync(FULL_MASK, p) >> (h * G)) & GMASK;
+            if (p) list[nr + __popc(b & ((1u << gl) - 1u))] = r;
+            nr += __popc(b);
         }
+        if (mine)
+            for (int r = k + 1 + gl; r < n; r += G) {  // the lane that tested row r above
+                mult[r] = LU[(size_t)r * n + k];
+                LU[(size_t)r * n + k] = 0.0;  // Y(r, k) before its terms: the identity's +0
+            }
         __syncwarp();
-        const int n0 = __popc(rows0), nr = n0 + __popc(rows1);
         const int w = k + 1;  // the columns 0..k
-        for (int e = lane; e < nr * w; e += 32) {
-            const int q = e / w, col = e % w;
-            uint32_t b = q < n0 ? rows0 : rows1;  // the q-th row of the set, in order
-            for (int s = q < n0 ? q : q - n0; s > 0; --s) b &= b - 1;
-            const int r = (q < n0 ? k + 1 : k + 33) + __ffs(b) - 1;
-            const double ykc = col == k ? 1.0 : LU[(size_t)k * n + col];  // Y(k, col)
-            LU[(size_t)r * n + col] = LU[(size_t)r * n + col] - mult[r] * ykc;
-        }
+        const unsigned magic = div_magic(w);
+        if (mine)
+            for (int e = gl; e < nr * w; e += G) {
+                const int q = div_by(e, w, magic), col = e - q * w;
+                const int r = list[q];
+                const double ykc = col == k ? 1.0 : LU[(size_t)k * n + col];  // Y(k, col)
+                LU[(size_t)r * n + col] = LU[(size_t)r * n + col] - mult[r] * ykc;
+            }
         __syncwarp();
     }
     // ---- out: U (the upper triangle with the diagonal) over conv1, L^-1 into the inverse's place,
     // and for each row r of U one past its last non-zero right of the diagonal (the back
     // substitution's terms end there: the rest are zeros it would skip)
-    double *X = A.inv + (size_t)c * n * n;
-    for (int e = lane; e < n * n; e += 32) {
-        const int r = e / n, col = e % n;
-        G[e] = LU[e];  // the back substitution reads U only (the diagonal and right of it)
-        X[e] = r > col ? LU[e] : (r == col ? 1.0 : 0.0);
+    if (mine) {
+        double *X = A.inv + (size_t)c * n * n;
+        for (int e = gl; e < n * n; e += G) {
+            const int r = e / n, col = e % n;
+            Gm[e] = LU[e];  // the back substitution reads U only (the diagonal and right of it)
+            X[e] = r > col ? LU[e] : (r == col ? 1.0 : 0.0);
+        }
     }
     int32_t *rend = A.rend + (size_t)c * n;
-    for (int r = 0; r < n; ++r) {
-        const uint32_t b0 = __ballot_sync(FULL_MASK, lane > r && lane < n && !is_zero(LU[(size_t)r * n + lane]));
-        const uint32_t b1 =
-            __ballot_sync(FULL_MASK, lane + 32 > r && lane + 32 < n && !is_zero(LU[(size_t)r * n + lane + 32]));
-        const int last = b1 ? 63 - __clz(b1) : (b0 ? 31 - __clz(b0) : r);
-        if (lane == 0) rend[r] = last + 1;
+    for (int r = 0; r < n; ++r) {  // (the lists are done with: their last readers passed a __syncwarp)
+        int last = r;
+#pragma unroll
+        for (int s = 0; s < NCH; ++s) {
+            const int col = s * G + gl;
+            const bool p = mine && col > r && col < n && !is_zero(LU[(size_t)r * n + col]);
+            const unsigned b = (__ballot_sync(FULL_MASK, p) >> (h * G)) & GMASK;
+            if (b) last = s * G + 31 - __clz(b);
+        }
+        if (mine && gl == 0) rend[r] = last + 1;
     }
 }
 
@@ -407,6 +513,25 @@ __global__ void k_convec_apply(CArgs A) {
 
 int gcd(int a, int b) { return b == 0 ? a : gcd(b, a % b); }
 
+template <int G>
+int launch_lu_g(gb_ctx *ctx, const CArgs &A) {
+    constexpr int MPW = 32 / G;
+    int warps = ctx->tune[GB_TUNE_LU_WARPS];
+    while (warps > 1 && (size_t)warps * MPW * warp_doubles(A.n) * sizeof(double) > 227 * 1024) warps /= 2;
+    const size_t smem = (size_t)warps * MPW * warp_doubles(A.n) * sizeof(double);
+    GB_CHECK_CUDA(cudaFuncSetAttribute(k_convec_lu<G>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    k_convec_lu<G><<<gb_blocks(A.ncol, warps * MPW), warps * 32, smem, ctx->stream>>>(A);
+    return gb_after_launch(ctx, "convec_lu");
+}
+
+int launch_lu(gb_ctx *ctx, const CArgs &A, int lanes) {
+    switch (lanes) {
+        case 8: return launch_lu_g<8>(ctx, A);
+        case 16: return launch_lu_g<16>(ctx, A);
+        default: return launch_lu_g<32>(ctx, A);
+    }
+}
+
 }  // namespace
 
 extern "C" int gb_convec(gb_ctx *ctx, const gb_view *m, const gb_view *rm, const gb_view *rxm, const gb_view *rym,
@@ -457,13 +582,9 @@ extern "C" int gb_convec(gb_ctx *ctx, const gb_view *m, const gb_view *rm, const
     GB_CHECK_CUDA(cudaStreamWaitEvent(ctx->side, ctx->fork, 0));
     k_convec_tri<<<gb_blocks(ncol, tcol), tcol, 0, ctx->side>>>(A);
     if (int rc = gb_after_launch(ctx, "convec_tri")) return rc;
-    // warps (columns) per LU block: the tuned count, fewer where their shared memory would not fit
-    int warps = ctx->tune[GB_TUNE_LU_WARPS];
-    while (warps > 1 && (size_t)warps * warp_doubles(lmax) * sizeof(double) > 227 * 1024) warps /= 2;
-    const size_t smem = (size_t)warps * warp_doubles(lmax) * sizeof(double);
-    GB_CHECK_CUDA(cudaFuncSetAttribute(k_convec_lu, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    k_convec_lu<<<gb_blocks(ncol, warps), warps * 32, smem, ctx->stream>>>(A);
-    if (int rc = gb_after_launch(ctx, "convec_lu")) return rc;
+    // warps per LU block and lanes per column: the tuned counts, fewer warps where their shared
+    // memory would not fit
+    if (int rc = launch_lu(ctx, A, ctx->tune[GB_TUNE_LU_LANES])) return rc;
     GB_CHECK_CUDA(cudaEventRecord(ctx->join, ctx->side));
     GB_CHECK_CUDA(cudaStreamWaitEvent(ctx->stream, ctx->join, 0));
     // whole columns per block, as many as make the block a whole number of warps (<= 1024

@@ -1,7 +1,8 @@
 """The autotuner: launch shapes per member class, and the ensemble's width.
 
 Shapes (pydyn_gb300.device.Device.tune: threads per block of the thread-per-column and
-thread-per-cell kernels, warps per block of the convection LU, the convection apply's block)
+thread-per-cell kernels, warps per block and lanes per column of the convection LU, the
+convection apply's block)
 are chosen by coordinate descent from the library's defaults: for each shape in turn, every
 candidate is set, the class's interval graph is captured again, replayed a few times and timed
 with CUDA events on the run's stream; the fastest candidate stays.  The width of an ensemble is
@@ -22,6 +23,7 @@ SPACE = {
     "cell_threads": (64, 128, 256, 512),
     "lu_warps": (1, 2, 4),
     "apply_threads": (64, 128, 256, 512),
+    "lu_lanes": (8, 16, 32),
 }
 WIDTHS = (4, 8, 16, 32, 64, 128, 256)
 CACHE = Path(os.environ.get("PYDYN_GB300_TUNE_CACHE", Path(__file__).resolve().parent / "_build" / "tune.json"))

@@ -100,8 +100,8 @@ def test_launch_shapes_keep_the_bits(built, name):
 
     spec = _golden_spec(0, name)
     run = GOLDEN[name]
-    for shapes in ({"column_threads": 32, "cell_threads": 512, "lu_warps": 1, "apply_threads": 512},
-                   {"column_threads": 256, "cell_threads": 64, "lu_warps": 4, "apply_threads": 64}):  # fmt: skip
+    for shapes in ({"column_threads": 32, "cell_threads": 512, "lu_warps": 1, "apply_threads": 512, "lu_lanes": 8},
+                   {"column_threads": 256, "cell_threads": 64, "lu_warps": 4, "apply_threads": 64, "lu_lanes": 32}):  # fmt: skip
         dev = Device(0)
         dev.tune(**shapes)
         assert dev.tuning() == shapes
@@ -118,7 +118,8 @@ def test_tune_set_rejects_bad_shapes(dev):
     from pydyn_gb300._native import DeviceError
 
     before = dev.tuning()
-    for bad in ({"column_threads": 48}, {"cell_threads": 1024}, {"lu_warps": 8}, {"apply_threads": 2048}):
+    for bad in ({"column_threads": 48}, {"cell_threads": 1024}, {"lu_warps": 8}, {"apply_threads": 2048},
+                {"lu_lanes": 12}):
         with pytest.raises((DeviceError, ValueError)):
             dev.tune(**bad)
     assert dev.tuning() == before

@@ -70,9 +70,11 @@ def _convection(rng, m, lmax, dt, frac=0.4):
 
 @pytest.mark.gpu
 @pytest.mark.parametrize(("shape", "lmax"), [((120, 90, 34, 1), 34), ((90, 70, 34, 1), 26), ((40, 30, 60, 2), 60)])
-def test_convec_matches_oracle_at_size(dev, shape, lmax):
+@pytest.mark.parametrize("lu_lanes", [8, 16, 32])
+def test_convec_matches_oracle_at_size(dev, shape, lmax, lu_lanes):
     """Convection on every column, then again on the same air mass: the second call reuses the
-    kept inverses, and both equal the oracle's two applications bitwise."""
+    kept inverses, and both equal the oracle's two applications bitwise, for every width of
+    the LU's lane groups."""
     from oracle import kernels as O
 
     from pydyn_gb300 import kernels as K
@@ -91,11 +93,16 @@ def test_convec_matches_oracle_at_size(dev, shape, lmax):
     cols = DevArray.from_host(dev, np.array([(i, j) for i in range(im) for j in range(jm)], dtype=np.int32))
     cache = (DevArray.zeros(dev, (0, ncol * lmax * lmax - 1)), DevArray.zeros(dev, (0, ncol * lmax - 1)),
              DevArray.zeros(dev, (0, ncol - 1), dtype=np.int32), DevArray.from_host(dev, np.array([7], np.int32)))
-    before = dev.launches()
-    for _ in range(2):
-        K.convec(d["m"], *(d[q] for q in TRACERS), d["entu"], d["detu"], d["entd"], d["detd"], d["dkg"],
-                 d["cloud_top"], d["cloud_lfs"], cols, 1800.0, lmax, cache=cache)  # fmt: skip
-    dev.sync()
+    saved = dev.tuning()["lu_lanes"]
+    dev.tune(lu_lanes=lu_lanes)
+    try:
+        before = dev.launches()
+        for _ in range(2):
+            K.convec(d["m"], *(d[q] for q in TRACERS), d["entu"], d["detu"], d["entd"], d["detd"], d["dkg"],
+                     d["cloud_top"], d["cloud_lfs"], cols, 1800.0, lmax, cache=cache)  # fmt: skip
+        dev.sync()
+    finally:
+        dev.tune(lu_lanes=saved)
     assert dev.launches() - before == 10  # two calls of five launches
     tags = cache[2].host()
     assert (tags == 7).all()
