@@ -3,20 +3,20 @@
 //
 // Five launches, shaped so that the FP64 pipe -- this GPU's scarcest unit -- issues with its
 // lanes full:
-//   k_convec_chains  one thread per owned column: whether its kept inverse still holds, and the
-//                    updraft and downdraft chains
+//   k_convec_chains  three threads per owned column: whether its kept inverse still holds, the
+//                    updraft chains, the downdraft chains
 //   k_convec_matrix  one thread per (column, column l of its matrix): the quotients that column
 //                    uses (each division once), conv1(., l) = I - dt (f(k-1, l) - f(k, l)), the
 //                    downdraft chain of f down from the diagonal and the updraft chain up from
 //                    it -- into a work space
 //   k_convec_tri     one thread per cloudless column (tridiagonal conv1): the same LU and L^-1
 //                    by the recurrence their non-zero elements follow
-//   k_convec_lu      one warp per other column whose inverse is made (beside k_convec_tri, on the
-//                    context's side stream): LU right-looking (each
-//                    step's trailing (row, column) elements packed onto the lanes), then L^-1 by forward
-//                    substitution (row k's terms applied to every later row at once, the
-//                    (row, column) elements packed onto the lanes).  U goes to the work space,
-//                    L^-1 to the inverse's place.
+//   k_convec_lu      a group of 8, 16 or 32 lanes per other column whose inverse is made
+//                    (beside k_convec_tri, on the context's side stream): LU right-looking
+//                    (each step's trailing (row, column) elements packed onto the lanes), then
+//                    L^-1 by forward substitution in place of L (row k's terms applied to every
+//                    later row at once, the (row, column) elements packed onto the lanes).  U
+//                    goes to the work space, L^-1 to the inverse's place.
 //   k_convec_apply   one thread per (column, column of the inverse): the back substitution
 //                    U X = L^-1; then, whole columns per block, one thread per (column, level):
 //                    the slopes times the inverse's diagonal and rm = C rm accumulated in k.
@@ -77,30 +77,26 @@ __device__ __forceinline__ bool ge_zero(double x) {
 constexpr int NCHAIN = 4;
 __device__ __forceinline__ double *chains(const CArgs &A, int c) { return A.chain + (size_t)c * NCHAIN * (A.n + 1); }
 
-// thread per column: whether the kept inverse still holds; the updraft and downdraft chains
-__global__ void __launch_bounds__(GB_TUNE_MAX_COLUMN) k_convec_chains(CArgs A) {
-    const int c = blockIdx.x * blockDim.x + threadIdx.x;
-    if (c >= A.ncol) return;
-    const int n = A.n;
-    const int i = A.cols[2 * c], j = A.cols[2 * c + 1];
+// The chain loops read their inputs CB levels at a time into registers before using them, so
+// that a batch's loads are in flight together (one column a thread: few warps hide little latency).
+constexpr int CB = 12;
 
-    // The loops read their inputs B levels at a time into registers before using them, so that a
-    // batch's loads are in flight together (one column a thread: few warps hide little latency).
-    constexpr int B = 8;
-    // ---- the kept inverse, when this column's air mass is bitwise the one it was made from
+// whether column c's kept inverse still holds: its air mass bitwise the one it was made from
+__device__ void chain_cache(const CArgs &A, int c, int i, int j) {
+    const int n = A.n;
     if (A.cache_m) {
         double *cm = A.cache_m + (size_t)c * n;
         bool same = A.cache_tag[c] == *A.epoch;
-        for (int l0 = 0; l0 < n; l0 += B) {
-            double mb[B], cb[B];
+        for (int l0 = 0; l0 < n; l0 += CB) {
+            double mb[CB], cb[CB];
 #pragma unroll
-            for (int u = 0; u < B; ++u)
+            for (int u = 0; u < CB; ++u)
                 if (l0 + u < n) {
                     mb[u] = AT(A.m, i, j, l0 + u);
                     cb[u] = cm[l0 + u];
                 }
 #pragma unroll
-            for (int u = 0; u < B; ++u)
+            for (int u = 0; u < CB; ++u)
                 if (l0 + u < n) {
                     same = same && (__double_as_longlong(cb[u]) == __double_as_longlong(mb[u]));
                     cm[l0 + u] = mb[u];  // unchanged bits where the column's mass is the kept one
@@ -113,21 +109,25 @@ __global__ void __launch_bounds__(GB_TUNE_MAX_COLUMN) k_convec_chains(CArgs A) {
         A.cache_tag[c] = *A.epoch;
     }
     A.fresh[c] = 1;
+}
 
-    double *amu = chains(A, c), *zu = amu + (n + 1), *amd = zu + (n + 1), *zd = amd + (n + 1);
-    const int top = A.top[i * A.ts0 + j * A.ts1], lfs = A.lfs[i * A.ts0 + j * A.ts1];
+// the updraft chains amu, zu of column c (levels 1..n from the bottom)
+__device__ void chain_up(const CArgs &A, int c, int i, int j) {
+    const int n = A.n;
+    double *amu = chains(A, c), *zu = amu + (n + 1);
+    const int top = A.top[i * A.ts0 + j * A.ts1];
     double mu = 0.0;
     amu[0] = 0.0;
-    for (int k0 = 1; k0 <= n; k0 += B) {
-        double eb[B], db[B];
+    for (int k0 = 1; k0 <= n; k0 += CB) {
+        double eb[CB], db[CB];
 #pragma unroll
-        for (int u = 0; u < B; ++u)
+        for (int u = 0; u < CB; ++u)
             if (k0 + u <= n) {
                 eb[u] = AT(A.entu, i, j, k0 + u - 1);
                 db[u] = AT(A.detu, i, j, k0 + u - 1);
             }
 #pragma unroll
-        for (int u = 0; u < B; ++u) {
+        for (int u = 0; u < CB; ++u) {
             const int k = k0 + u;
             if (k > n) break;
             const double eu = eb[u], du = db[u];
@@ -140,20 +140,27 @@ __global__ void __launch_bounds__(GB_TUNE_MAX_COLUMN) k_convec_chains(CArgs A) {
             zu[k] = act ? z : -1.0;  // -1 marks an inactive level
         }
     }
+}
+
+// the downdraft chains amd, zd of column c (levels n down to 2)
+__device__ void chain_down(const CArgs &A, int c, int i, int j) {
+    const int n = A.n;
+    double *amd = chains(A, c) + 2 * (n + 1), *zd = amd + (n + 1);
+    const int lfs = A.lfs[i * A.ts0 + j * A.ts1];
     double md = 0.0;
     amd[n] = 0.0;
     amd[0] = 0.0;
     zd[0] = zd[1] = -1.0;
-    for (int k0 = n; k0 >= 2; k0 -= B) {
-        double eb[B], db[B];
+    for (int k0 = n; k0 >= 2; k0 -= CB) {
+        double eb[CB], db[CB];
 #pragma unroll
-        for (int u = 0; u < B; ++u)
+        for (int u = 0; u < CB; ++u)
             if (k0 - u >= 2) {
                 eb[u] = AT(A.entd, i, j, k0 - u - 1);
                 db[u] = AT(A.detd, i, j, k0 - u - 1);
             }
 #pragma unroll
-        for (int u = 0; u < B; ++u) {
+        for (int u = 0; u < CB; ++u) {
             const int k = k0 - u;
             if (k < 2) break;
             const double ed = eb[u], dd = db[u];
@@ -166,6 +173,22 @@ __global__ void __launch_bounds__(GB_TUNE_MAX_COLUMN) k_convec_chains(CArgs A) {
             zd[k] = act ? z : -1.0;
         }
     }
+}
+
+// three threads per column, one part each (threadIdx.y, a warp's threads all take the same):
+// 0 whether the kept inverse still holds, 1 the updraft chains, 2 the downdraft chains.  The
+// chains are made whether or not the inverse is kept (k_convec_matrix reads them only for the
+// columns made fresh), so the three parts run side by side.
+__global__ void __launch_bounds__(3 * GB_TUNE_MAX_COLUMN) k_convec_chains(CArgs A) {
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= A.ncol) return;
+    const int i = A.cols[2 * c], j = A.cols[2 * c + 1];
+    if (threadIdx.y == 0)
+        chain_cache(A, c, i, j);
+    else if (threadIdx.y == 1)
+        chain_up(A, c, i, j);
+    else
+        chain_down(A, c, i, j);
 }
 
 // thread per (column, column l of its matrix): conv1(., l).  f(k, l), k = 0..n: the downdraft
@@ -572,7 +595,7 @@ extern "C" int gb_convec(gb_ctx *ctx, const gb_view *m, const gb_view *rm, const
     A.cache_tag = cache_tag;
     A.epoch = epoch;
     const int tcol = ctx->tune[GB_TUNE_COLUMN_THREADS], tcell = ctx->tune[GB_TUNE_CELL_THREADS];
-    k_convec_chains<<<gb_blocks(ncol, tcol), tcol, 0, ctx->stream>>>(A);
+    k_convec_chains<<<gb_blocks(ncol, tcol), dim3(tcol, 3), 0, ctx->stream>>>(A);
     if (int rc = gb_after_launch(ctx, "convec_chains")) return rc;
     k_convec_matrix<<<gb_blocks((int64_t)ncol * lmax, tcell), tcell, 0, ctx->stream>>>(A);
     if (int rc = gb_after_launch(ctx, "convec_matrix")) return rc;

@@ -12,33 +12,66 @@ __device__ __forceinline__ double &AT(const DV &v, int64_t i, int64_t j, int64_t
     return v.p[i * v.s0 + j * v.s1 + l * v.s2];
 }
 
+// The column loops read their inputs B levels at a time into registers before using them, so
+// that a batch's loads are in flight together (a thread per column: few warps hide little latency).
+constexpr int B = 8;
+
+// the convergence of cell (i, j, l): pu(i-1) - pu(i) + pv(j) - pv(j+1), left to right
+__device__ __forceinline__ double convergence(const DV &pu, const DV &pv, int i, int j, int l) {
+    return ((AT(pu, i, j, l) - AT(pu, i + 1, j, l)) + AT(pv, i, j, l)) - AT(pv, i, j + 1, l);
+}
+
 // One thread per (i, j) of the face grid [0, im] x [0, jm]: its am column (j < jm), its bm
 // column (i < im) and, for a cell column, cm from the convergence distributed by the hybrid b.
 __global__ void k_fluxes(DV pu, DV pv, const double *bt, double dt, DV am, DV bm, DV cm, int im, int jm, int lm) {
     int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (k >= (int64_t)(im + 1) * (jm + 1)) return;
     const int i = (int)(k / (jm + 1)), j = (int)(k % (jm + 1));
-    if (j < jm)
-        for (int l = 0; l < lm; ++l) AT(am, i, j, l) = dt * AT(pu, i, j, l);
-    if (i < im)
-        for (int l = 0; l < lm; ++l) AT(bm, i, j, l) = dt * AT(pv, i, j, l);
+    for (int l0 = 0; l0 < lm; l0 += B) {
+        double a[B], b[B];
+#pragma unroll
+        for (int u = 0; u < B; ++u)
+            if (l0 + u < lm) {
+                if (j < jm) a[u] = AT(pu, i, j, l0 + u);
+                if (i < im) b[u] = AT(pv, i, j, l0 + u);
+            }
+#pragma unroll
+        for (int u = 0; u < B; ++u)
+            if (l0 + u < lm) {
+                if (j < jm) AT(am, i, j, l0 + u) = dt * a[u];
+                if (i < im) AT(bm, i, j, l0 + u) = dt * b[u];
+            }
+    }
     if (i < im && j < jm) {
-        // conv = pu(i-1) - pu(i) + pv(j) - pv(j+1); pit = its column sum, bottom-up
+        // pit = the column sum of the convergence, bottom-up
         double pit = 0.0;
-        for (int l = 0; l < lm; ++l) {
-            double c = ((AT(pu, i, j, l) - AT(pu, i + 1, j, l)) + AT(pv, i, j, l)) - AT(pv, i, j + 1, l);
-            pit = (l == 0) ? c : pit + c;
+        for (int l0 = 0; l0 < lm; l0 += B) {
+            double c[B];
+#pragma unroll
+            for (int u = 0; u < B; ++u)
+                if (l0 + u < lm) c[u] = convergence(pu, pv, i, j, l0 + u);
+#pragma unroll
+            for (int u = 0; u < B; ++u)
+                if (l0 + u < lm) pit = (l0 + u == 0) ? c[u] : pit + c[u];
         }
         // sd(l) from the top down; cm = -dt sd on the interior interfaces
         double sd = 0.0;
         AT(cm, i, j, lm) = 0.0;
-        for (int l = lm - 1; l >= 1; --l) {
-            double c = ((AT(pu, i, j, l) - AT(pu, i + 1, j, l)) + AT(pv, i, j, l)) - AT(pv, i, j + 1, l);
-            if (l == lm - 1)
-                sd = c - (bt[lm - 1] - bt[lm]) * pit;
-            else
-                sd = (sd + c) - (bt[l] - bt[l + 1]) * pit;
-            AT(cm, i, j, l) = (-dt) * sd;
+        for (int l0 = lm - 1; l0 >= 1; l0 -= B) {
+            double c[B];
+#pragma unroll
+            for (int u = 0; u < B; ++u)
+                if (l0 - u >= 1) c[u] = convergence(pu, pv, i, j, l0 - u);
+#pragma unroll
+            for (int u = 0; u < B; ++u) {
+                const int l = l0 - u;
+                if (l < 1) break;
+                if (l == lm - 1)
+                    sd = c[u] - (bt[lm - 1] - bt[lm]) * pit;
+                else
+                    sd = (sd + c[u]) - (bt[l] - bt[l + 1]) * pit;
+                AT(cm, i, j, l) = (-dt) * sd;
+            }
         }
         AT(cm, i, j, 0) = 0.0;
     }

@@ -130,7 +130,7 @@ def test_tuner_picks_shapes_from_the_space(built, tmp_path):
     from pydyn_gb300.tune import tune_classes
 
     specs = member_specs((("two", 1),), seed=3, classes={"two": ("two", 8, 8, 21)})
-    space = {"lu_warps": (1, 2), "cell_threads": (64, 128)}
+    space = {"lu_warps": (1, 2), "cell_threads": (64, 128)}  # each holding the library's default
     out = tune_classes(specs, cache_path=tmp_path / "t.json", replays=2, space=space)
     shapes, ms = out["two"]
     assert shapes["lu_warps"] in (1, 2) and shapes["cell_threads"] in (64, 128)
