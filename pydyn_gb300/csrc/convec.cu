@@ -236,35 +236,30 @@ __global__ void __launch_bounds__(GB_TUNE_MAX_CELL) k_convec_matrix(CArgs A) {
     }
     double fd[NMAX];
     {
+        // Each statement below is one instruction for every lane of the warp (a lane's l selects its
+        // operands, not its branch): the FP64 pipe issues per instruction, whatever its lanes.
         double v = 0.0;
         for (int r = l; r >= 1; --r) {  // fd(r, l), r = k - 1 with k from l + 1 down to 2
             const double z = zd[r + 1];
-            const bool act = ge_zero(z);
-            if (r == l)
-                v = act ? qed * z : 0.0;
-            else
-                v = act ? v * z : 0.0;
+            v = ge_zero(z) ? ((r == l) ? qed : v) * z : 0.0;
             fd[r] = v;
         }
+        // the diagonal's terms (l == k: - qamu, then - qdk2) and the sub-diagonal's (l == k - 1:
+        // - qamd, then + qdk1) as f = (f - s1) + s2, where the other lanes' s1 = +0 and s2 = -0
+        // leave every f as it is (x - +0 = x, x + -0 = x, zeros and NaNs included), and
+        // x - y = x + (-y) exactly
+        const double nqdk2 = -qdk2;
         double u = 0.0, fprev = 0.0;
         for (int k = 1; k <= n; ++k) {
             const double z = zu[k];
-            const bool act = ge_zero(z);
-            if (l < k - 1)
-                u = act ? u * z : 0.0;
-            else if (l == k - 1)
-                u = act ? qeu * z : 0.0;
-            else
-                u = 0.0;
+            // the updraft chain from l + 1 up: qeu z at k = l + 1, then u z; zero below
+            u = (ge_zero(z) && l <= k - 1) ? ((l == k - 1) ? qeu : u) * z : 0.0;
             double fk = 0.0;
             if (k <= n - 1) {
                 double f = u + (k <= l ? fd[k] : 0.0);
-                if (l == k) f = f - qamu;
-                if (l == k - 1) {
-                    f = f - qamd;
-                    f = f + qdk1;
-                }
-                if (l == k) f = f - qdk2;
+                const double s1 = (l == k) ? qamu : ((l == k - 1) ? qamd : 0.0);
+                const double s2 = (l == k) ? nqdk2 : ((l == k - 1) ? qdk1 : -0.0);
+                f = (f - s1) + s2;
                 fk = f;
             }
             double e = mdt * (fprev - fk);
@@ -481,11 +476,15 @@ __global__ void __launch_bounds__(GB_TUNE_MAX_LU_WARPS * 32) k_convec_lu(CArgs A
 }
 
 __global__ void k_convec_apply(CArgs A) {
+    extern __shared__ double recip[];  // cols_per_block x n: RN(1 / U(r, r)) of each column's rows
     const int n = A.n;
     const int cl = threadIdx.x / n, x = threadIdx.x % n;  // column in the block, its thread
     const int c = blockIdx.x * A.cols_per_block + cl;
     const bool live = cl < A.cols_per_block && c < A.ncol;
     double *X = live ? A.inv + (size_t)c * n * n : nullptr;
+    const double *ud = live && A.fresh[c] == 2 ? A.tband + (size_t)c * 2 * n : nullptr;  // tri's diagonal
+    // ---- the reciprocals of U's diagonal, one a thread: every quotient of row r shares U(r, r)
+    if (live && A.fresh[c]) recip[cl * n + x] = recip_for(ud ? ud[x] : A.abuf[(size_t)c * n * n + (size_t)x * n + x]);
     // ---- a cloudless column's L^-1, column x: the forward substitution of the identity with L's
     // single band, Y(r, x) = +0 - L(r, r-1) Y(r-1, x) below the diagonal (the terms of a zero
     // L(r, r-1) it skips leave the +0 that this writes), 1 on it, +0 above
@@ -499,11 +498,13 @@ __global__ void k_convec_apply(CArgs A) {
             X[(size_t)r * n + x] = y;
         }
     }
-    // ---- back substitution of inverse column x: rows from the bottom, terms k in order
+    __syncthreads();
+    // ---- back substitution of inverse column x: rows from the bottom, terms k in order; each
+    // quotient by the row's shared reciprocal, correctly rounded (div_by_recip)
     if (live && A.fresh[c]) {
         const double *U = A.abuf + (size_t)c * n * n;
         const int32_t *rend = A.rend + (size_t)c * n;
-        const double *ud = A.fresh[c] == 2 ? A.tband + (size_t)c * 2 * n : nullptr;  // tri's diagonal
+        const double *rc = recip + cl * n;
         for (int r = n - 1; r >= 0; --r) {
             double a = X[(size_t)r * n + x];
             for (int k = r + 1; k < rend[r]; ++k) {
@@ -511,7 +512,7 @@ __global__ void k_convec_apply(CArgs A) {
                 if (is_zero(w)) continue;
                 a = a - w * X[(size_t)k * n + x];
             }
-            X[(size_t)r * n + x] = a / (ud ? ud[r] : U[(size_t)r * n + r]);
+            X[(size_t)r * n + x] = div_by_recip(a, ud ? ud[r] : U[(size_t)r * n + r], rc[r]);
         }
     }
     __syncthreads();
@@ -619,6 +620,6 @@ extern "C" int gb_convec(gb_ctx *ctx, const gb_view *m, const gb_view *rm, const
     while (per > 1 && ((per * lmax + 31) / 32) * 32 > 1024) --per;
     A.cols_per_block = per;
     const int threads = ((per * lmax + 31) / 32) * 32;
-    k_convec_apply<<<(ncol + per - 1) / per, threads, 0, ctx->stream>>>(A);
+    k_convec_apply<<<(ncol + per - 1) / per, threads, (size_t)per * lmax * sizeof(double), ctx->stream>>>(A);
     return gb_after_launch(ctx, "convec_apply");
 }

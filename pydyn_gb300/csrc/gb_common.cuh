@@ -91,6 +91,34 @@ __device__ __forceinline__ bool cfl_pass(double c, double mu) {
     return gb_abs(c / mu) < 1.0;
 }
 
+// a / d, correctly rounded, from y = RN(1 / d) shared by many quotients of one divisor
+// (Markstein's correction, IBM J. Res. Develop. 34(1), 1990): q0 = RN(a y), then twice
+// r = a - d q (exact by FMA while q is within an ulp of a / d) and q = RN(q + r y).  q0 is within
+// 1.5 ulp of a / d, the first correction brings it within half an ulp plus a few 2^-52 ulp, and
+// from within one ulp Markstein's theorem makes the second exact: RN(a / d).  One multiply and
+// four FMAs on the FP64 pipe, where a division costs eight.  The proof needs normal operands
+// and results away from overflow and underflow: a zero a (whose quotient is a y, signed as a / d),
+// and anything outside |a| >= 2^-960, |d| in [2^-1000, 2^1000], |a / d| in [2^-1001, 2^1001],
+// take the division itself, as does y = 0 (the caller's mark for a divisor outside that range).
+__device__ __forceinline__ double recip_for(double d) {
+    const int ed = (int)((__double_as_longlong(d) >> 52) & 0x7ff);
+    return (ed >= 23 && ed <= 2023) ? 1.0 / d : 0.0;
+}
+__device__ __forceinline__ double div_by_recip(double a, double d, double y) {
+    const unsigned long long ab = (unsigned long long)__double_as_longlong(a);
+    if (((unsigned long long)__double_as_longlong(y) << 1) != 0) {
+        if ((ab << 1) == 0) return a * y;
+        const int ea = (int)((ab >> 52) & 0x7ff), ed = (int)((__double_as_longlong(d) >> 52) & 0x7ff);
+        const int diff = ea - ed;
+        if (ea >= 63 && ea <= 2023 && diff >= -1000 && diff <= 1000) {
+            const double q0 = a * y;
+            const double q1 = __fma_rn(__fma_rn(-q0, d, a), y, q0);
+            return __fma_rn(__fma_rn(-q1, d, a), y, q1);
+        }
+    }
+    return a / d;
+}
+
 // ------------------------------------------------------------------ NumPy's element rules
 // np.clip(s, -|r|, |r|) exactly as NumPy evaluates it: a NaN in s wins, then max with the lower
 // bound ((s > lo) ? s : lo), then a NaN wins again, then min with the upper bound.

@@ -138,7 +138,9 @@ __global__ void k_math_eval(int op, const double *x, const double *y, double *ou
         case 1: r = gbm_log(x[k]); break;
         case 2: r = gbm_pow(x[k], y[k]); break;
         case 3: r = gbm_cos(x[k]); break;
-        default: r = gbm_sin(x[k]); break;
+        case 4: r = gbm_sin(x[k]); break;
+        case 5: r = div_by_recip(x[k], y[k], recip_for(y[k])); break;
+        default: r = x[k] / y[k]; break;
     }
     out[k] = r;
 }

@@ -65,7 +65,8 @@ class Forward:
             self.physics.init_state(self.st)
         self.graphs = {}
         self.last = {}
-        self.aux = None  # the captured interval's side contexts, one per region (with physics)
+        self.aux = None  # the captured interval's side contexts, one per region (a child's share of the step)
+        self.prep = None  # the captured interval's Calc_Kzz contexts, one per region (with physics)
         self.aux_cfl = None  # the captured interval's rehearsal context
         self._replays, self._side_per_replay = 0, 0
 
@@ -168,18 +169,21 @@ class Forward:
         conv = None
         joins = []
         forked = None
-        if self.aux is not None:  # the side contexts start from the step's own setup
+        sides = (self.prep or []) + (self.aux or [])
+        if sides:  # the side contexts start from the step's own setup
             if self.physics is not None:
                 self.physics.prepare_step(self.nread)
             forked = self.dev.event()
             forked.record()
-            for aux in self.aux:
+            for aux in sides:
                 aux.wait(forked)
         if self.physics is not None:
-            for r, aux in zip(zoom.regions(), self.aux, strict=True):  # each region on its own stream
-                with self.dev.redirect(aux):
+            # each region's Calc_Kzz on a stream of its own: beside the region's advection too,
+            # which a child runs on its own side context
+            for r, prep in zip(zoom.regions(), self.prep, strict=True):
+                with self.dev.redirect(prep):
                     self.physics.prepare_region(self, r)
-                joins.append(aux.event())
+                joins.append(prep.event())
                 joins[-1].record()
             # a region's side stream joins at the region's first convection (dkg; the rate
             # constants follow in chemistry).  Until then the step's advection and exchange run
@@ -204,7 +208,7 @@ class Forward:
             sched.join()
         if self.physics is not None:
             self.physics.join_all()
-        for aux in self.aux or ():  # every side stream is joined before the capture ends
+        for aux in sides:  # every side stream is joined before the capture ends
             done = aux.event()
             done.record()
             self.dev.wait(done)
@@ -251,14 +255,18 @@ class Forward:
             with self.dev.redirect(self.aux_cfl):
                 self._enqueue_rehearsal()
             self.aux_cfl.sync()
-            if self.physics is not None or (self.zoom.nregions > 1 and spreadable(self.zoom)):
-                # one per region: Calc_Kzz, and a child's share of the step; their work spaces
-                # as large as the run's own grew in its uncaptured interval
+            if self.physics is not None:
+                # one per region for Calc_Kzz, its work space sized by an uncaptured run of it
+                self.prep = [Device(self.dev.ordinal) for _ in self.zoom.regions()]
+                for r, prep in zip(self.zoom.regions(), self.prep, strict=True):
+                    with self.dev.redirect(prep):
+                        self.physics.prepare_region(self, r)
+                    prep.sync()
+            if self.zoom.nregions > 1 and spreadable(self.zoom):
+                # one per region for a child's share of the step, its work space as large as the
+                # run's own grew in its uncaptured interval
                 self.aux = [Device(self.dev.ordinal) for _ in self.zoom.regions()]
-                for r, aux in zip(self.zoom.regions(), self.aux, strict=True):
-                    if self.physics is not None:
-                        with self.dev.redirect(aux):
-                            self.physics.prepare_region(self, r)
+                for aux in self.aux:
                     aux.reserve_work(self.dev.work_size())
                     aux.sync()
         self.dev.sync()
@@ -280,8 +288,8 @@ class Forward:
         nread, put the state back and redo the interval uncaptured.  Returns (ndyn, n)."""
         self.dev.sync_stream()  # the replay, the side contexts' branches included
         failed = self.aux_cfl.cfl_failed()  # the rehearsal's flag, on its context
-        for aux in self.aux or ():
-            aux.sync()  # errors of the side contexts' kernels (Calc_Kzz) are raised here
+        for aux in (self.prep or []) + (self.aux or []):
+            aux.sync()  # errors of the side contexts' kernels (Calc_Kzz, a child's) are raised here
         if failed:  # the speculation was wrong: back to the interval's start
             for (r, k), a in self._spec.items():
                 self.st[r][k].assign(a)
@@ -306,12 +314,12 @@ class Forward:
         if self.physics is not None:
             self.physics.free()
         self.w.free()
-        for aux in (self.aux or []) + ([self.aux_cfl] if self.aux_cfl is not None else []):
+        for aux in (self.prep or []) + (self.aux or []) + ([self.aux_cfl] if self.aux_cfl is not None else []):
             aux.close()
-        self.aux, self.aux_cfl = None, None
+        self.prep, self.aux, self.aux_cfl = None, None, None
 
     def _side_launches(self):
-        side = (self.aux or []) + ([self.aux_cfl] if self.aux_cfl is not None else [])
+        side = (self.prep or []) + (self.aux or []) + ([self.aux_cfl] if self.aux_cfl is not None else [])
         return sum(aux.launches() for aux in side)
 
     def launches(self):

@@ -80,3 +80,47 @@ def test_device_math_equals_host_math(dev):
         assert (bits(got) == bits(want)).all(), name
         for a in (dx, dy, out):
             a.free()
+
+
+def _division_cases(rng):
+    """(a, d) pairs: random magnitudes over the whole range, quotients a hair off a rounding
+    midpoint, significands of all ones, and every kind of special value."""
+    n = 200_000
+    sig = lambda k: 1.0 + rng.integers(0, 2**52, k) / 2.0**52  # noqa: E731
+    a = sig(n) * np.exp2(rng.integers(-1074, 1023, n).astype(float)) * rng.choice([-1.0, 1.0], n)
+    d = sig(n) * np.exp2(rng.integers(-1074, 1023, n).astype(float)) * rng.choice([-1.0, 1.0], n)
+    a2 = sig(n) * np.exp2(rng.integers(-40, 40, n).astype(float))
+    d2 = sig(n) * np.exp2(rng.integers(-40, 40, n).astype(float))
+    q = sig(n)
+    d3 = sig(n)
+    a3 = d3 * (q + 2.0**-53)  # the product rounded: a quotient next to a midpoint
+    special = np.array([0.0, -0.0, 5e-324, -5e-324, 2.2250738585072014e-308, 1.7976931348623157e308, np.inf,
+                        -np.inf, np.nan, 1.0, -1.0, 2.0 - 2.0**-52, 1.0 + 2.0**-52, 3.0, 0.1, 2.0**-1000,
+                        2.0**1000, 2.0**-960, 2.0**1001, 2.0**-1001])  # fmt: skip
+    sa, sd = np.meshgrid(special, special)
+    return np.concatenate([a, a2, a3, sa.ravel()]), np.concatenate([d, d2, d3, sd.ravel()])
+
+
+@pytest.mark.gpu
+def test_shared_reciprocal_division_is_the_division(dev):
+    """div_by_recip equals the hardware division bit for bit (NaNs included), and both equal the
+    host's IEEE division wherever the quotient is not a NaN."""
+    from pydyn_gb300 import _native as N
+    from pydyn_gb300.device import DevArray
+
+    a, d = _division_cases(np.random.default_rng(5))
+    da, dd = DevArray.from_host(dev, a), DevArray.from_host(dev, d)
+    outs = []
+    for op in (5, 6):
+        out = DevArray.zeros(dev, (0, len(a) - 1))
+        N.check(dev.L.gb_math_eval(dev.h, op, da.ptr, dd.ptr, out.ptr, len(a)), "gb_math_eval")
+        outs.append(out.host())
+        out.free()
+    fast, hw = outs
+    assert (bits(fast) == bits(hw)).all()
+    with np.errstate(all="ignore"):
+        want = a / d
+    ok = ~np.isnan(want)
+    assert (bits(fast[ok]) == bits(want[ok])).all() and np.isnan(fast[~ok]).all()
+    for x in (da, dd):
+        x.free()
