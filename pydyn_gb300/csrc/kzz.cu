@@ -14,8 +14,9 @@
 //   k_kzz_raw2        thread per (column, level): the second sweep's level terms
 //   k_kzz_sweep2      thread per column: the second sweep (pblh) and the column constants of
 //                     the diffusivity (w*, the Prandtl stability terms)
-//   k_kzz_interfaces  thread per (column, interface): the free-troposphere and boundary-layer
-//                     diffusivities, then dkg of the interface (zero at lmax_conv - 1)
+//   k_kzz_interfaces  thread per (column, interface), a warp 32 columns at one interface: the
+//                     free-troposphere and boundary-layer diffusivities, then dkg of the
+//                     interface (zero at lmax_conv - 1)
 // Every value is the per-element statement of the reference in its order; exp / log / pow / cos
 // are gbmath.h.  Reference: pydyn diffusion.py:71-276 (jqif, ustar, geopotential, mass_t,
 // _winds, _pbl_pass, bldiff, dkg, calc_kzz).
@@ -246,12 +247,15 @@ __global__ void __launch_bounds__(GB_TUNE_MAX_COLUMN) k_kzz_sweep2(KArgs A) {
     cv[9] = sqrt(stab1);
 }
 
+// Lanes run along the columns and warps along the interfaces (a block: 32 columns at blockDim / 32
+// consecutive interfaces): the boundary layer's branches (the powers of its stability terms,
+// pow(1, y) = 1 returning at once above it) are then taken or left by whole warps.
 __global__ void __launch_bounds__(GB_TUNE_MAX_CELL) k_kzz_interfaces(KArgs A) {
-    const int lm = A.lm, ni = lm - 1;
-    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= (int64_t)A.im * A.jm * ni) return;
-    const int64_t c = t / ni;
-    const int k = (int)(t % ni) + 1;  // interface k, between layers k-1 and k
+    const int lm = A.lm, ni = lm - 1, lv = blockDim.x >> 5;
+    const int nkg = (ni + lv - 1) / lv;
+    const int64_t c = (int64_t)(blockIdx.x / nkg) * 32 + (threadIdx.x & 31);
+    const int k = (int)(blockIdx.x % nkg) * lv + (int)(threadIdx.x >> 5) + 1;  // interface k, between layers k-1 and k
+    if (c >= (int64_t)A.im * A.jm || k > ni) return;
     const int i = (int)(c / A.jm), j = (int)(c % A.jm);
     const double ONET = 1.0 / 3.0, CCON = SFFRAC * VKARMAN;
     const double *cv = A.col + c * NCOLVAL;
@@ -375,6 +379,8 @@ extern "C" int gb_calc_kzz(gb_ctx *ctx, const gb_view *spm, const gb_view *sp, c
     if (int rc = gb_after_launch(ctx, "kzz_raw2")) return rc;
     k_kzz_sweep2<<<gb_blocks(ncol, tcol), tcol, 0, ctx->stream>>>(A);
     if (int rc = gb_after_launch(ctx, "kzz_sweep2")) return rc;
-    k_kzz_interfaces<<<gb_blocks(ncol * (A.lm - 1), tcell), tcell, 0, ctx->stream>>>(A);
+    // blocks of 32 columns x (tcell / 32) interfaces
+    const int lv = tcell / 32;
+    k_kzz_interfaces<<<(unsigned)((ncol + 31) / 32 * ((A.lm - 1 + lv - 1) / lv)), tcell, 0, ctx->stream>>>(A);
     return gb_after_launch(ctx, "kzz_interfaces");
 }
