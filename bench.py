@@ -57,7 +57,7 @@ BYTES_PER_CELL = {"_dynamu_region1": 12, "_dynamv_region1": 12, "_dynamw_region1
 
 # DRAM bytes (read + write) per call of a body, from one ncu capture of an eager interval of
 # glb3x2+nam1x1 with physics (profiles/interval_dram_fp64_glb3x2+nam1x1.md): the roofline's traffic
-TRAFFIC_PER_CALL = {"glb3x2+nam1x1": {"convec_region@2": 119.0e6, "convec_region@1": 231.9e6}}
+TRAFFIC_PER_CALL = {"glb3x2+nam1x1": {"convec_region@2": 132.3e6, "convec_region@1": 250.5e6}}
 
 
 def metric_name(workload):

@@ -164,33 +164,29 @@ class Forward:
         rehearsed = self.aux_cfl.event()
         rehearsed.record()
         self.interpolate(st)
+        # Setup_MassFlow first: it rebuilds a parent's mass over a child's footprint and with it
+        # the parent's sp (m2phlb), which Calc_Kzz reads
+        D.setup_massflow(zoom, st, self.nread)
         kw = {"limits": self.limits}
         conv = None
         joins = []
-        metered = None
+        forked = None
+        sides = (self.prep or []) + (self.aux or [])
+        if sides:  # the side contexts start from the step's own setup
+            if self.physics is not None:
+                self.physics.prepare_step(self.nread)
+            forked = self.dev.event()
+            forked.record()
+            for aux in sides:
+                aux.wait(forked)
         if self.physics is not None:
-            # each region's Calc_Kzz on a stream of its own from the interpolated meteo on:
-            # beside Setup_MassFlow (both only read pu and pv) and the region's advection, which
-            # a child runs on its own side context
-            metered = self.dev.event()
-            metered.record()
+            # each region's Calc_Kzz on a stream of its own: beside the region's advection too,
+            # which a child runs on its own side context
             for r, prep in zip(zoom.regions(), self.prep, strict=True):
-                prep.wait(metered)
                 with self.dev.redirect(prep):
                     self.physics.prepare_region(self, r)
                 joins.append(prep.event())
                 joins[-1].record()
-        D.setup_massflow(zoom, st, self.nread)
-        forked = None
-        if self.physics is not None:
-            self.physics.prepare_step(self.nread)
-        if self.aux is not None:  # a child's side context starts from the step's own setup
-            forked = self.dev.event()
-            forked.record()
-            for aux in self.aux:
-                aux.wait(forked)
-        sides = (self.prep or []) + (self.aux or [])
-        if self.physics is not None:
             # a region's side stream joins at the region's first convection (dkg; the rate
             # constants follow in chemistry).  Until then the step's advection and exchange run
             # beside it: they read and write none of Calc_Kzz's arrays (sp, pu, pv, t, q in; dkg,
@@ -220,7 +216,7 @@ class Forward:
             self.dev.wait(done)
             joins.append(done)
         self.dev.wait(rehearsed)
-        self._fork_events = (fork, rehearsed, metered, forked, joins, sched.keep if sched else None)  # alive until the capture ends
+        self._fork_events = (fork, rehearsed, forked, joins, sched.keep if sched else None)  # alive until the capture ends
 
     def _enqueue_rehearsal(self):
         """Check_CFL's rehearsal of one step on the copy (save, reset the flag, meteo, the
