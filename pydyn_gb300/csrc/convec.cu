@@ -1,10 +1,12 @@
 // convec: implicit convection with Kzz diffusion folded into one matrix per column, inverted
 // by Crout LU without pivoting, applied to the tracer mass and (by its diagonal) the slopes.
 //
-// Five launches, shaped so that the FP64 pipe -- this GPU's scarcest unit -- issues with its
+// Six launches, shaped so that the FP64 pipe -- this GPU's scarcest unit -- issues with its
 // lanes full:
 //   k_convec_chains  three threads per owned column: whether its kept inverse still holds, the
-//                    updraft chains, the downdraft chains
+//                    updraft and the downdraft mass fluxes carried level to level
+//   k_convec_ratios  one thread per (column, level): the chains' ratios (a division each), which
+//                    the carried fluxes do not wait for
 //   k_convec_matrix  one thread per (column, column l of its matrix): the quotients that column
 //                    uses (each division once), conv1(., l) = I - dt (f(k-1, l) - f(k, l)), the
 //                    downdraft chain of f down from the diagonal and the updraft chain up from
@@ -111,10 +113,13 @@ __device__ void chain_cache(const CArgs &A, int c, int i, int j) {
     A.fresh[c] = 1;
 }
 
-// the updraft chains amu, zu of column c (levels 1..n from the bottom)
+// The chains' carried part: the updraft mass flux amu of column c (levels 1..n from the bottom)
+// and the downdraft's amd.  Each level's ratio z (a division, which the carried value does not
+// wait for) is k_convec_ratios', one thread a level, from the stored amu(k-1) / amd(k): the same
+// statements on the same values.
 __device__ void chain_up(const CArgs &A, int c, int i, int j) {
     const int n = A.n;
-    double *amu = chains(A, c), *zu = amu + (n + 1);
+    double *amu = chains(A, c);
     const int top = A.top[i * A.ts0 + j * A.ts1];
     double mu = 0.0;
     amu[0] = 0.0;
@@ -133,24 +138,20 @@ __device__ void chain_up(const CArgs &A, int c, int i, int j) {
             const double eu = eb[u], du = db[u];
             const bool act = top >= k;
             const double a = mu + eu - du;
-            const bool up = a > 0.0;
-            const double z = up ? max0(1.0 - du / (mu + eu)) : 0.0;
-            mu = (act && up) ? a : 0.0;
+            mu = (act && a > 0.0) ? a : 0.0;
             amu[k] = mu;
-            zu[k] = act ? z : -1.0;  // -1 marks an inactive level
         }
     }
 }
 
-// the downdraft chains amd, zd of column c (levels n down to 2)
+// the downdraft's carried part, amd of column c (levels n down to 2)
 __device__ void chain_down(const CArgs &A, int c, int i, int j) {
     const int n = A.n;
-    double *amd = chains(A, c) + 2 * (n + 1), *zd = amd + (n + 1);
+    double *amd = chains(A, c) + 2 * (n + 1);
     const int lfs = A.lfs[i * A.ts0 + j * A.ts1];
     double md = 0.0;
     amd[n] = 0.0;
     amd[0] = 0.0;
-    zd[0] = zd[1] = -1.0;
     for (int k0 = n; k0 >= 2; k0 -= CB) {
         double eb[CB], db[CB];
 #pragma unroll
@@ -166,12 +167,39 @@ __device__ void chain_down(const CArgs &A, int c, int i, int j) {
             const double ed = eb[u], dd = db[u];
             const bool act = lfs >= k;
             const double a = md - ed + dd;
-            const bool dn = a < 0.0;
-            const double z = dn ? max0(1.0 + dd / (md - ed)) : 0.0;
-            md = (act && dn) ? a : 0.0;
+            md = (act && a < 0.0) ? a : 0.0;
             amd[k - 1] = md;
-            zd[k] = act ? z : -1.0;
         }
+    }
+}
+
+// thread per (column made fresh, level k = 1..n): the chains' ratios.  Updraft at k:
+// a = amu(k-1) + entu - detu, z = 1 - detu / (amu(k-1) + entu) clipped at 0 where a > 0, else 0;
+// the downdraft at k >= 2 from amd(k) alike; -1 marks an inactive level (above the cloud top, or
+// the level of free sinking).
+__global__ void __launch_bounds__(GB_TUNE_MAX_CELL) k_convec_ratios(CArgs A) {
+    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const int n = A.n;
+    if (t >= (int64_t)A.ncol * n) return;
+    const int c = (int)(t / n), k = (int)(t % n) + 1;
+    if (!A.fresh[c]) return;
+    const int i = A.cols[2 * c], j = A.cols[2 * c + 1];
+    double *amu = chains(A, c), *zu = amu + (n + 1), *amd = zu + (n + 1), *zd = amd + (n + 1);
+    {
+        const double mu = amu[k - 1], eu = AT(A.entu, i, j, k - 1), du = AT(A.detu, i, j, k - 1);
+        const bool act = A.top[i * A.ts0 + j * A.ts1] >= k;
+        const double a = mu + eu - du;
+        const double z = a > 0.0 ? max0(1.0 - du / (mu + eu)) : 0.0;
+        zu[k] = act ? z : -1.0;
+    }
+    if (k >= 2) {
+        const double md = amd[k], ed = AT(A.entd, i, j, k - 1), dd = AT(A.detd, i, j, k - 1);
+        const bool act = A.lfs[i * A.ts0 + j * A.ts1] >= k;
+        const double a = md - ed + dd;
+        const double z = a < 0.0 ? max0(1.0 + dd / (md - ed)) : 0.0;
+        zd[k] = act ? z : -1.0;
+    } else {
+        zd[0] = zd[1] = -1.0;
     }
 }
 
@@ -598,6 +626,8 @@ extern "C" int gb_convec(gb_ctx *ctx, const gb_view *m, const gb_view *rm, const
     const int tcol = ctx->tune[GB_TUNE_COLUMN_THREADS], tcell = ctx->tune[GB_TUNE_CELL_THREADS];
     k_convec_chains<<<gb_blocks(ncol, tcol), dim3(tcol, 3), 0, ctx->stream>>>(A);
     if (int rc = gb_after_launch(ctx, "convec_chains")) return rc;
+    k_convec_ratios<<<gb_blocks((int64_t)ncol * lmax, tcell), tcell, 0, ctx->stream>>>(A);
+    if (int rc = gb_after_launch(ctx, "convec_ratios")) return rc;
     k_convec_matrix<<<gb_blocks((int64_t)ncol * lmax, tcell), tcell, 0, ctx->stream>>>(A);
     if (int rc = gb_after_launch(ctx, "convec_matrix")) return rc;
     // the cloudless columns' recurrence on the side stream, beside the LU of the others: each
