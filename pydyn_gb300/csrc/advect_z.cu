@@ -70,13 +70,16 @@ struct ZCol {
 __device__ void z_trials(const ZArgs &A, ZCol *zc, double *mx, double *cf, int p, int k, int64_t col0, int ncols,
                          bool scope) {
     const int lm = A.lm, P = A.P, NC = A.ncell;
-    // cf = cm / n over every column's lm + 1 interfaces, spread over the block's threads
+    // cf = cm / n over every column's lm + 1 interfaces, spread over the block's threads.  At
+    // n = 1 the quotient is cm itself (x / 1 = x exactly; a NaN fails the test either way), and
+    // these trial values decide only pass or fail, so the division is left out there.
     for (int e = threadIdx.x; e < P * (lm + 1); e += blockDim.x) {
         const int q = e / (lm + 1), kk = e % (lm + 1);
         if (q < ncols && zc[q].state == 1) {
             const int64_t col = col0 + q;
             const int i = (int)(col / A.jm), j = (int)(col % A.jm);
-            cf[q * NC + kk] = AT(A.cm, i, j, kk) / (double)zc[q].n;
+            const double v = AT(A.cm, i, j, kk);
+            cf[q * NC + kk] = zc[q].n == 1 ? v : v / (double)zc[q].n;
         }
     }
     const bool mine = p < ncols && zc[p].state == 1;

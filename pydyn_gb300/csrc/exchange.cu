@@ -174,19 +174,39 @@ __global__ void k_uncompress_y(RA R, int yr, int is, int ie, int ls, int le, int
 // One thread per (ring block, level, field, tracer): the block's mean, accumulated rows outer /
 // columns inner from 0 over q / (xr yr), spread over the block (exchange.py:178-229).  Ring
 // blocks: the first and last block column (when the x edges mix) and the first and last block
-// row (children touching no pole).
-__global__ void k_mix_edges(RA R, int xr, int yr, int xedges, int ysp, int ynp, int nfield) {
+// row (children touching no pole), each once, enumerated by ring_block -- only they get threads.
+struct Ring {
+    int imp, jmp, ncolb, x0, nx, nrow, ysp;
+    __host__ __device__ Ring(int imp_, int jmp_, int xedges, int ysp_, int ynp)
+        : imp(imp_), jmp(jmp_), ysp(ysp_) {
+        ncolb = xedges ? (imp > 1 ? 2 : 1) * jmp : 0;  // the x-edge block columns, all their rows
+        x0 = xedges ? 1 : 0;                            // the block columns between them
+        nx = (xedges ? imp - 1 : imp) - x0;
+        if (nx < 0) nx = 0;
+        nrow = (ysp ? 1 : 0) + (ynp && !(ysp && jmp == 1) ? 1 : 0);  // the first and last block rows
+    }
+    __host__ __device__ int64_t count() const { return ncolb + (int64_t)nrow * nx; }
+};
+__device__ __forceinline__ void ring_block(const Ring &g, int b, int &ip, int &jp) {
+    if (b < g.ncolb) {
+        ip = b / g.jmp == 0 ? 0 : g.imp - 1;
+        jp = b % g.jmp;
+    } else {
+        const int b2 = b - g.ncolb, row = b2 / g.nx;
+        ip = g.x0 + b2 % g.nx;
+        jp = (row == 0 && g.ysp) ? 0 : g.jmp - 1;
+    }
+}
+
+__global__ void k_mix_edges(RA R, int xr, int yr, Ring g, int nfield) {
     int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-    const int imp = R.im / xr, jmp = R.jm / yr;
-    const int64_t blocks = (int64_t)imp * jmp;
-    const int64_t per = blocks * R.lm;
+    const int64_t per = g.count() * R.lm;
     if (k >= per * nfield) return;
     const int ft = (int)(k / per);
     const int64_t rest = k % per;
     const int b = (int)(rest / R.lm), l = (int)(rest % R.lm) + 1;
-    const int ip = b / jmp, jp = b % jmp;
-    const bool ring = (xedges && (ip == 0 || ip == imp - 1)) || (ysp && jp == 0) || (ynp && jp == jmp - 1);
-    if (!ring) return;
+    int ip, jp;
+    ring_block(g, b, ip, jp);
     const int f = ft == 0 ? 0 : 1 + (ft - 1) / R.nt, t = ft == 0 ? 0 : (ft - 1) % R.nt;
     const double xyref = (double)(xr * yr);
     double acc = 0.0;
@@ -344,8 +364,10 @@ extern "C" int gb_mix_edges(gb_ctx *ctx, const gb_view *region, int xr, int yr, 
                             int tracers) {
     RA R = ra(region);
     const int nfield = tracers ? 1 + 4 * R.nt : 1;
-    const int64_t total = (int64_t)(R.im / xr) * (R.jm / yr) * R.lm * nfield;
-    k_mix_edges<<<grid_for(total), 128, 0, ctx->stream>>>(R, xr, yr, xedges, ysp, ynp, nfield);
+    const Ring g(R.im / xr, R.jm / yr, xedges, ysp, ynp);
+    const int64_t total = g.count() * R.lm * nfield;
+    if (total == 0) return GB_OK;
+    k_mix_edges<<<grid_for(total), 128, 0, ctx->stream>>>(R, xr, yr, g, nfield);
     return gb_after_launch(ctx, "mix_edges");
 }
 
