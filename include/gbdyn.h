@@ -81,6 +81,11 @@ int gb_device_name(gb_ctx *ctx, char *buf, int len); /* "<name> sm_<cc> x<SMs>":
  * from now on, and its present size -- a context that will run captured work first takes the
  * size another context's uncaptured run grew to. */
 int gb_work_reserve(gb_ctx *ctx, size_t bytes);
+/* The context's streams at `rank` steps above the device's least priority (0: the default,
+ * clamped to the greatest): the block scheduler serves a higher stream's kernels first.  A
+ * captured graph keeps each kernel at the priority of the stream it was captured on.  Waits for
+ * the context's work; not while capturing. */
+int gb_stream_priority(gb_ctx *ctx, int rank);
 size_t gb_work_size(gb_ctx *ctx);
 int gb_tune_set(gb_ctx *ctx, int key, int value); /* GB_EARG for a value outside the key's range */
 int gb_tune_get(gb_ctx *ctx, int key, int *value);
@@ -115,6 +120,10 @@ int gb_interp(gb_ctx *ctx, const gb_view *dst, const gb_view *a, const gb_view *
 /* counter[0] += delta on the stream (device int32): a step counter that a captured step
  * advances each time it replays (convection's inverse cache epoch). */
 int gb_iadd(gb_ctx *ctx, int32_t *counter, int delta);
+/* buf[slot] = the GPU's global nanosecond timer when the stream reaches this point (a one-thread
+ * kernel, capturable): the timeline of a captured interval's streams
+ * (python -m pydyn_gb300.profile --timeline).  No reference counterpart. */
+int gb_stamp(gb_ctx *ctx, uint64_t *buf, int slot);
 /* dst = seqsum of src over `axis` (src's extent along it), accumulated in index order
  * (ops.seqsum, ops.py:235); dst has src's extents with that axis dropped (n = 1). */
 int gb_seqsum(gb_ctx *ctx, const gb_view *dst, const gb_view *src, int axis, double post_mul);

@@ -58,6 +58,7 @@ SIGNATURES = {
     "gb_event_record": (_I, [_VP, _VP]),
     "gb_stream_wait": (_I, [_VP, _VP]),
     "gb_work_reserve": (_I, [_VP, ctypes.c_size_t]),
+    "gb_stream_priority": (_I, [_VP, _I]),
     "gb_work_size": (ctypes.c_size_t, [_VP]),
     "gb_device_name": (_I, [_VP, ctypes.c_char_p, _I]),
     "gb_tune_set": (_I, [_VP, _I, _I]),
@@ -70,6 +71,7 @@ SIGNATURES = {
     "gb_seqsum": (_I, [_VP, _P, _P, _I, _D]),
     "gb_interp": (_I, [_VP, _P, _P, _P, _VP]),
     "gb_iadd": (_I, [_VP, _VP, _I]),
+    "gb_stamp": (_I, [_VP, _VP, _I]),
     "gb_advect_x": (_I, [_VP, _P, _P, _P, _P, _P, _P, _VP, _I, _I, _I, _I, _I, _VP, _VP]),
     "gb_advect_y": (_I, [_VP, _P, _P, _P, _P, _P, _P, _P, _I, _I, _I, _VP]),
     "gb_advect_y_noalloc": (_I, [_VP, _P, _P, _P, _P, _P, _P, _P, _I, _I, _I, _VP]),

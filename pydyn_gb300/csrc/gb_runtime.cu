@@ -74,6 +74,32 @@ extern "C" int gb_create(int device, gb_ctx **out) {
     return GB_OK;
 }
 
+extern "C" int gb_stream_priority(gb_ctx *ctx, int rank) {
+    if (!ctx || rank < 0) return GB_EARG;
+    if (ctx->capturing) {
+        gb_set_error("gb_stream_priority: not while capturing");
+        return GB_EARG;
+    }
+    int least = 0, greatest = 0;
+    GB_CHECK_CUDA(cudaDeviceGetStreamPriorityRange(&least, &greatest));
+    const int prio = least - rank < greatest ? greatest : least - rank;  // numerically lower: served first
+    // new streams at that priority, once the old ones have drained (work enqueued later goes to them)
+    cudaStream_t s = nullptr, side = nullptr;
+    GB_CHECK_CUDA(cudaStreamCreateWithPriority(&s, cudaStreamNonBlocking, prio));
+    cudaError_t e = cudaStreamCreateWithPriority(&side, cudaStreamNonBlocking, prio);
+    if (e != cudaSuccess) {
+        cudaStreamDestroy(s);
+        return gb_cuda_fail(e, "gb_stream_priority");
+    }
+    GB_CHECK_CUDA(cudaStreamSynchronize(ctx->stream));
+    GB_CHECK_CUDA(cudaStreamSynchronize(ctx->side));
+    cudaStreamDestroy(ctx->stream);
+    cudaStreamDestroy(ctx->side);
+    ctx->stream = s;
+    ctx->side = side;
+    return GB_OK;
+}
+
 extern "C" int gb_work_reserve(gb_ctx *ctx, size_t bytes) {
     if (!ctx) return GB_EARG;
     return gb_work(ctx, bytes) ? GB_OK : GB_ECUDA;
@@ -230,7 +256,8 @@ extern "C" int gb_capture_end(gb_ctx *ctx, void **out) {
         delete g;
         return gb_cuda_fail(e, "cudaStreamEndCapture");
     }
-    e = cudaGraphInstantiate(&g->exec, g->graph, 0);
+    // each kernel node runs at the priority of the stream it was captured on (gb_stream_priority)
+    e = cudaGraphInstantiate(&g->exec, g->graph, cudaGraphInstantiateFlagUseNodePriority);
     if (e != cudaSuccess) {
         cudaGraphDestroy(g->graph);
         delete g;
@@ -382,6 +409,19 @@ extern "C" int gb_iadd(gb_ctx *ctx, int32_t *counter, int delta) {
     if (!ctx || !counter) return GB_EARG;
     k_iadd<<<1, 1, 0, ctx->stream>>>(counter, delta);
     return gb_after_launch(ctx, "iadd");
+}
+
+// the GPU's global nanosecond timer when the stream reaches this point
+__global__ void k_stamp(unsigned long long *buf, int slot) {
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    buf[slot] = t;
+}
+
+extern "C" int gb_stamp(gb_ctx *ctx, uint64_t *buf, int slot) {
+    if (!ctx || !buf || slot < 0) return GB_EARG;
+    k_stamp<<<1, 1, 0, ctx->stream>>>(reinterpret_cast<unsigned long long *>(buf), slot);
+    return gb_after_launch(ctx, "stamp");
 }
 
 extern "C" int gb_interp(gb_ctx *ctx, const gb_view *dst, const gb_view *a, const gb_view *b, const double *w) {

@@ -116,6 +116,11 @@ class Device:
     def work_size(self):
         return int(self.L.gb_work_size(self.h))
 
+    def set_priority(self, rank):
+        """The context's streams at `rank` steps above the device's least priority (gb_stream_priority);
+        outside a capture."""
+        N.check(self.L.gb_stream_priority(self.h, int(rank)), "gb_stream_priority")
+
     def reserve_work(self, nbytes):
         """At least nbytes of work space (outside a capture)."""
         N.check(self.L.gb_work_reserve(self.h, int(nbytes)), "gb_work_reserve")

@@ -24,6 +24,7 @@ from .state import TRACERS, ZoomState
 
 WINDOW = 6 * 3600.0
 SPECULATED = ("m", *TRACERS, "sp", "phlb")
+CHILD_PRIORITY = 2  # a child's side context: steps above the device's least stream priority
 
 
 def weights(t):
@@ -266,10 +267,14 @@ class Forward:
                     prep.sync()
             if self.zoom.nregions > 1 and spreadable(self.zoom):
                 # one per region for a child's share of the step, its work space as large as the
-                # run's own grew in its uncaptured interval
+                # run's own grew in its uncaptured interval.  Its streams get a higher priority:
+                # a child's chain of small kernels is the interval's critical path, and the block
+                # scheduler then serves it before the wide kernels beside it (the parent's, Calc_Kzz,
+                # the rehearsal), which have slack
                 self.aux = [Device(self.dev.ordinal) for _ in self.zoom.regions()]
                 for aux in self.aux:
                     aux.reserve_work(self.dev.work_size())
+                    aux.set_priority(CHILD_PRIORITY)
                     aux.sync()
         self.dev.sync()
         self.graphs.pop("interval", None)

@@ -1,6 +1,8 @@
 """Per-body device time of one eagerly enqueued interval: every body the driver calls through
 `st.lib` is bracketed by CUDA events on the context's stream (pydyn's CudaBackend
-profile_begin/end has the same role, gpu/backend.py:634-651)."""
+profile_begin/end has the same role, gpu/backend.py:634-651).  And the timeline of a captured
+interval: the GPU's timer stamped at each body's start and end on the stream it runs on
+(`timeline`)."""
 
 import functools
 from collections import defaultdict
@@ -76,13 +78,130 @@ class BodyProfiler:
         return out
 
 
+class Timeline:
+    """Stamps of the GPU's global timer (gb_stamp) at the start and end of a captured interval's
+    parts, each on the stream the part runs on: the scheduler's region bodies, the Check_CFL
+    rehearsal, each region's Calc_Kzz, Setup_MassFlow and the interval's ends."""
+
+    def __init__(self, fw, slots=8192):
+        import numpy as np
+
+        from .device import DevArray
+
+        self.fw, self.dev = fw, fw.dev
+        self.buf = DevArray.zeros(fw.dev, (0, slots - 1), dtype=np.int64)
+        self.slots = slots
+        self.marks = []  # slot -> (stream, part, "b" | "e")
+        self._saved = []
+
+    def _stream(self):
+        fw, h = self.fw, self.dev.h
+        if h == self._main:
+            return "main"
+        if fw.aux_cfl is not None and h == fw.aux_cfl.h:
+            return "rehearsal"
+        for kind, ctxs in (("kzz", fw.prep), ("region", fw.aux)):
+            for r, c in zip(fw.zoom.regions(), ctxs or (), strict=False):
+                if h == c.h:
+                    return f"{kind}{r}"
+        return "other"
+
+    def stamp(self, part, kind):
+        from . import _native as N
+
+        slot = len(self.marks)
+        if slot >= self.slots:
+            raise RuntimeError("Timeline: out of slots")
+        self.marks.append((self._stream(), part, kind))
+        N.check(self.dev.L.gb_stamp(self.dev.h, self.buf.ptr, slot), "gb_stamp")
+
+    def _bracket(self, owner, attr, part_of):
+        f = getattr(owner, attr)
+        tl = self
+
+        @functools.wraps(f)
+        def call(*a, **k):
+            part = part_of(*a, **k)
+            tl.stamp(part, "b")
+            out = f(*a, **k)
+            tl.stamp(part, "e")
+            return out
+
+        self._saved.append((owner, attr, f))
+        setattr(owner, attr, call)
+
+    def __enter__(self):
+        from contextlib import contextmanager
+
+        from . import driver as D
+        from . import forward as F
+        from . import physics as P
+        from . import schedule as S
+
+        self._main = self.dev.h
+        tl = self
+        body = S.Scheduler.body
+
+        @contextmanager
+        def stamped(sched, name, region):
+            with body(sched, name, region):
+                tl.stamp(f"{name}@{region}", "b")
+                yield
+                tl.stamp(f"{name}@{region}", "e")
+
+        self._saved.append((S.Scheduler, "body", body))
+        S.Scheduler.body = stamped
+        self._bracket(F.Forward, "_enqueue_rehearsal", lambda *a, **k: "check_cfl")
+        self._bracket(P.Physics, "prepare_region", lambda self_, fwd, r: f"calc_kzz@{r}")
+        self._bracket(D, "setup_massflow", lambda *a, **k: "setup_massflow")
+        self._bracket(F.Forward, "_enqueue_interval", lambda *a, **k: "interval")
+        return self
+
+    def __exit__(self, *exc):
+        for owner, attr, f in reversed(self._saved):
+            setattr(owner, attr, f)
+        self._saved.clear()
+        return False
+
+    def report(self):
+        """[(stream, part, start us, end us)] of the last replay, from the interval's first stamp."""
+        t = self.buf.host()[: len(self.marks)]
+        t0 = int(t.min())
+        open_, rows = {}, []
+        for (stream, part, kind), v in zip(self.marks, t, strict=True):
+            key = (stream, part)
+            if kind == "b":
+                open_.setdefault(key, []).append(int(v))
+            elif open_.get(key):
+                b = open_[key].pop(0)
+                rows.append((stream, part, (b - t0) / 1e3, (int(v) - t0) / 1e3))
+        return sorted(rows, key=lambda r: r[2])
+
+
+def timeline(fw, replays=5):
+    """The timeline of the run's captured interval: capture it with stamps, replay it, and return
+    Timeline.report() of the last replay."""
+    if "interval" not in fw.graphs:
+        fw.interval(graph=True)
+    with Timeline(fw) as tl:
+        fw.capture_interval()
+    for _ in range(replays):
+        fw.enqueue_interval_async(fw.t)
+        fw.settle_interval(fw.t)
+    rows = tl.report()
+    fw.capture_interval()  # the interval without stamps again
+    tl.buf.free()
+    return rows
+
+
 def main(argv=None):
     """One eagerly enqueued interval of a configuration -- every kernel launched once, no graph,
     no pinned copies -- for a launch list under a profiler:
 
         python -m pydyn_gb300.profile --config glb3x2+nam1x1 --levels 34 --intervals 1
 
-    With --fp64-rates it measures the GPU's FP64 issue rates instead (the step's compute ceiling).
+    With --fp64-rates it measures the GPU's FP64 issue rates instead (the step's compute ceiling);
+    with --timeline it prints the timeline of the captured interval's streams.
     """
     import argparse
     import sys
@@ -97,6 +216,7 @@ def main(argv=None):
     ap.add_argument("--physics", type=int, default=1, help="1: convection, Kzz, emission, chemistry; 0: advection")
     ap.add_argument("--lmax", type=int, default=None)
     ap.add_argument("--fp64-rates", action="store_true", help="measure the FP64 issue rates and exit")
+    ap.add_argument("--timeline", action="store_true", help="the captured interval's timeline per stream")
     a = ap.parse_args(argv)
     from __graft_entry__ import build
 
@@ -111,6 +231,23 @@ def main(argv=None):
         dev.close()
         return
     fw = Forward(dev, a.config, a.levels, a.seed, physics=bool(a.physics), lmax=a.lmax)
+    if a.timeline:
+        for _ in range(3):
+            fw.interval(graph=True)
+        rows = timeline(fw)
+        end = max(r[3] for r in rows)
+        print(f"captured interval of {a.config}: {end:.1f} us from its first stamp to its last")
+        print(f"{'stream':10s} {'part':34s} {'start us':>9s} {'end us':>9s} {'us':>8s}")
+        for stream, part, b, e in rows:
+            print(f"{stream:10s} {part[:34]:34s} {b:9.1f} {e:9.1f} {e - b:8.1f}")
+        busy = defaultdict(float)
+        for stream, part, b, e in rows:
+            if part != "interval":
+                busy[stream] += e - b
+        print("busy per stream (us, parts summed):", {k: round(v, 1) for k, v in sorted(busy.items())})
+        fw.close()
+        dev.close()
+        return
     n0 = dev.launches()
     for _ in range(a.intervals):
         fw.interval(graph=False)

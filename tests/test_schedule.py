@@ -3,6 +3,8 @@ device that records which stream each event is recorded on and which stream wait
 
 from contextlib import contextmanager
 
+import pytest
+
 from pydyn_gb300 import schedule as S
 
 
@@ -94,3 +96,26 @@ def test_spreadable_trees():
     assert S.spreadable(synth.tree("two", 4))
     assert S.spreadable(synth.tree("glb3x2+nam1x1", 4))
     assert not S.spreadable(synth.tree("three", 4))
+
+
+@pytest.mark.gpu
+def test_timeline_of_a_spread_interval(built):
+    """The captured interval's timeline: the region bodies on their streams, inside the interval,
+    and the interval graph itself unchanged afterwards (its digest still the run's)."""
+    from pydyn_gb300.device import Device
+    from pydyn_gb300.forward import Forward
+    from pydyn_gb300.profile import timeline
+
+    dev = Device(0)
+    fw = Forward(dev, "two", 8, seed=3, physics=True, lmax=8)
+    for _ in range(2):
+        fw.interval(graph=True)
+    rows = timeline(fw, replays=2)
+    streams = {s for s, _, _, _ in rows}
+    assert {"main", "region2", "rehearsal", "kzz1", "kzz2"} <= streams
+    (b0, e0), = [(b, e) for s, p, b, e in rows if p == "interval"]
+    assert b0 == 0.0 and all(b0 <= b <= e <= e0 for _, p, b, e in rows)
+    assert any(p.startswith("convec_region") and s == "region2" for s, p, _, _ in rows)
+    fw.interval(graph=True)  # the recaptured interval still runs
+    fw.close()
+    dev.close()
