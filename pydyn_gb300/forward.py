@@ -24,7 +24,12 @@ from .state import TRACERS, ZoomState
 
 WINDOW = 6 * 3600.0
 SPECULATED = ("m", *TRACERS, "sp", "phlb")
-CHILD_PRIORITY = 2  # a child's side context: steps above the device's least stream priority
+# stream priorities of the captured interval's side contexts, in steps above the device's least
+# (the run's own stream and the Check_CFL rehearsal stay at the least): a child's chain of small
+# kernels is the interval's critical path, each region's Calc_Kzz gates its first convection, and
+# the rehearsal has the most slack -- measured on glb3x2+nam1x1, 6.49 -> 6.42 ms per interval
+CHILD_PRIORITY = 3
+KZZ_PRIORITY = 1
 
 
 def weights(t):
@@ -264,13 +269,13 @@ class Forward:
                 for r, prep in zip(self.zoom.regions(), self.prep, strict=True):
                     with self.dev.redirect(prep):
                         self.physics.prepare_region(self, r)
+                    prep.set_priority(KZZ_PRIORITY)
                     prep.sync()
             if self.zoom.nregions > 1 and spreadable(self.zoom):
                 # one per region for a child's share of the step, its work space as large as the
-                # run's own grew in its uncaptured interval.  Its streams get a higher priority:
-                # a child's chain of small kernels is the interval's critical path, and the block
-                # scheduler then serves it before the wide kernels beside it (the parent's, Calc_Kzz,
-                # the rehearsal), which have slack
+                # run's own grew in its uncaptured interval.  Its streams get the highest
+                # priority (CHILD_PRIORITY): the block scheduler then serves a child's chain before
+                # the wide kernels beside it
                 self.aux = [Device(self.dev.ordinal) for _ in self.zoom.regions()]
                 for aux in self.aux:
                     aux.reserve_work(self.dev.work_size())
