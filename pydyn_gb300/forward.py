@@ -30,6 +30,7 @@ SPECULATED = ("m", *TRACERS, "sp", "phlb")
 # the rehearsal has the most slack -- measured on glb3x2+nam1x1, 6.49 -> 6.42 ms per interval
 CHILD_PRIORITY = 3
 KZZ_PRIORITY = 1
+FAR_PRIORITY = 0  # region 1's physics on its far segment (slack until the parent's m2phlb1)
 
 
 def weights(t):
@@ -203,7 +204,10 @@ class Forward:
         sched = None
         if self.aux is not None and zoom.nregions > 1 and spreadable(zoom):
             # the step's bodies spread over one stream per region (pydyn_gb300.schedule)
-            sched = Scheduler(self.dev, {r: aux for r, aux in zip(zoom.regions(), self.aux, strict=True) if r != 1})
+            # region 1's own side context (its bodies run on the run's stream) takes its physics
+            # on the far segment
+            sched = Scheduler(self.dev, {r: aux for r, aux in zip(zoom.regions(), self.aux, strict=True) if r != 1},
+                              far=self.aux[0] if self.physics is not None else None)
             for name in ("sources", "chemistry"):
                 if name in kw:
                     kw[name] = scheduled_physics(sched, kw[name], name)
@@ -277,9 +281,9 @@ class Forward:
                 # priority (CHILD_PRIORITY): the block scheduler then serves a child's chain before
                 # the wide kernels beside it
                 self.aux = [Device(self.dev.ordinal) for _ in self.zoom.regions()]
-                for aux in self.aux:
+                for r, aux in zip(self.zoom.regions(), self.aux, strict=True):
                     aux.reserve_work(self.dev.work_size())
-                    aux.set_priority(CHILD_PRIORITY)
+                    aux.set_priority(CHILD_PRIORITY if r != 1 else FAR_PRIORITY)
                     aux.sync()
         self.dev.sync()
         self.graphs.pop("interval", None)

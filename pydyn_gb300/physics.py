@@ -143,15 +143,20 @@ class Physics:
         return self.driver_args()
 
     def join(self, region):
-        """A forked preparation of the region (pending) joins the step's stream here."""
-        dev_event = self.pending.pop(region, None)
+        """A forked preparation of the region (pending) joins the stream the caller enqueues on
+        (the device's current context): every stream that runs a body reading Calc_Kzz's
+        output waits for it -- a region's physics can run on more than one stream (its
+        segments) -- and a stream that waited already adds nothing but a redundant edge."""
+        dev_event = self.pending.get(region)
         if dev_event is not None:
             dev, event = dev_event
             dev.wait(event)
 
     def join_all(self):
+        """The run's stream waits for every forked preparation; the step is done with them."""
         for r in list(self.pending):
             self.join(r)
+        self.pending = {}
 
     def prepare_step(self, ndyn):
         """The step's half-step length and the step counter (convection's kept inverses)."""

@@ -62,10 +62,12 @@ def parts(name, region):
 
 class Scheduler:
     """The dependency tracker of one captured step: `streams` maps a region to the Device its
-    bodies run on (None: the run's own)."""
+    bodies run on (None: the run's own); `far`, when given, is the Device region 1's physics on
+    its far segment runs on (it shares nothing with a child, so it need not wait in the run's
+    stream behind the edge segment's bodies, which wait for update_parent)."""
 
-    def __init__(self, dev, streams):
-        self.dev, self.streams = dev, streams
+    def __init__(self, dev, streams, far=None):
+        self.dev, self.streams, self.far = dev, streams, far
         self.writer = {}  # part -> (stream key, sequence number, event)
         self.readers = {}  # part -> [(stream key, sequence number, event)]
         self.seq = 0
@@ -73,13 +75,18 @@ class Scheduler:
         self.last = {}  # stream key -> its last event
         self.keep = []  # the events, alive until the capture ends
 
-    def _key(self, region):
+    def _key(self, name, region):
+        if region == 1 and self.far is not None and name.endswith(":far") and name.partition(":")[0] in PHYSICS:
+            return "far"
         return region if self.streams.get(region) is not None else 1
+
+    def _device(self, key):
+        return self.far if key == "far" else (self.streams.get(key) if key != 1 else None)
 
     @contextmanager
     def body(self, name, region):
         """Run a body's enqueues inside this block on the region's stream, after its waits."""
-        key = self._key(region)
+        key = self._key(name, region)
         reads, writes = parts(name, region)
         waits = []
         for p in reads | writes:
@@ -94,7 +101,7 @@ class Scheduler:
                 latest[k] = (n, ev)
         for k, (n, _) in latest.items():
             self.waited[(key, k)] = n
-        side = self.streams.get(region) if key != 1 else None
+        side = self._device(key)
         ctx = self.dev.redirect(side) if side is not None else _nothing()
         with ctx:
             for _, ev in latest.values():
@@ -113,7 +120,8 @@ class Scheduler:
             self.readers.setdefault(p, []).append(entry)
 
     def join(self):
-        """The run's own stream waits for every other stream's last body."""
+        """The run's own stream waits for every other stream's last body (the far segment's
+        included)."""
         for k, ev in self.last.items():
             if k != 1:
                 self.dev.wait(ev)

@@ -36,9 +36,9 @@ class FakeDev:
             self.current = old
 
 
-def _run(bodies):
+def _run(bodies, far=None):
     dev = FakeDev()
-    sched = S.Scheduler(dev, {2: "child"})
+    sched = S.Scheduler(dev, {2: "child"}, far=far)
     waits = []
     for name, region in bodies:
         n0 = len(dev.log)
@@ -88,6 +88,23 @@ def test_child_physics_beside_the_parent_advection():
     assert waits[1] == [("wait", "main", "child")]
     assert waits[3] == [] and waits[4] == []
     assert waits[5] == [("wait", "child", "main")]
+
+
+def test_far_segment_physics_on_its_own_stream():
+    waits = _run([
+        ("_dynamw_region1", 1),       # 0: the parent's z on the run's stream
+        ("convec_region:far", 1),     # 1: on the far stream, after the parent's z
+        ("convec_region:edge", 1),    # 2: the run's stream, nothing new to wait for
+        ("chemistry:far", 1),         # 3: the far stream's own order
+        ("update_parent", 2),         # 4: the child writes the footprint (edge, core)
+        ("chemistry:edge", 1),        # 5: after update_parent
+        ("m2phlb1", 1),               # 6: the whole parent: after the far stream's last body
+    ], far="far")  # fmt: skip
+    assert waits[1] == [("wait", "far", "main")]
+    assert waits[2] == [] and waits[3] == []
+    assert waits[4] == [("wait", "child", "main")]  # the edge segment's readers on the run's stream
+    assert waits[5] == [("wait", "main", "child")]
+    assert waits[6] == [("wait", "main", "far")]
 
 
 def test_spreadable_trees():
