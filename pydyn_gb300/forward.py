@@ -31,7 +31,6 @@ SPECULATED = ("m", *TRACERS, "sp", "phlb")
 CHILD_PRIORITY = 3
 KZZ_PRIORITY = 1
 FAR_PRIORITY = 0  # region 1's physics on its far segment (slack until the parent's m2phlb1)
-EDGE_PRIORITY = 4  # region 1's physics on its edge segment: the critical path from update_parent on
 
 
 def weights(t):
@@ -75,7 +74,6 @@ class Forward:
         self.last = {}
         self.aux = None  # the captured interval's side contexts, one per region (a child's share of the step)
         self.prep = None  # the captured interval's Calc_Kzz contexts, one per region (with physics)
-        self.edge = None  # the captured interval's context for region 1's physics on its edge segment
         self.aux_cfl = None  # the captured interval's rehearsal context
         self._replays, self._side_per_replay = 0, 0
 
@@ -180,7 +178,7 @@ class Forward:
         conv = None
         joins = []
         forked = None
-        sides = self._sides()
+        sides = (self.prep or []) + (self.aux or [])
         if sides:  # the side contexts start from the step's own setup
             if self.physics is not None:
                 self.physics.prepare_step(self.nread)
@@ -207,10 +205,9 @@ class Forward:
         if self.aux is not None and zoom.nregions > 1 and spreadable(zoom):
             # the step's bodies spread over one stream per region (pydyn_gb300.schedule)
             # region 1's own side context (its bodies run on the run's stream) takes its physics
-            # on the far segment, a context of its own the edge segment's
-            segs = {"far": self.aux[0], "edge": self.edge} if self.physics is not None else {}
+            # on the far segment
             sched = Scheduler(self.dev, {r: aux for r, aux in zip(zoom.regions(), self.aux, strict=True) if r != 1},
-                              segments=segs)
+                              far=self.aux[0] if self.physics is not None else None)
             for name in ("sources", "chemistry"):
                 if name in kw:
                     kw[name] = scheduled_physics(sched, kw[name], name)
@@ -288,11 +285,6 @@ class Forward:
                     aux.reserve_work(self.dev.work_size())
                     aux.set_priority(CHILD_PRIORITY if r != 1 else FAR_PRIORITY)
                     aux.sync()
-                if self.physics is not None:
-                    self.edge = Device(self.dev.ordinal)  # region 1's edge-segment physics
-                    self.edge.reserve_work(self.dev.work_size())
-                    self.edge.set_priority(EDGE_PRIORITY)
-                    self.edge.sync()
         self.dev.sync()
         self.graphs.pop("interval", None)
         side0 = self._side_launches()
@@ -312,7 +304,7 @@ class Forward:
         nread, put the state back and redo the interval uncaptured.  Returns (ndyn, n)."""
         self.dev.sync_stream()  # the replay, the side contexts' branches included
         failed = self.aux_cfl.cfl_failed()  # the rehearsal's flag, on its context
-        for aux in self._sides():
+        for aux in (self.prep or []) + (self.aux or []):
             aux.sync()  # errors of the side contexts' kernels (Calc_Kzz, a child's) are raised here
         if failed:  # the speculation was wrong: back to the interval's start
             for (r, k), a in self._spec.items():
@@ -338,16 +330,12 @@ class Forward:
         if self.physics is not None:
             self.physics.free()
         self.w.free()
-        for aux in self._sides() + ([self.aux_cfl] if self.aux_cfl is not None else []):
+        for aux in (self.prep or []) + (self.aux or []) + ([self.aux_cfl] if self.aux_cfl is not None else []):
             aux.close()
-        self.prep, self.aux, self.edge, self.aux_cfl = None, None, None, None
-
-    def _sides(self):
-        """The captured interval's side contexts but the rehearsal's."""
-        return (self.prep or []) + (self.aux or []) + ([self.edge] if self.edge is not None else [])
+        self.prep, self.aux, self.aux_cfl = None, None, None
 
     def _side_launches(self):
-        side = self._sides() + ([self.aux_cfl] if self.aux_cfl is not None else [])
+        side = (self.prep or []) + (self.aux or []) + ([self.aux_cfl] if self.aux_cfl is not None else [])
         return sum(aux.launches() for aux in side)
 
     def launches(self):

@@ -100,9 +100,7 @@ class Timeline:
             return "main"
         if fw.aux_cfl is not None and h == fw.aux_cfl.h:
             return "rehearsal"
-        if fw.edge is not None and h == fw.edge.h:
-            return "edge1"
-        for kind, ctxs in (("kzz", fw.prep), ("region", fw.aux)):  # region1: its far segment's physics
+        for kind, ctxs in (("kzz", fw.prep), ("region", fw.aux)):
             for r, c in zip(fw.zoom.regions(), ctxs or (), strict=False):
                 if h == c.h:
                     return f"{kind}{r}"

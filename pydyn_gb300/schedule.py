@@ -62,14 +62,12 @@ def parts(name, region):
 
 class Scheduler:
     """The dependency tracker of one captured step: `streams` maps a region to the Device its
-    bodies run on (None: the run's own); `segments` maps a segment of region 1's owned columns
-    ("far", "edge") to the Device region 1's physics on that segment runs on.  The far segment
-    shares nothing with a child, so it need not wait in the run's stream behind the edge
-    segment's bodies, which wait for update_parent; the edge segment's bodies, on the step's
-    critical path from update_parent on, can run at a priority of their own."""
+    bodies run on (None: the run's own); `far`, when given, is the Device region 1's physics on
+    its far segment runs on (it shares nothing with a child, so it need not wait in the run's
+    stream behind the edge segment's bodies, which wait for update_parent)."""
 
-    def __init__(self, dev, streams, segments=None):
-        self.dev, self.streams, self.segments = dev, streams, dict(segments or {})
+    def __init__(self, dev, streams, far=None):
+        self.dev, self.streams, self.far = dev, streams, far
         self.writer = {}  # part -> (stream key, sequence number, event)
         self.readers = {}  # part -> [(stream key, sequence number, event)]
         self.seq = 0
@@ -78,15 +76,12 @@ class Scheduler:
         self.keep = []  # the events, alive until the capture ends
 
     def _key(self, name, region):
-        body, _, seg = name.partition(":")
-        if region == 1 and body in PHYSICS and self.segments.get(seg) is not None:
-            return seg
+        if region == 1 and self.far is not None and name.endswith(":far") and name.partition(":")[0] in PHYSICS:
+            return "far"
         return region if self.streams.get(region) is not None else 1
 
     def _device(self, key):
-        if isinstance(key, str):
-            return self.segments[key]
-        return self.streams.get(key) if key != 1 else None
+        return self.far if key == "far" else (self.streams.get(key) if key != 1 else None)
 
     @contextmanager
     def body(self, name, region):
@@ -125,7 +120,7 @@ class Scheduler:
             self.readers.setdefault(p, []).append(entry)
 
     def join(self):
-        """The run's own stream waits for every other stream's last body (the segments'
+        """The run's own stream waits for every other stream's last body (the far segment's
         included)."""
         for k, ev in self.last.items():
             if k != 1:

@@ -36,9 +36,9 @@ class FakeDev:
             self.current = old
 
 
-def _run(bodies, segments=None):
+def _run(bodies, far=None):
     dev = FakeDev()
-    sched = S.Scheduler(dev, {2: "child"}, segments=segments)
+    sched = S.Scheduler(dev, {2: "child"}, far=far)
     waits = []
     for name, region in bodies:
         n0 = len(dev.log)
@@ -99,28 +99,12 @@ def test_far_segment_physics_on_its_own_stream():
         ("update_parent", 2),         # 4: the child writes the footprint (edge, core)
         ("chemistry:edge", 1),        # 5: after update_parent
         ("m2phlb1", 1),               # 6: the whole parent: after the far stream's last body
-    ], segments={"far": "far"})  # fmt: skip
+    ], far="far")  # fmt: skip
     assert waits[1] == [("wait", "far", "main")]
     assert waits[2] == [] and waits[3] == []
     assert waits[4] == [("wait", "child", "main")]  # the edge segment's readers on the run's stream
     assert waits[5] == [("wait", "main", "child")]
     assert waits[6] == [("wait", "main", "far")]
-
-
-def test_edge_segment_physics_on_its_own_stream():
-    waits = _run([
-        ("_dynamw_region1", 1),       # 0: the run's stream
-        ("update_parent", 2),         # 1: after the parent's z (it reads the footprint's core)
-        ("convec_region:edge", 1),    # 2: on the edge stream, after update_parent (itself after the z)
-        ("convec_region:far", 1),     # 3: on the far stream, after the parent's z
-        ("chemistry:edge", 1),        # 4: the edge stream's own order
-        ("m2phlb1", 1),               # 5: after both segments and update_parent (the core)
-    ], segments={"far": "far", "edge": "edge"})  # fmt: skip
-    assert waits[1] == [("wait", "child", "main")]
-    assert waits[2] == [("wait", "edge", "child")]
-    assert waits[3] == [("wait", "far", "main")]
-    assert waits[4] == []
-    assert sorted(waits[5]) == [("wait", "main", "child"), ("wait", "main", "edge"), ("wait", "main", "far")]
 
 
 def test_spreadable_trees():
