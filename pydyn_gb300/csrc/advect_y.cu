@@ -4,8 +4,9 @@
 // reference does -- every column of the layer tried at n = 1, 2, ... until all pass -- with
 // the progressively rescaled faces recomputed from the untouched bm (the rescale is a fixed
 // chain per face), and rescales the faces of the halo'd layer that the columns do not own.
-// k_y_steps: one warp per (i, l) column stages the column in shared memory, runs the layer's
-// sub-steps on chip and writes the column and its faces (rescaled, then times nloop) once.
+// k_y_steps: one thread per (column, cell) over blocks of whole columns of one layer stages the
+// columns in shared memory, runs the layer's sub-steps on chip and writes the columns and their
+// faces (rescaled, then times nloop) once.
 // Two column kinds:
 //   polar  region 1: jm cells, jm+1 faces with the polar ones closed; flow out of a pole cell
 //          carries no slope; the pole cells keep rxm and rym
@@ -33,6 +34,7 @@ struct YArgs {
     int limits, nmax;
     int ncell;                // nc + 2
     int tc;                   // tracers staged at once (launch_y)
+    int P;                    // k_y_steps: columns (one layer's) per block
     int held;
     int32_t *nloop;           // nl, written by the search
     int32_t *nloop_out;
@@ -260,22 +262,48 @@ __global__ void __launch_bounds__(SEARCH_THREADS) k_y_search_done(YArgs A, YSear
     }
 }
 
+// Lines per block of k_y_steps for columns of nc cells: P = 32 / gcd(nc, 32), halved while the
+// block exceeds YMAX_THREADS -- a whole number of warps where it fits (8 held columns of 70
+// cells are 17.5 warps of which the last is half full, against 70 cells on 3 warps of 32)
+constexpr int YMAX_THREADS = 576;  // two blocks an SM at <= 56 registers a thread
+int y_lines_per_block(int nc) {
+    int g = 32, a = nc;
+    while (a % 2 == 0 && g > 1) { a /= 2; g /= 2; }  // g = 32 / gcd(nc, 32)
+    int P = g;
+    while (P > 1 && P * nc > YMAX_THREADS) P /= 2;
+    return P;
+}
+
+// One thread per (column, cell) over blocks of P columns of one layer (so the layer's nloop is
+// the block's): each block stages its columns in shared memory, runs the layer's sub-steps on
+// chip and writes the columns and their faces (rescaled, then times nloop) once.  A column's
+// threads meet at block barriers; the faces are staged and written back spread over the
+// block's threads.
 template <bool MASS_ONLY>
-__global__ void __launch_bounds__(STEP_WARPS * 32) k_y_steps(YArgs A) {
+__global__ void __launch_bounds__(YMAX_THREADS, 2) k_y_steps(YArgs A) {
     extern __shared__ double smem[];
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int64_t col = (int64_t)blockIdx.x * STEP_WARPS + warp;
-    if (col >= (int64_t)A.ni * A.nl) return;
-    if (MASS_ONLY && __shfl_sync(FULL_MASK, *(volatile int *)&A.ctl->cfl_failed, 0)) return;
-    const int i = (int)(col / A.nl), l = (int)(col % A.nl);
+    __shared__ int s_skip;
+    const int nc = A.nc, P = A.P, NC = A.ncell;
+    const int bpl = (A.ni + P - 1) / P;  // blocks per layer
+    const int l = blockIdx.x / bpl, i0 = (blockIdx.x % bpl) * P;
+    const int nlines = min(P, A.ni - i0);
+    const int p = threadIdx.x / nc, k = threadIdx.x % nc;  // the block's column, the thread's cell
+    const bool live = p < nlines;
+    const int i = i0 + p;
+    if (threadIdx.x == 0) s_skip = MASS_ONLY && *(volatile int *)&A.ctl->cfl_failed;  // block-uniform
+    __syncthreads();
+    if (s_skip) return;
     const int nloop = A.nloop[l];
     if (nloop > A.nmax) return;
     const bool held = A.held != 0;
-    const int nc = A.nc, nt = MASS_ONLY ? 0 : A.nt, NC = A.ncell;
+    const int nt = MASS_ONLY ? 0 : A.nt;
     const int tc = MASS_ONLY ? 0 : A.tc;  // tracers staged at once (a chunk)
     const int kf0 = held ? 1 : 0, kf1 = held ? nc - 1 : nc;  // faces held in smem (inclusive)
     const int c0 = held ? 1 : 0, c1 = held ? nc - 1 : nc;    // cells that move
-    double *m_s = smem + (size_t)warp * NC * (3 + 8 * tc);
+    const int nf = kf1 - kf0 + 1;
+    const bool moves = live && k >= c0 && k < c1;
+    const size_t per = (size_t)NC * (3 + 8 * tc);  // doubles of one column's shared memory
+    double *m_s = smem + p * per;
     double *b_s = m_s + NC;
     double *m0_s = b_s + NC;           // the staged mass, each chunk's start
     double *q_s = m0_s + NC;           // [4][tc]: rm, rxm, rym, rzm
@@ -283,108 +311,114 @@ __global__ void __launch_bounds__(STEP_WARPS * 32) k_y_steps(YArgs A) {
     auto Q = [&](int w, int t) { return q_s + (size_t)(w * tc + t) * NC; };
     auto F = [&](int w, int t) { return f_s + (size_t)(w * tc + t) * NC; };
 
-    for (int k = kf0 + lane; k <= kf1; k += GB_WARP) b_s[k] = progressive_chain(BF(A, i, k, l), nloop);
-    for (int k = lane; k < nc; k += GB_WARP) {
+    for (int e = threadIdx.x; e < nlines * nf; e += blockDim.x) {  // every column's faces
+        const int q = e / nf, kk = kf0 + e % nf;
+        smem[q * per + NC + kk] = progressive_chain(BF(A, i0 + q, kk, l), nloop);
+    }
+    if (live) {
         m_s[k] = AT(A.m, i, k, l);
         m0_s[k] = m_s[k];
     }
-    __syncwarp();
+    __syncthreads();
 
-    if (MASS_ONLY) {  // dynamvm: the layer's nloop advances, then b * nloop
-        for (int s = 0; s < nloop; ++s) {
-            for (int k = c0 + lane; k < c1; k += GB_WARP) m_s[k] = (m_s[k] + b_s[k]) - b_s[k + 1];
-            __syncwarp();
-        }
-        for (int k = c0 + lane; k < c1; k += GB_WARP) AT(A.m, i, k, l) = m_s[k];
+    if constexpr (MASS_ONLY) {  // dynamvm: the layer's nloop advances, then b * nloop
+        for (int s = 0; s < nloop; ++s)  // each thread its own cell
+            if (moves) m_s[k] = (m_s[k] + b_s[k]) - b_s[k + 1];
+        if (moves) AT(A.m, i, k, l) = m_s[k];
         if (nloop > 1)
-            for (int k = kf0 + lane; k <= kf1; k += GB_WARP) BF(A, i, k, l) = b_s[k] * (double)nloop;
-        return;
-    }
-
-    // the tracers, tc at a time: each chunk restarts from the staged mass and repeats the same
-    // mass updates; tracers never mix, so the chunking changes no value
-    for (int t0 = 0; t0 < nt; t0 += tc) {
-        const int ntc = min(tc, nt - t0);
-        for (int k = lane; k < nc; k += GB_WARP) {
-            m_s[k] = m0_s[k];
-            for (int w = 0; w < 4; ++w)
-                for (int t = 0; t < ntc; ++t) Q(w, t)[k] = AT4(A.q[w], i, k, l, t0 + t);
-            if (A.limits)  // every cell of the column, the poles / held ends included
-                for (int t = 0; t < ntc; ++t) Q(2, t)[k] = np_limit(Q(2, t)[k], Q(0, t)[k]);
-        }
-        if (!held && lane == 0)  // closed polar faces
-            for (int w = 0; w < 4; ++w)
-                for (int t = 0; t < ntc; ++t) F(w, t)[0] = F(w, t)[nc] = 0.0;
-        __syncwarp();
-
-        for (int s = 0; s < nloop; ++s) {
-            for (int k = 1 + lane; k < nc; k += GB_WARP) {
-                const double bk = b_s[k];
-                const int up = (bk >= 0.0) ? k - 1 : k;
-                const double beta = bk / m_s[up];
-                for (int t = 0; t < ntc; ++t) {
-                    double f, pf, fx, fz;
-                    // the along slope is rym, the cross slopes rxm, rzm
-                    slopes_flux(bk, beta, Q(0, t)[up], Q(2, t)[up], Q(1, t)[up], Q(3, t)[up], f, pf, fx, fz);
-                    if (!held) {  // flow out of a pole cell carries no slope (Fortran faces 2 and jmr)
-                        if (k == 1 && bk >= 0.0) {
-                            f = beta * Q(0, t)[0];
-                            pf = (-3.0 * bk) * f;
-                            fx = 0.0;
-                            fz = beta * Q(3, t)[0];
-                        }
-                        if (k == nc - 1 && bk < 0.0) {
-                            f = beta * Q(0, t)[nc - 1];
-                            pf = (-3.0 * bk) * f;
-                            fx = 0.0;
-                            fz = beta * Q(3, t)[nc - 1];
-                        }
-                    }
-                    F(0, t)[k] = f; F(1, t)[k] = pf; F(2, t)[k] = fx; F(3, t)[k] = fz;
-                }
+            for (int e = threadIdx.x; e < nlines * nf; e += blockDim.x) {
+                const int q = e / nf, kk = kf0 + e % nf;
+                BF(A, i0 + q, kk, l) = smem[q * per + NC + kk] * (double)nloop;
             }
-            __syncwarp();
-            for (int j = c0 + lane; j < c1; j += GB_WARP) {
-                const double mo = m_s[j], blo = b_s[j], bhi = b_s[j + 1];
-                const double mn = (mo + blo) - bhi;
-                const double inv = 1.0 / mn;  // production dynamv hoists the reciprocal
-                const double fc = blo - bhi;
-                const double fm = 3.0 * (blo + bhi);
-                const double mx3 = 3.0 * mo;
-                const bool pole = !held && ((j == 0) || (j == nc - 1));
-                for (int t = 0; t < ntc; ++t) {
-                    const double *f = F(0, t), *pf = F(1, t), *fx = F(2, t), *fz = F(3, t);
-                    // region 1: rm - (f(j+1) - f(j)); a child: rm + (f(j) - f(j+1))
-                    const double rmn = held ? Q(0, t)[j] + (f[j] - f[j + 1]) : Q(0, t)[j] - (f[j + 1] - f[j]);
-                    const double ry = Q(2, t)[j];
-                    double ryn = ry + ((((pf[j] - pf[j + 1]) - fc * ry) + fm * rmn) - mx3 * (f[j] + f[j + 1])) * inv;
-                    if (A.limits) ryn = np_limit(ryn, rmn);
-                    const double rx = Q(1, t)[j], rz = Q(3, t)[j];
-                    const double rxn = held ? rx + (fx[j] - fx[j + 1]) : rx - (fx[j + 1] - fx[j]);
-                    Q(3, t)[j] = held ? rz + (fz[j] - fz[j + 1]) : rz - (fz[j + 1] - fz[j]);
-                    Q(0, t)[j] = rmn;
-                    if (!pole) {  // the poles keep rxm, rym (only rm, rzm are updated there)
-                        Q(2, t)[j] = ryn;
-                        Q(1, t)[j] = rxn;
+    } else {
+        // the tracers, tc at a time: each chunk restarts from the staged mass and repeats the same
+        // mass updates; tracers never mix, so the chunking changes no value
+        for (int t0 = 0; t0 < nt; t0 += tc) {
+            const int ntc = min(tc, nt - t0);
+            if (live) {
+                m_s[k] = m0_s[k];
+                for (int w = 0; w < 4; ++w)
+                    for (int t = 0; t < ntc; ++t) Q(w, t)[k] = AT4(A.q[w], i, k, l, t0 + t);
+                if (A.limits)  // every cell of the column, the poles / held ends included
+                    for (int t = 0; t < ntc; ++t) Q(2, t)[k] = np_limit(Q(2, t)[k], Q(0, t)[k]);
+                if (!held && k == 0)  // closed polar faces
+                    for (int w = 0; w < 4; ++w)
+                        for (int t = 0; t < ntc; ++t) F(w, t)[0] = F(w, t)[nc] = 0.0;
+            }
+            __syncthreads();
+
+            for (int s = 0; s < nloop; ++s) {
+                if (live && k >= 1) {  // the interior faces 1 .. nc-1
+                    const double bk = b_s[k];
+                    const int up = (bk >= 0.0) ? k - 1 : k;
+                    const double beta = bk / m_s[up];
+                    for (int t = 0; t < ntc; ++t) {
+                        double f, pf, fx, fz;
+                        // the along slope is rym, the cross slopes rxm, rzm
+                        slopes_flux(bk, beta, Q(0, t)[up], Q(2, t)[up], Q(1, t)[up], Q(3, t)[up], f, pf, fx, fz);
+                        if (!held) {  // flow out of a pole cell carries no slope (Fortran faces 2 and jmr)
+                            if (k == 1 && bk >= 0.0) {
+                                f = beta * Q(0, t)[0];
+                                pf = (-3.0 * bk) * f;
+                                fx = 0.0;
+                                fz = beta * Q(3, t)[0];
+                            }
+                            if (k == nc - 1 && bk < 0.0) {
+                                f = beta * Q(0, t)[nc - 1];
+                                pf = (-3.0 * bk) * f;
+                                fx = 0.0;
+                                fz = beta * Q(3, t)[nc - 1];
+                            }
+                        }
+                        F(0, t)[k] = f; F(1, t)[k] = pf; F(2, t)[k] = fx; F(3, t)[k] = fz;
                     }
                 }
-                m_s[j] = mn;
+                __syncthreads();
+                if (moves) {
+                    const int j = k;
+                    const double mo = m_s[j], blo = b_s[j], bhi = b_s[j + 1];
+                    const double mn = (mo + blo) - bhi;
+                    const double inv = 1.0 / mn;  // production dynamv hoists the reciprocal
+                    const double fc = blo - bhi;
+                    const double fm = 3.0 * (blo + bhi);
+                    const double mx3 = 3.0 * mo;
+                    const bool pole = !held && ((j == 0) || (j == nc - 1));
+                    for (int t = 0; t < ntc; ++t) {
+                        const double *f = F(0, t), *pf = F(1, t), *fx = F(2, t), *fz = F(3, t);
+                        // region 1: rm - (f(j+1) - f(j)); a child: rm + (f(j) - f(j+1))
+                        const double rmn = held ? Q(0, t)[j] + (f[j] - f[j + 1]) : Q(0, t)[j] - (f[j + 1] - f[j]);
+                        const double ry = Q(2, t)[j];
+                        double ryn = ry + ((((pf[j] - pf[j + 1]) - fc * ry) + fm * rmn) - mx3 * (f[j] + f[j + 1])) * inv;
+                        if (A.limits) ryn = np_limit(ryn, rmn);
+                        const double rx = Q(1, t)[j], rz = Q(3, t)[j];
+                        const double rxn = held ? rx + (fx[j] - fx[j + 1]) : rx - (fx[j + 1] - fx[j]);
+                        Q(3, t)[j] = held ? rz + (fz[j] - fz[j + 1]) : rz - (fz[j + 1] - fz[j]);
+                        Q(0, t)[j] = rmn;
+                        if (!pole) {  // the poles keep rxm, rym (only rm, rzm are updated there)
+                            Q(2, t)[j] = ryn;
+                            Q(1, t)[j] = rxn;
+                        }
+                    }
+                    m_s[j] = mn;
+                }
+                __syncthreads();
             }
-            __syncwarp();
+            if (moves)
+                for (int w = 0; w < 4; ++w)
+                    for (int t = 0; t < ntc; ++t) AT4(A.q[w], i, k, l, t0 + t) = Q(w, t)[k];
+            if (live && held && A.limits && k == 0)  // the held ends keep their limited rym
+                for (int t = 0; t < ntc; ++t) {
+                    AT4(A.q[2], i, 0, l, t0 + t) = Q(2, t)[0];
+                    AT4(A.q[2], i, nc - 1, l, t0 + t) = Q(2, t)[nc - 1];
+                }
+            __syncthreads();  // the next chunk overwrites the staged tracers
         }
-        for (int k = c0 + lane; k < c1; k += GB_WARP)
-            for (int w = 0; w < 4; ++w)
-                for (int t = 0; t < ntc; ++t) AT4(A.q[w], i, k, l, t0 + t) = Q(w, t)[k];
-        if (held && A.limits && lane == 0)  // the held ends keep their limited rym
-            for (int t = 0; t < ntc; ++t) {
-                AT4(A.q[2], i, 0, l, t0 + t) = Q(2, t)[0];
-                AT4(A.q[2], i, nc - 1, l, t0 + t) = Q(2, t)[nc - 1];
-            }
-        __syncwarp();  // the next chunk overwrites the staged tracers
+        if (moves) AT(A.m, i, k, l) = m_s[k];
+        for (int e = threadIdx.x; e < nlines * nf; e += blockDim.x) {
+            const int q = e / nf, kk = kf0 + e % nf;
+            BF(A, i0 + q, kk, l) = smem[q * per + NC + kk] * (double)nloop;
+        }
     }
-
-    for (int k = c0 + lane; k < c1; k += GB_WARP) AT(A.m, i, k, l) = m_s[k];
-    for (int k = kf0 + lane; k <= kf1; k += GB_WARP) BF(A, i, k, l) = b_s[k] * (double)nloop;
 }
 
 // tracers a warp stages at once: as many as fit in the block's shared memory (all when they do)
@@ -429,14 +463,25 @@ int launch_y(gb_ctx *ctx, YArgs &A, int32_t *scratch = nullptr) {
         k_y_search<<<A.nl, SEARCH_THREADS, smem_s, ctx->stream>>>(A);
         if (int rc = gb_after_launch(ctx, "y_search")) return rc;
     }
-    A.tc = A.mass_only ? 0 : tracer_chunk(STEP_WARPS, A.ncell, 3, 8, A.nt);
-    size_t smem = (size_t)STEP_WARPS * A.ncell * (3 + 8 * A.tc) * sizeof(double);
+    if (A.nc > YMAX_THREADS) {
+        gb_set_error("gb_advect_y: at most 576 cells a column");
+        return GB_EARG;
+    }
+    A.P = y_lines_per_block(A.nc);
+    A.tc = A.mass_only ? 0 : tracer_chunk(A.P, A.ncell, 3, 8, A.nt);
+    const size_t smem = (size_t)A.P * A.ncell * (3 + 8 * A.tc) * sizeof(double);
+    if (smem > 227 * 1024) {
+        gb_set_error("gb_advect_y: the columns of a block do not fit in shared memory");
+        return GB_EARG;
+    }
+    const int sthreads = (A.P * A.nc + 31) / 32 * 32;
+    const int sblocks = A.nl * ((A.ni + A.P - 1) / A.P);
     if (A.mass_only) {
         GB_CHECK_CUDA(cudaFuncSetAttribute(k_y_steps<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-        k_y_steps<true><<<blocks, STEP_WARPS * 32, smem, ctx->stream>>>(A);
+        k_y_steps<true><<<sblocks, sthreads, smem, ctx->stream>>>(A);
     } else {
         GB_CHECK_CUDA(cudaFuncSetAttribute(k_y_steps<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-        k_y_steps<false><<<blocks, STEP_WARPS * 32, smem, ctx->stream>>>(A);
+        k_y_steps<false><<<sblocks, sthreads, smem, ctx->stream>>>(A);
     }
     return gb_after_launch(ctx, A.mass_only ? "cfl_y" : "y_steps");
 }
