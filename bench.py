@@ -56,7 +56,8 @@ BYTES_PER_CELL = {"_dynamu_region1": 12, "_dynamv_region1": 12, "_dynamw_region1
 
 
 # DRAM bytes (read + write) per call of a body, from one ncu capture of an eager interval of
-# glb3x2+nam1x1 with physics (profiles/interval_dram_fp64_glb3x2+nam1x1.md): the roofline's traffic
+# glb3x2+nam1x1 with physics (dram__bytes_read.sum + dram__bytes_write.sum of the body's kernels,
+# averaged over its calls; the parent's per v, both segments): the roofline's traffic
 TRAFFIC_PER_CALL = {"glb3x2+nam1x1": {"convec_region@2": 132.3e6, "convec_region@1": 250.5e6}}
 
 
