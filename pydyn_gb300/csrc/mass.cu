@@ -1,4 +1,5 @@
-// dynam0 and m2phlb: the per-half-step mass fluxes from the meteo fluxes, and the surface
+// dynam0 (k_fluxes_ambm elementwise, k_fluxes_cm the columns' serial sums) and m2phlb: the
+// per-half-step mass fluxes from the meteo fluxes, and the surface
 // pressure / half-level pressures from the column mass.
 // Reference: pydyn kernels.py:102-125 (fluxes_from_meteo), ops.py:273-274 (convergence),
 // zoom/massflow.py:24-56 (m2phlb1, m2phlb), balance.py:222-226.
@@ -21,28 +22,25 @@ __device__ __forceinline__ double convergence(const DV &pu, const DV &pv, int i,
     return ((AT(pu, i, j, l) - AT(pu, i + 1, j, l)) + AT(pv, i, j, l)) - AT(pv, i, j + 1, l);
 }
 
-// One thread per (i, j) of the face grid [0, im] x [0, jm]: its am column (j < jm), its bm
-// column (i < im) and, for a cell column, cm from the convergence distributed by the hybrid b.
-__global__ void k_fluxes(DV pu, DV pv, const double *bt, double dt, DV am, DV bm, DV cm, int im, int jm, int lm) {
+// One thread per (i, j, l) of the face grid [0, im] x [0, jm] x lm: am = dt pu (j < jm) and
+// bm = dt pv (i < im), element by element.
+__global__ void k_fluxes_ambm(DV pu, DV pv, double dt, DV am, DV bm, int im, int jm, int lm) {
+    const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (t >= (int64_t)(im + 1) * (jm + 1) * lm) return;
+    const int l = (int)(t % lm);
+    const int64_t c = t / lm;
+    const int i = (int)(c / (jm + 1)), j = (int)(c % (jm + 1));
+    if (j < jm) AT(am, i, j, l) = dt * AT(pu, i, j, l);
+    if (i < im) AT(bm, i, j, l) = dt * AT(pv, i, j, l);
+}
+
+// One thread per cell column (i, j) of [0, im) x [0, jm): cm from the convergence distributed by
+// the hybrid b (the column's serial sums).
+__global__ void k_fluxes_cm(DV pu, DV pv, const double *bt, double dt, DV cm, int im, int jm, int lm) {
     int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-    if (k >= (int64_t)(im + 1) * (jm + 1)) return;
-    const int i = (int)(k / (jm + 1)), j = (int)(k % (jm + 1));
-    for (int l0 = 0; l0 < lm; l0 += B) {
-        double a[B], b[B];
-#pragma unroll
-        for (int u = 0; u < B; ++u)
-            if (l0 + u < lm) {
-                if (j < jm) a[u] = AT(pu, i, j, l0 + u);
-                if (i < im) b[u] = AT(pv, i, j, l0 + u);
-            }
-#pragma unroll
-        for (int u = 0; u < B; ++u)
-            if (l0 + u < lm) {
-                if (j < jm) AT(am, i, j, l0 + u) = dt * a[u];
-                if (i < im) AT(bm, i, j, l0 + u) = dt * b[u];
-            }
-    }
-    if (i < im && j < jm) {
+    if (k >= (int64_t)im * jm) return;
+    const int i = (int)(k / jm), j = (int)(k % jm);
+    {
         // pit = the column sum of the convergence, bottom-up
         double pit = 0.0;
         for (int l0 = 0; l0 < lm; l0 += B) {
@@ -108,10 +106,11 @@ extern "C" int gb_fluxes_from_meteo(gb_ctx *ctx, const gb_view *pu, const gb_vie
         gb_set_error("gb_fluxes_from_meteo: inconsistent shapes");
         return GB_EARG;
     }
-    int64_t total = (int64_t)(im + 1) * (jm + 1);
-    k_fluxes<<<(int)((total + 127) / 128), 128, 0, ctx->stream>>>(dv(pu), dv(pv), bt, dt, dv(am), dv(bm), dv(cm), im,
-                                                                  jm, lm);
-    return gb_after_launch(ctx, "fluxes_from_meteo");
+    const int64_t faces = (int64_t)(im + 1) * (jm + 1) * lm, cols = (int64_t)im * jm;
+    k_fluxes_ambm<<<(int)((faces + 255) / 256), 256, 0, ctx->stream>>>(dv(pu), dv(pv), dt, dv(am), dv(bm), im, jm, lm);
+    if (int rc = gb_after_launch(ctx, "fluxes_ambm")) return rc;
+    k_fluxes_cm<<<(int)((cols + 63) / 64), 64, 0, ctx->stream>>>(dv(pu), dv(pv), bt, dt, dv(cm), im, jm, lm);
+    return gb_after_launch(ctx, "fluxes_cm");
 }
 
 extern "C" int gb_m2phlb(gb_ctx *ctx, const gb_view *m, const gb_view *sp, const gb_view *phlb, const double *dxyp,
