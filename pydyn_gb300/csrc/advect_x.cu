@@ -61,7 +61,7 @@ __device__ int row_search(double *m_s, double *mx_s, double *a_s, int n, bool he
             double cmax = 0.0;
             for (int k = k0 + lane; k <= k1; k += GB_WARP) {
                 double f = a_s[k];
-                int up = (f >= 0.0) ? (k == 0 ? n - 1 : k - 1) : (k == n ? 0 : k);
+                int up = ge_zero(f) ? (k == 0 ? n - 1 : k - 1) : (k == n ? 0 : k);
                 if (want_amax) {
                     double c = gb_abs(f / mx_s[up]);
                     lok = lok && (c < 1.0);
@@ -185,7 +185,7 @@ __global__ void __launch_bounds__(WARPS * 32) k_advect_x(XArgs A) {
             for (int s = 0; s < nloop; ++s) {
                 for (int k = k0 + lane; k <= k1; k += GB_WARP) {
                     double f = a_s[k];
-                    int up = (f >= 0.0) ? k - 1 : (k == n ? 0 : k);
+                    int up = ge_zero(f) ? k - 1 : (k == n ? 0 : k);
                     double alpha = f * minv_s[up];  // the reciprocal form of production dynamu
                     for (int t = 0; t < ntc; ++t) {
                         double ff, pf, fy, fz;

@@ -68,7 +68,7 @@ __device__ bool column_trial(const YArgs &A, int i, int l, int n, double *mx, do
         bool lok = true;
         for (int k = k0 + lane; k <= k1 - (A.held ? 0 : 0) && k < nc; k += GB_WARP) {
             double f = bf[k];
-            double mu = (f >= 0.0) ? mx[k - 1] : mx[k];
+            double mu = ge_zero(f) ? mx[k - 1] : mx[k];
             lok = lok && cfl_pass(f, mu);
         }
         if (!__all_sync(FULL_MASK, lok)) return false;
@@ -350,20 +350,20 @@ __global__ void __launch_bounds__(YMAX_THREADS, 2) k_y_steps(YArgs A) {
             for (int s = 0; s < nloop; ++s) {
                 if (live && k >= 1) {  // the interior faces 1 .. nc-1
                     const double bk = b_s[k];
-                    const int up = (bk >= 0.0) ? k - 1 : k;
+                    const int up = ge_zero(bk) ? k - 1 : k;
                     const double beta = bk / m_s[up];
                     for (int t = 0; t < ntc; ++t) {
                         double f, pf, fx, fz;
                         // the along slope is rym, the cross slopes rxm, rzm
                         slopes_flux(bk, beta, Q(0, t)[up], Q(2, t)[up], Q(1, t)[up], Q(3, t)[up], f, pf, fx, fz);
                         if (!held) {  // flow out of a pole cell carries no slope (Fortran faces 2 and jmr)
-                            if (k == 1 && bk >= 0.0) {
+                            if (k == 1 && ge_zero(bk)) {
                                 f = beta * Q(0, t)[0];
                                 pf = (-3.0 * bk) * f;
                                 fx = 0.0;
                                 fz = beta * Q(3, t)[0];
                             }
-                            if (k == nc - 1 && bk < 0.0) {
+                            if (k == nc - 1 && lt_zero(bk)) {
                                 f = beta * Q(0, t)[nc - 1];
                                 pf = (-3.0 * bk) * f;
                                 fx = 0.0;

@@ -96,7 +96,7 @@ __device__ void z_trials(const ZArgs &A, ZCol *zc, double *mx, double *cf, int p
         const bool run = mine && s < zc[p].n && zc[p].state == 1;
         if (run && k >= 1) {
             const double ck = c[k];
-            const double mu = (ck >= 0.0) ? x[k - 1] : x[k];
+            const double mu = ge_zero(ck) ? x[k - 1] : x[k];
             if (!cfl_pass(ck, mu)) zc[p].state = 2;  // every failing thread writes the same value
         }
         __syncthreads();
@@ -249,7 +249,7 @@ __global__ void __launch_bounds__(MAX_THREADS, 2) k_z_steps(ZArgs A) {
             for (int s = 0; s < n; ++s) {
                 if (live && k >= 1) {
                     const double ck = c_s[k];
-                    const int up = (ck >= 0.0) ? k - 1 : k;
+                    const int up = ge_zero(ck) ? k - 1 : k;
                     const double gamma = ck / m_s[up];
                     for (int t = 0; t < ntc; ++t) {
                         double f, pf, fx, fy;

@@ -69,11 +69,6 @@ __device__ __forceinline__ double &AT4(const DV &v, int64_t i, int64_t j, int64_
 __device__ __forceinline__ double max0(double x) { return gb_isnan(x) ? x : (0.0 > x ? 0.0 : x); }
 // x == 0.0 (either sign), tested on the integer pipe: the FP64 pipe is kept for arithmetic
 __device__ __forceinline__ bool is_zero(double x) { return (__double_as_longlong(x) << 1) == 0; }
-// x >= 0.0 on the integer pipe: +0 up to +inf, or -0 (a NaN compares false)
-__device__ __forceinline__ bool ge_zero(double x) {
-    const unsigned long long b = (unsigned long long)__double_as_longlong(x);
-    return b <= 0x7ff0000000000000ULL || b == 0x8000000000000000ULL;
-}
 
 // the work space's per-column chains amu, zu, amd, zd (n+1 each, indexed by level k = 0..n)
 constexpr int NCHAIN = 4;

@@ -119,6 +119,17 @@ __device__ __forceinline__ double div_by_recip(double a, double d, double y) {
     return a / d;
 }
 
+// x >= 0.0 and x < 0.0 on the integer pipe (an FP64 compare issues on the FP64 pipe): >= holds
+// from +0 to +inf and at -0; < from the smallest negative to -inf; a NaN fails both
+__device__ __forceinline__ bool ge_zero(double x) {
+    const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+    return b <= 0x7ff0000000000000ULL || b == 0x8000000000000000ULL;
+}
+__device__ __forceinline__ bool lt_zero(double x) {
+    const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+    return b > 0x8000000000000000ULL && b <= 0xfff0000000000000ULL;
+}
+
 // ------------------------------------------------------------------ NumPy's element rules
 // np.clip(s, -|r|, |r|) exactly as NumPy evaluates it: a NaN in s wins, then max with the lower
 // bound ((s > lo) ? s : lo), then a NaN wins again, then min with the upper bound.
@@ -143,7 +154,7 @@ __device__ __forceinline__ void slopes_flux(double flux, double c, double rm_u, 
                                             double t_u, double w_u, double &f, double &pf,
                                             double &ft, double &fw) {
     double ff;
-    if (flux >= 0.0)
+    if (ge_zero(flux))
         ff = c * (rm_u + (1.0 - c) * s_u);
     else
         ff = c * (rm_u - (1.0 + c) * s_u);
