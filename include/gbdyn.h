@@ -124,6 +124,11 @@ int gb_iadd(gb_ctx *ctx, int32_t *counter, int delta);
  * kernel, capturable): the timeline of a captured interval's streams
  * (python -m pydyn_gb300.profile --timeline).  No reference counterpart. */
 int gb_stamp(gb_ctx *ctx, uint64_t *buf, int slot);
+/* n device-to-device copies in one launch: `table` (device memory, 3n uint64) holds each copy's
+ * destination, source and byte count (a multiple of 8, each at most max_bytes, the ranges
+ * disjoint): a captured interval's first copies (its speculation backup) in one node instead of
+ * one each.  No reference counterpart. */
+int gb_copy_many(gb_ctx *ctx, const uint64_t *table, int n, size_t max_bytes);
 /* dst = seqsum of src over `axis` (src's extent along it), accumulated in index order
  * (ops.seqsum, ops.py:235); dst has src's extents with that axis dropped (n = 1). */
 int gb_seqsum(gb_ctx *ctx, const gb_view *dst, const gb_view *src, int axis, double post_mul);

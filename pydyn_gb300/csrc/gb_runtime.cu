@@ -411,6 +411,27 @@ extern "C" int gb_iadd(gb_ctx *ctx, int32_t *counter, int delta) {
     return gb_after_launch(ctx, "iadd");
 }
 
+// n device-to-device copies in one launch: table[3b .. 3b+2] = (dst, src, bytes) of copy b (blocks
+// along y), 8-byte elements
+__global__ void k_copy_many(const unsigned long long *table) {
+    const int b = blockIdx.y;
+    double *dst = reinterpret_cast<double *>(table[3 * b]);
+    const double *src = reinterpret_cast<const double *>(table[3 * b + 1]);
+    const unsigned long long cnt = table[3 * b + 2] / 8;
+    for (unsigned long long e = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x; e < cnt;
+         e += (unsigned long long)gridDim.x * blockDim.x)
+        dst[e] = src[e];
+}
+
+extern "C" int gb_copy_many(gb_ctx *ctx, const uint64_t *table, int n, size_t max_bytes) {
+    if (!ctx || (n > 0 && !table) || n < 0 || n > 65535 || max_bytes % 8 != 0) return GB_EARG;
+    if (n == 0 || max_bytes == 0) return GB_OK;
+    const unsigned long long elems = max_bytes / 8;
+    const unsigned gx = (unsigned)((elems + 255) / 256 < 1024 ? (elems + 255) / 256 : 1024);
+    k_copy_many<<<dim3(gx, (unsigned)n), 256, 0, ctx->stream>>>(reinterpret_cast<const unsigned long long *>(table));
+    return gb_after_launch(ctx, "copy_many");
+}
+
 // the GPU's global nanosecond timer when the stream reaches this point
 __global__ void k_stamp(unsigned long long *buf, int slot) {
     unsigned long long t;

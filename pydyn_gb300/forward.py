@@ -16,6 +16,7 @@ graph serves every step."""
 
 import numpy as np
 
+from . import _native as N
 from . import driver as D
 from . import synth
 from .device import DevArray, Device
@@ -158,11 +159,9 @@ class Forward:
         Every kernel gets the inputs of the sequential order; only the overlap is new."""
         zoom, cst, st = self.zoom, self.cfl_st, self.st
         lib = st.lib
-        for r in zoom.regions():
-            for name in SPECULATED:
-                self._spec[(r, name)].assign(st[r][name])
-            for name in ("m", "sp"):
-                cst[r][name].assign(st[r][name])
+        # the speculation's backup and the rehearsal's m and sp: one launch of every copy
+        table, n, most = self._prologue
+        N.check(self.dev.L.gb_copy_many(self.dev.h, table.ptr, n, most), "gb_copy_many")
         fork = self.dev.event()
         fork.record()
         self.aux_cfl.wait(fork)
@@ -257,6 +256,15 @@ class Forward:
             self._spec = {(r, k): DevArray.zeros(self.dev, *((lo, lo + n - 1) for lo, n in
                                                          zip(a.lower, a.shape, strict=True)))
                           for r in self.zoom.regions() for k, a in self.st[r].items() if k in SPECULATED}  # fmt: skip
+            pairs = [(self._spec[(r, k)], self.st[r][k]) for r in self.zoom.regions() for k in SPECULATED]
+            pairs += [(self.cfl_st[r][k], self.st[r][k]) for r in self.zoom.regions() for k in ("m", "sp")]
+            rows = []
+            for dst, src in pairs:  # whole arrays of one layout: flat copies
+                if not (dst.contiguous() and src.contiguous() and dst.shape == src.shape and dst.dtype == src.dtype):
+                    raise RuntimeError("capture_interval: a speculated array is not a whole contiguous array")
+                rows.append((dst.ptr, src.ptr, dst.size * dst.dtype.itemsize))
+            self._prologue = (DevArray.from_host(self.dev, np.array(rows, dtype=np.uint64)), len(rows),
+                              max(b for _, _, b in rows))
         self.st.lib.save(self.cfl_st, "check_cfl", ("m", "am", "bm", "cm"))
         if self.aux_cfl is None:
             # the captured interval's side contexts, their work spaces and scratch sized by one
@@ -327,6 +335,8 @@ class Forward:
                 pv.free()
         for a in getattr(self, "_spec", {}).values():
             a.free()
+        if hasattr(self, "_prologue"):
+            self._prologue[0].free()
         if self.physics is not None:
             self.physics.free()
         self.w.free()
