@@ -61,6 +61,14 @@ BYTES_PER_CELL = {"_dynamu_region1": 12, "_dynamv_region1": 12, "_dynamw_region1
 TRAFFIC_PER_CALL = {"glb3x2+nam1x1": {"convec_region@2": 132.3e6, "convec_region@1": 250.5e6}}
 
 
+def workload_config(workload, n_gpus):
+    """The `config` of a workload's line, the same in both arms."""
+    tree, lm, physics, seed, lmax = WORKLOADS[workload]
+    return {"workload": workload, "tree": tree, "levels": lm, "nt": 1, "physics": physics, "lmax": lmax,
+            "seed": seed, "step": "Check_CFL rehearsal + Setup_MassFlow + xyzvsc|csvzyx (one read interval)",
+            "l2": "flushed between timed steps (256 MiB write)", "parallelism": f"replicas x{n_gpus}"}  # fmt: skip
+
+
 def metric_name(workload):
     """The headline metric's name for the full-physics glb3x2 + nam1x1 tree, else the workload's."""
     if workload == "glb3x2+nam1x1":
@@ -167,7 +175,8 @@ def run_reference_ensemble(args):
     """The reference arm of the ensemble: the oracle port looped over the members, timed on a
     bounded sample -- one interval of one member of each class -- and scaled by the mix."""
     from oracle.forward import OracleRun
-    from pydyn_gb300.ensemble import CLASSES, MIX
+    from pydyn_gb300.synth import ENSEMBLE_CLASSES as CLASSES
+    from pydyn_gb300.synth import ENSEMBLE_MIX as MIX
 
     mix = MIX if not args.mix else tuple((c, int(n)) for c, n in (x.split(":") for x in args.mix.split(",")))
     per_step, sample = 0.0, []
@@ -196,12 +205,14 @@ def run_reference_ensemble(args):
 
 
 def run_reference(args, ws, rank):
-    """--impl reference: the CPU reference arm on rank 0 (the oracle port of pydyn)."""
+    """--impl reference: the CPU reference arm on rank 0 -- the oracle port of pydyn (its C
+    restatement and its restatement of pydyn's driver; nothing of the package runs but the
+    synthetic-input generator)."""
     if rank != 0:
         return
-    from __graft_entry__ import build
+    from oracle.build import build as build_oracle
 
-    build()
+    build_oracle()
     from oracle.forward import OracleRun
 
     if args.config == "ensemble":
@@ -221,7 +232,7 @@ def run_reference(args, ws, rank):
         "unit": "sim-years/hour", "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": per * 1e3, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f64", "data": "synthetic",
-        "config": {"workload": args.config, "tree": tree, "levels": lm, "physics": physics, "lmax": lmax},
+        "config": workload_config(args.config, args.gpus),
         "cpu_baseline": {"value": v, "unit": "sim-years/hour", "cores": 1, "kind": "port",
                          "sample": f"{args.steps} whole intervals of {args.config} (oracle, one host thread)"},
         "e2e": {"value": v, "unit": "sim-years/hour", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
@@ -598,9 +609,7 @@ def main():
         "ms_per_step": sec_per_step * 1e3,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
         "data": "synthetic (seeded meteo of the configuration's shape; pydyn_gb300.synth)",
-        "config": {"workload": args.config, "tree": tree, "levels": lm, "nt": 1, "physics": physics, "lmax": lmax,
-                   "step": "Check_CFL rehearsal + Setup_MassFlow + xyzvsc|csvzyx, one CUDA graph",
-                   "l2": "flushed between timed steps (256 MiB write)", "parallelism": f"replicas x{ws}"},
+        "config": workload_config(args.config, ws),
         "roofline": roof,
         "step_bytes": step_bytes,
         "step_hbm_frac": step_bytes / sec_per_step / 1e9 / hbm,

@@ -1,15 +1,13 @@
-"""The operator sequence of a dynamic step and of Check_CFL on a region tree, as pydyn's driver
-runs it (pydyn zoom/steps.py:29-88, zoom/advect.py:42-199, zoom/check_cfl.py:32-290,
-zoom/massflow.py:319-442, cfl.py:208-213), calling the bodies through `st.lib` -- the device
-bodies of pydyn_gb300.zoom for a ZoomState on the GPU.
+"""ORACLE -- test infrastructure.  A restatement of pydyn's driver: the operator sequence of a
+dynamic step and of Check_CFL on a region tree as pydyn runs it (pydyn zoom/steps.py:29-88,
+zoom/advect.py:42-199, zoom/check_cfl.py:32-290, zoom/massflow.py:61-73 and 174-184, cfl.py:208-213),
+calling the bodies through `st.lib` with pydyn's signatures and consuming their returns as
+pydyn does: a mass-only body's return is the rehearsal's ok flag for its region, and the
+rehearsal unwinds at the first failure.
 
-Everything here is host control: which body runs next, on which rows / columns / scope.  No
-decision waits for the device inside a step: sub-cycle counts are found and used on the device,
-errors are raised at the next sync, and the Check_CFL rehearsal's failure is a device flag that
-its later kernels honour and the host reads once per rehearsed step.  A whole step can therefore
-be captured as one CUDA graph (pydyn_gb300.forward)."""
-
-from contextlib import nullcontext
+It drives the oracle's host bodies (oracle.zoom) for the oracle's whole intervals, and the
+device bodies (pydyn_gb300.zoom) in the tests that hold the device module to pydyn's body
+contract.  The product plans its own sequence (pydyn_gb300.plan); the tests compare the two."""
 
 from .tree import CFL_N_OPERATORS, CFL_SPLITORDER, N_OPERATORS, nint
 
@@ -216,63 +214,79 @@ def setup_massflow(zoom, st, ndyn):
         st.lib.coarsen_ambm(zoom, st, r)
 
 
-# ------------------------------------------------------------------ Check_CFL
+# ------------------------------------------------------------------ Check_CFL (pydyn zoom/check_cfl.py)
 class _CFLRun:
-    """advectm_cfl's module state for one Check_CFL: the CFL split order and status counters."""
+    """advectm_cfl's module state for one Check_CFL: the CFL split order, the status counters and
+    each region's ok flag (check_cfl.py:57-70)."""
 
     def __init__(self, zoom, caps=None):
         self.caps = caps
         self.order = zoom.split_orders(CFL_SPLITORDER, CFL_N_OPERATORS)
         self.status = [0] * (zoom.nregions + 1)
+        self.ok = [True] * (zoom.nregions + 1)
+
+    def all_ok(self):
+        return all(self.ok[1:])
 
 
 def _advectm(zoom, st, run, region, axis):
+    """advectm{x,y,z}zoom (check_cfl.py:79-92, 140-153, 196-203): the body's return is the ok."""
     lib, lm = st.lib, zoom.lm
     s = run.status[region]
     block, _ = _block(zoom, region, s, run.order[region], CFL_N_OPERATORS)
     second = _second_half(zoom, region, s, CFL_N_OPERATORS)
-    cap = None if run.caps is None else run.caps["xyz".index(axis)]
+    cap = {"x": 10, "y": 1, "z": 1}[axis] if run.caps is None else run.caps["xyz".index(axis)]
     if axis == "x":
         lib.put_xedges(zoom, st, region, tracers=False)
         js, je = x_scope(zoom, region, block)
         with lib.outer_x_faces_zeroed(zoom, st, region, second):
             if region == 1:
-                lib._dynamum_region1(zoom, st, js, je, 10 if cap is None else cap)
+                ok = lib._dynamum_region1(zoom, st, js, je, cap)
             else:
-                lib._dynamum_child(zoom, st, region, js, je, 1, lm, 10 if cap is None else cap)
+                ok = lib._dynamum_child(zoom, st, region, js, je, 1, lm, cap)
+            run.ok[region] = ok
     elif axis == "y":
         lib.put_yedges(zoom, st, region, tracers=False)
         is_, ie = y_scope(zoom, region, block)
         with lib.outer_y_faces_zeroed(zoom, st, region, second):
             if region == 1:
-                lib._dynamvm_region1(zoom, st, 1 if cap is None else cap)
+                ok = lib._dynamvm_region1(zoom, st, cap)
             else:
-                lib._dynamvm_child(zoom, st, region, is_, ie, 1, lm, 1 if cap is None else cap)
+                ok = lib._dynamvm_child(zoom, st, region, is_, ie, 1, lm, cap)
+            run.ok[region] = ok
     else:
         is_, ie, js, je = z_scope(zoom, region, block)
-        lib._dynamwm(zoom, st, region, is_, ie, js, je, 1 if cap is None else cap)
-        if region != 1:
+        run.ok[region] = lib._dynamwm(zoom, st, region, is_, ie, js, je, cap)
+        if run.ok[region] and region != 1:
             lib.mix_edges(zoom, st, region, tracers=False)
 
 
 def _cfl_do_steps(zoom, st, run, region):
+    """do_steps of advectm_cfl (check_cfl.py:222-235): returns as soon as any region failed."""
     for _ in range(CFL_N_OPERATORS):
         _advectm(zoom, st, run, region, run.order[region][run.status[region]])
+        if not run.all_ok():
+            return
         run.status[region] += 1
         if run.status[region] % CFL_N_OPERATORS == 0:
             return
 
 
 def determine_cfl_iter(zoom, st, run, region):
-    """advectm_cfl determine_cfl_iter: the region's tref_ blocks, each followed by its
-    children, then updatem_parent.  A failed operator sets the device's rehearsal flag; every
-    later rehearsal kernel then returns without work (the Fortran's early return)."""
+    """determine_cfl_iter (check_cfl.py:238-255): any failure unwinds back to Check_CFL."""
+    run.ok[region] = True
     for _ in range(zoom.ref(region, "t")):
         _cfl_do_steps(zoom, st, run, region)
+        if not run.ok[region]:
+            return
         for child in zoom.children[region]:
+            if not run.all_ok():
+                break
             determine_cfl_iter(zoom, st, run, child)
-        if run.status[region] % CFL_N_OPERATORS != 0:
+        if run.status[region] % CFL_N_OPERATORS != 0 and run.all_ok():
             _cfl_do_steps(zoom, st, run, region)
+            if not run.ok[region]:
+                return
     if region != 1:
         st.lib.update_parent(zoom, st, region, tracers=False)
 
@@ -286,40 +300,30 @@ def new_valid_timestep(dtime, nread, cfl_outputstep, tref_max=1):
     raise ValueError("new_valid_timestep: no valid time step")
 
 
-def check_cfl_zoom(zoom, st, ndyn, n, nread, interpolate=None, max_iteration=100, caps=None, rehearse=None):
-    """advectm_cfl Check_CFL on a region tree (pydyn zoom/check_cfl.py:258-290): for each of the
-    n steps Setup_MassFlow (after `interpolate(zoom, st, i, ndyn)`) and the xyz / zyx mass-only
+def check_cfl_zoom(zoom, st, ndyn, n, nread, interpolate=None, max_iteration=100, caps=None):
+    """Check_CFL on a region tree (check_cfl.py:258-290): for each of the n steps
+    Setup_MassFlow (after `interpolate(zoom, st, i, ndyn)`) and the xyz / zyx mass-only
     rehearsals; on a failure m, am, bm, cm are restored, ndyn goes to the next valid step and
-    the stored fluxes are scaled by ndyn_new / ndyn_old.  Returns (ndyn, n, iterations).
-    rehearse(st, i, n, ndyn) -- if given -- replaces the enqueueing of step i's rehearsal (a
-    captured graph of it, for instance)."""
-    lib = st.lib
+    the stored fluxes are scaled by ndyn_new / ndyn_old.  Returns (ndyn, n, iterations)."""
     tref_max = max(zoom.g(r).tref for r in zoom.regions())
     for iteration in range(1, max_iteration + 1):
-        lib.save(st, "check_cfl", ("m", "am", "bm", "cm"))
-        lib.cfl_begin(st)
-        ok = True
+        run = _CFLRun(zoom, caps)
+        st.lib.save(st, "check_cfl", ("m", "am", "bm", "cm"))
         for i in range(1, n + 1):
-            if rehearse is not None:
-                rehearse(st, i, n, ndyn)
-            else:
-                if interpolate is not None:
-                    interpolate(zoom, st, i, ndyn)
-                setup_massflow(zoom, st, ndyn)
-                run = _CFLRun(zoom, caps)
+            if interpolate is not None:
+                interpolate(zoom, st, i, ndyn)
+            setup_massflow(zoom, st, ndyn)
+            determine_cfl_iter(zoom, st, run, 1)
+            if run.all_ok():
                 determine_cfl_iter(zoom, st, run, 1)
-                determine_cfl_iter(zoom, st, run, 1)
-            if not lib.cfl_all_ok(st):
-                ok = False
+            if not run.all_ok():
                 break
-        lib.restore(st, "check_cfl")
-        if ok:
+            run.status = [0] * (zoom.nregions + 1)
+        st.lib.restore(st, "check_cfl")
+        if run.all_ok():
             return ndyn, n, iteration
         ndyn_old = ndyn
         ndyn = new_valid_timestep(ndyn, nread, nread, tref_max)
         n = nint(float(n * ndyn_old) / float(ndyn))
-        lib.scale(st, ("am", "bm", "cm"), float(ndyn) / float(ndyn_old))
+        st.lib.scale(st, ("am", "bm", "cm"), float(ndyn) / float(ndyn_old))
     raise RuntimeError("check_cfl_zoom: exceeded maximum number of time steps")
-
-
-_ = nullcontext

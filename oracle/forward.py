@@ -1,16 +1,18 @@
 """ORACLE -- test infrastructure.  Whole read intervals on the host (pydyn forward.py:388-451
-recomposed for a region tree, as pydyn_gb300.forward runs them on the device): Check_CFL on a
-copy of m and sp, then each step's interpolated meteo, Setup_MassFlow and the operator
-sequence -- the bodies of oracle.zoom, the inputs of pydyn_gb300.synth."""
+recomposed for a region tree): Check_CFL on a copy of m and sp, then each step's interpolated
+meteo, Setup_MassFlow and the operator sequence -- the oracle's restatement of pydyn's driver
+(oracle.driver) over the oracle's bodies (oracle.zoom) on the oracle's own region tree
+(oracle.tree).  Only the synthetic inputs come from the package (pydyn_gb300.synth, a pure NumPy
+generator that loads no native code)."""
 
 import hashlib
 
 import numpy as np
 
-from pydyn_gb300 import driver as D
-from pydyn_gb300 import forward as F
 from pydyn_gb300 import synth
 
+from . import driver as D
+from . import tree as T
 from .zoom import HostState
 
 STATE_FIELDS = ("m", "rm", "rxm", "rym", "rzm", "am", "bm", "cm", "pu", "pv", "sp", "phlb")
@@ -24,9 +26,22 @@ def digest(st):
     return h.hexdigest()
 
 
+def oracle_tree(zoom):
+    """The oracle's own Zoom of a tree the input generator describes (its regions' parameters)."""
+    regions = []
+    for g in zoom.region[1:]:
+        rg = g.redgrid
+        if rg is not None:
+            rg = T.RedGrid(rg.im, rg.jm, [row + 1 for row, _, _ in rg.bands], [c for _, c, _ in rg.bands])
+        regions.append(T.Region(g.name, g.im, g.jm, g.xbeg, g.xend, g.ybeg, g.yend, g.xref, g.yref, g.zref, g.tref,
+                                g.parent, g.xcyc, g.touch_sp, g.touch_np, rg))  # fmt: skip
+    return T.Zoom(regions, zoom.lm, zoom.at, zoom.bt)
+
+
 class OracleRun:
     def __init__(self, config, lm, seed, nt=1, umax=40.0, physics=False, lmax=None):
-        self.zoom, self.met, fields = synth.case(config, lm, seed, nt, umax=umax)
+        gen_zoom, self.met, fields = synth.case(config, lm, seed, nt, umax=umax)
+        self.zoom = oracle_tree(gen_zoom)
         self.st, self.cst = HostState(self.zoom, nt), HostState(self.zoom, nt)
         self.st.load(fields)
         for r in self.zoom.regions():
@@ -36,12 +51,13 @@ class OracleRun:
         if physics:
             from .physics import OraclePhysics
 
-            self.physics = OraclePhysics(self.zoom, self.met, seed, lm if lmax is None else lmax)
+            spec = synth.Physics(gen_zoom, self.met, seed, lm if lmax is None else lmax)
+            self.physics = OraclePhysics(self.zoom, spec)
             self.physics.init(self.st)
         self.t = 0.0
 
     def interpolate(self, st, t):
-        a1, a2 = F.weights(t)
+        a1, a2 = synth.weights(t)
         for r in self.zoom.regions():
             (pu0, pv0), (pu1, pv1) = self.meteo[r]
             st[r]["pu"].data[...] = a1 * pu0 + a2 * pu1

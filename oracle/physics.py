@@ -4,9 +4,6 @@ Setup_MassFlow (spm the meteo's at the step's middle, sp the region's at its sta
 `s`, `c` on the owned columns with dt = ndyn / (2 tref) -- the C oracle's calc_kzz, convec and
 loss_rates, NumPy for the emission and the decay's application."""
 
-import numpy as np
-
-from pydyn_gb300 import forward as F
 from pydyn_gb300 import synth
 
 from . import kernels as O
@@ -15,8 +12,9 @@ N_OPERATORS = 6
 
 
 class OraclePhysics:
-    def __init__(self, zoom, met, seed, lmax):
-        self.spec = synth.Physics(zoom, met, seed, lmax)
+    def __init__(self, zoom, spec):
+        """zoom: the oracle's tree; spec: the physics inputs of pydyn_gb300.synth.Physics."""
+        self.spec = spec
         self.zoom = zoom
 
     def init(self, st):
@@ -30,7 +28,7 @@ class OraclePhysics:
     def step(self, st, t0, ndyn):
         """(conv, driver kwargs) of the step from t0, after Setup_MassFlow."""
         spec, zoom = self.spec, self.zoom
-        a1, a2 = F.weights(t0 + ndyn / 2.0)
+        a1, a2 = synth.weights(t0 + ndyn / 2.0)
         conv = {}
         for r in zoom.regions():
             g, R, f = zoom.g(r), spec.region[r], st[r]

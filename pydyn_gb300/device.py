@@ -24,6 +24,7 @@ class Device:
         self.L = L
         self.ordinal = device
         self._owned = []
+        self.capturing = False  # inside capture(): nothing may read the device back
 
     def close(self):
         if self.h:
@@ -78,9 +79,11 @@ class Device:
         """Capture everything enqueued in the block into a Graph (yielded, filled on exit)."""
         g = Graph(self)
         N.check(self.L.gb_capture_begin(self.h), "gb_capture_begin")
+        self.capturing = True
         try:
             yield g
         finally:
+            self.capturing = False
             p = ctypes.c_void_p()
             N.check(self.L.gb_capture_end(self.h, ctypes.byref(p)), "gb_capture_end")
             g.p = p.value

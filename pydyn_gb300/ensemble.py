@@ -28,14 +28,8 @@ import numpy as np
 
 from .device import Device
 from .forward import Forward
-
-# class: (tree, levels, convection levels, the class's meteo seed)
-CLASSES = {
-    "glb6x4": ("glb6x4", 25, 25, 11),
-    "glb3x2": ("glb3x2", 34, 34, 41),
-    "glb3x2+nam1x1": ("glb3x2+nam1x1", 34, 34, 42),
-}
-MIX = (("glb6x4", 128), ("glb3x2", 96), ("glb3x2+nam1x1", 32))
+from .synth import ENSEMBLE_CLASSES as CLASSES
+from .synth import ENSEMBLE_MIX as MIX
 
 
 @dataclass(frozen=True)

@@ -17,13 +17,13 @@ graph serves every step."""
 import numpy as np
 
 from . import _native as N
-from . import driver as D
+from . import plan as P
 from . import synth
 from .device import DevArray, Device
 from .schedule import ScheduledLib, Scheduler, scheduled_physics, spreadable
 from .state import TRACERS, ZoomState
+from .synth import weights
 
-WINDOW = 6 * 3600.0
 SPECULATED = ("m", *TRACERS, "sp", "phlb")
 # stream priorities of the captured interval's side contexts, in steps above the device's least
 # (the run's own stream and the Check_CFL rehearsal stay at the least): a child's chain of small
@@ -32,14 +32,6 @@ SPECULATED = ("m", *TRACERS, "sp", "phlb")
 CHILD_PRIORITY = 3
 KZZ_PRIORITY = 1
 FAR_PRIORITY = 0  # region 1's physics on its far segment (slack until the parent's m2phlb1)
-
-
-def weights(t):
-    """(alfa1, alfa2) of the two meteo instants at time t (s): a triangle wave between them."""
-    cycle = t / WINDOW
-    k = int(np.floor(cycle))
-    frac = cycle - k
-    return (1.0 - frac, frac) if k % 2 == 0 else (frac, 1.0 - frac)
 
 
 class Forward:
@@ -102,10 +94,7 @@ class Forward:
 
     # -------------------------------------------------------------- Check_CFL, the step
     def _rehearse(self, st, i, n, ndyn):
-        D.setup_massflow(self.zoom, st, ndyn)
-        run = D._CFLRun(self.zoom)
-        D.determine_cfl_iter(self.zoom, st, run, 1)
-        D.determine_cfl_iter(self.zoom, st, run, 1)
+        P.rehearse_step(self.zoom, st, ndyn)
 
     def check_cfl(self, t0):
         """Check_CFL on the copy of m and sp (Forward._carry); (ndyn, n, iterations)."""
@@ -117,8 +106,8 @@ class Forward:
             self.put_weights(t0 + (i - 0.5) * ndyn)
             self.interpolate(st)
 
-        return D.check_cfl_zoom(self.zoom, self.cfl_st, self.ndyn_max, self.nread // self.ndyn_max, self.nread,
-                                interpolate)  # fmt: skip
+        return P.check_cfl(self.zoom, self.cfl_st, self.ndyn_max, self.nread // self.ndyn_max, self.nread,
+                           interpolate)  # fmt: skip
 
     def step(self, t0, ndyn):
         """One step from t0 (Forward._step): meteo at the middle, Setup_MassFlow, the sequence."""
@@ -128,13 +117,13 @@ class Forward:
     def enqueue_step(self, ndyn):
         st = self.st
         self.interpolate(st)
-        D.setup_massflow(self.zoom, st, ndyn)
+        P.setup_massflow(self.zoom, st, ndyn)
         kw = {"limits": self.limits}
         conv = None
         if self.physics is not None:
             conv, kw2 = self.physics.prepare(self, ndyn)
             kw.update(kw2)
-        D.step(self.zoom, st, conv, ndyn, **kw)
+        P.step(self.zoom, st, conv, ndyn, **kw)
 
     def interval(self, graph=False):
         """One read interval: Check_CFL, then its steps.  Returns (ndyn, n)."""
@@ -172,7 +161,7 @@ class Forward:
         self.interpolate(st)
         # Setup_MassFlow first: it rebuilds a parent's mass over a child's footprint and with it
         # the parent's sp (m2phlb), which Calc_Kzz reads
-        D.setup_massflow(zoom, st, self.nread)
+        P.setup_massflow(zoom, st, self.nread)
         kw = {"limits": self.limits}
         conv = None
         joins = []
@@ -212,7 +201,7 @@ class Forward:
                     kw[name] = scheduled_physics(sched, kw[name], name)
             st.lib = ScheduledLib(lib, sched)
         try:
-            D.step(zoom, st, conv, self.nread, **kw)
+            P.step(zoom, st, conv, self.nread, **kw)
         finally:
             st.lib = lib
         if sched is not None:
@@ -228,11 +217,10 @@ class Forward:
         self._fork_events = (fork, rehearsed, forked, joins, sched.keep if sched else None)  # alive until the capture ends
 
     def _enqueue_rehearsal(self):
-        """Check_CFL's rehearsal of one step on the copy (save, reset the flag, meteo, the
+        """Check_CFL's rehearsal of one step on the copy (save, which clears the flag, meteo, the
         mass-only operators, restore), enqueued on whatever context the device points to."""
         cst, lib = self.cfl_st, self.st.lib
         lib.save(cst, "check_cfl", ("m", "am", "bm", "cm"))
-        lib.cfl_begin(cst)
         self.interpolate(cst)
         self._rehearse(cst, 1, 1, self.nread)
         lib.restore(cst, "check_cfl")

@@ -133,9 +133,9 @@ class Timeline:
     def __enter__(self):
         from contextlib import contextmanager
 
-        from . import driver as D
         from . import forward as F
         from . import physics as P
+        from . import plan as PL
         from . import schedule as S
 
         self._main = self.dev.h
@@ -153,7 +153,7 @@ class Timeline:
         S.Scheduler.body = stamped
         self._bracket(F.Forward, "_enqueue_rehearsal", lambda *a, **k: "check_cfl")
         self._bracket(P.Physics, "prepare_region", lambda self_, fwd, r: f"calc_kzz@{r}")
-        self._bracket(D, "setup_massflow", lambda *a, **k: "setup_massflow")
+        self._bracket(PL, "setup_massflow", lambda *a, **k: "setup_massflow")
         self._bracket(F.Forward, "_enqueue_interval", lambda *a, **k: "interval")
         return self
 

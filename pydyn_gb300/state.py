@@ -12,27 +12,7 @@ contiguous.  `lib` is the module of bodies the driver calls: pydyn_gb300.zoom.""
 import numpy as np
 
 from .device import DevArray
-
-FIELDS = ("m", "rm", "rxm", "rym", "rzm", "am", "bm", "cm", "pu", "pv", "sp", "phlb", "dxyp")
-TRACERS = ("rm", "rxm", "rym", "rzm")
-
-
-def bounds(name, im, jm, lm, nt=1):
-    """The declared (lower, upper) bounds of a state array."""
-    cells = [(-1, im + 2), (-1, jm + 2)]
-    faces = [(0, im + 1), (0, jm + 1), (0, lm + 1)]
-    table = {
-        "m": [*cells, (1, lm)],
-        "am": faces, "bm": faces, "cm": faces,
-        "pu": [(0, im), (1, jm), (1, lm)],
-        "pv": [(1, im), (1, jm + 1), (1, lm)],
-        "sp": [*cells, (1, 1)],
-        "phlb": [*cells, (1, lm + 1)],
-        "dxyp": [(1, jm)],
-    }  # fmt: skip
-    for q in TRACERS:
-        table[q] = [*cells, (1, lm), (1, nt)]
-    return table[name]
+from .layout import FIELDS, TRACERS, bounds  # noqa: F401  (re-exported)
 
 
 class ZoomState:

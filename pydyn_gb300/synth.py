@@ -10,6 +10,8 @@ Configurations (dims as the benchmark names them):
     glb6x4      60 x 45 x 25, reduced grid jred (1, 2, 3, 45) clustsize (60, 20, 10, 60)
     glb3x2      120 x 90 x 34, reduced grid of the production fixture
     glb3x2+nam1x1  the above with a 90 x 70 child at 140W-50W, 10N-80N, xref 3, yref 2, tref 2
+    glb3x2+nam72x44  glb3x2 with a 72 x 44 child at 132W-60W, 20N-64N, xref 3, yref 2, tref 2
+                   (the tree pydyn's own GPU benchmark times)
 
 Air mass from a surface pressure of 1e5 Pa +- 2 % smooth noise on hybrid a / b levels; mass
 fluxes from a seeded streamfunction of eight low spherical modes (winds up to 40 m/s, so the
@@ -116,6 +118,13 @@ def nam1x1():
     return Region("nam1x1", 90, 70, xbeg=-141, xend=-51, ybeg=10, yend=80, xref=3, yref=2, tref=2, parent=1)
 
 
+def nam72x44():
+    """The 72 x 44 child over North America of pydyn's own GPU benchmark tree: 132W-60W,
+    20N-64N at xref 3, yref 2, tref 2 -- corners on glb3x2's 3 x 2 degree lines, footprint
+    i 17..40, j 56..77."""
+    return Region("nam1x1", 72, 44, xbeg=-132, xend=-60, ybeg=20, yend=64, xref=3, yref=2, tref=2, parent=1)
+
+
 def two():
     """A 24 x 18 parent (15 x 10 degrees) and one child at nam1x1's refinements (xref 3,
     yref 2, tref 2): the shape of the reference's small tree tests."""
@@ -141,7 +150,8 @@ def three():
 
 
 def tree(name, lm):
-    regions = {"glb6x4": glb6x4, "glb3x2": glb3x2, "glb3x2+nam1x1": lambda: [*glb3x2(), nam1x1()], "two": two,
+    regions = {"glb6x4": glb6x4, "glb3x2": glb3x2, "glb3x2+nam1x1": lambda: [*glb3x2(), nam1x1()],
+               "glb3x2+nam72x44": lambda: [*glb3x2(), nam72x44()], "two": two,
                "three": three, "one": one}[name]()  # fmt: skip
     at, bt = levels(lm)
     return Zoom(regions, lm, at, bt)
@@ -413,7 +423,7 @@ def case(name, lm, seed=0, nt=1, umax=40.0, wind_scale=1.0):
     declared (halo'd) shapes: m and rm from the meteo's surface pressure, slopes zero, dxyp.
     pu / pv are set per step by the run (interpolated between the meteo instants); wind_scale
     multiplies the winds (an ensemble member's perturbation)."""
-    from .state import bounds
+    from .layout import bounds
 
     zoom = tree(name, lm)
     met = Meteo(zoom, seed, umax=umax, wind_scale=wind_scale)
@@ -434,3 +444,25 @@ def case(name, lm, seed=0, nt=1, umax=40.0, wind_scale=1.0):
         f["dxyp"][:] = cell_area(g)
         fields[r] = f
     return zoom, met, fields
+
+
+# ------------------------------------------------------------------ the ensemble's member classes
+# class: (tree, levels, convection levels, the class's meteo seed)
+ENSEMBLE_CLASSES = {
+    "glb6x4": ("glb6x4", 25, 25, 11),
+    "glb3x2": ("glb3x2", 34, 34, 41),
+    "glb3x2+nam1x1": ("glb3x2+nam1x1", 34, 34, 42),
+}
+ENSEMBLE_MIX = (("glb6x4", 128), ("glb3x2", 96), ("glb3x2+nam1x1", 32))
+
+
+# ------------------------------------------------------------------ the meteo's time weights
+WINDOW = 6 * 3600.0  # seconds between the two meteo instants
+
+
+def weights(t):
+    """(alfa1, alfa2) of the two meteo instants at time t (s): a triangle wave between them."""
+    cycle = t / WINDOW
+    k = int(np.floor(cycle))
+    frac = cycle - k
+    return (1.0 - frac, frac) if k % 2 == 0 else (frac, 1.0 - frac)

@@ -4,7 +4,13 @@ leaving the device state as the host body leaves the host state.  Region 1's adv
 the row / column kernels on its interior views; a child's to the held-end kernels on its scope;
 the exchange statements are box statements on Fortran sections.
 
-Nothing here waits for the device, except cfl_all_ok (the rehearsal's one host decision)."""
+The Check_CFL bodies keep pydyn's contract: each returns whether the rehearsal still holds
+after it -- pydyn's Check_CFL takes that as the region's ok flag and unwinds at the first False
+(pydyn zoom/check_cfl.py:87-91, 148-152, 201).  The outcome lives in a device flag that every
+later rehearsal kernel honours; returning it costs one device-to-host read per body.  The
+package's own planned rehearsal (pydyn_gb300.plan) passes report=False and reads the flag once
+per rehearsed step instead (cfl_all_ok), so a rehearsal can be captured in a graph.  Nothing
+else here waits for the device."""
 
 from contextlib import contextmanager
 
@@ -71,29 +77,37 @@ def cfl_begin(st):
 
 def cfl_all_ok(st):
     """The rehearsal's outcome so far (a device -> host read of one flag)."""
+    if st.dev.capturing:
+        raise RuntimeError("Check_CFL: a captured rehearsal's outcome is read after the graph's replay")
     return not st.dev.cfl_failed()
 
 
-def _dynamum_region1(zoom, st, js, je, max_nloop):
+def _outcome(st, report):
+    """A mass-only body's return: the rehearsal's outcome after it (True when not reported)."""
+    return cfl_all_ok(st) if report else True
+
+
+def _dynamum_region1(zoom, st, js, je, max_nloop, report=True):
     """cfl.dynamum on region 1 with its halos (zoom/check_cfl.py:94-110)."""
     g, f, lm = zoom.g(1), st[1], zoom.lm
     K.cfl_x(f["m"][1 : g.im, 1 : g.jm, 1:lm], f["am"][0 : g.im, 1 : g.jm, 1:lm], clust=_clust(st, 1), halo=True,
             js=js, je=je, max_nloop=max_nloop)  # fmt: skip
-    return True
+    return _outcome(st, report)
 
 
-def _dynamvm_region1(zoom, st, max_nloop):
+def _dynamvm_region1(zoom, st, max_nloop, report=True):
+    """cfl.dynamvm on region 1 (zoom/check_cfl.py:156-161)."""
     g, f, lm = zoom.g(1), st[1], zoom.lm
     K.cfl_y(f["m"][1 : g.im, 1 : g.jm, 1:lm], f["bm"][1 : g.im, 1 : g.jm + 1, 1:lm], max_nloop=max_nloop)
-    return True
+    return _outcome(st, report)
 
 
-def _dynamwm(zoom, st, region, is_, ie, js, je, iter_limit):
+def _dynamwm(zoom, st, region, is_, ie, js, je, iter_limit, report=True):
     """dynamwm: the search over the region, the mass advanced on the scope (check_cfl.py:206)."""
     g, f, lm = zoom.g(region), st[region], zoom.lm
     K.cfl_z(f["m"][1 : g.im, 1 : g.jm, 1:lm], f["cm"][1 : g.im, 1 : g.jm, 0:lm], scope=(is_ - 1, ie, js - 1, je),
             iter_limit=iter_limit)  # fmt: skip
-    return True
+    return _outcome(st, report)
 
 
 # ------------------------------------------------------------------ mass fluxes, pressure
@@ -141,9 +155,14 @@ def assign(dst, src, region, names):
 
 def save(st, key, names):
     """Device copies of the named arrays of every region, for restore(st, key); the copies are
-    kept and reused by the next save under the same key (fixed addresses for graph replay)."""
+    kept and reused by the next save under the same key (fixed addresses for graph replay).
+    A save under the key "check_cfl" opens a Check_CFL rehearsal and clears the device's
+    rehearsal flag with it: pydyn's Check_CFL saves m and the fluxes at the start of every try
+    (pydyn zoom/check_cfl.py:275) and calls nothing else a device could reset the flag in."""
     from .device import DevArray
 
+    if key == "check_cfl":
+        cfl_begin(st)
     slot = st.saved.setdefault(key, {})
     for r, f in st.fields.items():
         for k in names:
@@ -287,18 +306,20 @@ def _dynamw_child(zoom, st, region, is_, ie, js, je, limits, stats, iter_limit=1
                iter_limit=iter_limit)  # fmt: skip
 
 
-def _dynamum_child(zoom, st, region, js, je, ls, le, max_nloop):
+def _dynamum_child(zoom, st, region, js, je, ls, le, max_nloop, report=True):
+    """dynamum (mass only) of a child with its edge exchange (zoom/check_cfl.py:113-137)."""
     from . import child
 
     child.dynamum(zoom, st, region, js, je, ls, le, max_nloop)
-    return True
+    return _outcome(st, report)
 
 
-def _dynamvm_child(zoom, st, region, is_, ie, ls, le, max_nloop):
+def _dynamvm_child(zoom, st, region, is_, ie, ls, le, max_nloop, report=True):
+    """dynamvm (mass only) of a child with its edge exchange (zoom/check_cfl.py:164-193)."""
     from . import child
 
     child.dynamvm(zoom, st, region, is_, ie, ls, le, max_nloop)
-    return True
+    return _outcome(st, report)
 
 
 # ------------------------------------------------------------------ physics on owned cells

@@ -1,7 +1,7 @@
 """Make the golden fixtures of tests/golden/ from the reference itself.
 
-Run where the pydyn reference is importable (its checkout is on PYDYN_REFERENCE, default
-/root/reference); the fixtures it writes are what the tests compare the oracle and the device
+Run where the pydyn reference is importable, with PYDYN_REFERENCE set to its checkout (the
+directory holding the `pydyn` package); the fixtures it writes are what the tests compare the oracle and the device
 against on machines that do not have the reference:
 
     python tests/golden/make_golden.py kernels     -> tests/golden/kernels.npz
@@ -20,11 +20,13 @@ from pathlib import Path
 
 import numpy as np
 
-REF = Path(os.environ.get("PYDYN_REFERENCE", "/root/reference"))
+REF = Path(os.environ["PYDYN_REFERENCE"]) if os.environ.get("PYDYN_REFERENCE") else None
 HERE = Path(__file__).resolve().parent
 
 
 def _reference():
+    if REF is None:
+        raise SystemExit("make_golden: set PYDYN_REFERENCE to the pydyn reference checkout")
     sys.path.insert(0, str(REF))
     import pydyn  # noqa: F401
 
@@ -225,10 +227,10 @@ class _RefPhysics:
         from pydyn import chem, diffusion
         from pydyn import zoom as Z
 
-        from pydyn_gb300 import forward
+        from pydyn_gb300 import synth
 
         spec, zref = self.spec, self.zref
-        a1, a2 = forward.weights(t0 + ndyn / 2.0)
+        a1, a2 = synth.weights(t0 + ndyn / 2.0)
         conv = {}
         for r in zref.regions():
             g, R = zref.g(r), spec.region[r]
@@ -266,12 +268,12 @@ def _reference_case(config, lm, seed, nt=1, physics=False, umax=40.0, lmax=None)
     from pydyn import redgrid as RG
     from pydyn import zoom as Z
 
-    from pydyn_gb300 import forward, synth
+    from pydyn_gb300 import synth
 
     zoom, met, fields = synth.case(config, lm, seed, nt, umax=umax)
     regions = []
     for g in zoom.region[1:]:
-        kw = {k: getattr(g, k) for k in g.__dataclass_fields__ if k != "redgrid"}
+        kw = {k: getattr(g, k) for k in g._fields if k != "redgrid"}
         rg = None
         if g.redgrid is not None:
             rg = RG.RedGrid(g.im, g.jm, [b[0] + 1 for b in g.redgrid.bands], [b[1] for b in g.redgrid.bands])
@@ -285,7 +287,7 @@ def _reference_case(config, lm, seed, nt=1, physics=False, umax=40.0, lmax=None)
     meteo = {r: [met.fluxes(r, k) for k in (0, 1)] for r in zref.regions()}
 
     def interp(s, t):
-        a1, a2 = forward.weights(t)
+        a1, a2 = synth.weights(t)
         for r in zref.regions():
             (pu0, pv0), (pu1, pv1) = meteo[r]
             s[r]["pu"].data[...] = a1 * pu0 + a2 * pu1
@@ -366,12 +368,12 @@ def reference_run(config, lm, seed, nsteps, nt=1, physics=False, keep=None, umax
     from pydyn import redgrid as RG
     from pydyn import zoom as Z
 
-    from pydyn_gb300 import forward, synth
+    from pydyn_gb300 import synth
 
     zoom, met, fields = synth.case(config, lm, seed, nt, umax=umax)
     regions = []
     for g in zoom.region[1:]:
-        kw = {k: getattr(g, k) for k in g.__dataclass_fields__ if k != "redgrid"}
+        kw = {k: getattr(g, k) for k in g._fields if k != "redgrid"}
         rg = None
         if g.redgrid is not None:
             rg = RG.RedGrid(g.im, g.jm, [b[0] + 1 for b in g.redgrid.bands], [b[1] for b in g.redgrid.bands])
@@ -385,7 +387,7 @@ def reference_run(config, lm, seed, nsteps, nt=1, physics=False, keep=None, umax
     meteo = {r: [met.fluxes(r, k) for k in (0, 1)] for r in zref.regions()}
 
     def interp(s, t):
-        a1, a2 = forward.weights(t)
+        a1, a2 = synth.weights(t)
         for r in zref.regions():
             (pu0, pv0), (pu1, pv1) = meteo[r]
             s[r]["pu"].data[...] = a1 * pu0 + a2 * pu1
@@ -432,6 +434,7 @@ STEP_RUNS = {  # name: (tree, lm, seed, intervals, umax[, physics lmax, interval
     "config0-strong": ("glb6x4", 25, 12, 6, 160.0),
     "two": ("two", 5, 13, 6, 40.0),
     "two-strong": ("two", 5, 14, 6, 120.0),
+    "two-reject": ("two", 5, 14, 4, 1000.0),  # Check_CFL halves ndyn on the child's tree
     "three": ("three", 4, 15, 4, 40.0),
     "config2-adv": ("glb3x2+nam1x1", 34, 31, 3, 40.0),
     "two-phys": ("two", 8, 21, 6, 40.0, 8, 6),
@@ -468,6 +471,173 @@ def step_goldens(names=None):
     return res
 
 
+# ------------------------------------------------------------------ call traces of pydyn's driver
+TRACE_TREES = {  # name: the regions' parameters (pydyn zoom.Region keywords) and lm
+    "one": None, "two": None, "three": None, "glb6x4": None, "glb3x2+nam1x1": None, "glb3x2+nam72x44": None,
+    "eur": ([{"name": "glb600x400", "im": 60, "jm": 45, "xcyc": 1, "touch_sp": 1, "touch_np": 1},
+             {"name": "eur300x200", "im": 30, "jm": 36, "xbeg": -36, "xend": 54, "ybeg": 2, "yend": 74, "xref": 2,
+              "yref": 2, "tref": 2, "parent": 1},
+             {"name": "eur100x100", "im": 60, "jm": 54, "xbeg": -21, "xend": 39, "ybeg": 12, "yend": 66, "xref": 6,
+              "yref": 4, "tref": 4, "parent": 2}], 3),
+}  # fmt: skip
+TRACE_RUNS = ("config0-strong", "two-reject")  # runs whose Check_CFL rejects steps
+
+
+def trace_tree_regions(name):
+    """(regions as keyword dicts, lm) of a traced tree: pydyn_gb300.synth's trees by name."""
+    if TRACE_TREES[name] is not None:
+        return TRACE_TREES[name]
+    sys.path.insert(0, str(HERE.parents[1]))
+    from pydyn_gb300 import synth
+
+    zoom = synth.tree(name, 4)
+    return [{k: getattr(g, k) for k in g._fields if k != "redgrid"} for g in zoom.region[1:]], 4
+
+
+def _json_arg(a):
+    if a is None or isinstance(a, (bool, int, float, str)):
+        return a
+    if isinstance(a, (np.integer,)):
+        return int(a)
+    if isinstance(a, (np.floating,)):
+        return float(a)
+    if isinstance(a, dict) and "lmax" in a:
+        return "<conv>"
+    raise TypeError(f"trace: argument {type(a)} not recorded")
+
+
+MASS_ONLY = ("_dynamum_region1", "_dynamvm_region1", "_dynamwm", "_dynamum_child", "_dynamvm_child")
+
+
+class _Trace:
+    """A `lib` for pydyn's driver that records every body call as [name, *args after (zoom, st)]
+    (save / restore / scale: after st), a kwargs dict last when given, a mass-only body's return
+    as {"return": ok}, and for a context-manager body ["enter:<name>", ...] / ["exit:<name>"].
+    `inner` (a real lib) does the work when given; else the mass-only bodies answer ok."""
+
+    def __init__(self, inner=None):
+        self.calls, self.inner = [], inner
+
+    def __getattr__(self, name):
+        inner = getattr(self.inner, name) if self.inner is not None else None
+        rec = self
+
+        def row(args, kw, tag):
+            first = 1 if name in ("save", "restore", "scale") else 2
+            out = [tag, *[[_json_arg(x) for x in a] if isinstance(a, tuple) else _json_arg(a) for a in args[first:]]]
+            if kw:
+                out.append({k: _json_arg(v) for k, v in kw.items()})
+            return out
+
+        if name in ("outer_x_faces_zeroed", "outer_y_faces_zeroed"):
+            from contextlib import contextmanager
+
+            @contextmanager
+            def cm(*args, **kw):
+                rec.calls.append(row(args, kw, "enter:" + name))
+                if inner is None:
+                    yield
+                else:
+                    with inner(*args, **kw):
+                        yield
+                rec.calls.append(["exit:" + name])
+
+            return cm
+
+        def call(*args, **kw):
+            out = inner(*args, **kw) if inner is not None else (True if name in MASS_ONLY else None)
+            r = row(args, kw, name)
+            if name in MASS_ONLY:
+                r.append({"return": bool(out)})
+            rec.calls.append(r)
+            return out
+
+        return call
+
+
+class _Bare:
+    """A state for the recording lib alone: pydyn's driver reads nothing of it but `lib`."""
+
+    def __init__(self, lib):
+        self.lib = lib
+
+
+def plan_traces():
+    """pydyn's own driver (zoom.setup_massflow, zoom.step, zoom.check_cfl_zoom) on a recording
+    lib, per traced tree: the calls the package's planner must reproduce."""
+    _reference()
+    from pydyn import zoom as Z
+
+    out = {}
+    for name in TRACE_TREES:
+        regions, lm = trace_tree_regions(name)
+        at, bt = np.linspace(2000.0, 0.0, lm + 1), np.linspace(1.0, 0.0, lm + 1)
+        zref = Z.Zoom([Z.Region(**kw) for kw in regions], lm, at, bt)
+        conv = {r: {"lmax": lm} for r in zref.regions()}
+        res = {"regions": regions, "lm": lm}
+        lib = _Trace()
+        st = _Bare(lib)
+        Z.setup_massflow(zref, st, 3600)
+        res["massflow"], lib.calls = lib.calls, []
+
+        def hook(kind):
+            return lambda zoom, s, region: lib.calls.append([kind, region, zoom.status[region]])
+
+        Z.step(zref, st, conv, 3600, sources=hook("sources"), chemistry=hook("chemistry"))
+        res["step"], lib.calls = lib.calls, []
+        Z.check_cfl_zoom(zref, st, 3600, 1, 3600)
+        res["check_cfl"] = lib.calls
+        out[name] = res
+    return out
+
+
+def run_traces(names=TRACE_RUNS):
+    """pydyn's own driver over its real host bodies on the runs whose Check_CFL rejects steps,
+    every body call recorded with the mass-only bodies' returns, plus ["interpolate", state,
+    t] where the run sets the meteo of a time and ["interval", ndyn, n] at each interval's end:
+    the sequence a device module must reproduce call for call."""
+    out = {}
+    for name in names:
+        config, lm, seed, nsteps, umax = STEP_RUNS[name][:5]
+        zref, st, cst, _, _ = _reference_case(config, lm, seed, umax=umax)
+        from pydyn import zoom as Z
+
+        from pydyn_gb300 import synth
+
+        zoom, met, _ = synth.case(config, lm, seed, 1, umax=umax)
+        meteo = {r: [met.fluxes(r, k) for k in (0, 1)] for r in zref.regions()}
+        real = st.lib
+        lib = _Trace(real)
+        st.lib = cst.lib = lib
+
+        def interp(s, t):
+            lib.calls.append(["interpolate", "<main>" if s is st else "<cfl>", float(t)])
+            a1, a2 = synth.weights(t)
+            for r in zref.regions():
+                (pu0, pv0), (pu1, pv1) = meteo[r]
+                s[r]["pu"].data[...] = a1 * pu0 + a2 * pu1
+                s[r]["pv"].data[...] = a1 * pv0 + a2 * pv1
+
+        t = 0.0
+        conv = {r: _no_convection(zref, r) for r in zref.regions()}
+        for _ in range(nsteps):
+            for r in zref.regions():
+                for fname in ("m", "sp"):
+                    cst[r][fname].data[...] = st[r][fname].data
+            lib.calls.append(["copy_m_sp"])
+            t0 = t
+            ndyn, n, _ = Z.check_cfl_zoom(zref, cst, 3600, 1, 3600, lambda z, s, i, nd: interp(s, t0 + (i - 0.5) * nd))
+            for k in range(n):
+                interp(st, t0 + k * ndyn + ndyn / 2.0)
+                Z.setup_massflow(zref, st, ndyn)
+                Z.step(zref, st, conv, ndyn, limits=True, inverse="crout")
+            lib.calls.append(["interval", ndyn, n])
+            t = t0 + 3600.0
+        st.lib = cst.lib = real
+        out[name] = lib.calls
+    return out
+
+
 def save(cases, path):
     flat = {}
     for name, (ins, outs, meta) in cases.items():
@@ -501,6 +671,10 @@ if __name__ == "__main__":
     if "adjoint" in what:
         save(adjoint_goldens(), HERE / "adjoint.npz")
         print("wrote", HERE / "adjoint.npz")
+    if "traces" in what:
+        path = HERE / "traces.json"
+        path.write_text(json.dumps({"plans": plan_traces(), "runs": run_traces()}) + "\n")
+        print("wrote", path)
     if "steps" in what:  # `steps [name ...]`: those runs only, the others kept
         path = HERE / "steps.json"
         old = json.loads(path.read_text()) if path.exists() else {}

@@ -1,27 +1,28 @@
 """The device against the oracle body by body through whole intervals of the production trees
-(glb6x4, glb3x2, glb3x2 + nam1x1): after every body the driver calls, every state array of
-every region must be bitwise equal; a failure names the first body that diverged."""
+(glb6x4, glb3x2, glb3x2 + nam1x1): the package's planned sequence (pydyn_gb300.plan) issues every
+body on both, and after each every state array of every region must be bitwise equal; a failure
+names the first body that diverged."""
 
 import pytest
 from lockstep import LockState
 
 
 def _interval(zoom, lock, cst_lock, t0, weights_dev, orc):
-    from pydyn_gb300 import driver as D
+    from pydyn_gb300 import plan as P
 
     def interpolate(z, s, i, ndyn):
         t = t0 + (i - 0.5) * ndyn
         weights_dev(s.dev_st, t)
         orc.interpolate(s.orc_st, t)
 
-    ndyn, n, _ = D.check_cfl_zoom(zoom, cst_lock, 3600, 1, 3600, interpolate)
+    ndyn, n, _ = P.check_cfl(zoom, cst_lock, 3600, 1, 3600, interpolate)
     for k in range(n):
         t = t0 + k * ndyn + ndyn / 2.0
         weights_dev(lock.dev_st, t)
         orc.interpolate(lock.orc_st, t)
         lock.compare("interpolation")
-        D.setup_massflow(zoom, lock, ndyn)
-        D.step(zoom, lock, None, ndyn, limits=True)
+        P.setup_massflow(zoom, lock, ndyn)
+        P.step(zoom, lock, None, ndyn, limits=True)
     return ndyn, n
 
 
