@@ -41,13 +41,19 @@ sys.path.insert(0, str(ROOT))
 
 SECONDS_A_YEAR = 365.0 * 86400.0
 WORKLOADS = {
-    # name: (tree, levels, physics, seed, convection levels)
+    # name: (tree, levels, physics (False, True: full, "convection"), seed, convection levels)
     "glb6x4": ("glb6x4", 25, False, 11, None),
     "glb3x2-adv": ("glb3x2", 34, False, 21, None),
     "glb3x2+nam1x1-adv": ("glb3x2+nam1x1", 34, False, 31, None),
     "glb3x2": ("glb3x2", 34, True, 41, 34),
     "glb3x2+nam1x1": ("glb3x2+nam1x1", 34, True, 42, 34),
+    # pydyn's own GPU benchmark case (pydyn gpu/bench.py:34-41): glb3x2 + a 72 x 44 child, convection
+    # over 26 levels on a given dkg, no Calc_Kzz, emission or chemistry
+    "a100-case": ("glb3x2+nam72x44", 34, "convection", 51, 26),
 }
+# published numbers of the same metric on the same workload: the A100's interval replayed as a
+# CUDA graph, 6.8 ms (pydyn docs/gpu_port.md:196-202)
+PUBLISHED = {"a100-case": 60.1}
 DEFAULT = "glb3x2+nam1x1"
 BYTES_PER_CELL = {"_dynamu_region1": 12, "_dynamv_region1": 12, "_dynamw_region1": 11, "_dynamu_child": 12,
                   "_dynamv_child": 12, "_dynamw_child": 11, "convec_region": 14, "chemistry_region": 11,
@@ -73,7 +79,17 @@ def metric_name(workload):
     """The headline metric's name for the full-physics glb3x2 + nam1x1 tree, else the workload's."""
     if workload == "glb3x2+nam1x1":
         return "sim-years/hour glb3×2+nam1×1 FP64-bitwise"
+    if workload == "a100-case":
+        return "sim-years/hour glb3×2+nam1×1 (72×44) lmax 26 convection-only interval FP64-bitwise"
     return f"sim-years/hour {workload} FP64-bitwise"
+
+
+def step_bytes_per_cell(physics, tref):
+    """Algorithmic bytes a cell of a region with time refinement tref moves per step at nt = 1:
+    2 tref half steps of x, y, z (296 B), plus v (112 B) with any physics and c (88 B) with full
+    physics; then dynam0 (40 B), Calc_Kzz (40 B, full physics) and Check_CFL (248 B) once."""
+    b_half = 296 + (112 if physics else 0) + (88 if physics is True else 0)
+    return 2 * tref * b_half + 40 + (40 if physics is True else 0) + 248
 
 
 def sim_years_per_hour(seconds_per_step, step_seconds=3600.0):
@@ -350,10 +366,9 @@ def run_ensemble(args, ws, rank):
     step_bytes = 0
     hbm, how = peaks()
     for fw in ens.runs:
-        b_half = 496
         for r in fw.zoom.regions():
             g = fw.zoom.g(r)
-            step_bytes += g.im * g.jm * fw.zoom.lm * (2 * g.tref * b_half + 40 + 40 + 248)
+            step_bytes += g.im * g.jm * fw.zoom.lm * step_bytes_per_cell(True, g.tref)
     line = {
         "metric": "member-years/hour, 256-member ensemble (128 glb6×4, 96 glb3×2, 32 glb3×2+nam1×1) FP64-bitwise",
         "value": n * sim_years_per_hour(batched) * ws,
@@ -598,8 +613,7 @@ def main():
                         "note": "dense-equivalent flops of the reference's inverse per second; peak = the "
                                 "measured DMUL/DADD issue rate"}  # fmt: skip
 
-    b_half = (496 if physics else 296)  # bytes per cell per half step at nt = 1
-    step_bytes = sum(n * (2 * fw.zoom.g(r).tref * b_half + 40 + (40 if physics else 0) + 248) for r, n in cells.items())
+    step_bytes = sum(n * step_bytes_per_cell(physics, fw.zoom.g(r).tref) for r, n in cells.items())
     total_time = sum(v[1] for v in bodies.values())
     line = {
         "metric": metric_name(args.config),
@@ -607,7 +621,9 @@ def main():
         "unit": "sim-years/hour",
         "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": sec_per_step * 1e3,
-        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "higher_is_better": True, "scaling": "weak", "dtype": "f64",
+        "vs_baseline": (sim_years_per_hour(sec_per_step) * ws / PUBLISHED[args.config]
+                        if args.config in PUBLISHED else None),
         "data": "synthetic (seeded meteo of the configuration's shape; pydyn_gb300.synth)",
         "config": workload_config(args.config, ws),
         "roofline": roof,

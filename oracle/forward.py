@@ -40,6 +40,7 @@ def oracle_tree(zoom):
 
 class OracleRun:
     def __init__(self, config, lm, seed, nt=1, umax=40.0, physics=False, lmax=None):
+        """physics: False, True (or "full") or "convection", as pydyn_gb300.forward.Forward's."""
         gen_zoom, self.met, fields = synth.case(config, lm, seed, nt, umax=umax)
         self.zoom = oracle_tree(gen_zoom)
         self.st, self.cst = HostState(self.zoom, nt), HostState(self.zoom, nt)
@@ -51,7 +52,8 @@ class OracleRun:
         if physics:
             from .physics import OraclePhysics
 
-            spec = synth.Physics(gen_zoom, self.met, seed, lm if lmax is None else lmax)
+            kind = "full" if physics is True else physics
+            spec = synth.Physics(gen_zoom, self.met, seed, lm if lmax is None else lmax, kind=kind)
             self.physics = OraclePhysics(self.zoom, spec)
             self.physics.init(self.st)
         self.t = 0.0

@@ -28,6 +28,9 @@ class OraclePhysics:
     def step(self, st, t0, ndyn):
         """(conv, driver kwargs) of the step from t0, after Setup_MassFlow."""
         spec, zoom = self.spec, self.zoom
+        if spec.kind == "convection":  # pydyn's GPU benchmark inputs: convection on a given dkg alone
+            return {r: {**spec.region[r]["conv"], "dkg": spec.region[r]["dkg"], "lmax": spec.lmax}
+                    for r in zoom.regions()}, {}  # fmt: skip
         a1, a2 = synth.weights(t0 + ndyn / 2.0)
         conv = {}
         for r in zoom.regions():

@@ -39,9 +39,10 @@ class Forward:
 
     def __init__(self, dev, config="glb6x4", lm=25, seed=0, nt=1, ndyn=3600, nread=3600, limits=True, physics=False,
                  umax=40.0, lmax=None, wind_scale=1.0, physics_seed=None):  # fmt: skip
-        """physics: with convection (Kzz folded in), emission and CH4 chemistry over lmax levels
-        (default lm), on the inputs of pydyn_gb300.synth.Physics drawn from physics_seed (default
-        seed); without, advection only.  wind_scale multiplies the meteo's winds."""
+        """physics: True (or "full") with convection (Kzz folded in), emission and CH4 chemistry
+        over lmax levels (default lm), on the inputs of pydyn_gb300.synth.Physics drawn from
+        physics_seed (default seed); "convection": convection alone on a given dkg, the inputs of
+        pydyn's own GPU benchmark; False: advection only.  wind_scale multiplies the meteo's winds."""
         self.dev = dev
         self.zoom, self.met, fields = synth.case(config, lm, seed, nt, umax=umax, wind_scale=wind_scale)
         self.st = ZoomState.from_host(dev, self.zoom, fields)
@@ -60,7 +61,8 @@ class Forward:
             from .physics import Physics
 
             pseed = seed if physics_seed is None else physics_seed
-            spec = synth.Physics(self.zoom, self.met, pseed, lm if lmax is None else lmax)
+            kind = "full" if physics is True else physics
+            spec = synth.Physics(self.zoom, self.met, pseed, lm if lmax is None else lmax, kind=kind)
             self.physics = Physics(dev, self.zoom, spec, {r: self.st[r]["dxyp"] for r in self.zoom.regions()})
             self.physics.init_state(self.st)
         self.graphs = {}
@@ -167,26 +169,27 @@ class Forward:
         joins = []
         forked = None
         sides = (self.prep or []) + (self.aux or [])
+        if self.physics is not None:
+            self.physics.prepare_step(self.nread)
         if sides:  # the side contexts start from the step's own setup
-            if self.physics is not None:
-                self.physics.prepare_step(self.nread)
             forked = self.dev.event()
             forked.record()
             for aux in sides:
                 aux.wait(forked)
         if self.physics is not None:
-            # each region's Calc_Kzz on a stream of its own: beside the region's advection too,
-            # which a child runs on its own side context
-            for r, prep in zip(zoom.regions(), self.prep, strict=True):
-                with self.dev.redirect(prep):
-                    self.physics.prepare_region(self, r)
-                joins.append(prep.event())
-                joins[-1].record()
-            # a region's side stream joins at the region's first convection (dkg; the rate
-            # constants follow in chemistry).  Until then the step's advection and exchange run
-            # beside it: they read and write none of Calc_Kzz's arrays (sp, pu, pv, t, q in; dkg,
-            # krates out) -- sp changes only in m2phlb after the region's first v
-            self.physics.pending = {r: (self.dev, j) for r, j in zip(zoom.regions(), joins, strict=True)}
+            if self.prep:
+                # each region's Calc_Kzz on a stream of its own: beside the region's advection
+                # too, which a child runs on its own side context
+                for r, prep in zip(zoom.regions(), self.prep, strict=True):
+                    with self.dev.redirect(prep):
+                        self.physics.prepare_region(self, r)
+                    joins.append(prep.event())
+                    joins[-1].record()
+                # a region's side stream joins at the region's first convection (dkg; the rate
+                # constants follow in chemistry).  Until then the step's advection and exchange
+                # run beside it: they read and write none of Calc_Kzz's arrays (sp, pu, pv, t, q
+                # in; dkg, krates out) -- sp changes only in m2phlb after the region's first v
+                self.physics.pending = {r: (self.dev, j) for r, j in zip(zoom.regions(), joins, strict=True)}
             conv, kw2 = self.physics.driver_args()
             kw.update(kw2)
         sched = None
@@ -263,7 +266,7 @@ class Forward:
             with self.dev.redirect(self.aux_cfl):
                 self._enqueue_rehearsal()
             self.aux_cfl.sync()
-            if self.physics is not None:
+            if self.physics is not None and self.physics.full:
                 # one per region for Calc_Kzz, its work space sized by an uncaptured run of it
                 self.prep = [Device(self.dev.ordinal) for _ in self.zoom.regions()]
                 for r, prep in zip(self.zoom.regions(), self.prep, strict=True):

@@ -38,8 +38,10 @@ class Physics:
     bodies that use them."""
 
     def __init__(self, dev, zoom, spec, dxyp):
-        """dxyp: {region: DevArray (jm)} the cell areas."""
+        """dxyp: {region: DevArray (jm)} the cell areas.  A spec of kind "convection" carries
+        convection's inputs with a given dkg alone: no Calc_Kzz, emission or chemistry."""
         self.dev, self.zoom, self.spec = dev, zoom, spec
+        self.full = spec.kind == "full"
         self.lmax = spec.lmax
         up = lambda a, dtype=np.float64: DevArray.from_host(dev, np.ascontiguousarray(a, dtype=dtype))  # noqa: E731
         self.at, self.bt = up(zoom.at), up(zoom.bt)
@@ -63,40 +65,50 @@ class Physics:
             ncol = len(cols)
             d = {
                 "conv": {k: up(v, np.int32 if k.startswith("cloud") else np.float64) for k, v in R["conv"].items()},
-                "t": up(R["kzz"]["t"]), "q": up(R["kzz"]["q"]),
-                "surface": [up(R["kzz"]["surface"][k]) for k in K.KZZ_SURFACE],
-                "spm": [up(s) for s in R["kzz"]["spm"]],
-                "spm_now": DevArray.zeros(dev, (0, g.im - 1), (0, g.jm - 1)),
-                "dkg": DevArray.zeros(dev, (0, g.im - 1), (0, g.jm - 1), (0, self.lmax - 1)),
-                "krates": DevArray.zeros(dev, (0, g.im - 1), (0, g.jm - 1), (0, zoom.lm - 1), (0, 1)),
-                "chem": {k: up(v) for k, v in R["chem"].items()},
-                "flux": up(R["flux"]),
-                "factors": DevArray.zeros(dev, (0, 2 * g.tref - 1), (0, g.im - 1)),
+                # dkg: Calc_Kzz's output each step, or the case's given field (convection-only inputs)
+                "dkg": DevArray.zeros(dev, (0, g.im - 1), (0, g.jm - 1), (0, self.lmax - 1)) if self.full
+                       else up(R["dkg"]),
                 "cols": up(cols if ncol else np.zeros((0, 2)), np.int32),
                 "ncol": ncol,
-                "cache": (DevArray.zeros(dev, (0, max(ncol, 1) * self.lmax * self.lmax - 1)),
-                          DevArray.zeros(dev, (0, max(ncol, 1) * self.lmax - 1)),
-                          DevArray.from_host(dev, np.full(max(ncol, 1), -1, dtype=np.int32)), self.epoch),
-                # chemistry's paired-call cache: 8 doubles per owned cell, keyed by the step counter
-                "chem_cache": DevArray.zeros(dev, (0, max(ncol, 1) * zoom.lm * 8 - 1)),
+                "cache": self._inverse_cache(ncol),
                 "dxyp": dxyp[r],
                 "grid": ((g.xend - g.xbeg) / g.im, (g.yend - g.ybeg) / g.jm, float(g.ybeg)),
             }  # fmt: skip
+            if self.full:
+                d.update({
+                    "t": up(R["kzz"]["t"]), "q": up(R["kzz"]["q"]),
+                    "surface": [up(R["kzz"]["surface"][k]) for k in K.KZZ_SURFACE],
+                    "spm": [up(s) for s in R["kzz"]["spm"]],
+                    "spm_now": DevArray.zeros(dev, (0, g.im - 1), (0, g.jm - 1)),
+                    "krates": DevArray.zeros(dev, (0, g.im - 1), (0, g.jm - 1), (0, zoom.lm - 1), (0, 1)),
+                    "chem": {k: up(v) for k, v in R["chem"].items()},
+                    "flux": up(R["flux"]),
+                    "factors": DevArray.zeros(dev, (0, 2 * g.tref - 1), (0, g.im - 1)),
+                    # chemistry's paired-call cache: 8 doubles per owned cell, keyed by the step counter
+                    "chem_cache": DevArray.zeros(dev, (0, max(ncol, 1) * zoom.lm * 8 - 1)),
+                })  # fmt: skip
+            else:
+                d["chem_cache"] = None
             segs = [("far", listed(own & ~inside)), ("edge", listed(own & inside))] if inside.any() else []
             d["segments"] = [{"name": "all", "cols": d["cols"], "ncol": ncol, "cache": d["cache"],
                               "chem_cache": d["chem_cache"]}] if not segs else [
                 {"name": name, "cols": up(c if len(c) else np.zeros((0, 2)), np.int32), "ncol": len(c),
-                 "cache": (DevArray.zeros(dev, (0, max(len(c), 1) * self.lmax * self.lmax - 1)),
-                           DevArray.zeros(dev, (0, max(len(c), 1) * self.lmax - 1)),
-                           DevArray.from_host(dev, np.full(max(len(c), 1), -1, dtype=np.int32)), self.epoch),
-                 "chem_cache": DevArray.zeros(dev, (0, max(len(c), 1) * zoom.lm * 8 - 1))}
+                 "cache": self._inverse_cache(len(c)),
+                 "chem_cache": DevArray.zeros(dev, (0, max(len(c), 1) * zoom.lm * 8 - 1)) if self.full else None}
                 for name, c in segs]  # fmt: skip
             if segs:  # the whole list's caches are the segments' now
                 for a in (*d["cache"][:3], d["chem_cache"]):
-                    a.free()
+                    if a is not None:
+                        a.free()
                 d["cache"], d["chem_cache"] = None, None
             self.r[r] = d
         self.ndyn = None
+
+    def _inverse_cache(self, ncol):
+        """Convection's kept inverses of ncol columns, the masses they were made from, their tags."""
+        dev, n = self.dev, self.lmax
+        return (DevArray.zeros(dev, (0, max(ncol, 1) * n * n - 1)), DevArray.zeros(dev, (0, max(ncol, 1) * n - 1)),
+                DevArray.from_host(dev, np.full(max(ncol, 1), -1, dtype=np.int32)), self.epoch)  # fmt: skip
 
     # -------------------------------------------------------------- host side, outside capture
     pending = {}  # region -> (device, event): a forked preparation not yet joined
@@ -129,6 +141,8 @@ class Physics:
     def put_factors(self, t0, ndyn):
         """The OH factors of every region's half steps of the step from t0, into device memory
         (stream-ordered: a step already enqueued still reads the previous ones)."""
+        if not self.full:
+            return
         for r, d in self.r.items():
             d["factors"].upload(self.spec.factors(r, t0, ndyn))
 
@@ -164,7 +178,10 @@ class Physics:
         N.check(self.dev.L.gb_iadd(self.dev.h, self.epoch.ptr, 1), "gb_iadd")
 
     def prepare_region(self, fwd, r):
-        """Region r's spm at the step's middle, Calc_Kzz and the rate constants."""
+        """Region r's spm at the step's middle, Calc_Kzz and the rate constants (nothing for
+        convection-only inputs)."""
+        if not self.full:
+            return
         d, g, f = self.r[r], self.zoom.g(r), fwd.st[r]
         fwd.interp_into(d["spm_now"], d["spm"][0], d["spm"][1])
         dx, dy, ybeg = d["grid"]
@@ -175,6 +192,8 @@ class Physics:
 
     def driver_args(self):
         """The driver's (conv, kwargs) of a prepared step."""
+        if not self.full:
+            return {r: self for r in self.r}, {}
         return {r: self for r in self.r}, {"sources": self.sources, "chemistry": self.chemistry}
 
     def convec_region(self, zoom, st, region, ndyn, inverse="crout"):

@@ -321,15 +321,38 @@ class Physics:
             child), injected at level 1 as flux x area x the region's half step
 
     The temperature falls from 270-300 K at the surface to about 215 K at the top (200-300 K),
-    so the Kzz boundary layers grow over heated land and stay shallow over the sea."""
+    so the Kzz boundary layers grow over heated land and stay shallow over the sea.
 
-    def __init__(self, zoom, met, seed, lmax, ns=24, ntrop=10, child_density=3.0):
-        self.zoom, self.lmax, self.ns, self.ntrop = zoom, lmax, ns, ntrop
+    kind = "convection" makes the inputs of pydyn's own GPU benchmark instead (convection with a
+    given dkg; no Calc_Kzz, emission or chemistry): per region a rate of 5 % of the mean cell
+    mass per 1800 s, entu, detu and dkg uniform in [0, rate), entd, detd in [0, 0.3 rate), and
+    cloud_top, cloud_lfs uniform in 0..lmax -- nearly every column convective."""
+
+    def __init__(self, zoom, met, seed, lmax, ns=24, ntrop=10, child_density=3.0, kind="full"):
+        if kind not in ("full", "convection"):
+            raise ValueError(f"synth.Physics: kind {kind!r} is neither 'full' nor 'convection'")
+        self.zoom, self.lmax, self.ns, self.ntrop, self.kind = zoom, lmax, ns, ntrop, kind
         self.settings = dict(CHEM_SETTINGS)
         self.region = {}
         for r in zoom.regions():
             rng = np.random.default_rng([seed, 7919, r])
-            self.region[r] = self._region(rng, r, met, 1.0 if r == 1 else child_density)
+            if kind == "convection":
+                self.region[r] = self._convection_only(rng, r, met)
+            else:
+                self.region[r] = self._region(rng, r, met, 1.0 if r == 1 else child_density)
+
+    def _convection_only(self, rng, r, met):
+        g, lmax = self.zoom.g(r), self.lmax
+        m = met.mass(g, met.surface_pressure(g))
+        rate = 0.05 * (math.fsum(m.ravel()) / m.size) / 1800.0
+        shape = (g.im, g.jm, lmax)
+        conv = {
+            "entu": rate * rng.random(shape), "detu": rate * rng.random(shape),
+            "entd": 0.3 * rate * rng.random(shape), "detd": 0.3 * rate * rng.random(shape),
+            "cloud_top": np.floor(rng.random((g.im, g.jm)) * (lmax + 1)).astype(np.int32),
+            "cloud_lfs": np.floor(rng.random((g.im, g.jm)) * (lmax + 1)).astype(np.int32),
+        }  # fmt: skip
+        return {"conv": conv, "dkg": rate * rng.random(shape)}
 
     def _region(self, rng, r, met, density):
         z, g = self.zoom, self.zoom.g(r)

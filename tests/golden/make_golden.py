@@ -230,6 +230,9 @@ class _RefPhysics:
         from pydyn_gb300 import synth
 
         spec, zref = self.spec, self.zref
+        if spec.kind == "convection":  # pydyn's own GPU benchmark's physics: convection on a given dkg
+            return {r: {**spec.region[r]["conv"], "dkg": spec.region[r]["dkg"], "lmax": spec.lmax}
+                    for r in zref.regions()}, {}  # fmt: skip
         a1, a2 = synth.weights(t0 + ndyn / 2.0)
         conv = {}
         for r in zref.regions():
@@ -358,7 +361,7 @@ def adjoint_goldens(nbasis=None, ny=2, seed=5):
     return {"adjoint": ({"y": ys, "delta": delta, "index": idx}, {"ATy": vals, "A_delta": a_delta}, dict(c))}
 
 
-def reference_run(config, lm, seed, nsteps, nt=1, physics=False, keep=None, umax=40.0, lmax=None):
+def reference_run(config, lm, seed, nsteps, nt=1, physics=False, keep=None, umax=40.0, lmax=None, kind="full"):
     """pydyn's own driver (zoom.check_cfl_zoom on a copy of m and sp, then setup_massflow and
     zoom.step, as pydyn forward.py:388-451 runs an interval of one step) on the synthetic case
     of pydyn_gb300.synth.  Returns [(ndyn, n, digest)] per interval; keep: a list that receives
@@ -395,7 +398,7 @@ def reference_run(config, lm, seed, nsteps, nt=1, physics=False, keep=None, umax
 
     phys = None
     if physics:
-        phys = _RefPhysics(zref, synth.Physics(zoom, met, seed, lm if lmax is None else lmax), fields)
+        phys = _RefPhysics(zref, synth.Physics(zoom, met, seed, lm if lmax is None else lmax, kind=kind), fields)
         phys.init(st)
     out, t = [], 0.0
     for _ in range(nsteps):
@@ -439,11 +442,13 @@ STEP_RUNS = {  # name: (tree, lm, seed, intervals, umax[, physics lmax, interval
     "config2-adv": ("glb3x2+nam1x1", 34, 31, 3, 40.0),
     "two-phys": ("two", 8, 21, 6, 40.0, 8, 6),
     "three-phys": ("three", 6, 22, 4, 40.0, 6, 4),
-    "config1": ("glb3x2", 34, 41, 3, 40.0, 34, 1),
+    "config1": ("glb3x2", 34, 41, 24, 40.0, 34, 1),  # one simulated day
     "config2": ("glb3x2+nam1x1", 34, 42, 2, 40.0, 34, 1),
     "two-phys-nt3": ("two", 8, 24, 4, 40.0, 8, 2, {"nt": 3}),
     "config0-nt8": ("glb6x4", 25, 16, 3, 40.0, {"nt": 8}),
     "config1-nt12": ("glb3x2", 34, 43, 2, 40.0, 34, 1, {"nt": 12}),
+    # pydyn's own GPU benchmark case: glb3x2 + a 72 x 44 child, convection over 26 levels on a given dkg
+    "a100-case": ("glb3x2+nam72x44", 34, 51, 24, 40.0, 26, 1, {"kind": "convection"}),
 }
 
 
@@ -458,15 +463,16 @@ def step_goldens(names=None):
         spec = spec[:-1] if opts else spec
         config, lm, seed, nsteps, umax = spec[:5]
         lmax = spec[5] if len(spec) > 5 else None
-        nt = opts.get("nt", 1)
+        nt, kind = opts.get("nt", 1), opts.get("kind", "full")
         t = time.perf_counter()
-        runs = reference_run(config, lm, seed, nsteps, nt=nt, umax=umax, physics=lmax is not None, lmax=lmax)
+        runs = reference_run(config, lm, seed, nsteps, nt=nt, umax=umax, physics=lmax is not None, lmax=lmax,
+                             kind=kind)  # fmt: skip
         res[name] = {"config": config, "lm": lm, "seed": seed, "umax": umax, "steps": [list(x) for x in runs],
                      "reference_seconds_per_interval": (time.perf_counter() - t) / nsteps}  # fmt: skip
         if nt != 1:
             res[name]["nt"] = nt
         if lmax is not None:
-            res[name].update(physics=True, lmax=lmax, cpu_prefix=spec[6])
+            res[name].update(physics=True if kind == "full" else kind, lmax=lmax, cpu_prefix=spec[6])
         print(name, runs[-1], res[name]["reference_seconds_per_interval"])
     return res
 
