@@ -1,7 +1,7 @@
 // convec: implicit convection with Kzz diffusion folded into one matrix per column, inverted
 // by Crout LU without pivoting, applied to the tracer mass and (by its diagonal) the slopes.
 //
-// Six launches, shaped so that the FP64 pipe -- this GPU's scarcest unit -- issues with its
+// Seven launches, shaped so that the FP64 pipe -- this GPU's scarcest unit -- issues with its
 // lanes full:
 //   k_convec_chains  three threads per owned column: whether its kept inverse still holds, the
 //                    updraft and the downdraft mass fluxes carried level to level
@@ -14,14 +14,18 @@
 //   k_convec_tri     one thread per cloudless column (tridiagonal conv1): the same LU and L^-1
 //                    by the recurrence their non-zero elements follow
 //   k_convec_lu      a group of 8, 16 or 32 lanes per other column whose inverse is made
-//                    (beside k_convec_tri, on the context's side stream): LU right-looking
-//                    (each step's trailing (row, column) elements packed onto the lanes), then
-//                    L^-1 by forward substitution in place of L (row k's terms applied to every
-//                    later row at once, the (row, column) elements packed onto the lanes).  U
-//                    goes to the work space, L^-1 to the inverse's place.
-//   k_convec_apply   one thread per (column, column of the inverse): the back substitution
-//                    U X = L^-1; then, whole columns per block, one thread per (column, level):
-//                    the slopes times the inverse's diagonal and rm = C rm accumulated in k.
+//                    (beside k_convec_tri, on the context's side stream), on the leading block
+//                    of its matrix that holds every off-band non-zero (the cloud's levels): LU
+//                    right-looking (each step's trailing (row, column) elements packed onto the
+//                    lanes), then L^-1 by forward substitution in place of L (row k's terms
+//                    applied to every later row at once, the (row, column) elements packed onto
+//                    the lanes).  U goes to the work space, L^-1 to the inverse's place.
+//   k_convec_tail    one thread per column k_convec_lu split: the band recurrence of the rows
+//                    above its block (tridiagonal there), continued from the block's last pivot
+//   k_convec_apply   one thread per (column, column of the inverse): the band rows of L^-1,
+//                    then the back substitution U X = L^-1; then, whole columns per block, one
+//                    thread per (column, level): the slopes times the inverse's diagonal and
+//                    rm = C rm accumulated in k.
 // The reference's operation order is kept element by element -- every element receives its
 // terms in the same k order as in the row-by-row form -- and work is skipped only where a
 // multiplier is exactly zero (x - w * y with w = +-0 returns x unless x is a zero, and the
@@ -54,6 +58,7 @@ struct CArgs {
     int32_t *fresh;      // ncol work space: 1 where this call makes the column's inverse
     int32_t *rend;       // ncol * n work space: per row of U, one past its last non-zero
     double *tband;       // ncol * 2n work space: a tridiagonal column's U diagonal, then L's band
+    int32_t *eblk;       // ncol work space: the leading block k_convec_lu factorised (n: all of it)
     double *cache_m;     // ncol * n, or null (no reuse)
     int32_t *cache_tag;  // ncol
     const int32_t *epoch;
@@ -106,6 +111,7 @@ __device__ void chain_cache(const CArgs &A, int c, int i, int j) {
         A.cache_tag[c] = *A.epoch;
     }
     A.fresh[c] = 1;
+    A.eblk[c] = A.n;
 }
 
 // The chains' carried part: the updraft mass flux amu of column c (levels 1..n from the bottom)
@@ -180,19 +186,25 @@ __global__ void __launch_bounds__(GB_TUNE_MAX_CELL) k_convec_ratios(CArgs A) {
     if (!A.fresh[c]) return;
     const int i = A.cols[2 * c], j = A.cols[2 * c + 1];
     double *amu = chains(A, c), *zu = amu + (n + 1), *amd = zu + (n + 1), *zd = amd + (n + 1);
-    {
-        const double mu = amu[k - 1], eu = AT(A.entu, i, j, k - 1), du = AT(A.detu, i, j, k - 1);
+    {  // a level above the cloud top is inactive whatever its ratio: its division is not made
         const bool act = A.top[i * A.ts0 + j * A.ts1] >= k;
-        const double a = mu + eu - du;
-        const double z = a > 0.0 ? max0(1.0 - du / (mu + eu)) : 0.0;
-        zu[k] = act ? z : -1.0;
+        double z = -1.0;
+        if (act) {
+            const double mu = amu[k - 1], eu = AT(A.entu, i, j, k - 1), du = AT(A.detu, i, j, k - 1);
+            const double a = mu + eu - du;
+            z = a > 0.0 ? max0(1.0 - du / (mu + eu)) : 0.0;
+        }
+        zu[k] = z;
     }
     if (k >= 2) {
-        const double md = amd[k], ed = AT(A.entd, i, j, k - 1), dd = AT(A.detd, i, j, k - 1);
         const bool act = A.lfs[i * A.ts0 + j * A.ts1] >= k;
-        const double a = md - ed + dd;
-        const double z = a < 0.0 ? max0(1.0 + dd / (md - ed)) : 0.0;
-        zd[k] = act ? z : -1.0;
+        double z = -1.0;
+        if (act) {
+            const double md = amd[k], ed = AT(A.entd, i, j, k - 1), dd = AT(A.detd, i, j, k - 1);
+            const double a = md - ed + dd;
+            z = a < 0.0 ? max0(1.0 + dd / (md - ed)) : 0.0;
+        }
+        zd[k] = z;
     } else {
         zd[0] = zd[1] = -1.0;
     }
@@ -228,15 +240,22 @@ __global__ void __launch_bounds__(GB_TUNE_MAX_CELL) k_convec_matrix(CArgs A) {
     const int i = A.cols[2 * c], j = A.cols[2 * c + 1];
     // the quotients this column of the matrix uses, each divided once: at level k = l + 1 the
     // chain starts (qed, qeu) and the sub-diagonal terms (qamd, qdk1); at k = l the diagonal's
-    // (qamu, qdk2)
+    // (qamu, qdk2).  They share the divisor m(l): one reciprocal, each quotient correctly
+    // rounded from it (div_by_recip: the division's bits)
     const double ml = AT(A.m, i, j, l);
-    const double qed = -AT(A.entd, i, j, l) / ml, qeu = AT(A.entu, i, j, l) / ml;
+    const double yl = recip_for(ml);
     const bool sub = l + 1 <= n - 1, dia = l >= 1;
-    const double qamd = sub ? amd[l + 1] / ml : 0.0, qdk1 = sub ? AT(A.dkg, i, j, l) / ml : 0.0;
-    const double qamu = dia ? amu[l] / ml : 0.0, qdk2 = dia ? AT(A.dkg, i, j, l - 1) / ml : 0.0;
+    const double qamd = sub ? div_by_recip(amd[l + 1], ml, yl) : 0.0;
+    const double qdk1 = sub ? div_by_recip(AT(A.dkg, i, j, l), ml, yl) : 0.0;
+    const double qamu = dia ? div_by_recip(amu[l], ml, yl) : 0.0;
+    const double qdk2 = dia ? div_by_recip(AT(A.dkg, i, j, l - 1), ml, yl) : 0.0;
     double *out = A.abuf + (size_t)c * n * n;
     const double mdt = -A.dt;
     const int top = A.top[i * A.ts0 + j * A.ts1], lfs = A.lfs[i * A.ts0 + j * A.ts1];
+    // every element of rows k >= kend (1-based) is -dt (+0 - +0): above both the cloud and the
+    // diagonal's two levels, the updraft chain u is +0 (its ratios are inactive), the downdraft
+    // chain ends at the diagonal, and f(k - 1, l), f(k, l) are (+0 - +0) + -0 = +0
+    const double off = mdt * (0.0 - 0.0);
     if (top <= 0 && lfs <= 1) {
         // no cloud: every chain level is inactive, so u and fd are +0 throughout and f(k, l) is
         // +0 except f(l, l) = (+0 - qamu) - qdk2 and f(l+1, l) = (+0 - qamd) + qdk1 -- the
@@ -244,7 +263,6 @@ __global__ void __launch_bounds__(GB_TUNE_MAX_CELL) k_convec_matrix(CArgs A) {
         // -dt (+0 - +0) off the three bands
         const double fll = (dia && l <= n - 1) ? (0.0 - qamu) - qdk2 : 0.0;
         const double fl1 = sub ? (0.0 - qamd) + qdk1 : 0.0;
-        const double off = mdt * (0.0 - 0.0);
         for (int k = 1; k <= n; ++k) {
             double e = off;
             if (k >= l && k <= l + 2) {
@@ -257,6 +275,8 @@ __global__ void __launch_bounds__(GB_TUNE_MAX_CELL) k_convec_matrix(CArgs A) {
         }
         return;
     }
+    const double qed = div_by_recip(-AT(A.entd, i, j, l), ml, yl), qeu = div_by_recip(AT(A.entu, i, j, l), ml, yl);
+    const int kend = min(n, max(top, l + 1) + 1);  // the last row with terms of its own
     double fd[NMAX];
     {
         // Each statement below is one instruction for every lane of the warp (a lane's l selects its
@@ -273,7 +293,7 @@ __global__ void __launch_bounds__(GB_TUNE_MAX_CELL) k_convec_matrix(CArgs A) {
         // x - y = x + (-y) exactly
         const double nqdk2 = -qdk2;
         double u = 0.0, fprev = 0.0;
-        for (int k = 1; k <= n; ++k) {
+        for (int k = 1; k <= kend; ++k) {
             const double z = zu[k];
             // the updraft chain from l + 1 up: qeu z at k = l + 1, then u z; zero below
             u = (ge_zero(z) && l <= k - 1) ? ((l == k - 1) ? qeu : u) * z : 0.0;
@@ -290,6 +310,7 @@ __global__ void __launch_bounds__(GB_TUNE_MAX_CELL) k_convec_matrix(CArgs A) {
             out[(size_t)(k - 1) * n + l] = e;
             fprev = fk;
         }
+        for (int k = kend + 1; k <= n; ++k) out[(size_t)(k - 1) * n + l] = off;
     }
 }
 
@@ -373,9 +394,32 @@ __device__ __forceinline__ int div_by(int e, int d, unsigned magic) {
     return d > 1 ? (int)__umulhi((unsigned)e, magic) : e;
 }
 
+// Where the warp LU stops: above its cloud a column's conv1 is tridiagonal (diffusion alone), and
+// Crout's LU there does, in its non-zero elements, only the band recurrence of k_convec_tri.  E is
+// one past the last row or column of an off-band non-zero of conv1: the LU of the leading E x E
+// block is the reference's on those elements (no step k < E - 1 reaches a column >= E, and the rows
+// >= E take only terms with a +-0 multiplier L(r, k), which leave a finite value as it is up to
+// the sign of a zero -- never read again: the inverse's tail rows are built from the band), and
+// from row E on the band recurrence continues from the block's last pivot (k_convec_tail).  The
+// split is taken when the band from row E on passes k_convec_tri's test (finite, non-zero) and
+// the block's elements and pivots stay finite and non-zero; otherwise E = n (the whole LU here).
 // G lanes per column (32 / G columns a warp): every step's divisions and ballots serve the warp's
 // columns at once.  Lanes of a group whose column is not made here (reused, k_convec_tri's, or past
 // the list) take part in the warp's ballots with false predicates and do nothing else.
+template <int G>
+__device__ __forceinline__ int group_max(int v) {
+#pragma unroll
+    for (int o = G / 2; o > 0; o >>= 1) v = max(v, __shfl_xor_sync(FULL_MASK, v, o, G));
+    return v;
+}
+template <int G>
+__device__ __forceinline__ bool group_all(bool p, unsigned gmask_shifted) {
+    return (__ballot_sync(FULL_MASK, !p) & gmask_shifted) == 0;
+}
+__device__ __forceinline__ bool finite(double v) {
+    return (__double_as_longlong(v) & 0x7fffffffffffffffLL) < 0x7ff0000000000000LL;
+}
+
 template <int G>
 __global__ void __launch_bounds__(GB_TUNE_MAX_LU_WARPS * 32) k_convec_lu(CArgs A) {
     extern __shared__ double smem[];
@@ -383,6 +427,7 @@ __global__ void __launch_bounds__(GB_TUNE_MAX_LU_WARPS * 32) k_convec_lu(CArgs A
     constexpr unsigned GMASK = G == 32 ? 0xffffffffu : ((1u << (G % 32)) - 1u);
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int h = lane / G, gl = lane % G;  // the group (column) in the warp, the lane in the group
+    const unsigned gshift = G == 32 ? 0xffffffffu : (GMASK << (h * G));
     const int c = (blockIdx.x * (blockDim.x >> 5) + warp) * MPW + h;
     const int n = A.n;
     // made in this call (k_convec_tri, beside this kernel, turns its columns' 1 into 2: the test
@@ -402,100 +447,181 @@ __global__ void __launch_bounds__(GB_TUNE_MAX_LU_WARPS * 32) k_convec_lu(CArgs A
     double *mult = LU + (size_t)n * n;                                 // n: step k's multipliers L(r, k)
     int32_t *list = reinterpret_cast<int32_t *>(mult + n);             // NMAX: a step's columns or rows
     double *Gm = A.abuf + (size_t)c * n * n;
+    // ---- the leading block: E from conv1's off-band non-zeros, then the band's test from row E on
     if (mine)
         for (int e = gl; e < n * n; e += G) LU[e] = Gm[e];
     __syncwarp();
-    // ---- LU, right-looking: at step k, L's column k (its rows below k divided by U(k, k), final
-    // after the steps before k), then every later element (r, c) receives its term k,
-    // A(r, c) - L(r, k) U(k, c) -- the (row, column) elements packed onto the group's lanes.  Each
-    // element receives its terms in k order, each skipped exactly where Crout's column-by-column
-    // form skips it (the multiplier U(k, c) a zero: above a column's first non-zero such zeros
-    // stay zero), and L's column is divided after all its terms: the same operations on every
-    // element, the same bits.
-    for (int k = 0; k < n; ++k) {
-        if (mine) {
-            const double d = LU[(size_t)k * n + k];
-            for (int r = k + 1 + gl; r < n; r += G) LU[(size_t)r * n + k] = LU[(size_t)r * n + k] / d;
+    int last = -1;
+    if (mine)
+        for (int e = gl; e < n * n; e += G) {
+            const int r = e / n, col = e - r * n;
+            if ((r - col > 1 || col - r > 1) && !is_zero(LU[e])) last = max(last, max(r, col));
         }
-        // row k's non-zeros right of the diagonal, listed in order: the columns step k updates
-        int ncols = 0;
-#pragma unroll
-        for (int s = 0; s < NCH; ++s) {
-            const int col = s * G + gl;
-            const bool p = mine && col > k && col < n && !is_zero(LU[(size_t)k * n + col]);
-            const unsigned b = (__ballot_sync(FULL_MASK, p) >> (h * G)) & GMASK;
-            if (p) list[ncols + __popc(b & ((1u << gl) - 1u))] = col;
-            ncols += __popc(b);
-        }
-        __syncwarp();
-        const int nrow = n - k - 1;
-        const unsigned magic = div_magic(nrow);
+    int E = group_max<G>(last) + 1;
+    {
+        bool tail_ok = true;
         if (mine)
-            for (int e = gl; e < nrow * ncols; e += G) {
-                const int q = div_by(e, nrow, magic), r = k + 1 + (e - q * nrow);
-                const int col = list[q];
-                LU[(size_t)r * n + col] = LU[(size_t)r * n + col] - LU[(size_t)r * n + k] * LU[(size_t)k * n + col];
+            for (int r = E + gl; r < n; r += G)  // rows >= E: the diagonal, and the band's two entries to row r - 1
+                tail_ok = tail_ok && band_ok(LU[(size_t)r * n + r]) &&
+                          (r == 0 || (band_ok(LU[(size_t)r * n + r - 1]) && band_ok(LU[(size_t)(r - 1) * n + r])));
+        bool block_ok = true;
+        if (mine)
+            for (int e = gl; e < E * n; e += G) block_ok = block_ok && (e % n >= E || finite(LU[e]));
+        if (!group_all<G>(tail_ok && block_ok, gshift)) E = n;
+    }
+    // Every loop below runs the warp's largest count (its ballots and __syncwarp take every lane);
+    // a group acts on its own column's steps only (act, k < E).
+    bool act = mine;
+    for (int pass = 0; pass < 2; ++pass) {
+        const int Ew = __reduce_max_sync(FULL_MASK, act ? E : 0);
+        // ---- LU of the leading E x E block, right-looking: at step k, L's column k (its rows below
+        // k divided by U(k, k), final after the steps before k), then every later element (r, c)
+        // receives its term k, A(r, c) - L(r, k) U(k, c) -- the (row, column) elements packed onto
+        // the group's lanes.  Each element receives its terms in k order, each skipped exactly where
+        // Crout's column-by-column form skips it (the multiplier U(k, c) a zero: above a column's
+        // first non-zero such zeros stay zero), and L's column is divided after all its terms: the
+        // same operations on every element, the same bits.
+        for (int k = 0; k < Ew; ++k) {
+            const bool on = act && k < E;
+            if (on) {
+                const double d = LU[(size_t)k * n + k];
+                for (int r = k + 1 + gl; r < E; r += G) LU[(size_t)r * n + k] = LU[(size_t)r * n + k] / d;
             }
+            // row k's non-zeros right of the diagonal inside the block, listed in order: the
+            // columns step k updates
+            int ncols = 0;
+#pragma unroll
+            for (int s = 0; s < NCH; ++s) {
+                const int col = s * G + gl;
+                const bool p = on && col > k && col < E && !is_zero(LU[(size_t)k * n + col]);
+                const unsigned b = (__ballot_sync(FULL_MASK, p) >> (h * G)) & GMASK;
+                if (p) list[ncols + __popc(b & ((1u << gl) - 1u))] = col;
+                ncols += __popc(b);
+            }
+            __syncwarp();
+            if (on) {
+                const int nrow = E - k - 1;
+                const unsigned magic = div_magic(nrow);
+                for (int e = gl; e < nrow * ncols; e += G) {
+                    const int q = div_by(e, nrow, magic), r = k + 1 + (e - q * nrow);
+                    const int col = list[q];
+                    LU[(size_t)r * n + col] = LU[(size_t)r * n + col] - LU[(size_t)r * n + k] * LU[(size_t)k * n + col];
+                }
+            }
+            __syncwarp();
+        }
+        // a split block keeps finite values and non-zero pivots, or the column is made whole
+        bool fine = true;
+        if (act && E < n)
+            for (int e = gl; e < E * n; e += G) {
+                const int r = e / n, col = e - r * n;
+                if (col < E) fine = fine && finite(LU[e]) && (col != r || !is_zero(LU[e]));
+            }
+        const bool all_fine = group_all<G>(fine, gshift);  // every lane: a ballot
+        const bool redo = act && E < n && !all_fine;
+        if (pass == 1 || __ballot_sync(FULL_MASK, redo) == 0) break;
+        // a singular or overflowing block: the whole LU over conv1 again, for those columns alone
+        act = redo;
+        if (redo) {
+            E = n;
+            for (int e = gl; e < n * n; e += G) LU[e] = Gm[e];
+        }
         __syncwarp();
     }
     // ---- forward substitution of the identity: Y = L^-1, in place of L's strict lower triangle
-    // (Y's diagonal is 1 and its upper triangle +0, U stays where it is).  Row k of Y is final
-    // once the terms of rows < k are in; its term then goes to every later row r with
-    // L(r, k) != 0 at once, Y(r, c) = Y(r, c) - L(r, k) Y(k, c) for the columns c <= k, the
-    // (r, c) elements packed onto the group's lanes -- each element still in k order.  Step k is
-    // the first to touch column k of Y: its elements start as the identity's +0 (Y(k, k) is the
+    // (Y's diagonal is 1 and its upper triangle +0, U stays where it is), on the block's rows.
+    // Row k of Y is final once the terms of rows < k are in; its term then goes to every later
+    // row r with L(r, k) != 0 at once, Y(r, c) = Y(r, c) - L(r, k) Y(k, c) for the columns c <= k,
+    // the (r, c) elements packed onto the group's lanes -- each element still in k order.  Step k
+    // is the first to touch column k of Y: its elements start as the identity's +0 (Y(k, k) is the
     // identity's 1), and L(r, k) is taken into `mult` first, since the step overwrites it.
-    for (int k = 0; k < n - 1; ++k) {
+    const int Ew = __reduce_max_sync(FULL_MASK, mine ? E : 0);
+    for (int k = 0; k < Ew - 1; ++k) {
+        const bool on = mine && k < E - 1;
         // the rows below k with L(r, k) != 0, listed in order
         int nr = 0;
 #pragma unroll
         for (int s = 0; s < NCH; ++s) {
             const int r = k + 1 + s * G + gl;
-            const bool p = mine && r < n && !is_zero(LU[(size_t)r * n + k]);
+            const bool p = on && r < E && !is_zero(LU[(size_t)r * n + k]);
             const unsigned b = (__ballot_sync(FULL_MASK, p) >> (h * G)) & GMASK;
             if (p) list[nr + __popc(b & ((1u << gl) - 1u))] = r;
             nr += __popc(b);
         }
-        if (mine)
-            for (int r = k + 1 + gl; r < n; r += G) {  // the lane that tested row r above
+        if (on)
+            for (int r = k + 1 + gl; r < E; r += G) {  // the lane that tested row r above
                 mult[r] = LU[(size_t)r * n + k];
                 LU[(size_t)r * n + k] = 0.0;  // Y(r, k) before its terms: the identity's +0
             }
         __syncwarp();
-        const int w = k + 1;  // the columns 0..k
-        const unsigned magic = div_magic(w);
-        if (mine)
+        if (on) {
+            const int w = k + 1;  // the columns 0..k
+            const unsigned magic = div_magic(w);
             for (int e = gl; e < nr * w; e += G) {
                 const int q = div_by(e, w, magic), col = e - q * w;
                 const int r = list[q];
                 const double ykc = col == k ? 1.0 : LU[(size_t)k * n + col];  // Y(k, col)
                 LU[(size_t)r * n + col] = LU[(size_t)r * n + col] - mult[r] * ykc;
             }
+        }
         __syncwarp();
     }
-    // ---- out: U (the upper triangle with the diagonal) over conv1, L^-1 into the inverse's place,
-    // and for each row r of U one past its last non-zero right of the diagonal (the back
-    // substitution's terms end there: the rest are zeros it would skip)
+    // ---- out: the block's rows -- U (the upper triangle with the diagonal) over conv1, L^-1 into
+    // the inverse's place -- and for each of them one past its last non-zero right of the diagonal
+    // (the back substitution's terms end there: the rest are zeros it would skip).  The rows from
+    // E on are k_convec_tail's and the apply's (their conv1 band stays in place).
     if (mine) {
         double *X = A.inv + (size_t)c * n * n;
-        for (int e = gl; e < n * n; e += G) {
+        for (int e = gl; e < E * n; e += G) {
             const int r = e / n, col = e % n;
             Gm[e] = LU[e];  // the back substitution reads U only (the diagonal and right of it)
             X[e] = r > col ? LU[e] : (r == col ? 1.0 : 0.0);
         }
+        if (gl == 0) A.eblk[c] = E;
     }
     int32_t *rend = A.rend + (size_t)c * n;
-    for (int r = 0; r < n; ++r) {  // (the lists are done with: their last readers passed a __syncwarp)
-        int last = r;
+    for (int r = 0; r < Ew; ++r) {  // (the lists are done with: their last readers passed a __syncwarp)
+        const bool on = mine && r < E;
+        int lastc = r;
 #pragma unroll
         for (int s = 0; s < NCH; ++s) {
             const int col = s * G + gl;
-            const bool p = mine && col > r && col < n && !is_zero(LU[(size_t)r * n + col]);
+            const bool p = on && col > r && col < n && !is_zero(LU[(size_t)r * n + col]);
             const unsigned b = (__ballot_sync(FULL_MASK, p) >> (h * G)) & GMASK;
-            if (b) last = s * G + 31 - __clz(b);
+            if (b) lastc = s * G + 31 - __clz(b);
         }
-        if (mine && gl == 0) rend[r] = last + 1;
+        if (on && gl == 0) rend[r] = lastc + 1;
     }
+}
+
+// thread per column k_convec_lu split (E < n): the band recurrence of k_convec_tri from row E on,
+// continued from the block's last pivot U(E - 1, E - 1) (conv1's own U(0, 0) when E = 0): U's
+// diagonal and L's band for the rows >= E into the band buffer, and their rows' term ends.
+__global__ void __launch_bounds__(GB_TUNE_MAX_COLUMN) k_convec_tail(CArgs A) {
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= A.ncol || A.fresh[c] != 1) return;
+    const int n = A.n, E = A.eblk[c];
+    if (E >= n) return;
+    const double *G = A.abuf + (size_t)c * n * n;
+    int32_t *rend = A.rend + (size_t)c * n;
+    double *ud = A.tband + (size_t)c * 2 * n, *lb = ud + n;
+    int r = E;
+    double uprev;
+    if (E == 0) {
+        uprev = G[0];
+        ud[0] = uprev;
+        r = 1;
+    } else {
+        uprev = G[(size_t)(E - 1) * n + E - 1];
+    }
+    for (; r < n; ++r) {
+        const double l = G[(size_t)r * n + r - 1] / uprev;
+        const double v = G[(size_t)r * n + r] - l * G[(size_t)(r - 1) * n + r];
+        ud[r] = v;
+        lb[r] = l;
+        uprev = v;
+    }
+    for (r = E; r < n; ++r) rend[r] = r + 1 < n ? r + 2 : r + 1;
 }
 
 __global__ void k_convec_apply(CArgs A) {
@@ -505,18 +631,32 @@ __global__ void k_convec_apply(CArgs A) {
     const int c = blockIdx.x * A.cols_per_block + cl;
     const bool live = cl < A.cols_per_block && c < A.ncol;
     double *X = live ? A.inv + (size_t)c * n * n : nullptr;
-    const double *ud = live && A.fresh[c] == 2 ? A.tband + (size_t)c * 2 * n : nullptr;  // tri's diagonal
+    // the rows from E on are band rows (k_convec_tri's columns: all of them; a column k_convec_lu
+    // split: those past its block): U's diagonal and L's band in the band buffer
+    const int fr = live ? A.fresh[c] : 0;
+    const int E = fr == 2 ? 0 : (fr == 1 ? A.eblk[c] : n);
+    const double *ud = E < n ? A.tband + (size_t)c * 2 * n : nullptr;
+    const double *U = live ? A.abuf + (size_t)c * n * n : nullptr;
     // ---- the reciprocals of U's diagonal, one a thread: every quotient of row r shares U(r, r)
-    if (live && A.fresh[c]) recip[cl * n + x] = recip_for(ud ? ud[x] : A.abuf[(size_t)c * n * n + (size_t)x * n + x]);
-    // ---- a cloudless column's L^-1, column x: the forward substitution of the identity with L's
-    // single band, Y(r, x) = +0 - L(r, r-1) Y(r-1, x) below the diagonal (the terms of a zero
-    // L(r, r-1) it skips leave the +0 that this writes), 1 on it, +0 above
-    if (live && A.fresh[c] == 2) {
-        const double *lb = A.tband + (size_t)c * 2 * n + n;
-        for (int r = 0; r < x; ++r) X[(size_t)r * n + x] = 0.0;
-        X[(size_t)x * n + x] = 1.0;
-        double y = 1.0;
-        for (int r = x + 1; r < n; ++r) {
+    if (fr) recip[cl * n + x] = recip_for(x >= E ? ud[x] : U[(size_t)x * n + x]);
+    // ---- the band rows of L^-1, column x: the forward substitution of the identity with L's
+    // single band there, Y(r, x) = +0 - L(r, r-1) Y(r-1, x) below the diagonal (the terms of a
+    // zero L(r, r-1) it skips leave the +0 that this writes), 1 on it, +0 above; from Y(E - 1, x)
+    // (the block's last row, k_convec_lu's) in the block's columns
+    if (fr && E < n) {
+        const double *lb = ud + n;
+        double y;
+        int r0;
+        if (x >= E) {
+            for (int r = E; r < x; ++r) X[(size_t)r * n + x] = 0.0;
+            X[(size_t)x * n + x] = 1.0;
+            y = 1.0;
+            r0 = x + 1;
+        } else {
+            y = X[(size_t)(E - 1) * n + x];
+            r0 = E;
+        }
+        for (int r = r0; r < n; ++r) {
             y = 0.0 - lb[r] * y;
             X[(size_t)r * n + x] = y;
         }
@@ -524,8 +664,7 @@ __global__ void k_convec_apply(CArgs A) {
     __syncthreads();
     // ---- back substitution of inverse column x: rows from the bottom, terms k in order; each
     // quotient by the row's shared reciprocal, correctly rounded (div_by_recip)
-    if (live && A.fresh[c]) {
-        const double *U = A.abuf + (size_t)c * n * n;
+    if (fr) {
         const int32_t *rend = A.rend + (size_t)c * n;
         const double *rc = recip + cl * n;
         for (int r = n - 1; r >= 0; --r) {
@@ -535,7 +674,7 @@ __global__ void k_convec_apply(CArgs A) {
                 if (is_zero(w)) continue;
                 a = a - w * X[(size_t)k * n + x];
             }
-            X[(size_t)r * n + x] = div_by_recip(a, ud ? ud[r] : U[(size_t)r * n + r], rc[r]);
+            X[(size_t)r * n + x] = div_by_recip(a, r >= E ? ud[r] : U[(size_t)r * n + r], rc[r]);
         }
     }
     __syncthreads();
@@ -606,14 +745,15 @@ extern "C" int gb_convec(gb_ctx *ctx, const gb_view *m, const gb_view *rm, const
     const size_t nchain = (size_t)NCHAIN * (lmax + 1) * ncol, nflag = ((size_t)ncol + 1) / 2;
     const size_t nrend = ((size_t)ncol * lmax + 1) / 2;
     const size_t ntband = (size_t)ncol * 2 * lmax;
-    const size_t doubles = nn * ncol + nchain + nflag + nrend + ntband + (cache_inv ? 0 : nn * ncol);
+    const size_t doubles = nn * ncol + nchain + 2 * nflag + nrend + ntband + (cache_inv ? 0 : nn * ncol);
     double *w = gb_work(ctx, doubles * sizeof(double));
     if (!w) return GB_ECUDA;
     A.abuf = w;
     A.chain = w + nn * ncol;
     A.fresh = reinterpret_cast<int32_t *>(A.chain + nchain);
-    A.rend = reinterpret_cast<int32_t *>(A.chain + nchain + nflag);
-    A.tband = A.chain + nchain + nflag + nrend;
+    A.eblk = reinterpret_cast<int32_t *>(A.chain + nchain + nflag);
+    A.rend = reinterpret_cast<int32_t *>(A.chain + nchain + 2 * nflag);
+    A.tband = A.chain + nchain + 2 * nflag + nrend;
     A.inv = cache_inv ? cache_inv : A.tband + ntband;
     A.cache_m = cache_inv ? cache_m : nullptr;
     A.cache_tag = cache_tag;
@@ -634,6 +774,9 @@ extern "C" int gb_convec(gb_ctx *ctx, const gb_view *m, const gb_view *rm, const
     // warps per LU block and lanes per column: the tuned counts, fewer warps where their shared
     // memory would not fit
     if (int rc = launch_lu(ctx, A, ctx->tune[GB_TUNE_LU_LANES])) return rc;
+    // the band rows above the blocks k_convec_lu split off, thread per column
+    k_convec_tail<<<gb_blocks(ncol, tcol), tcol, 0, ctx->stream>>>(A);
+    if (int rc = gb_after_launch(ctx, "convec_tail")) return rc;
     GB_CHECK_CUDA(cudaEventRecord(ctx->join, ctx->side));
     GB_CHECK_CUDA(cudaStreamWaitEvent(ctx->stream, ctx->join, 0));
     // whole columns per block, as many as make the block a whole number of warps (<= 1024
