@@ -87,6 +87,9 @@ int gb_work_reserve(gb_ctx *ctx, size_t bytes);
  * the context's work; not while capturing. */
 int gb_stream_priority(gb_ctx *ctx, int rank);
 size_t gb_work_size(gb_ctx *ctx);
+/* The context's int32 scratch (the sub-cycle searches' counts and candidates): its device
+ * address and length in elements, for diagnostics and tests.  No reference counterpart. */
+int gb_scratch_info(gb_ctx *ctx, int32_t **ptr, size_t *n);
 int gb_tune_set(gb_ctx *ctx, int key, int value); /* GB_EARG for a value outside the key's range */
 int gb_tune_get(gb_ctx *ctx, int key, int *value);
 
@@ -161,7 +164,9 @@ int gb_advect_y(gb_ctx *ctx, const gb_view *m, const gb_view *rm, const gb_view 
  * device, shared by every context and stream: calls that can overlap (two streams, two host
  * threads) race on it and must be serialised by the caller.  The first call on a device looks
  * the array's address up (cudaGetSymbolAddress); make it before any stream capture begins.
- * The current device must be the context's. */
+ * The looked-up address is kept for the life of the process: after a cudaDeviceReset the
+ * library's module is loaded anew and the array may move, so the entry point must not be
+ * called again in that process.  The current device must be the context's. */
 #define GB_NOALLOC_MAX_LEVELS 1024
 int gb_advect_y_noalloc(gb_ctx *ctx, const gb_view *m, const gb_view *rm, const gb_view *rxm,
                         const gb_view *rym, const gb_view *rzm, const gb_view *bm,

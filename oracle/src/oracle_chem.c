@@ -64,33 +64,36 @@ int or_loss_rates(const ov *temper, const ov *phlb, const double *lat, const ov 
     const int im = (int)temper->n[0], jm = (int)temper->n[1], lm = (int)temper->n[2];
     const int ns = (int)strat_press->n[1];
     const int ntrop = pl_trop ? (int)pl_trop->n[2] : 0;
+    int rc = 0;
+#pragma omp parallel
+    {  /* latitudes are independent: each thread its own work arrays */
     double *edges = malloc(sizeof(double) * (ns + 1));
     double *tedges = malloc(sizeof(double) * (ntrop + 2));
     double *col = malloc(sizeof(double) * (lm + 1));
-    int rc = 0;
-    for (int j = 0; j < jm && !rc; j++) {
+#pragma omp for schedule(dynamic, 1) reduction(| : rc)
+    for (int j = 0; j < jm; j++) {
         /* strat_edges: midpoints, a half layer below the first, 0 above the last; hPa -> Pa */
         const double p0 = A2(strat_press, j, 0), p1 = ns > 1 ? A2(strat_press, j, 1) : 0.0;
         edges[0] = (p0 + 0.5 * (p0 - p1)) * 100.0;
         for (int k = 1; k < ns; k++) edges[k] = ((A2(strat_press, j, k - 1) + A2(strat_press, j, k)) / 2.0) * 100.0;
         edges[ns] = 0.0 * 100.0;
         if (!descending(edges, ns + 1)) {
-            rc = 4;
-            break;
+            rc |= 4;
+            continue;
         }
         const double c = gbm_cos(lat[j]);
         const double trop = 30000.0 - 21500.0 * (c * c);
         for (int i = 0; i < im && !rc; i++) {
             for (int l = 0; l <= lm; l++) col[l] = A3(phlb, i, j, l);
             if (!descending(col, lm + 1)) {
-                rc = 4;
+                rc |= 4;
                 break;
             }
             if (ntrop) {
                 for (int k = 0; k < ntrop; k++) tedges[k] = A3(pl_trop, i, j, k);
                 tedges[ntrop] = 0.0;
                 if (!descending(tedges, ntrop + 1)) {
-                    rc = 4;
+                    rc |= 4;
                     break;
                 }
             }
@@ -134,5 +137,6 @@ int or_loss_rates(const ov *temper, const ov *phlb, const double *lat, const ov 
     free(edges);
     free(tedges);
     free(col);
+    }
     return rc;
 }

@@ -94,11 +94,14 @@ void or_convec(const ov *m, const ov *rm, const ov *rxm, const ov *rym, const ov
                int64_t ts1, const int32_t *cols, int ncol, double dt, int lmax) {
     const int n = lmax, nt = (int)rm->n[3];
     if (n <= 0) return;
+#pragma omp parallel
+    {  /* columns are independent: each thread its own work arrays */
     double *col = malloc(sizeof(double) * 6 * n);
     double *conv1 = malloc(sizeof(double) * n * n), *inv = malloc(sizeof(double) * n * n);
     double *y = malloc(sizeof(double) * n * n);
     double *work = malloc(sizeof(double) * (2 * (n + 1) * n + 2 * (n + 1)));
     double *srm = malloc(sizeof(double) * n), *zrm = malloc(sizeof(double) * n);
+#pragma omp for schedule(dynamic, 8)
     for (int c = 0; c < ncol; c++) {
         const int i = cols[2 * c], j = cols[2 * c + 1];
         double *cm = col, *ce = col + n, *cd = col + 2 * n, *ced = col + 3 * n, *cdd = col + 4 * n, *ck = col + 5 * n;
@@ -133,4 +136,5 @@ void or_convec(const ov *m, const ov *rm, const ov *rxm, const ov *rym, const ov
     free(work);
     free(srm);
     free(zrm);
+    }
 }

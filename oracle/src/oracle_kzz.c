@@ -68,10 +68,13 @@ void or_calc_kzz(const ov *spm, const ov *sp, const ov *pu, const ov *pv, const 
     const double GTOR = PI_ / 180.0;
     const ov *oro = &surf[0], *lsm = &surf[1], *sr = &surf[2], *srols = &surf[3], *u10m = &surf[4], *v10m = &surf[5];
     const ov *sshf = &surf[6], *slhf = &surf[7], *ewss = &surf[8], *nsss = &surf[9];
+#pragma omp parallel
+    {  /* columns are independent: each thread its own work arrays */
     double *w = malloc(sizeof(double) * (lm + 2) * 16);
     double *gph = w, *phlb = gph + (lm + 2), *m = phlb + (lm + 2), *pf = m + (lm + 2), *wthm = pf + (lm + 2);
     double *zthvk = wthm + (lm + 2), *whm = zthvk + (lm + 2), *uw = whm + (lm + 2), *vw = uw + (lm + 2);
     double *qc = vw + (lm + 2), *tc = qc + (lm + 2), *kvh = tc + (lm + 2), *logpf = kvh + (lm + 2);
+#pragma omp for schedule(dynamic, 1)
     for (int j = 0; j < jm; j++) {
         const double lat = ybeg + 0.5 * dy + dy * j;
         const double dxx = AE * dx * GTOR * gbm_cos(lat * GTOR), dyy = AE * dy * GTOR;
@@ -199,4 +202,5 @@ void or_calc_kzz(const ov *spm, const ov *sp, const ov *pu, const ov *pv, const 
         }
     }
     free(w);
+    }
 }

@@ -73,6 +73,7 @@ SIGNATURES = {
     "gb_iadd": (_I, [_VP, _VP, _I]),
     "gb_stamp": (_I, [_VP, _VP, _I]),
     "gb_copy_many": (_I, [_VP, _VP, _I, ctypes.c_size_t]),
+    "gb_scratch_info": (_I, [_VP, ctypes.POINTER(_VP), ctypes.POINTER(ctypes.c_size_t)]),
     "gb_advect_x": (_I, [_VP, _P, _P, _P, _P, _P, _P, _VP, _I, _I, _I, _I, _I, _VP, _VP]),
     "gb_advect_y": (_I, [_VP, _P, _P, _P, _P, _P, _P, _P, _I, _I, _I, _VP]),
     "gb_advect_y_noalloc": (_I, [_VP, _P, _P, _P, _P, _P, _P, _P, _I, _I, _I, _VP]),

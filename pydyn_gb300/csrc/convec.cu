@@ -605,23 +605,38 @@ __global__ void __launch_bounds__(GB_TUNE_MAX_COLUMN) k_convec_tail(CArgs A) {
     const double *G = A.abuf + (size_t)c * n * n;
     int32_t *rend = A.rend + (size_t)c * n;
     double *ud = A.tband + (size_t)c * 2 * n, *lb = ud + n;
-    int r = E;
+    int r0 = E;
     double uprev;
     if (E == 0) {
         uprev = G[0];
         ud[0] = uprev;
-        r = 1;
+        r0 = 1;
     } else {
         uprev = G[(size_t)(E - 1) * n + E - 1];
     }
-    for (; r < n; ++r) {
-        const double l = G[(size_t)r * n + r - 1] / uprev;
-        const double v = G[(size_t)r * n + r] - l * G[(size_t)(r - 1) * n + r];
-        ud[r] = v;
-        lb[r] = l;
-        uprev = v;
+    constexpr int B = 8;  // rows whose bands are read into registers at once (loads in flight together)
+    for (; r0 < n; r0 += B) {
+        double sub[B], dia[B], sup[B];
+#pragma unroll
+        for (int u = 0; u < B; ++u)
+            if (r0 + u < n) {
+                const int r = r0 + u;
+                sub[u] = G[(size_t)r * n + r - 1];
+                dia[u] = G[(size_t)r * n + r];
+                sup[u] = G[(size_t)(r - 1) * n + r];
+            }
+#pragma unroll
+        for (int u = 0; u < B; ++u) {
+            const int r = r0 + u;
+            if (r >= n) break;
+            const double l = sub[u] / uprev;
+            const double v = dia[u] - l * sup[u];
+            ud[r] = v;
+            lb[r] = l;
+            uprev = v;
+        }
     }
-    for (r = E; r < n; ++r) rend[r] = r + 1 < n ? r + 2 : r + 1;
+    for (int r = E; r < n; ++r) rend[r] = r + 1 < n ? r + 2 : r + 1;
 }
 
 __global__ void k_convec_apply(CArgs A) {

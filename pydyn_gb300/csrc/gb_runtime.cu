@@ -107,6 +107,13 @@ extern "C" int gb_work_reserve(gb_ctx *ctx, size_t bytes) {
 
 extern "C" size_t gb_work_size(gb_ctx *ctx) { return ctx ? ctx->work_bytes : 0; }
 
+extern "C" int gb_scratch_info(gb_ctx *ctx, int32_t **ptr, size_t *n) {
+    if (!ctx || !ptr || !n) return GB_EARG;
+    *ptr = ctx->scratch_i;
+    *n = ctx->scratch_i_n;
+    return GB_OK;
+}
+
 extern "C" int gb_device_name(gb_ctx *ctx, char *buf, int len) {
     if (!ctx || !buf || len <= 0) return GB_EARG;
     cudaDeviceProp prop;

@@ -32,6 +32,8 @@ SPECULATED = ("m", *TRACERS, "sp", "phlb")
 CHILD_PRIORITY = 3
 KZZ_PRIORITY = 1
 FAR_PRIORITY = 0  # region 1's physics on its far segment (slack until the parent's m2phlb1)
+MAIN_PRIORITY = 0  # the run's own stream (region 1's bodies on the edge segment)
+CFL_PRIORITY = 0  # the Check_CFL rehearsal's context
 
 
 class Forward:
@@ -249,23 +251,24 @@ class Forward:
                           for r in self.zoom.regions() for k, a in self.st[r].items() if k in SPECULATED}  # fmt: skip
             pairs = [(self._spec[(r, k)], self.st[r][k]) for r in self.zoom.regions() for k in SPECULATED]
             pairs += [(self.cfl_st[r][k], self.st[r][k]) for r in self.zoom.regions() for k in ("m", "sp")]
-            rows = []
             for dst, src in pairs:  # whole arrays of one layout: flat copies
                 if not (dst.contiguous() and src.contiguous() and dst.shape == src.shape and dst.dtype == src.dtype):
                     raise RuntimeError("capture_interval: a speculated array is not a whole contiguous array")
-                rows.append((dst.ptr, src.ptr, dst.size * dst.dtype.itemsize))
-            self._prologue = (DevArray.from_host(self.dev, np.array(rows, dtype=np.uint64)), len(rows),
-                              max(b for _, _, b in rows))
+            self._prologue = copy_table(self.dev, pairs)
         self.st.lib.save(self.cfl_st, "check_cfl", ("m", "am", "bm", "cm"))
         if self.aux_cfl is None:
             # the captured interval's side contexts, their work spaces and scratch sized by one
             # uncaptured run of what they will run (harmless: the rehearsal's copy is refilled at
             # every interval's start, and every step recomputes what Calc_Kzz writes)
             self.dev.sync()
+            if MAIN_PRIORITY:
+                self.dev.set_priority(MAIN_PRIORITY)
             self.aux_cfl = Device(self.dev.ordinal)
             with self.dev.redirect(self.aux_cfl):
                 self._enqueue_rehearsal()
             self.aux_cfl.sync()
+            if CFL_PRIORITY:
+                self.aux_cfl.set_priority(CFL_PRIORITY)
             if self.physics is not None and self.physics.full:
                 # one per region for Calc_Kzz, its work space sized by an uncaptured run of it
                 self.prep = [Device(self.dev.ordinal) for _ in self.zoom.regions()]
@@ -350,6 +353,22 @@ class Forward:
         self.put_step_inputs(t0, self.nread)
         self.graphs["interval"].launch()
         self._replays += 1
+
+
+def copy_table(dev, pairs):
+    """gb_copy_many's table of whole-array copies [(dst, src) DevArrays]: (device table, n, the
+    largest byte count).  Every copy moves whole 8-byte elements: a count that is not a multiple
+    of 8, or an empty copy, is refused here, since the kernel copies 8 bytes at a time."""
+    rows = []
+    for dst, src in pairs:
+        nbytes = src.size * src.dtype.itemsize
+        if nbytes <= 0 or nbytes % 8 or dst.size * dst.dtype.itemsize < nbytes:
+            raise ValueError(f"copy_table: a copy of {nbytes} bytes into {dst.size * dst.dtype.itemsize} "
+                             "(8-byte elements, non-empty, the destination at least as large)")  # fmt: skip
+        rows.append((dst.ptr, src.ptr, nbytes))
+    if len(rows) > 65535:
+        raise ValueError("copy_table: at most 65535 copies in one launch")
+    return DevArray.from_host(dev, np.array(rows, dtype=np.uint64)), len(rows), max(b for _, _, b in rows)
 
 
 def _interp(dst, a, b, w):

@@ -60,7 +60,10 @@ class BodyProfiler:
             e0.record()
             out = f(*a, **k)
             e1.record()
-            region = a[2] if len(a) > 2 and isinstance(a[2], int) else (1 if name.endswith("region1") else None)
+            if name.endswith("region1"):  # region 1's bodies take no region argument
+                region = 1
+            else:
+                region = a[2] if len(a) > 2 and isinstance(a[2], int) and not isinstance(a[2], bool) else None
             key = name if region is None else f"{name}@{region}"
             self.pairs[key].append((e0, e1))
             self.launches[key] += dev.launches() - n0

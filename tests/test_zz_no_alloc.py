@@ -87,3 +87,44 @@ def test_noalloc_y_rejects_more_levels_than_its_array(dev):
     assert dev.launches() == before
     for v in a.values():
         v.free()
+
+
+def _scratch(dev):
+    """The context's int32 scratch as (device pointer, length)."""
+    from pydyn_gb300 import _native as N
+
+    p, n = ctypes.c_void_p(), ctypes.c_size_t()
+    N.check(N.lib().gb_scratch_info(dev.h, ctypes.byref(p), ctypes.byref(n)), "gb_scratch_info")
+    return p.value, n.value
+
+
+@pytest.mark.gpu
+def test_noalloc_y_leaves_the_context_scratch_and_device_memory_alone(dev):
+    """The entry point exists for callers that cannot allocate: its calls take no device memory
+    (the free memory is the same before and after calls past the first) and keep their counts
+    out of the context's scratch (a pattern written there is intact after them)."""
+    torch = pytest.importorskip("torch")
+    from pydyn_gb300 import _native as N
+    from pydyn_gb300.device import DevArray
+
+    rng = np.random.default_rng(7)
+    im, jm, lm, nt = 24, 20, 10, 1
+    host = _inputs(rng, im, jm, lm, nt, 0.8)
+    n1 = DevArray.zeros(dev, (0, lm - 1), dtype=np.int32)
+    _run(dev, "gb_advect_y_noalloc", host, n1)  # the first call looks the fixed array's address up
+    ptr, n = _scratch(dev)
+    pattern = (np.arange(n, dtype=np.int64) * 2654435761 % 2**31).astype(np.int32)
+    N.check(N.lib().gb_put(dev.h, ptr, pattern.ctypes.data, pattern.nbytes), "gb_put")
+    dev.sync()
+    free0, _ = torch.cuda.mem_get_info(0)
+    for _ in range(3):
+        _run(dev, "gb_advect_y_noalloc", host, n1)
+    free1, _ = torch.cuda.mem_get_info(0)
+    back = np.empty_like(pattern)
+    N.check(N.lib().gb_get(dev.h, back.ctypes.data, ptr, back.nbytes), "gb_get")
+    dev.sync()
+    np.testing.assert_array_equal(back, pattern)
+    # _run's own device copies of the inputs come and go through the caching of the test's
+    # DevArrays; the entry point itself must not leave the free memory lower
+    assert free1 >= free0
+    n1.free()
