@@ -136,6 +136,36 @@ int gb_copy_many(gb_ctx *ctx, const uint64_t *table, int n, size_t max_bytes);
  * (ops.seqsum, ops.py:235); dst has src's extents with that axis dropped (n = 1). */
 int gb_seqsum(gb_ctx *ctx, const gb_view *dst, const gb_view *src, int axis, double post_mul);
 
+/* ------------------------------------------------------------------ Meteo_Setup_Mass (pydyn/balance.py, zoom_meteo.py)
+ * pydyn's layout without halos: pu (im+1, jm, lm), pv (im, jm+1, lm), pw (im, jm, lm+1), dm_dt
+ * and the residual (im, jm, lm), sp (im, jm); levi_db (lm) and area (jm) are device float64.
+ * dm_dt = ((|levi_db| (sp2 - sp1) / g) area) / dt (balance.py:76-82). */
+int gb_fill_mass_change(gb_ctx *ctx, const gb_view *dm_dt, const gb_view *sp1, const gb_view *sp2,
+                        const double *levi_db, const double *area, double dt_sec);
+/* CheckMassBalance (balance.py:85-94): out (device, 2 float64) = the rms and the largest
+ * |diff| of the column convergence's relative mismatch with the pressure tendency (the rms
+ * summed in a fixed tree order, not NumPy's). */
+int gb_mass_check(gb_ctx *ctx, const gb_view *pu, const gb_view *pv, const gb_view *sp1,
+                  const gb_view *sp2, const double *area, double dt_sec, double *out);
+/* One BalanceMassFluxes_m of a doubly periodic region (balance.py:107-124, 183-199): every
+ * level's residual divergence solved by the periodic Poisson equation -- a float64 discrete
+ * Fourier transform (tw_i, tw_j: cos and sin of 2 pi t / N, 2N each; fac (im, jm) the
+ * Laplacian's eigenvalues, fac(0, 0) = 1) -- and its gradient added to pu, pv. */
+int gb_balance_fft(gb_ctx *ctx, const gb_view *pu, const gb_view *pv, const gb_view *pw,
+                   const gb_view *dm_dt, const double *tw_i, const double *tw_j, const double *fac);
+/* Match 'sum' of a child to its parent (zoom_meteo.py:87-119): kind 0 the x faces, 1 the y
+ * faces, 2 the cells; ri, rj the refinement, ci1..ci2, cj1..cj2 the parent cells covered
+ * (1-based); every level; the child in place. */
+int gb_match_sum(gb_ctx *ctx, int kind, const gb_view *parent, const gb_view *child, int ri, int rj,
+                 int ci1, int ci2, int cj1, int cj2);
+/* One BalanceMassFluxes_m of a child against its parent (zoom_meteo.py:163-181): the residual
+ * of every level, then per parent cell (cj outer, ci inner) its block's residual through the
+ * direct matrices m_to_u (n x (ri+1) rj), m_to_v (n x ri (rj+1)) -- row k the correction of
+ * the unit divergence at cell k, n = ri rj <= 64 -- added to the block's faces. */
+int gb_balance_direct(gb_ctx *ctx, const gb_view *pu, const gb_view *pv, const gb_view *pw,
+                      const gb_view *dm_dt, const double *m_to_u, const double *m_to_v, int ri, int rj,
+                      int ci1, int ci2, int cj1, int cj2);
+
 /* ------------------------------------------------------------------ advection (pydyn/kernels.py)
  * x: dynamu on every (j, l) row of a region (kernels.py:129-220, redgrid.py:56-110,
  * zoom/advect.py:237-275).  m (im, jm, lm), tracers (im, jm, lm, nt) sharing strides,

@@ -74,6 +74,11 @@ SIGNATURES = {
     "gb_stamp": (_I, [_VP, _VP, _I]),
     "gb_copy_many": (_I, [_VP, _VP, _I, ctypes.c_size_t]),
     "gb_scratch_info": (_I, [_VP, ctypes.POINTER(_VP), ctypes.POINTER(ctypes.c_size_t)]),
+    "gb_fill_mass_change": (_I, [_VP, _P, _P, _P, _VP, _VP, _D]),
+    "gb_mass_check": (_I, [_VP, _P, _P, _P, _P, _VP, _D, _VP]),
+    "gb_balance_fft": (_I, [_VP, _P, _P, _P, _P, _VP, _VP, _VP]),
+    "gb_match_sum": (_I, [_VP, _I, _P, _P, _I, _I, _I, _I, _I, _I]),
+    "gb_balance_direct": (_I, [_VP, _P, _P, _P, _P, _VP, _VP, _I, _I, _I, _I, _I, _I]),
     "gb_advect_x": (_I, [_VP, _P, _P, _P, _P, _P, _P, _VP, _I, _I, _I, _I, _I, _VP, _VP]),
     "gb_advect_y": (_I, [_VP, _P, _P, _P, _P, _P, _P, _P, _I, _I, _I, _VP]),
     "gb_advect_y_noalloc": (_I, [_VP, _P, _P, _P, _P, _P, _P, _P, _I, _I, _I, _VP]),

@@ -6,6 +6,7 @@ against on machines that do not have the reference:
 
     python tests/golden/make_golden.py kernels     -> tests/golden/kernels.npz
     python tests/golden/make_golden.py adjoint     -> tests/golden/adjoint.npz
+    python tests/golden/make_golden.py balance     -> tests/golden/balance.npz
 
 kernels.npz holds, per case, the inputs pydyn.synth makes and the outputs of the reference
 function on them (pydyn.kernels, pydyn.redgrid, pydyn.cfl, pydyn.balance): keys
@@ -185,6 +186,85 @@ def kernel_cases():
     dxyp = 1e10 * rng.uniform(0.5, 1.5, JM)
     sp, phlb = balance.m2phlb1(m, at, bt, dxyp)
     put("m2phlb1", {"m": m, "at": at, "bt": bt, "dxyp": dxyp}, {"sp": sp, "phlb": phlb}, op="m2phlb1")
+    return cases
+
+
+def balance_inputs(rng, im, jm, lm, periodic=True, noise=3e-7):
+    """Meteo_Setup_Mass inputs near balance: fluxes ~1e9 kg/s (x faces periodic and pole faces
+    closed on a global grid), no vertical flux, level weights |db| summing to 1, and an sp2 whose
+    tendency is the column convergence's up to a relative `noise`, so that the pre-check passes
+    and the tight check asks for the Poisson correction."""
+    GRAV = 9.80665
+    area = 1.0e10 * (0.5 + rng.random(jm))
+    db = rng.random(lm) + 0.2
+    db = -(db / db.sum())
+    pu = 1.0e9 * rng.standard_normal((im + 1, jm, lm))
+    pv = 1.0e9 * rng.standard_normal((im, jm + 1, lm))
+    if periodic:
+        pu[im] = pu[0]
+        pv[:, 0] = 0.0
+        pv[:, jm] = 0.0
+    pw = np.zeros((im, jm, lm + 1))
+    sp1 = 1.0e5 * (1.0 + 0.01 * rng.standard_normal((im, jm)))
+    dt = 10800.0
+    su, sv = pu.sum(axis=2), pv.sum(axis=2)
+    conv = su[:-1] - su[1:] + sv[:, :-1] - sv[:, 1:]
+    sp2 = sp1 + dt * conv * GRAV / area[None, :] * (1.0 + noise * rng.standard_normal((im, jm)))
+    return {"pu": pu, "pv": pv, "pw": pw, "sp1": sp1, "sp2": sp2, "levi_db": db, "area": area, "dt": dt}
+
+
+def balance_cases():
+    """pydyn's Meteo_Setup_Mass balancing on such inputs, with NumPy's FFT (balance.NumpyPoisson):
+    region 1 (balance.setup_mass) and a child at 3 x 2 under a 10 x 8 parent
+    (zoom_meteo.setup_mass_child with PoissonDirect)."""
+    _reference()
+    import types
+
+    # pydyn.zoom_meteo imports pydyn.meteo, which imports netCDF4 for its archive reader; the
+    # balancing functions read no file, so a stand-in module lets them import here
+    sys.modules.setdefault("netCDF4", types.SimpleNamespace(Dataset=None))
+    from pydyn import balance
+    from pydyn import zoom_meteo as ZM
+
+    cases = {}
+    for k, (im, jm, lm) in enumerate(((24, 18, 5), (36, 20, 8))):
+        rng = np.random.default_rng(300 + k)
+        ins = balance_inputs(rng, im, jm, lm)
+        pu, pv = ins["pu"].copy(), ins["pv"].copy()
+        info = balance.setup_mass(pu, pv, ins["pw"], ins["sp1"], ins["sp2"], ins["levi_db"], ins["area"],
+                                  ins["dt"], solver=balance.NumpyPoisson(im, jm))  # fmt: skip
+        cases[f"balance{k}"] = ({n: v for n, v in ins.items() if n != "dt"}, {"pu": pu, "pv": pv},
+                                {"op": "balance", "dt": ins["dt"], "tries": info["tries"], "ok": bool(info["ok"])})
+    # a child: parent 10 x 8 (balanced), child under parent cells i 3..6, j 2..5 at 3 x 2
+    rng = np.random.default_rng(320)
+    imp, jmp, lm = 10, 8, 4
+    rf = ZM.Refinement(3, 2, 3, 6, 2, 5)
+    parent = balance_inputs(rng, imp, jmp, lm)
+    ppw = 1.0e7 * rng.standard_normal((imp, jmp, lm + 1))
+    im, jm = 4 * 3, 4 * 2
+    raw = (1.0e9 / 3 * rng.standard_normal((im + 1, jm, lm)), 1.0e9 / 2 * rng.standard_normal((im, jm + 1, lm)),
+           1.0e7 / 6 * rng.standard_normal((im, jm, lm + 1)))  # fmt: skip
+    area = 1.0e9 * (0.5 + rng.random(jm))
+    db = rng.random(lm) + 0.2
+    db = -(db / db.sum())
+    # the child's surface pressures follow its matched fluxes' column convergence
+    mpu, mpv, mpw = (q.copy() for q in raw)
+    ZM.match_u_sum(parent["pu"], mpu, rf)
+    ZM.match_v_sum(parent["pv"], mpv, rf)
+    su, sv = mpu.sum(axis=2), mpv.sum(axis=2)
+    sp1 = 1.0e5 * (1.0 + 0.01 * rng.standard_normal((im, jm)))
+    sp2 = sp1 + 10800.0 * (su[:-1] - su[1:] + sv[:, :-1] - sv[:, 1:]) * 9.80665 / area[None, :] * (
+        1.0 + 3e-7 * rng.standard_normal((im, jm)))  # fmt: skip
+    from pydyn import balance
+
+    poisson = ZM.PoissonDirect(3, 2, solver=balance.NumpyPoisson(3, 2))
+    pu, pv, pw, info = ZM.setup_mass_child(raw, (parent["pu"], parent["pv"], ppw), sp1, sp2, db, area, 10800.0, rf,
+                                           poisson)  # fmt: skip
+    ins = {"pu": raw[0], "pv": raw[1], "pw": raw[2], "ppu": parent["pu"], "ppv": parent["pv"], "ppw": ppw,
+           "sp1": sp1, "sp2": sp2, "levi_db": db, "area": area, "m_to_u": poisson.m_to_u, "m_to_v": poisson.m_to_v}
+    cases["balchild0"] = (ins, {"pu": pu, "pv": pv, "pw": pw},
+                          {"op": "balchild", "dt": 10800.0, "rf": [3, 2, 3, 6, 2, 5], "tries": info["tries"],
+                           "ok": bool(info["ok"])})  # fmt: skip
     return cases
 
 
@@ -674,6 +754,9 @@ if __name__ == "__main__":
     if "kernels" in what:
         save(kernel_cases(), HERE / "kernels.npz")
         print("wrote", HERE / "kernels.npz")
+    if "balance" in what:
+        save(balance_cases(), HERE / "balance.npz")
+        print("wrote", HERE / "balance.npz")
     if "adjoint" in what:
         save(adjoint_goldens(), HERE / "adjoint.npz")
         print("wrote", HERE / "adjoint.npz")
