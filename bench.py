@@ -62,9 +62,10 @@ BYTES_PER_CELL = {"_dynamu_region1": 12, "_dynamv_region1": 12, "_dynamw_region1
 
 
 # DRAM bytes (read + write) per call of a body, from one ncu capture of an eager interval of
-# glb3x2+nam1x1 with physics (dram__bytes_read.sum + dram__bytes_write.sum of the body's kernels,
-# averaged over its calls; the parent's per v, both segments): the roofline's traffic
-TRAFFIC_PER_CALL = {"glb3x2+nam1x1": {"convec_region@2": 132.3e6, "convec_region@1": 250.5e6}}
+# glb3x2+nam1x1 with physics on the current kernels (dram__bytes_read.sum + dram__bytes_write.sum
+# of the body's seven k_convec launches, averaged over its calls; the parent's per v, both
+# segments): the roofline's traffic (profiles/interval_dram_fp64_glb3x2+nam1x1.md)
+TRAFFIC_PER_CALL = {"glb3x2+nam1x1": {"convec_region@2": 138.1e6, "convec_region@1": 249.5e6}}
 
 
 def workload_config(workload, n_gpus):
@@ -535,7 +536,9 @@ def main():
     dev = Device(local)
     fw = Forward(dev, tree, lm, seed=seed, physics=physics, lmax=lmax)  # every replica runs the same case
 
-    # per-body device time of one eager interval: the roofline's dominant body
+    # per-body device time of one eager interval (after a first one has made every lazily
+    # allocated array and grown the work space): the roofline's dominant body
+    fw.interval(graph=False)
     with BodyProfiler(dev, fw.physics) as prof:
         fw.interval(graph=False)
     bodies = prof.report()

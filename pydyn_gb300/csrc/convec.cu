@@ -801,6 +801,9 @@ extern "C" int gb_convec(gb_ctx *ctx, const gb_view *m, const gb_view *rm, const
     const int least = ctx->tune[GB_TUNE_APPLY_THREADS];
     if (per * lmax < least) per = (least + lmax - 1) / lmax;
     while (per > 1 && ((per * lmax + 31) / 32) * 32 > 1024) --per;
+    // a call of few columns (a segment along a child's footprint) spread over the device: its
+    // FP64 work would otherwise queue on the few multiprocessors its few blocks land on
+    while (per > 1 && (ncol + per - 1) / per < ctx->sms) per /= 2;
     A.cols_per_block = per;
     const int threads = ((per * lmax + 31) / 32) * 32;
     k_convec_apply<<<(ncol + per - 1) / per, threads, (size_t)per * lmax * sizeof(double), ctx->stream>>>(A);

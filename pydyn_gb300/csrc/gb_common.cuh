@@ -38,6 +38,7 @@ struct gb_ctx {
     int tune[GB_TUNE_N] = {64, 128, 2, 128, 32};  // launch shapes (GB_TUNE_*)
     bool capturing = false;
     int64_t capture_launches = 0;
+    int sms = 1;  // the device's multiprocessors (grids of small calls are spread over them)
 };
 
 void gb_set_error(const std::string &msg);

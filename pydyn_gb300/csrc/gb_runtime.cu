@@ -61,6 +61,7 @@ extern "C" int gb_create(int device, gb_ctx **out) {
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&ctx->side, cudaStreamNonBlocking);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ctx->fork, cudaEventDisableTiming);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ctx->join, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&ctx->sms, cudaDevAttrMultiProcessorCount, device);
     if (e == cudaSuccess) e = cudaMalloc(&ctx->ctl, sizeof(gb_ctl));
     if (e == cudaSuccess) e = cudaMemset(ctx->ctl, 0, sizeof(gb_ctl));
     ctx->scratch_i_n = 1 << 16;
