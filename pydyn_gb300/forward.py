@@ -288,6 +288,11 @@ class Forward:
                     aux.set_priority(CHILD_PRIORITY if r != 1 else FAR_PRIORITY)
                     aux.sync()
         self.dev.sync()
+        # the side contexts launch with the run's own shapes (gb_tune_set), re-read at every
+        # capture: a tuner that changes the run's shapes re-captures
+        shapes = self.dev.tuning()
+        for side in (self.prep or []) + (self.aux or []) + ([self.aux_cfl] if self.aux_cfl is not None else []):
+            side.tune(**shapes)
         self.graphs.pop("interval", None)
         side0 = self._side_launches()
         with self.dev.capture() as g:
