@@ -256,44 +256,53 @@ __global__ void __launch_bounds__(GB_TUNE_MAX_CELL) k_convec_matrix(CArgs A) {
     // diagonal's two levels, the updraft chain u is +0 (its ratios are inactive), the downdraft
     // chain ends at the diagonal, and f(k - 1, l), f(k, l) are (+0 - +0) + -0 = +0
     const double off = mdt * (0.0 - 0.0);
+    // The band of matrix column l where the chains are +0: f(l, l) and f(l+1, l) are the
+    // general statements below with u = fd = +0, (+0 - qamu) + (-qdk2) and (+0 - qamd) + qdk1
+    // (x - y = x + (-y) exactly), and the rows k = l, l+1, l+2 take -dt (f(k-1, l) - f(k, l)),
+    // plus 1 at k = l+1; every other row of such a stretch is -dt (+0 - +0).  The band's values
+    // are made once a lane and each row picks its own, so that no FP64 instruction is issued
+    // row by row for the few lanes whose band that row is.
+    const double nqdk2 = -qdk2;
+    const double fl = dia ? (0.0 - qamu) + nqdk2 : 0.0;  // f(0, l) = 0: the surface
+    const double fl1 = sub ? (0.0 - qamd) + qdk1 : 0.0;
+    const double eb1 = mdt * (fl - fl1) + 1.0, eb2 = mdt * (fl1 - 0.0);
     if (top <= 0 && lfs <= 1) {
-        // no cloud: every chain level is inactive, so u and fd are +0 throughout and f(k, l) is
-        // +0 except f(l, l) = (+0 - qamu) - qdk2 and f(l+1, l) = (+0 - qamd) + qdk1 -- the
-        // general statements below with their zero operands; conv1(., l) is then the constant
-        // -dt (+0 - +0) off the three bands
-        const double fll = (dia && l <= n - 1) ? (0.0 - qamu) - qdk2 : 0.0;
-        const double fl1 = sub ? (0.0 - qamd) + qdk1 : 0.0;
+        // no cloud: every chain level is inactive, so u and fd are +0 throughout; f(l-1, l) = +0
+        const double eb0 = mdt * (0.0 - fl);
         for (int k = 1; k <= n; ++k) {
-            double e = off;
-            if (k >= l && k <= l + 2) {
-                const double fprev = (k - 1 == l) ? fll : (k - 1 == l + 1 ? fl1 : 0.0);
-                const double fk = (k == l) ? fll : (k == l + 1 && k <= n - 1 ? fl1 : 0.0);
-                e = mdt * (fprev - fk);
-                if (l == k - 1) e = e + 1.0;
-            }
-            out[(size_t)(k - 1) * n + l] = e;
+            const int b = k - l;
+            out[(size_t)(k - 1) * n + l] = b == 0 ? eb0 : (b == 1 ? eb1 : (b == 2 ? eb2 : off));
         }
         return;
     }
-    const double qed = div_by_recip(-AT(A.entd, i, j, l), ml, yl), qeu = div_by_recip(AT(A.entu, i, j, l), ml, yl);
     const int kend = min(n, max(top, l + 1) + 1);  // the last row with terms of its own
+    // R: the chains reach no row past it.  Above the cloud top the updraft's ratios are inactive
+    // (u is +0, assigned), and fd(r, l) is +0, assigned, wherever r >= lfs (the downdraft's ratio
+    // at r + 1 inactive); so in rows k > R both chains are +0 and only the band is left.  The
+    // chain loops stop there: a warp's trip is then R, not the l + 2 of its highest lane.
+    const int R = max(top, lfs) + 1;
+    const int kg = min(kend, R);  // rows 1 .. kg by the chains' statements
+    // the chains' first quotients, used only when a chain starts at or below R
+    const double qed = l <= R ? div_by_recip(-AT(A.entd, i, j, l), ml, yl) : 0.0;
+    const double qeu = l <= R ? div_by_recip(AT(A.entu, i, j, l), ml, yl) : 0.0;
     double fd[NMAX];
+    double fprev = 0.0;
     {
         // Each statement below is one instruction for every lane of the warp (a lane's l selects its
         // operands, not its branch): the FP64 pipe issues per instruction, whatever its lanes.
+        // fd(r, l) for r from l down: +0 from l down to R (each such ratio inactive), so the loop
+        // starts at min(l, R) with the carried +0.
         double v = 0.0;
-        for (int r = l; r >= 1; --r) {  // fd(r, l), r = k - 1 with k from l + 1 down to 2
+        for (int r = min(l, R); r >= 1; --r) {  // fd(r, l), r = k - 1 with k from l + 1 down to 2
             const double z = zd[r + 1];
             v = ge_zero(z) ? ((r == l) ? qed : v) * z : 0.0;
             fd[r] = v;
         }
         // the diagonal's terms (l == k: - qamu, then - qdk2) and the sub-diagonal's (l == k - 1:
         // - qamd, then + qdk1) as f = (f - s1) + s2, where the other lanes' s1 = +0 and s2 = -0
-        // leave every f as it is (x - +0 = x, x + -0 = x, zeros and NaNs included), and
-        // x - y = x + (-y) exactly
-        const double nqdk2 = -qdk2;
-        double u = 0.0, fprev = 0.0;
-        for (int k = 1; k <= kend; ++k) {
+        // leave every f as it is (x - +0 = x, x + -0 = x, zeros and NaNs included)
+        double u = 0.0;
+        for (int k = 1; k <= kg; ++k) {
             const double z = zu[k];
             // the updraft chain from l + 1 up: qeu z at k = l + 1, then u z; zero below
             u = (ge_zero(z) && l <= k - 1) ? ((l == k - 1) ? qeu : u) * z : 0.0;
@@ -310,8 +319,17 @@ __global__ void __launch_bounds__(GB_TUNE_MAX_CELL) k_convec_matrix(CArgs A) {
             out[(size_t)(k - 1) * n + l] = e;
             fprev = fk;
         }
-        for (int k = kend + 1; k <= n; ++k) out[(size_t)(k - 1) * n + l] = off;
     }
+    // rows kg+1 .. kend (a lane whose band lies above R): f(k, l) is the band's, +0 below row l;
+    // f(l-1, l) is the chains' last value when row l-1 is kg, else +0
+    if (kend > kg) {
+        const double eb0 = mdt * ((l - 1 == kg ? fprev : 0.0) - fl);
+        for (int k = kg + 1; k <= kend; ++k) {
+            const int b = k - l;
+            out[(size_t)(k - 1) * n + l] = b == 0 ? eb0 : (b == 1 ? eb1 : (b == 2 ? eb2 : off));
+        }
+    }
+    for (int k = kend + 1; k <= n; ++k) out[(size_t)(k - 1) * n + l] = off;
 }
 
 // thread per cloudless column: conv1 is tridiagonal.  When its three bands are finite and
