@@ -166,6 +166,17 @@ int gb_balance_direct(gb_ctx *ctx, const gb_view *pu, const gb_view *pv, const g
                       const gb_view *dm_dt, const double *m_to_u, const double *m_to_v, int ri, int rj,
                       int ci1, int ci2, int cj1, int cj2);
 
+/* ------------------------------------------------------------------ the replay of a dump set
+ * (pydyn/replay.py, gpu/engine.py)
+ * The engine's comparison of a state array with a dump's (DeviceEngine.compare and .report,
+ * which pydyn's engine makes on the host after downloading the state array; replay.py:277-289,
+ * harness.py:140-179): a and b of one extent, any strides.  out, a device buffer of 5 int64,
+ * receives the number of elements whose bit patterns differ, the largest ulp distance, the bit
+ * patterns of the largest |a - b| and of the largest |a - b| / max(|a|, |b|) over the differing
+ * elements (NaN propagating), and the first differing element's row-major index (INT64_MAX when
+ * none differs).  Stream-ordered. */
+int gb_compare(gb_ctx *ctx, const gb_view *a, const gb_view *b, long long *out);
+
 /* ------------------------------------------------------------------ advection (pydyn/kernels.py)
  * x: dynamu on every (j, l) row of a region (kernels.py:129-220, redgrid.py:56-110,
  * zoom/advect.py:237-275).  m (im, jm, lm), tracers (im, jm, lm, nt) sharing strides,

@@ -79,6 +79,7 @@ SIGNATURES = {
     "gb_balance_fft": (_I, [_VP, _P, _P, _P, _P, _VP, _VP, _VP]),
     "gb_match_sum": (_I, [_VP, _I, _P, _P, _I, _I, _I, _I, _I, _I]),
     "gb_balance_direct": (_I, [_VP, _P, _P, _P, _P, _VP, _VP, _I, _I, _I, _I, _I, _I]),
+    "gb_compare": (_I, [_VP, _P, _P, _VP]),
     "gb_advect_x": (_I, [_VP, _P, _P, _P, _P, _P, _P, _VP, _I, _I, _I, _I, _I, _VP, _VP]),
     "gb_advect_y": (_I, [_VP, _P, _P, _P, _P, _P, _P, _P, _I, _I, _I, _VP]),
     "gb_advect_y_noalloc": (_I, [_VP, _P, _P, _P, _P, _P, _P, _P, _I, _I, _I, _VP]),

@@ -287,17 +287,25 @@ def chemistry_region(zoom, st, region, decay, tracers):
 
 
 def _footprints(zoom, region):
-    """The children's footprints inside the region's scope as inclusive 0-based (i0, i1, j0, j1):
-    together exactly the scope's cells the region does not own."""
+    """The cells of the region's scope that it does not own, as inclusive 0-based boxes (i0, i1,
+    j0, j1), one per child: the part of the child's footprint the child owns (the ring of parent
+    cells under the child's edge stays the parent's).  Together exactly the scope's unowned
+    cells."""
     si, sj = zoom.scope(region)
     own = zoom.owned(region)
     boxes, cover = [], np.zeros_like(own)
     for c in zoom.children[region]:
         i0, i1 = max(zoom.ibeg[c] - 1, si.start), min(zoom.iend[c] - 1, si.stop - 1)
         j0, j1 = max(zoom.jbeg[c] - 1, sj.start), min(zoom.jend[c] - 1, sj.stop - 1)
-        if i0 <= i1 and j0 <= j1:
-            boxes.append((i0, i1, j0, j1))
-            cover[i0 : i1 + 1, j0 : j1 + 1] = True
+        if i0 > i1 or j0 > j1:
+            continue
+        taken = np.argwhere(~own[i0 : i1 + 1, j0 : j1 + 1])
+        if len(taken) == 0:
+            continue
+        (a0, b0), (a1, b1) = taken.min(axis=0), taken.max(axis=0)
+        box = (i0 + int(a0), i0 + int(a1), j0 + int(b0), j0 + int(b1))
+        boxes.append(box)
+        cover[box[0] : box[1] + 1, box[2] : box[3] + 1] = True
     scope = np.zeros_like(own)
     scope[si, sj] = True
     if not np.array_equal(cover, scope & ~own):

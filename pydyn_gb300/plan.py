@@ -178,6 +178,15 @@ def _block_end(pos, n_ops=N_OPERATORS):
     return (pos // n_ops + 1) * n_ops
 
 
+def operator_calls(zoom, r, status):
+    """The calls of the operator at position `status` of region r's order, on its own: what
+    pydyn's zoom.OPERATORS[op](zoom, st, r) (or the v / s / c body) does at that position, as a
+    replay of one dumped operator issues it."""
+    order = zoom.splitorderzoom[r]
+    block, second = _block_at(order, status, N_OPERATORS, zoom.ref(r, "t"))
+    return _operator(zoom, r, order[status], status, block, second, zoom.lm)
+
+
 def step_plan(zoom):
     """The calls of one step (tm5.F90's two half steps over the tree), fluxes already set."""
     return _cached(zoom, "step", lambda: _make_step_plan(zoom))

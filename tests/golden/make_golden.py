@@ -7,6 +7,7 @@ against on machines that do not have the reference:
     python tests/golden/make_golden.py kernels     -> tests/golden/kernels.npz
     python tests/golden/make_golden.py adjoint     -> tests/golden/adjoint.npz
     python tests/golden/make_golden.py balance     -> tests/golden/balance.npz
+    python tests/golden/make_golden.py dumps       -> tests/golden/dumps.json
 
 kernels.npz holds, per case, the inputs pydyn.synth makes and the outputs of the reference
 function on them (pydyn.kernels, pydyn.redgrid, pydyn.cfl, pydyn.balance): keys
@@ -724,6 +725,63 @@ def run_traces(names=TRACE_RUNS):
     return out
 
 
+# ------------------------------------------------------------------ dump sets (pydyn.dump, pydyn.replay)
+# name: (tree, lm, seed, tracers, ranks) of a synthetic set written by oracle/dumpset.py
+DUMP_SETS = {"two": ("two", 5, 3, 1, 1), "one": ("one", 5, 4, 1, 1), "two-ranks": ("two", 4, 6, 2, 2)}
+REPLAY_TAGS = ("x", "y", "z", "v", "s", "c", "cfl", "massflow", "m2phlb")
+
+
+def parse_digest(events):
+    """sha1 of a reader's view of a set: every event's identity, header, array bounds and types,
+    and its arrays' values (row-major bytes), in sequence order."""
+    import hashlib
+
+    h = hashlib.sha1()
+    for ev in events:
+        meta = {k: list(v) if isinstance(v, tuple) else v for k, v in sorted(ev.meta.items())}
+        h.update(json.dumps([ev.tag, ev.seq, ev.region, meta], sort_keys=True).encode())
+        for name in sorted(ev.arrays):
+            a = ev[name]
+            h.update(json.dumps([name, list(a.lower), list(a.data.shape), str(a.data.dtype)]).encode())
+            h.update(np.ascontiguousarray(a.data).tobytes())
+    return h.hexdigest()
+
+
+def write_dump_set(name, out):
+    sys.path.insert(0, str(HERE.parents[1]))
+    from oracle import dumpset
+
+    tree, lm, seed, nt, ranks = DUMP_SETS[name]
+    return dumpset.write_set(out, tree, lm=lm, seed=seed, nt=nt, ranks=ranks), dumpset.digest(out)
+
+
+def dump_goldens():
+    """Per set: its sha1, the digest of pydyn's reader's view of it (merged ranks), and what
+    pydyn's replay reports event by event -- with the Crout inverse (TM5 built without LAPACK,
+    the device's path) and pydyn's libm routed through the package's gbmath."""
+    import io
+    import tempfile
+    import types
+
+    sys.modules.setdefault("netCDF4", types.SimpleNamespace(Dataset=None))  # pydyn.inputs imports it
+    _reference()
+    from pydyn import dump, ops, replay
+
+    ops.use_libm(str(_gbmath()))
+    out = {}
+    for name in DUMP_SETS:
+        with tempfile.TemporaryDirectory() as d:
+            (ndyn, n), sha = write_dump_set(name, d)
+            events = dump.load_events(d, merge=True)
+            entry = {"sha1": sha, "ndyn": ndyn, "n": n, "events": len(events), "parse": parse_digest(events)}
+            res = replay.replay(d, lapack="crout", tags=set(REPLAY_TAGS), out=io.StringIO())
+            entry["results"] = [[ev.seq, kind, ev.region, [r["name"] for r in reports],
+                                 all(r["equal"] for r in reports)] for ev, kind, reports, _ in res]  # fmt: skip
+            entry["failures"] = [list(f) for f in res.failures]
+            out[name] = entry
+    return out
+
+
 def save(cases, path):
     flat = {}
     for name, (ins, outs, meta) in cases.items():
@@ -763,6 +821,10 @@ if __name__ == "__main__":
     if "traces" in what:
         path = HERE / "traces.json"
         path.write_text(json.dumps({"plans": plan_traces(), "runs": run_traces()}) + "\n")
+        print("wrote", path)
+    if "dumps" in what:
+        path = HERE / "dumps.json"
+        path.write_text(json.dumps(dump_goldens(), indent=1) + "\n")
         print("wrote", path)
     if "steps" in what:  # `steps [name ...]`: those runs only, the others kept
         path = HERE / "steps.json"
