@@ -73,7 +73,9 @@ int gb_graph_destroy(void *graph);
 #define GB_TUNE_COLUMN_THREADS 0 /* thread-per-column kernels (convection chains, Kzz columns): 32..256 */
 #define GB_TUNE_CELL_THREADS 1   /* thread-per-cell kernels (convection matrix, Kzz, chemistry): 32..512 */
 #define GB_TUNE_LU_WARPS 2       /* columns (one warp each) per block of the convection LU: 1, 2, 4 */
-#define GB_TUNE_APPLY_THREADS 3  /* the convection apply's smallest block (whole columns): 32..1024 */
+#define GB_TUNE_APPLY_THREADS 3  /* the convection apply's smallest block (whole columns): 32..1024;
+                                   0 (the default): the columns a block that even out the FP64
+                                   work over the SMs */
 #define GB_TUNE_LU_LANES 4       /* lanes per column of the convection LU (32 / lanes columns a warp): 8, 16, 32 */
 #define GB_TUNE_N 5
 int gb_device_name(gb_ctx *ctx, char *buf, int len); /* "<name> sm_<cc> x<SMs>": the tuning cache's key */

@@ -732,6 +732,37 @@ __global__ void k_convec_apply(CArgs A) {
 
 int gcd(int a, int b) { return b == 0 ? a : gcd(b, a % b); }
 
+// Columns per block of k_convec_apply (whole columns: a column's threads share its reciprocals
+// and meet at the block's barriers).  least > 0: at least `least` threads, as many columns as
+// make whole warps, and a call of few columns spread over the device.  least == 0: the count
+// that evens out the FP64 work over the SMs -- a block issues as many warp instructions as it
+// has warps (a part-filled warp issues as a full one), and the busiest SM runs ceil(blocks /
+// SMs) of them; the fewest such warps, with the most columns a block among equals.
+int apply_columns_per_block(int ncol, int lmax, int least, int sms) {
+    const int whole = 32 / gcd(lmax, 32);  // columns that fill whole warps
+    int per = whole;
+    while (per > 1 && per * lmax > 1024) per /= 2;
+    if (least > 0) {
+        if (per * lmax < least) per = (least + lmax - 1) / lmax;
+        while (per > 1 && ((per * lmax + 31) / 32) * 32 > 1024) --per;
+        // a call of few columns (a segment along a child's footprint) spread over the device: its
+        // FP64 work would otherwise queue on the few multiprocessors its few blocks land on
+        while (per > 1 && (ncol + per - 1) / per < sms) per /= 2;
+        return per;
+    }
+    int best = per;
+    long long best_cost = -1;
+    for (int p = per; p >= 1; --p) {
+        const long long blocks = (ncol + p - 1) / p;
+        const long long cost = ((blocks + sms - 1) / sms) * ((p * lmax + 31) / 32);
+        if (best_cost < 0 || cost < best_cost) {
+            best_cost = cost;
+            best = p;
+        }
+    }
+    return best;
+}
+
 template <int G>
 int launch_lu_g(gb_ctx *ctx, const CArgs &A) {
     constexpr int MPW = 32 / G;
@@ -814,15 +845,8 @@ extern "C" int gb_convec(gb_ctx *ctx, const gb_view *m, const gb_view *rm, const
     GB_CHECK_CUDA(cudaStreamWaitEvent(ctx->stream, ctx->join, 0));
     // whole columns per block, as many as make the block a whole number of warps (<= 1024
     // threads), and at least the tuned block size
-    int per = 32 / gcd(lmax, 32);
-    while (per > 1 && per * lmax > 1024) per /= 2;
-    const int least = ctx->tune[GB_TUNE_APPLY_THREADS];
-    if (per * lmax < least) per = (least + lmax - 1) / lmax;
-    while (per > 1 && ((per * lmax + 31) / 32) * 32 > 1024) --per;
-    // a call of few columns (a segment along a child's footprint) spread over the device: its
-    // FP64 work would otherwise queue on the few multiprocessors its few blocks land on
-    while (per > 1 && (ncol + per - 1) / per < ctx->sms) per /= 2;
-    A.cols_per_block = per;
+    A.cols_per_block = apply_columns_per_block(ncol, lmax, ctx->tune[GB_TUNE_APPLY_THREADS], ctx->sms);
+    const int per = A.cols_per_block;
     const int threads = ((per * lmax + 31) / 32) * 32;
     k_convec_apply<<<(ncol + per - 1) / per, threads, (size_t)per * lmax * sizeof(double), ctx->stream>>>(A);
     return gb_after_launch(ctx, "convec_apply");

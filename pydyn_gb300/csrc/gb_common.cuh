@@ -35,7 +35,7 @@ struct gb_ctx {
     double *work = nullptr;        // per-op float64 work space, grown outside capture (gb_work)
     size_t work_bytes = 0;
     int64_t launches = 0;
-    int tune[GB_TUNE_N] = {64, 128, 2, 128, 32};  // launch shapes (GB_TUNE_*)
+    int tune[GB_TUNE_N] = {64, 128, 2, 0, 32};  // launch shapes (GB_TUNE_*)
     bool capturing = false;
     int64_t capture_launches = 0;
     int sms = 1;  // the device's multiprocessors (grids of small calls are spread over them)

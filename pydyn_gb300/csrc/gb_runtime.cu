@@ -131,7 +131,7 @@ extern "C" int gb_tune_set(gb_ctx *ctx, int key, int value) {
         case GB_TUNE_COLUMN_THREADS: ok = pow2 && value >= 32 && value <= GB_TUNE_MAX_COLUMN; break;
         case GB_TUNE_CELL_THREADS: ok = pow2 && value >= 32 && value <= GB_TUNE_MAX_CELL; break;
         case GB_TUNE_LU_WARPS: ok = pow2 && value <= GB_TUNE_MAX_LU_WARPS; break;
-        case GB_TUNE_APPLY_THREADS: ok = value >= 32 && value <= 1024; break;
+        case GB_TUNE_APPLY_THREADS: ok = value == 0 || (value >= 32 && value <= 1024); break;
         case GB_TUNE_LU_LANES: ok = value == 8 || value == 16 || value == 32; break;
     }
     if (!ok) {

@@ -216,7 +216,9 @@ def main(argv=None):
     ap.add_argument("--levels", type=int, default=34)
     ap.add_argument("--seed", type=int, default=42)
     ap.add_argument("--intervals", type=int, default=1)
-    ap.add_argument("--physics", type=int, default=1, help="1: convection, Kzz, emission, chemistry; 0: advection")
+    ap.add_argument("--physics", default="1",
+                    help="1: convection, Kzz, emission, chemistry; convection: convection alone on a given dkg "
+                         "(pydyn's GPU benchmark inputs); 0: advection")  # fmt: skip
     ap.add_argument("--lmax", type=int, default=None)
     ap.add_argument("--fp64-rates", action="store_true", help="measure the FP64 issue rates and exit")
     ap.add_argument("--timeline", action="store_true", help="the captured interval's timeline per stream")
@@ -233,7 +235,8 @@ def main(argv=None):
             print(f"{name}: {rate:.1f} G instructions/s")
         dev.close()
         return
-    fw = Forward(dev, a.config, a.levels, a.seed, physics=bool(a.physics), lmax=a.lmax)
+    physics = {"1": True, "0": False}.get(a.physics, a.physics)
+    fw = Forward(dev, a.config, a.levels, a.seed, physics=physics, lmax=a.lmax)
     if a.timeline:
         for _ in range(3):
             fw.interval(graph=True)

@@ -22,7 +22,7 @@ SPACE = {
     "column_threads": (32, 64, 128, 256),
     "cell_threads": (64, 128, 256, 512),
     "lu_warps": (1, 2, 4),
-    "apply_threads": (64, 128, 256, 512),
+    "apply_threads": (0, 64, 128, 256, 512),  # 0: the block that evens out the FP64 work over the SMs
     "lu_lanes": (8, 16, 32),
 }
 WIDTHS = (4, 8, 16, 32, 64, 128, 256)
