@@ -2,8 +2,9 @@
 
 CPU: the fixture of the transposed reference operator (tests/golden/adjoint.npz, pydyn's own
 interval applied to every basis vector of the `one` tree) is a transpose -- <A delta, y> equals
-<delta, A^T y> within the reference itself -- and the cost's samples.  GPU: the device adjoint of
-the same interval equals the reference's transpose; the dot-product test <A x, y> = <x, A^T y>
+<delta, A^T y> within the reference itself -- and the cost's samples.  GPU: the device's
+limits-off interval is bitwise pydyn's (A delta), the device adjoint of the same interval equals
+the reference's transpose; the dot-product test <A x, y> = <x, A^T y>
 to 1e-12 relative on glb6x4 and glb3x2 with physics; central finite differences of J against
 the checkpointed gradient; the torch.autograd wrapper."""
 
@@ -11,6 +12,7 @@ from pathlib import Path
 
 import numpy as np
 import pytest
+from conftest import assert_bitwise
 from make_golden import load
 
 from pydyn_gb300 import synth
@@ -52,7 +54,7 @@ def test_adjoint_is_the_reference_transpose(dev):
     ins, outs, meta = FIX
     fw, prob = _run(dev, meta["config"], meta["lm"], meta["seed"], meta["lmax"])
     got, atys = prob.interval_pair(ins["delta"], ins["y"])
-    np.testing.assert_allclose(got, outs["A_delta"], rtol=1e-13, atol=1e-13 * np.abs(outs["A_delta"]).max())
+    assert_bitwise(got, outs["A_delta"], "A delta: the limits-off interval, pydyn's bits")
     for k, aty in enumerate(atys):
         aty = aty.ravel()[ins["index"]]
         want = outs["ATy"][k]
