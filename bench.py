@@ -14,8 +14,11 @@ the step's meteo copied in from pinned host memory and the step's tracer mass co
 on the host clock.  roofline: the body that takes the most device time in an eagerly enqueued
 interval, its algorithmic bytes (per cell per application: x, y 2(2+4nt), z (2+4nt)+(1+4nt),
 v 6+8nt, c 3+8nt, m2phlb 2, dynam0 5 values of 8 bytes) over its measured time, against the
-measured HBM copy bandwidth.  cpu_baseline: the oracle (a scalar C restatement of pydyn) on this
-host's cores on a bounded sample of the same workload.
+measured HBM copy bandwidth; and, since the float64 step is bound by FP64 issue and not by HBM,
+its FP64 warp instructions per call (an ncu capture of the same kernels) x 32 lanes over the same
+time, against the DMUL/DADD issue rate measured in the run (`roofline.fp64`).  cpu_baseline:
+the oracle (a scalar C restatement of pydyn) on this host's cores on a bounded sample of the
+same workload.
 
 --impl reference runs the CPU reference arm: the oracle port of pydyn (the Python reference
 itself cannot be installed where this runs) on the same workload, with the same metric.
@@ -61,11 +64,16 @@ BYTES_PER_CELL = {"_dynamu_region1": 12, "_dynamv_region1": 12, "_dynamw_region1
                   "dynam0": 5}  # fmt: skip  (values of 8 bytes per cell and application at nt = 1)
 
 
-# DRAM bytes (read + write) per call of a body, from one ncu capture of an eager interval of
-# glb3x2+nam1x1 with physics on the current kernels (dram__bytes_read.sum + dram__bytes_write.sum
-# of the body's seven k_convec launches, averaged over its calls; the parent's per v, both
-# segments): the roofline's traffic (profiles/interval_dram_fp64_glb3x2+nam1x1.md)
-TRAFFIC_PER_CALL = {"glb3x2+nam1x1": {"convec_region@2": 138.1e6, "convec_region@1": 249.5e6}}
+# Per call of a convection body, from one ncu capture of an eager interval of each workload on
+# the current kernels (its seven k_convec launches, averaged over the body's calls in the
+# interval -- fresh and reusing its inverses; the parent's per v, both segments): DRAM bytes
+# (dram__bytes_read.sum + dram__bytes_write.sum), the roofline's traffic, and FP64 warp
+# instructions (smsp__inst_executed_pipe_fp64.sum), whose issue bounds the step
+# (profiles/interval_dram_fp64_glb3x2+nam1x1.md, profiles/interval_dram_fp64_a100-case.md)
+TRAFFIC_PER_CALL = {"glb3x2+nam1x1": {"convec_region@2": 130.0e6, "convec_region@1": 243.3e6},
+                    "a100-case": {"convec_region@2": 48.57e6, "convec_region@1": 179.1e6}}
+FP64_PER_CALL = {"glb3x2+nam1x1": {"convec_region@2": 4.134e6, "convec_region@1": 5.257e6},
+                 "a100-case": {"convec_region@2": 2.262e6, "convec_region@1": 6.229e6}}
 
 
 def workload_config(workload, n_gpus):
@@ -613,17 +621,16 @@ def main():
             "bytes_per_launch": per_call_bytes, "ms_per_launch": total_ms / calls,
             "fp64_rates_g_per_s": fp64,
             "note": "float64 with no contraction: the FP64 pipe (fp64_rates, measured in this run) bounds the step"}  # fmt: skip
-    if body == "convec_region" and fw.physics is not None:
-        # the reference's dense explicit inverse, (8/3) lmax^3 flops per column and inverse, plus
-        # 2 lmax^2 per call's tracer product; the kernels skip its exact zeros (most columns are
-        # tridiagonal), so this is an effective rate, not the pipe's
-        d = fw.physics.r[int(region) if region else 1]
-        inverses = calls - 1  # one call a step reuses the inverses (the `v` after `c s` on the same air mass)
-        flops = d["ncol"] * (inverses * (8.0 / 3.0) * lmax**3 + calls * 2.0 * lmax * lmax)
-        gflops = flops / (total_ms / 1e3) / 1e9
-        roof["fp64"] = {"effective_gflops": gflops, "peak_gflops": fp64["dmul_dadd"], "flops_per_interval": flops,
-                        "note": "dense-equivalent flops of the reference's inverse per second; peak = the "
-                                "measured DMUL/DADD issue rate"}  # fmt: skip
+    inst = FP64_PER_CALL.get(args.config, {}).get(name)
+    if inst is not None:
+        # the FP64 pipe holds a warp instruction for the same time whatever its active lanes: the
+        # body's issue rate is its warp instructions x 32 lanes over its time per call, against
+        # the DMUL/DADD issue rate measured in this run
+        issued = inst * 32 / (total_ms / calls / 1e3) / 1e9
+        roof["fp64"] = {"bound": "fp64", "achieved": issued, "peak": fp64["dmul_dadd"], "unit": "G FP64 lane-op/s",
+                        "frac": issued / fp64["dmul_dadd"], "warp_inst_per_launch": inst,
+                        "note": "FP64 warp instructions per call from an ncu capture of the same kernels "
+                                "(smsp__inst_executed_pipe_fp64.sum) x 32 / the live time per call"}  # fmt: skip
 
     step_bytes = sum(n * step_bytes_per_cell(physics, fw.zoom.g(r).tref) for r, n in cells.items())
     total_time = sum(v[1] for v in bodies.values())
