@@ -102,6 +102,9 @@ int gb_event_record(gb_ctx *ctx, void *ev);
  * another context's stream): how an ensemble bounds how many members run at once. */
 int gb_stream_wait(gb_ctx *ctx, void *ev);
 int gb_event_elapsed_ms(void *start, void *stop, float *ms);
+/* The host waits until the work before the event's last record has completed (a host pipeline's
+ * wait for one step's result while the next runs). */
+int gb_event_sync(void *ev);
 int gb_event_destroy(void *ev);
 
 /* The Check_CFL rehearsal flag: the mass-only kernels set it on a failed operator, and every

@@ -64,6 +64,7 @@ SIGNATURES = {
     "gb_tune_set": (_I, [_VP, _I, _I]),
     "gb_tune_get": (_I, [_VP, _I, ctypes.POINTER(_I)]),
     "gb_event_elapsed_ms": (_I, [_VP, _VP, ctypes.POINTER(ctypes.c_float)]),
+    "gb_event_sync": (_I, [_VP]),
     "gb_event_destroy": (_I, [_VP]),
     "gb_cfl_reset": (_I, [_VP]),
     "gb_cfl_failed": (_I, [_VP, ctypes.POINTER(_I)]),

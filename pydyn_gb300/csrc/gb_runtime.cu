@@ -314,6 +314,11 @@ extern "C" int gb_event_elapsed_ms(void *start, void *stop, float *ms) {
     GB_CHECK_CUDA(cudaEventElapsedTime(ms, (cudaEvent_t)start, (cudaEvent_t)stop));
     return GB_OK;
 }
+extern "C" int gb_event_sync(void *ev) {
+    if (!ev) return GB_EARG;
+    GB_CHECK_CUDA(cudaEventSynchronize((cudaEvent_t)ev));
+    return GB_OK;
+}
 extern "C" int gb_event_destroy(void *ev) {
     GB_CHECK_CUDA(cudaEventDestroy((cudaEvent_t)ev));
     return GB_OK;

@@ -186,6 +186,10 @@ class Event:
     def record(self):
         N.check(self.dev.L.gb_event_record(self.dev.h, self.p), "gb_event_record")
 
+    def synchronize(self):
+        """Wait on the host until the work before the last record has completed."""
+        N.check(self.dev.L.gb_event_sync(self.p), "gb_event_sync")
+
     def elapsed_ms(self, later):
         ms = ctypes.c_float()
         N.check(self.dev.L.gb_event_elapsed_ms(self.p, later.p, ctypes.byref(ms)), "gb_event_elapsed_ms")
