@@ -524,7 +524,7 @@ STEP_RUNS = {  # name: (tree, lm, seed, intervals, umax[, physics lmax, interval
     "two-phys": ("two", 8, 21, 6, 40.0, 8, 6),
     "three-phys": ("three", 6, 22, 4, 40.0, 6, 4),
     "config1": ("glb3x2", 34, 41, 24, 40.0, 34, 1),  # one simulated day
-    "config2": ("glb3x2+nam1x1", 34, 42, 2, 40.0, 34, 1),
+    "config2": ("glb3x2+nam1x1", 34, 42, 168, 40.0, 34, 1),  # one simulated week
     "two-phys-nt3": ("two", 8, 24, 4, 40.0, 8, 2, {"nt": 3}),
     "config0-nt8": ("glb6x4", 25, 16, 3, 40.0, {"nt": 8}),
     "config1-nt12": ("glb3x2", 34, 43, 2, 40.0, 34, 1, {"nt": 12}),
