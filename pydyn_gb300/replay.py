@@ -155,7 +155,7 @@ class DeviceEngine:
             ours, own = on_device(self.dev, np.asarray(ours, dtype=float))
         src, owner = on_device(self.dev, model, ours.lower)
         try:
-            return self._report(src.reshape_axes(src.shape, src.strides, ours.lower), ours, name, lambda i: model[i])
+            return self._report(src, ours, name, lambda i: model[i])
         finally:
             owner.free()
             if own is not None:
@@ -177,8 +177,8 @@ class DeviceEngine:
         loss = DevArray.zeros(self.dev, (0, ni - 1), (0, nj - 1), (0, lm - 1), (0, 3))
         decay = DevArray.zeros(self.dev, (0, ni - 1), (0, nj - 1), (0, lm - 1))
         fields = {k: d[k] for k in K.CHEM_FIELDS if k in d}
-        K.loss_rates(_zero_based(temper), _zero_based(d["phlb"]), d["lat"], {k: _zero_based(v) for k, v in fields.items()},
-                     float(dt_sec), loss=loss, decay=decay, oh_scale=inputs.get("oh_scale", 1.0),
+        K.loss_rates(temper, d["phlb"], d["lat"], fields, float(dt_sec), loss=loss, decay=decay,
+                     oh_scale=inputs.get("oh_scale", 1.0),
                      cl_scale=inputs.get("cl_scale", 1.0), o1d_scale=inputs.get("o1d_scale", 1.0),
                      soil_rate=inputs.get("soil_rate", 0.0))  # fmt: skip
         self.dev.sync()
@@ -382,7 +382,7 @@ def _chem_inputs(engine, zm, ev):
     """loss_rates' inputs of a chem event, cut to the region's scope (ch4_loss_kernel's cells),
     on the device; and the arrays to free."""
     m = ev.meta
-    im, jm, lm = m["im"], m["jm"], m["lm"]
+    lm = m["lm"]
     si, sj = zm.scope(ev.region)
     i0, i1, j0, j1 = si.start + 1, si.stop, sj.start + 1, sj.stop
     owned, out = [], {}
@@ -407,7 +407,6 @@ def _chem_inputs(engine, zm, ev):
         out["soil"] = up("soil", (slice(i0, i1), slice(j0, j1)))
         out["soil_rate"] = m["soil_rate"]
     out.update({k: m[k] for k in ("oh_scale", "cl_scale", "o1d_scale")})
-    del im, jm
     return out, owned
 
 
