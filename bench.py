@@ -18,7 +18,8 @@ measured HBM copy bandwidth; and, since the float64 step is bound by FP64 issue 
 its FP64 warp instructions per call (an ncu capture of the same kernels) x 32 lanes over the same
 time, against the DMUL/DADD issue rate measured in the run (`roofline.fp64`).  cpu_baseline:
 the oracle (a scalar C restatement of pydyn) on this host's cores on a bounded sample of the
-same workload.
+same workload.  published_case (the default workload at N = 1): pydyn's own GPU benchmark case,
+timed after the headline by the same rules, with its value over the A100's published 60.1.
 
 --impl reference runs the CPU reference arm: the oracle port of pydyn (the Python reference
 itself cannot be installed where this runs) on the same workload, with the same metric.
@@ -499,6 +500,41 @@ def run_adjoint(args, ws, rank):
     dev.close()
 
 
+def published_case(dev, flush, steps, warmup, gpu):
+    """The a100-case workload (pydyn gpu/bench.py:34-41) on the same device, timed as the
+    headline is: graph replays after `warmup` of them, the L2 flushed between replays, CUDA
+    events on the run's stream, clocks sampled during the timed region."""
+    from pydyn_gb300.forward import Forward
+
+    tree, lm, physics, seed, lmax = WORKLOADS["a100-case"]
+    fw = Forward(dev, tree, lm, seed=seed, physics=physics, lmax=lmax)
+    fw.interval(graph=False)
+    for _ in range(warmup):
+        fw.interval(graph=True)
+    evs = [(dev.event(), dev.event()) for _ in range(steps)]
+    dev.sync()
+    with Clocks(gpu) as clk:
+        t = fw.t
+        for k in range(steps):
+            flush.fill(float(k))
+            a, b = evs[k]
+            a.record()
+            fw.enqueue_interval_async(t)
+            b.record()
+            t += fw.nread
+        dev.sync()
+    if fw.rehearsal_failed():
+        raise RuntimeError("bench: Check_CFL rejected ndyn = nread in the published case")
+    fw.t = t
+    sec = sum(a.elapsed_ms(b) for a, b in evs) / steps / 1e3
+    fw.close()
+    value = sim_years_per_hour(sec)
+    return {"workload": "a100-case", "metric": metric_name("a100-case"), "value": value,
+            "unit": "sim-years/hour", "ms_per_step": sec * 1e3, "published": PUBLISHED["a100-case"],
+            "vs_published": value / PUBLISHED["a100-case"], "steps": steps, "warmup": warmup,
+            "config": workload_config("a100-case", 1), "clocks": clk.summary()}  # fmt: skip
+
+
 def main():
     ap = argparse.ArgumentParser(description=__doc__.split("\n")[0])
     ap.add_argument("--gpus", type=int, default=1)
@@ -667,9 +703,13 @@ def main():
     }  # fmt: skip
     if rank == 0 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(args.config)
+    fw.close()
+    if ws == 1 and args.config == DEFAULT:
+        # pydyn's own GPU benchmark case beside the headline, the only workload with a
+        # published number: timed after the headline's timed region, by the same rules
+        line["published_case"] = published_case(dev, flush, args.steps, args.warmup, local)
     if rank == 0:
         print(json.dumps(line), flush=True)
-    fw.close()
     dev.close()
     if ws > 1:
         import torch.distributed as dist
