@@ -726,8 +726,10 @@ def run_traces(names=TRACE_RUNS):
 
 
 # ------------------------------------------------------------------ dump sets (pydyn.dump, pydyn.replay)
-# name: (tree, lm, seed, tracers, ranks) of a synthetic set written by oracle/dumpset.py
-DUMP_SETS = {"two": ("two", 5, 3, 1, 1), "one": ("one", 5, 4, 1, 1), "two-ranks": ("two", 4, 6, 2, 2)}
+# name: (tree, lm, seed, tracers, ranks, umax) of a synthetic set written by oracle/dumpset.py;
+# two-reject's winds make Check_CFL halve the step (two steps of 1800 s in the interval)
+DUMP_SETS = {"two": ("two", 5, 3, 1, 1, 40.0), "one": ("one", 5, 4, 1, 1, 40.0), "two-ranks": ("two", 4, 6, 2, 2, 40.0),
+             "two-reject": ("two", 5, 14, 1, 1, 1000.0)}
 REPLAY_TAGS = ("x", "y", "z", "v", "s", "c", "cfl", "massflow", "m2phlb")
 
 
@@ -751,8 +753,8 @@ def write_dump_set(name, out):
     sys.path.insert(0, str(HERE.parents[1]))
     from oracle import dumpset
 
-    tree, lm, seed, nt, ranks = DUMP_SETS[name]
-    return dumpset.write_set(out, tree, lm=lm, seed=seed, nt=nt, ranks=ranks), dumpset.digest(out)
+    tree, lm, seed, nt, ranks, umax = DUMP_SETS[name]
+    return dumpset.write_set(out, tree, lm=lm, seed=seed, nt=nt, ranks=ranks, umax=umax), dumpset.digest(out)
 
 
 def dump_goldens():
