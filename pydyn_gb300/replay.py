@@ -7,9 +7,10 @@ compare, report, chemistry, sync (pydyn gpu/engine.py:17-74; replay.py:291-353) 
 ZoomState whose bodies are pydyn_gb300.zoom.  A dump array goes to the device as its file holds
 it (Fortran order) and a device kernel copies the section the state needs; a comparison is made
 on the device (gb_compare) and only its report comes back, the state never.  The report is the
-reference's (harness.compare's keys and values).  Its states are reused: `zeros` with the tree
-and tracer count of a state it made before zeroes that state and returns it -- the replay of
-one event holds one state; the free run, which keeps its own across events, is not served.
+reference's (harness.compare's keys and values).  `zeros` reuses a state it made before for the
+same tree and tracer count, zeroed on the device, when no caller holds it any more (the replay
+of one event holds one state), and makes a new one otherwise.  The free run, which reads state
+arrays on the host, is not served.
 
 `replay()` is the reference's replay of a set from the model's own inputs (replay.py:
 _Session.run, replay_operator, replay_m2phlb, replay_massflow, replay_cfl, physics), on this
@@ -92,15 +93,19 @@ class DeviceEngine:
 
     # -------------------------------------------------------------- states
     def zeros(self, zm, nt):
-        key = (id(zm), nt)
-        st = self._states.get(key)
-        if st is None:
-            st = self._states[key] = ZoomState.zeros(self.dev, zm, nt)
-        else:
-            for f in st.fields.values():
-                for a in f.values():
-                    a.fill(0.0)
-            st.saved.clear()
+        """A zero state of the tree with nt tracers: one made before and no longer held by
+        anyone (its only references the engine's list and this loop), zeroed on the device, or a
+        new one.  A caller that keeps a state across events keeps it from being reused."""
+        pool = self._states.setdefault((id(zm), nt), [])
+        for st in pool:
+            if sys.getrefcount(st) <= 3:  # the pool's list, the loop variable, the call's argument
+                for f in st.fields.values():
+                    for a in f.values():
+                        a.fill(0.0)
+                st.saved.clear()
+                return st
+        st = ZoomState.zeros(self.dev, zm, nt)
+        pool.append(st)
         return st
 
     def copy_into(self, view, arr):
@@ -199,10 +204,11 @@ class DeviceEngine:
         self.dev.sync()
 
     def free(self):
-        for st in self._states.values():
-            for f in st.fields.values():
-                for a in f.values():
-                    a.free()
+        for pool in self._states.values():
+            for st in pool:
+                for f in st.fields.values():
+                    for a in f.values():
+                        a.free()
         self._states = {}
         self._out.free()
 

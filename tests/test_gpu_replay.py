@@ -70,6 +70,26 @@ def test_planted_difference_is_reported_as_the_reference_reports_it(dev, tmp_pat
 
 
 @pytest.mark.gpu
+def test_engine_reuses_only_states_no_one_holds(dev):
+    from pydyn_gb300 import synth
+    from pydyn_gb300.replay import DeviceEngine
+
+    engine = DeviceEngine(dev)
+    zm = synth.tree("two", 4)
+    a = engine.zeros(zm, 1)
+    a[1]["m"].fill(5.0)
+    b = engine.zeros(zm, 1)  # `a` is held: a new state
+    assert b is not a and (a[1]["m"].host() == 5.0).all()
+    a_id = id(a)
+    del a
+    c = engine.zeros(zm, 1)  # the first state is free again: reused, and zeroed
+    assert id(c) == a_id and (c[1]["m"].host() == 0.0).all()
+    assert engine.zeros(zm, 2) is not c  # another tracer count: another state
+    del b, c
+    engine.free()
+
+
+@pytest.mark.gpu
 def test_device_comparison_is_the_reference_report(dev):
     from oracle.compare import compare
 
