@@ -198,10 +198,13 @@ __global__ void __launch_bounds__(WARPS * 32) k_advect_x(XArgs A) {
                     const int lo = (i == 0) ? n : i;
                     const double mo = m_s[i], alo = a_s[i], ahi = a_s[i + 1];
                     const double mn = (mo + alo) - ahi;
+                    // 1 / mn, the next sub-step's Courant factor, also gives the slope's quotient
+                    const double inv = 1.0 / mn, y = recip_mark(mn, inv);
                     for (int t = 0; t < ntc; ++t) {
                         double *f = F(0, t), *pf = F(1, t), *fy = F(2, t), *fz = F(3, t);
                         double rmn = Q(0, t)[i] - (f[i + 1] - f[lo]);
-                        double rxn = along_slope(Q(1, t)[i], pf[lo], pf[i + 1], alo, ahi, rmn, f[lo], f[i + 1], mo, mn);
+                        double rxn = along_slope_y(Q(1, t)[i], pf[lo], pf[i + 1], alo, ahi, rmn, f[lo], f[i + 1], mo,
+                                                   mn, y);
                         if (A.limits) rxn = np_limit(rxn, rmn);
                         Q(0, t)[i] = rmn;
                         Q(1, t)[i] = rxn;
@@ -209,7 +212,7 @@ __global__ void __launch_bounds__(WARPS * 32) k_advect_x(XArgs A) {
                         Q(3, t)[i] = Q(3, t)[i] - (fz[i + 1] - fz[lo]);
                     }
                     m_s[i] = mn;
-                    minv_s[i] = 1.0 / mn;
+                    minv_s[i] = inv;
                 }
                 __syncwarp();
             }

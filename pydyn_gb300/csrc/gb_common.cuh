@@ -105,6 +105,11 @@ __device__ __forceinline__ double recip_for(double d) {
     const int ed = (int)((__double_as_longlong(d) >> 52) & 0x7ff);
     return (ed >= 23 && ed <= 2023) ? 1.0 / d : 0.0;
 }
+// recip_for(d) from an inv = 1.0 / d the caller makes anyway (an integer test, no division)
+__device__ __forceinline__ double recip_mark(double d, double inv) {
+    const int ed = (int)((__double_as_longlong(d) >> 52) & 0x7ff);
+    return (ed >= 23 && ed <= 2023) ? inv : 0.0;
+}
 __device__ __forceinline__ double div_by_recip(double a, double d, double y) {
     const unsigned long long ab = (unsigned long long)__double_as_longlong(a);
     if (((unsigned long long)__double_as_longlong(y) << 1) != 0) {
@@ -133,12 +138,25 @@ __device__ __forceinline__ bool lt_zero(double x) {
 
 // ------------------------------------------------------------------ NumPy's element rules
 // np.clip(s, -|r|, |r|) exactly as NumPy evaluates it: a NaN in s wins, then max with the lower
-// bound ((s > lo) ? s : lo), then a NaN wins again, then min with the upper bound.
+// bound ((s > lo) ? s : lo), then a NaN wins again, then min with the upper bound.  Both compares
+// are made on the integer pipe from the magnitudes' bit patterns (which order as the values do):
+// with lo = -|r|, s > lo holds for a negative s (either zero included) where |s| < |r|, and for
+// a non-negative s unless s and r are both zeros (+0 > -0 is false); t < hi = |r| holds for a
+// negative t where t and r are not both zeros, for a non-negative t where |t| < |r|.  A NaN r
+// makes lo a NaN: s > lo fails, and t = lo is returned.
 __device__ __forceinline__ double np_limit(double s, double r) {
-    double hi = gb_abs(r);
-    double lo = gb_neg(hi);
-    double t = gb_isnan(s) ? s : (s > lo ? s : lo);
-    return gb_isnan(t) ? t : (t < hi ? t : hi);
+    const unsigned long long MAG = 0x7fffffffffffffffULL, INF = 0x7ff0000000000000ULL;
+    const unsigned long long bs = (unsigned long long)__double_as_longlong(s);
+    const unsigned long long as = bs & MAG, ar = (unsigned long long)__double_as_longlong(r) & MAG;
+    const double hi = __longlong_as_double((long long)ar), lo = __longlong_as_double((long long)(ar | ~MAG));
+    if (as > INF) return s;
+    if (ar > INF) return lo;
+    const bool sneg = (bs >> 63) != 0;
+    const bool gt = sneg ? as < ar : (as | ar) != 0;  // s > lo
+    const unsigned long long at = gt ? as : ar;      // |t|, t = gt ? s : lo
+    const bool tneg = gt ? sneg : true;
+    const bool lt = tneg ? (at | ar) != 0 : at < ar;  // t < hi
+    return lt ? (gt ? s : lo) : hi;
 }
 
 // np.maximum(a, b): NaN in a, else NaN in b, else (a > b ? a : b).
@@ -172,6 +190,14 @@ __device__ __forceinline__ double along_slope(double s, double pf_lo, double pf_
                                               double m_old, double m_new) {
     double num = ((pf_lo - pf_hi) - (lo - hi) * s) + 3.0 * ((lo + hi) * rm_new - (f_lo + f_hi) * m_old);
     return s + num / m_new;
+}
+// the same with the division num / m_new made from y_new = recip_for(m_new) (div_by_recip: the
+// division's bits), where the caller has the reciprocal of the new mass for other uses
+__device__ __forceinline__ double along_slope_y(double s, double pf_lo, double pf_hi, double lo,
+                                                double hi, double rm_new, double f_lo, double f_hi,
+                                                double m_old, double m_new, double y_new) {
+    double num = ((pf_lo - pf_hi) - (lo - hi) * s) + 3.0 * ((lo + hi) * rm_new - (f_lo + f_hi) * m_old);
+    return s + div_by_recip(num, m_new, y_new);
 }
 
 // The progressive rescale of dynamu / dynamv (ops.py:304-307): f * (n - 1) / n, evaluated
