@@ -72,7 +72,7 @@ __device__ void rebin_span(const Edges &ip, int nip, double bot, double top, int
     int a = 0, b = nip;
     while (a < b) {
         const int mid = (a + b) >> 1;
-        if (ip[mid + 1] >= bot)
+        if (gb_ge(ip[mid + 1], bot))
             a = mid + 1;
         else
             b = mid;
@@ -82,7 +82,7 @@ __device__ void rebin_span(const Edges &ip, int nip, double bot, double top, int
     b = nip;
     while (a < b) {
         const int mid = (a + b) >> 1;
-        if (ip[mid] > top)
+        if (gb_gt(ip[mid], top))
             a = mid + 1;
         else
             b = mid;
@@ -98,10 +98,37 @@ __device__ double rebin_layer(const Edges &ip, int first, int last, const double
     double overlap = 0.0;
     for (int k = first; k < last; ++k) {
         const double thickness = np_min(bot, ip[k]) - np_max(top, ip[k + 1]);
-        if (thickness > 0.0) overlap = overlap + data[k * stride] * thickness;
+        if (gb_gt0(thickness)) overlap = overlap + data[k * stride] * thickness;
     }
     const double width = bot - top;
-    return width > 0.0 ? overlap / width : overlap;
+    return gb_gt0(width) ? overlap / width : overlap;
+}
+
+// rebin_layer of three columns on the same edges at once (the zonal OH, Cl and O(1D) columns):
+// each layer's overlap is made once and added to each column's sum, in input order as before
+template <class Edges>
+__device__ void rebin_layer3(const Edges &ip, int first, int last, const double *d0, int64_t s0, const double *d1,
+                             int64_t s1, const double *d2, int64_t s2, double bot, double top, double &r0, double &r1,
+                             double &r2) {
+    double o0 = 0.0, o1 = 0.0, o2 = 0.0;
+    for (int k = first; k < last; ++k) {
+        const double thickness = np_min(bot, ip[k]) - np_max(top, ip[k + 1]);
+        if (gb_gt0(thickness)) {
+            o0 = o0 + d0[k * s0] * thickness;
+            o1 = o1 + d1[k * s1] * thickness;
+            o2 = o2 + d2[k * s2] * thickness;
+        }
+    }
+    const double width = bot - top;
+    if (gb_gt0(width)) {
+        r0 = o0 / width;
+        r1 = o1 / width;
+        r2 = o2 / width;
+    } else {
+        r0 = o0;
+        r1 = o1;
+        r2 = o2;
+    }
 }
 
 // thread per latitude: the zonal columns' edges (strat_edges, chem.py:91-98: midpoints, a half
@@ -123,7 +150,7 @@ __global__ void k_chem_rows(CArgs A) {
             e = 0.0;
         }
         edges[k] = e * 100.0;
-        if (k > 0) ok = ok && (edges[k] - edges[k - 1] < 0.0);
+        if (k > 0) ok = ok && gb_lt(edges[k], edges[k - 1]);  // = (edges[k] - edges[k-1] < 0) for every input
     }
     if (!ok) raise_status(A.ctl, GB_ELEVELS);
     const double cl = gbm_cos(A.lat[j]);
@@ -160,12 +187,12 @@ __global__ void __launch_bounds__(GB_TUNE_MAX_CELL) k_chem(CArgs A) {
     const int ns = A.ns, nt = A.ntrop;
     const double *edges = A.edges + (int64_t)j * (ns + 1);
     const double bot = E3(A.phlb, i, j, l), top = E3(A.phlb, i, j, l + 1);
-    bool ok = top - bot < 0.0;
+    bool ok = gb_lt(top, bot);  // = (top - bot < 0), exactly: a difference of unequal doubles is never 0
     TropEdges tedges{nullptr, 0, 0};
     if (A.has_trop) {
         tedges = TropEdges{&E3(A.pltrop, i, j, 0), A.pltrop.s2, nt};
         if (l == 0)  // the column's tropospheric edges, checked once
-            for (int k = 0; k < nt; ++k) ok = ok && (tedges[k + 1] - tedges[k] < 0.0);
+            for (int k = 0; k < nt; ++k) ok = ok && gb_lt(tedges[k + 1], tedges[k]);
     }
     if (!ok) {
         raise_status(A.ctl, GB_ELEVELS);
@@ -175,7 +202,7 @@ __global__ void __launch_bounds__(GB_TUNE_MAX_CELL) k_chem(CArgs A) {
     const double *doh = &E2(A.soh, j, 0), *dcl = &E2(A.scl, j, 0), *dod = &E2(A.sod, j, 0);
 
     {
-        const bool strat = bot < trop;
+        const bool strat = gb_lt(bot, trop);
         const double T = E3(A.temper, i, j, l);
         double *cc = A.cache ? A.cache + u : nullptr;  // value v at cc[v * ncell]
         const bool hit = cc && __double_as_longlong(cc[0]) == __double_as_longlong(bot) &&
@@ -187,21 +214,20 @@ __global__ void __launch_bounds__(GB_TUNE_MAX_CELL) k_chem(CArgs A) {
             L1 = cc[4 * ncell];
             L2 = cc[5 * ncell];
         } else {
-            const bool below = bot > edges[0];
+            const bool below = gb_gt(bot, edges[0]);
             double s_cl = dcl[0], s_od = dod[0];
             s_oh = doh[0];
             if (!below) {  // the three zonal columns share their edges: one overlap search
                 int first, last;
                 rebin_span(edges, ns, bot, top, first, last);
-                s_oh = rebin_layer(edges, first, last, doh, A.soh.s1, bot, top);
-                s_cl = rebin_layer(edges, first, last, dcl, A.scl.s1, bot, top);
-                s_od = rebin_layer(edges, first, last, dod, A.sod.s1, bot, top);
+                rebin_layer3(edges, first, last, doh, A.soh.s1, dcl, A.scl.s1, dod, A.sod.s1, bot, top, s_oh, s_cl,
+                             s_od);
             }
             double trop_cl = 0.0;
             if (A.has_trop) {
                 const double *dtr = &E3(A.cltrop, i, j, 0);
                 double v = dtr[0];
-                if (!(bot > tedges[0])) {
+                if (!gb_gt(bot, tedges[0])) {
                     int first, last;
                     rebin_span(tedges, nt, bot, top, first, last);
                     v = rebin_layer(tedges, first, last, dtr, A.cltrop.s2, bot, top);

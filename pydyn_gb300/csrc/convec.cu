@@ -71,7 +71,7 @@ __device__ __forceinline__ double &AT(const DV &v, int64_t i, int64_t j, int64_t
 __device__ __forceinline__ double &AT4(const DV &v, int64_t i, int64_t j, int64_t l, int64_t t) {
     return v.p[i * v.s0 + j * v.s1 + l * v.s2 + t * v.s3];
 }
-__device__ __forceinline__ double max0(double x) { return gb_isnan(x) ? x : (0.0 > x ? 0.0 : x); }
+__device__ __forceinline__ double max0(double x) { return gb_isnan(x) ? x : (lt_zero(x) ? 0.0 : x); }  // 0.0 > x: lt_zero
 // x == 0.0 (either sign), tested on the integer pipe: the FP64 pipe is kept for arithmetic
 __device__ __forceinline__ bool is_zero(double x) { return (__double_as_longlong(x) << 1) == 0; }
 
@@ -139,7 +139,7 @@ __device__ void chain_up(const CArgs &A, int c, int i, int j) {
             const double eu = eb[u], du = db[u];
             const bool act = top >= k;
             const double a = mu + eu - du;
-            mu = (act && a > 0.0) ? a : 0.0;
+            mu = (act && gb_gt0(a)) ? a : 0.0;
             amu[k] = mu;
         }
     }
@@ -168,7 +168,7 @@ __device__ void chain_down(const CArgs &A, int c, int i, int j) {
             const double ed = eb[u], dd = db[u];
             const bool act = lfs >= k;
             const double a = md - ed + dd;
-            md = (act && a < 0.0) ? a : 0.0;
+            md = (act && lt_zero(a)) ? a : 0.0;
             amd[k - 1] = md;
         }
     }
@@ -192,7 +192,7 @@ __global__ void __launch_bounds__(GB_TUNE_MAX_CELL) k_convec_ratios(CArgs A) {
         if (act) {
             const double mu = amu[k - 1], eu = AT(A.entu, i, j, k - 1), du = AT(A.detu, i, j, k - 1);
             const double a = mu + eu - du;
-            z = a > 0.0 ? max0(1.0 - du / (mu + eu)) : 0.0;
+            z = gb_gt0(a) ? max0(1.0 - du / (mu + eu)) : 0.0;
         }
         zu[k] = z;
     }
@@ -202,7 +202,7 @@ __global__ void __launch_bounds__(GB_TUNE_MAX_CELL) k_convec_ratios(CArgs A) {
         if (act) {
             const double md = amd[k], ed = AT(A.entd, i, j, k - 1), dd = AT(A.detd, i, j, k - 1);
             const double a = md - ed + dd;
-            z = a < 0.0 ? max0(1.0 + dd / (md - ed)) : 0.0;
+            z = lt_zero(a) ? max0(1.0 + dd / (md - ed)) : 0.0;
         }
         zd[k] = z;
     } else {

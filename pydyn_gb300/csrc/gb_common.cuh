@@ -81,6 +81,27 @@ __device__ __forceinline__ double gb_neg(double x) {
     return __longlong_as_double(__double_as_longlong(x) ^ (long long)0x8000000000000000ULL);
 }
 
+// The ordered compares a < b, a <= b, a > b, a >= b, x > 0 on the integer pipe, true and false
+// exactly where the FP64 compares are: false when either operand is a NaN, +0 equal to -0.  The
+// sign-magnitude image of the bit patterns (the bits where the sign is clear, INT64_MIN - bits
+// where it is set) orders every non-NaN double as its value, both zeros at 0.
+__device__ __forceinline__ long long gb_ord(double x) {
+    const long long b = __double_as_longlong(x);
+    return b >= 0 ? b : (long long)(0x8000000000000000ULL - (unsigned long long)b);
+}
+__device__ __forceinline__ bool gb_lt(double a, double b) {
+    return !gb_isnan(a) && !gb_isnan(b) && gb_ord(a) < gb_ord(b);
+}
+__device__ __forceinline__ bool gb_le(double a, double b) {
+    return !gb_isnan(a) && !gb_isnan(b) && gb_ord(a) <= gb_ord(b);
+}
+__device__ __forceinline__ bool gb_gt(double a, double b) { return gb_lt(b, a); }
+__device__ __forceinline__ bool gb_ge(double a, double b) { return gb_le(b, a); }
+__device__ __forceinline__ bool gb_gt0(double x) {  // x > 0.0: positive, not a zero, not a NaN
+    const long long b = __double_as_longlong(x);
+    return b > 0 && b <= 0x7ff0000000000000LL;
+}
+
 // abs(c / mu) < 1.0 (the sub-cycle searches' Courant test, ops.py:330-341) without the division
 // where the answer is certain: |c| < fl(0.9999 |mu|) puts the quotient below 0.9999 (1 + 2^-53)
 // < 1 - 2^-54, so it rounds below 1 (for subnormal |mu| too); |c| > |mu| puts it above 1.  The
@@ -159,12 +180,13 @@ __device__ __forceinline__ double np_limit(double s, double r) {
     return lt ? (gt ? s : lo) : hi;
 }
 
-// np.maximum(a, b): NaN in a, else NaN in b, else (a > b ? a : b).
+// np.maximum(a, b): NaN in a, else NaN in b, else (a > b ? a : b), the compare on the integer pipe
+// (gb_ord; neither is a NaN by then).
 __device__ __forceinline__ double np_max(double a, double b) {
-    return gb_isnan(a) ? a : (gb_isnan(b) ? b : (a > b ? a : b));
+    return gb_isnan(a) ? a : (gb_isnan(b) ? b : (gb_ord(a) > gb_ord(b) ? a : b));
 }
 __device__ __forceinline__ double np_min(double a, double b) {
-    return gb_isnan(a) ? a : (gb_isnan(b) ? b : (a < b ? a : b));
+    return gb_isnan(a) ? a : (gb_isnan(b) ? b : (gb_ord(a) < gb_ord(b) ? a : b));
 }
 
 // Tracer fluxes of the slopes scheme through one face (pydyn kernels.py:75-84): the flux,

@@ -142,7 +142,7 @@ __global__ void __launch_bounds__(GB_TUNE_MAX_COLUMN) k_kzz_surface(KArgs A) {
     const double sr_help = np_min(S2(A.surf[2], i, j), 0.03);
     double land = VKARMAN * wind10m / gbm_log(10.0 / sr_help) * gbm_log(75.0 / sr_help);
     land = land / gbm_log(10.0 / sr_land);
-    const double ustar_land = xland > 0.0 ? land : 0.0;
+    const double ustar_land = gb_gt0(xland) ? land : 0.0;
     const double ustar_loc = xland * ustar_land + (1.0 - xland) * ustar_sea;
 
     const double ph0 = A.at[0] + A.bt[0] * sm, ph1 = A.at[1] + A.bt[1] * sm;
@@ -306,7 +306,8 @@ __global__ void __launch_bounds__(GB_TUNE_MAX_CELL) k_kzz_interfaces(KArgs A) {
     const double fmt = gbm_pow(zslask, ONET);
     const double wsc = U * fmt;
     zpblk = (1.0 - jq5) * zpblk + jq5 * wsc * VKARMAN * z * zzh;
-    const double term1 = jq3 != 0.0 ? cv[8] : cv[6], term2 = jq3 != 0.0 ? cv[9] : cv[7];
+    const bool jq3_on = (__double_as_longlong(jq3) << 1) != 0;  // jq3 != 0.0, on the integer pipe
+    const double term1 = jq3_on ? cv[8] : cv[6], term2 = jq3_on ? cv[9] : cv[7];
     const double term3 = CCON * FAKN * zwstr / (U * term1);
     const double pr = jq3 * (term1 / term2 + term3) + (1.0 - jq3);
     const double kv = jq3 * np_max(zpblk / pr, KVHMIN) + (1.0 - jq3) * zkvh;
