@@ -29,7 +29,11 @@ constexpr double GRAV = 9.80665, PI_ = 3.14159265358979, AE = 6.371e6, VKARMAN =
 constexpr double LVAP = 2.5e6, RGAS = 8.3144, XMAIR = 28.94, RHO_AIR = 1.2, CKMIN = 1.0e-15, SFFRAC = 0.1;
 constexpr double APZERO = 100000.0, BETAH = 15.0, FAK = 8.5, FAKN = 7.2, TINY = 1.0e-9, ZACB = 100.0;
 constexpr double RICR = 0.3, SSFRAC = 0.1, KVHMIN = 0.1;
-constexpr int NCOLVAL = 12;  // z0, pblh, wobkl, wheatv, ustr, zwstr, t1a, t2a, t1b, t2b, wtseff, thvparc
+// z0, pblh, wobkl, wheatv, ustr, zwstr, t1a, t2a, t1b, t2b, wtseff, thvparc, then the interfaces'
+// column constants: the Prandtl sums for jq3 = 0 and 1 and the reciprocal of the second, the free-convection
+// stability 1 - SSFRAC BETAH pblh / wobkl and its cube root, the reciprocals of pblh and wobkl
+constexpr int NCOLVAL = 19;
+constexpr double RGRAV = 1.0 / GRAV;  // correctly rounded: the divisor's reciprocal for div_by_recip
 
 struct KArgs {
     DV spm, sp, pu, pv, t, q, surf[10], dkg, pblh;
@@ -70,7 +74,7 @@ __global__ void __launch_bounds__(GB_TUNE_MAX_CELL) k_kzz_levels(KArgs A) {
     const double ZKAPPA = rair() / CP_AIR, ZCRDQ = zcrdq();
     const double sm = S2(A.spm, i, j);
     const double ph0 = A.at[l] + A.bt[l] * sm, ph1 = A.at[l + 1] + A.bt[l + 1] * sm;
-    const double m = (ph0 - ph1) * A.dxyp[j] / GRAV;
+    const double m = div_by_recip((ph0 - ph1) * A.dxyp[j], GRAV, RGRAV);
     const double pf = (ph0 + ph1) * 0.5;
     const double tl = S3(A.t, i, j, l), ql = S3(A.q, i, j, l);
     const double wthm = tl * gbm_pow(APZERO / pf, ZKAPPA);
@@ -82,7 +86,7 @@ __global__ void __launch_bounds__(GB_TUNE_MAX_CELL) k_kzz_levels(KArgs A) {
         const double s = S2(A.sp, i, j);
         const double tv = tl * (1.0 + 0.608 * ql);
         const double pdown = A.at[l] + A.bt[l] * s, pup = A.at[l + 1] + A.bt[l + 1] * s;
-        A.dzg[t] = tv * 287.05 * gbm_log(pdown / pup) / GRAV;
+        A.dzg[t] = div_by_recip(tv * 287.05 * gbm_log(pdown / pup), GRAV, RGRAV);
     }
     const double dyy = AE * A.dy * (PI_ / 180.0);
     A.uw[t] = A.dxx[j] * (S3(A.pu, i + 1, j, l) + S3(A.pu, i, j, l)) * 0.5 / m;
@@ -245,6 +249,17 @@ __global__ void __launch_bounds__(GB_TUNE_MAX_COLUMN) k_kzz_sweep2(KArgs A) {
     cv[7] = sqrt(stab0);
     cv[8] = gbm_pow(stab1, ONET);
     cv[9] = sqrt(stab1);
+    // the interface's pr = jq3 (t1 / t2 + CCON FAKN w* / (U t1)) + (1 - jq3) takes t1, t2 from one of
+    // the two pairs above: both sums, each in the statement's own order
+    const double CCON = SFFRAC * VKARMAN, zwstr = cv[5], U = cv[4];
+    cv[12] = cv[6] / cv[7] + CCON * FAKN * zwstr / (U * cv[6]);
+    cv[13] = cv[8] / cv[9] + CCON * FAKN * zwstr / (U * cv[8]);
+    cv[14] = recip_for(cv[13]);
+    const double stabw = 1.0 - SSFRAC * BETAH * pblh / wobkl;
+    cv[15] = stabw;
+    cv[16] = gbm_pow(stabw, ONET);
+    cv[17] = recip_for(pblh);
+    cv[18] = recip_for(wobkl);
 }
 
 // Lanes run along the columns and warps along the interfaces (a block: 32 columns at blockDim / 32
@@ -257,16 +272,18 @@ __global__ void __launch_bounds__(GB_TUNE_MAX_CELL) k_kzz_interfaces(KArgs A) {
     const int k = (int)(blockIdx.x % nkg) * lv + (int)(threadIdx.x >> 5) + 1;  // interface k, between layers k-1 and k
     if (c >= (int64_t)A.im * A.jm || k > ni) return;
     const int i = (int)(c / A.jm), j = (int)(c % A.jm);
-    const double ONET = 1.0 / 3.0, CCON = SFFRAC * VKARMAN;
+    const double ONET = 1.0 / 3.0;
     const double *cv = A.col + c * NCOLVAL;
-    const double z0 = cv[0], P = cv[1], Wb = cv[2], HV = cv[3], U = cv[4], zwstr = cv[5];
+    const double z0 = cv[0], P = cv[1], Wb = cv[2], HV = cv[3], U = cv[4];
+    const double yP = cv[17], yWb = cv[18];
     const int64_t ck = c * lm + k;
     const double *gph = A.gph + c * (lm + 1);
 
     const double z = gph[k] - z0;
     double jq = jqif(1000.0, z);
-    const double zlambdac = jq * 300.0 + (1.0 - jq) * (30.0 + 270.0 * gbm_exp(1.0 - z / 1000.0));
-    double cml2 = 1.0 / (1.0 / zlambdac + 1.0 / (VKARMAN * z));
+    const double zlambdac = jq * 300.0 + (1.0 - jq) * (30.0 + 270.0 * gbm_exp(1.0 - div_by_recip(z, 1000.0, 1.0e-3)));
+    const double rkz = 1.0 / (VKARMAN * z);
+    double cml2 = 1.0 / (1.0 / zlambdac + rkz);
     cml2 = cml2 * cml2;
     const double du = A.uw[ck] - A.uw[ck - 1], dv = A.vw[ck] - A.vw[ck - 1];
     double zdup2 = np_max(du * du + dv * dv, 1.0e-10);
@@ -284,15 +301,16 @@ __global__ void __launch_bounds__(GB_TUNE_MAX_CELL) k_kzz_interfaces(KArgs A) {
     jq = jqif(zrinub, 0.0);
     const double wkvf = jq * np_max(CKMIN, zkvn * zfstabh) + (1.0 - jq) * np_max(CKMIN, zkvn * zfunst);
     jq = jqif(P, z);
-    const double zh = jq * z / P;
-    const double zl = jq * z / Wb + (1.0 - jq);
+    const double jz = jq * z;
+    const double zh = div_by_recip(jz, P, yP);
+    const double zl = div_by_recip(jz, Wb, yWb) + (1.0 - jq);
     const double zzh = jq * ((1.0 - zh) * (1.0 - zh));
     double jq1 = jqif(HV, 0.0);
     const double jq2 = jq * (1.0 - jq1), jq3 = jq * jq1;
     const double jq6 = jq1 * jqif(P, whk1) * jqif(whk, P);
     jq1 = jqif(SFFRAC, zh);
     const double jq4 = jq3 * jq1, jq5 = jq3 * (1.0 - jq1);
-    cml2 = 1.0 / (1.0 / (VKARMAN * z) + 1.0 / 450.0);
+    cml2 = 1.0 / (rkz + 1.0 / 450.0);
     cml2 = cml2 * cml2;
     const double jqq = jqif(zrinub, 0.0);
     zfstabh = jqq / (1.0 + 10.0 * zrinub * sqrt(1.0 + jqq * zrinub)) + (1.0 - jqq);
@@ -301,16 +319,23 @@ __global__ void __launch_bounds__(GB_TUNE_MAX_CELL) k_kzz_interfaces(KArgs A) {
     double zslask = 1.0 - BETAH * zl;
     zslask = jq4 * zslask + (1.0 - jq4);
     zpblk = (1.0 - jq4) * zkvh + jq4 * (U * VKARMAN * z * zzh * gbm_pow(zslask, ONET));
-    zslask = 1.0 - SSFRAC * BETAH * P / Wb;
-    zslask = jq5 * zslask + (1.0 - jq5);
-    const double fmt = gbm_pow(zslask, ONET);
+    // jq5 is 0 or 1: at 1 the base is the column's stabw (stabw + 0.0, whose cube root is stabw's)
+    const bool jq5_on = (__double_as_longlong(jq5) << 1) != 0;
+    double fmt;
+    if (jq5_on) {
+        fmt = cv[16];
+    } else {
+        zslask = jq5 * cv[15] + (1.0 - jq5);
+        fmt = gbm_pow(zslask, ONET);
+    }
     const double wsc = U * fmt;
     zpblk = (1.0 - jq5) * zpblk + jq5 * wsc * VKARMAN * z * zzh;
     const bool jq3_on = (__double_as_longlong(jq3) << 1) != 0;  // jq3 != 0.0, on the integer pipe
-    const double term1 = jq3_on ? cv[8] : cv[6], term2 = jq3_on ? cv[9] : cv[7];
-    const double term3 = CCON * FAKN * zwstr / (U * term1);
-    const double pr = jq3 * (term1 / term2 + term3) + (1.0 - jq3);
-    const double kv = jq3 * np_max(zpblk / pr, KVHMIN) + (1.0 - jq3) * zkvh;
+    const double pr = jq3 * (jq3_on ? cv[13] : cv[12]) + (1.0 - jq3);
+    // pr's reciprocal: the sum's at jq3 = 1 (pr = sum + 0.0), 1 where jq3 = 0 left pr at exactly 1,
+    // else none (div_by_recip divides)
+    const double ypr = jq3_on ? cv[14] : (__double_as_longlong(pr) == 0x3ff0000000000000LL ? 1.0 : 0.0);
+    const double kv = jq3 * np_max(div_by_recip(zpblk, pr, ypr), KVHMIN) + (1.0 - jq3) * zkvh;
     const double thvgrad = dthv / zdz;
     const double kvhentr = 0.2 * HV / thvgrad;
     const double kvh = jq6 * kvhentr + (1.0 - jq6) * kv;
@@ -321,7 +346,8 @@ __global__ void __launch_bounds__(GB_TUNE_MAX_CELL) k_kzz_interfaces(KArgs A) {
         const double sm = S2(A.spm, i, j);
         const double p0 = A.at[l] + A.bt[l] * sm, p1 = A.at[l + 1] + A.bt[l + 1] * sm,
                      p2 = A.at[l + 2] + A.bt[l + 2] * sm;
-        const double m0 = (p0 - p1) * A.dxyp[j] / GRAV, m1 = (p1 - p2) * A.dxyp[j] / GRAV;
+        const double m0 = div_by_recip((p0 - p1) * A.dxyp[j], GRAV, RGRAV),
+                     m1 = div_by_recip((p1 - p2) * A.dxyp[j], GRAV, RGRAV);
         const double dz = gph[l + 2] - gph[l];
         S3(A.dkg, i, j, l) = np_max(0.0, kvh) * 2.0 * (m1 + m0) / (dz * dz);
     }
