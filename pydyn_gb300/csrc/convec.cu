@@ -690,7 +690,7 @@ __global__ void k_convec_apply(CArgs A) {
             r0 = E;
         }
         for (int r = r0; r < n; ++r) {
-            y = 0.0 - lb[r] * y;
+            y = zero_minus(lb[r] * y);  // 0.0 - lb[r] y
             X[(size_t)r * n + x] = y;
         }
     }
@@ -705,7 +705,7 @@ __global__ void k_convec_apply(CArgs A) {
             for (int k = r + 1; k < rend[r]; ++k) {
                 const double w = U[(size_t)r * n + k];
                 if (is_zero(w)) continue;
-                a = a - w * X[(size_t)k * n + x];
+                a = sub_ip(a, w * X[(size_t)k * n + x]);
             }
             X[(size_t)r * n + x] = div_by_recip(a, r >= E ? ud[r] : U[(size_t)r * n + r], rc[r]);
         }
@@ -724,7 +724,7 @@ __global__ void k_convec_apply(CArgs A) {
     for (int t = 0; t < A.nt; ++t) {
         double zr = 0.0;
         if (live)
-            for (int k = 0; k < n; ++k) zr = zr + C[k] * AT4(A.q[0], i, j, k, t);
+            for (int k = 0; k < n; ++k) zr = add_ip(zr, C[k] * AT4(A.q[0], i, j, k, t));
         __syncthreads();  // every thread of the column has read rm(., t)
         if (live) AT4(A.q[0], i, j, l, t) = zr;
     }

@@ -113,15 +113,21 @@ __device__ __forceinline__ bool cfl_pass(double c, double mu) {
     return gb_abs(c / mu) < 1.0;
 }
 
-// a / d, correctly rounded, from y = RN(1 / d) shared by many quotients of one divisor
-// (Markstein's correction, IBM J. Res. Develop. 34(1), 1990): q0 = RN(a y), then twice
-// r = a - d q (exact by FMA while q is within an ulp of a / d) and q = RN(q + r y).  q0 is within
-// 1.5 ulp of a / d, the first correction brings it within half an ulp plus a few 2^-52 ulp, and
-// from within one ulp Markstein's theorem makes the second exact: RN(a / d).  One multiply and
-// four FMAs on the FP64 pipe, where a division costs eight.  The proof needs normal operands
-// and results away from overflow and underflow: a zero a (whose quotient is a y, signed as a / d),
-// and anything outside |a| >= 2^-960, |d| in [2^-1000, 2^1000], |a / d| in [2^-1001, 2^1001],
-// take the division itself, as does y = 0 (the caller's mark for a divisor outside that range).
+// a / d, correctly rounded, from y = RN(1 / d) shared by many quotients of one divisor: one
+// multiply on the FP64 pipe, the rest on the integer pipe.  q0 = RN(a y) carries a relative
+// error below 2^-52 ((1 + 2^-53)^2), so it lies within 2 ulp of a / d.  Where q0's significand
+// mq is at least 1 and 5 ulp inside its binade, a / d lies in that binade, and the correctly
+// rounded quotient is q0 + k ulp for k in -2..2: k = round(R / md), R = a - q0 d in units of
+// ulp(q0) d / md.  With a = ma 2^Ea, d = md 2^Ed, q0 = mq 2^Eq (53-bit integer significands),
+// R = ma 2^t - mq md for t = Ea - Eq - Ed (52 or 53 when q0 d is that close to a), an integer
+// below 2 md < 2^54 in magnitude: its low 64 bits, (ma << t) - mq md, are all of it.  Rounding
+// to nearest even compares 2|R| with md and 3 md (a tie -- which a quotient of two doubles
+// never is -- goes to the even neighbour), and the neighbour is q0's bit pattern plus or minus k
+// (the patterns of one sign run in the order of their magnitudes).  A zero a gives a y, signed
+// as a / d.  y = 0 (the caller's mark for a divisor whose reciprocal is not a normal number),
+// and any a, d or q0 outside that -- a zero d, subnormal, infinite or NaN operands, q0 at a
+// binade's edge or not normal -- take the division itself, on the FP64 pipe, through a call
+// (a predicated-off division beside the integer path would hold the FP64 pipe on every call).
 __device__ __forceinline__ double recip_for(double d) {
     const int ed = (int)((__double_as_longlong(d) >> 52) & 0x7ff);
     return (ed >= 23 && ed <= 2023) ? 1.0 / d : 0.0;
@@ -131,20 +137,95 @@ __device__ __forceinline__ double recip_mark(double d, double inv) {
     const int ed = (int)((__double_as_longlong(d) >> 52) & 0x7ff);
     return (ed >= 23 && ed <= 2023) ? inv : 0.0;
 }
+static __device__ __noinline__ double div_fp64_pipe(double a, double d) { return a / d; }
 __device__ __forceinline__ double div_by_recip(double a, double d, double y) {
-    const unsigned long long ab = (unsigned long long)__double_as_longlong(a);
-    if (((unsigned long long)__double_as_longlong(y) << 1) != 0) {
-        if ((ab << 1) == 0) return a * y;
-        const int ea = (int)((ab >> 52) & 0x7ff), ed = (int)((__double_as_longlong(d) >> 52) & 0x7ff);
-        const int diff = ea - ed;
-        if (ea >= 63 && ea <= 2023 && diff >= -1000 && diff <= 1000) {
-            const double q0 = a * y;
-            const double q1 = __fma_rn(__fma_rn(-q0, d, a), y, q0);
-            return __fma_rn(__fma_rn(-q1, d, a), y, q1);
-        }
-    }
-    return a / d;
+    constexpr unsigned long long SIGN = 0x8000000000000000ULL, FRAC = 0xfffffffffffffULL, ONE = 0x10000000000000ULL;
+    const double q0 = a * y;
+    const unsigned long long ua = (unsigned long long)__double_as_longlong(a),
+                             ud = (unsigned long long)__double_as_longlong(d),
+                             uq = (unsigned long long)__double_as_longlong(q0);
+    const int ea = (int)((ua >> 52) & 0x7ff), ed = (int)((ud >> 52) & 0x7ff), eq = (int)((uq >> 52) & 0x7ff);
+    const int t = ea - eq - ed + 1075;
+    const unsigned long long fq = uq & FRAC;
+    const bool az = (ua << 1) == 0 && ((unsigned long long)__double_as_longlong(y) << 1) != 0;
+    const bool fast = (unsigned)(ea - 1) < 2046u && (unsigned)(ed - 1) < 2046u && (unsigned)(eq - 1) < 2046u &&
+                      (t == 52 || t == 53) && fq - 1 < FRAC - 4;  // 1 <= fq <= 2^52 - 5
+    const unsigned long long ma = (ua & FRAC) | ONE, md = (ud & FRAC) | ONE, mq = fq | ONE;
+    const long long R = (long long)((ma << (t & 63)) - mq * md);
+    const unsigned long long v = (unsigned long long)(R < 0 ? -R : R) << 1, m3 = md * 3, odd = mq & 1;
+    const unsigned long long k = (unsigned long long)(v > md || (v == md && odd)) +
+                                 (unsigned long long)(v > m3 || (v == m3 && !odd));
+    const unsigned long long mag = (uq & ~SIGN) + (R < 0 ? 0ULL - k : k);
+    double r = __longlong_as_double((long long)((uq & SIGN) | mag));
+    if (az) r = q0;
+    else if (!fast) r = div_fp64_pipe(a, d);
+    return r;
 }
+
+// ------------------------------------------------------------------ addition on the integer pipe
+// a + b, IEEE binary64 round to nearest even, bit for bit the FP64 pipe's sum.  On this GPU the
+// FP64 pipe issues a warp instruction about every 76 cycles of a sub-partition while the integer
+// ALU issues one every two: a chain of products and sums (x = x + c q) that keeps the multiply on
+// the FP64 pipe and moves the sum here runs well above the rate of both on the FP64 pipe.
+//
+// The integer path takes the operand of the larger exponent, x, normal and below the top binade,
+// and y a zero (of either sign), or a normal or subnormal number of x's sign -- the sums of
+// like-signed terms -- and two zeros.  y's significand (53 bits; a subnormal's without the
+// implicit bit, at the exponent of the smallest normal) is shifted right by the exponents'
+// difference d (63 at most: further down it only sets the sticky bit, as at 63) across three
+// 32-bit words, the third a guard word, with the bits that fall below it kept as a sticky bit;
+// the two significands are added, the sum put back in [2^52, 2^53) by at most one right shift
+// (its bit kept as sticky), and rounded to nearest even on the guard word: up when it exceeds
+// half, or is half and the last kept bit is odd.  A carry out of the rounding lands in the
+// exponent field, which is the representation of the rounded value (the largest finite x
+// rounding up gives infinity, as the FP64 pipe's overflow does).  A zero y adds nothing: the sum
+// is x.  Two zeros sum to -0 when both are -0, else +0.  Everything else -- signs that differ on
+// non-zero operands, a subnormal, infinite or NaN x, x in the top binade -- is the FP64 pipe's,
+// through a call: a fallback inlined beside the integer path is issued on every call, its lanes
+// predicated off, and a predicated-off FP64 instruction holds the FP64 pipe as long as a live one.
+static __device__ __noinline__ double add_fp64_pipe(double a, double b) { return a + b; }
+__device__ __forceinline__ double add_ip(double a, double b) {
+    const uint32_t ha = (uint32_t)__double2hiint(a), la = (uint32_t)__double2loint(a);
+    const uint32_t hb = (uint32_t)__double2hiint(b), lb = (uint32_t)__double2loint(b);
+    const uint32_t fa = ha & 0x7ff00000u, fb = hb & 0x7ff00000u;  // the exponent fields
+    const bool sw = fa < fb;
+    const uint32_t hx = sw ? hb : ha, lx = sw ? lb : la, hy = sw ? ha : hb, ly = sw ? la : lb;
+    const uint32_t fx = sw ? fb : fa, fy = sw ? fa : fb;
+    const bool yz = ((hy << 1) | ly) == 0, bz = yz && ((hx << 1) | lx) == 0;
+    const bool fast = (fx - 0x00100000u < 0x7fd00000u && (yz || ((ha ^ hb) >> 31) == 0)) || bz;
+    const uint32_t d = min((fx - max(fy, 0x00100000u)) >> 20, 63u), s = d & 31;
+    const uint32_t mxh = (hx & 0xfffffu) | 0x100000u, myh = (hy & 0xfffffu) | (fy != 0 ? 0x100000u : 0u);
+    // y >> d over (yh, yl, g): the words (myh, ly, 0), or (0, myh, ly) for d >= 32, shifted by d mod 32
+    const bool big = d >= 32;
+    const uint32_t w2 = big ? 0u : myh, w1 = big ? myh : ly, w0 = big ? ly : 0u;
+    const uint32_t yh = w2 >> s, yl = __funnelshift_r(w1, w2, s);
+    uint32_t g = __funnelshift_r(w0, w1, s) | (uint32_t)(__funnelshift_r(0u, w0, s) != 0u);
+    const uint64_t S = (((uint64_t)mxh << 32) | lx) + (((uint64_t)yh << 32) | yl);
+    uint32_t sh = (uint32_t)(S >> 32), sl = (uint32_t)S;
+    const uint32_t c = sh >> 21;  // 1 where the sum reached 2^53
+    g = __funnelshift_r(g, sl, c) | (g & c);
+    sl = __funnelshift_r(sl, sh, c);
+    sh >>= c;
+    const uint32_t up = (g | (sl & 1u)) > 0x80000000u;
+    const uint64_t M = (((uint64_t)sh << 32) | sl) + up;
+    const uint32_t hr = (hx & 0xfff00000u) + (c << 20) - 0x100000u + (uint32_t)(M >> 32);
+    double r = __hiloint2double((int)(bz ? ha & hb : hr), bz ? 0 : (int)(uint32_t)M);
+    if (!fast) r = add_fp64_pipe(a, b);
+    return r;
+}
+// a - b as a + (-b): the same bits (IEEE subtraction is addition of the negated operand)
+__device__ __forceinline__ double sub_ip(double a, double b) {
+    return add_ip(a, __longlong_as_double(__double_as_longlong(b) ^ (long long)0x8000000000000000ULL));
+}
+// +0.0 + p and +0.0 - p, the first term of a sum or a difference that starts from +0: p (or -p)
+// itself, +0 where p is a zero of either sign, the FP64 pipe's own result for a NaN
+__device__ __forceinline__ double zero_plus(double p) {
+    const unsigned long long b = (unsigned long long)__double_as_longlong(p);
+    if ((b << 1) == 0) return 0.0;
+    if ((b << 1) > 0xffe0000000000000ULL) return add_fp64_pipe(0.0, p);
+    return p;
+}
+__device__ __forceinline__ double zero_minus(double p) { return zero_plus(gb_neg(p)); }
 
 // x >= 0.0 and x < 0.0 on the integer pipe (an FP64 compare issues on the FP64 pipe): >= holds
 // from +0 to +inf and at -0; < from the smallest negative to -inf; a NaN fails both
