@@ -63,7 +63,7 @@ __device__ int row_search(double *m_s, double *mx_s, double *a_s, int n, bool he
                 double f = a_s[k];
                 int up = ge_zero(f) ? (k == 0 ? n - 1 : k - 1) : (k == n ? 0 : k);
                 if (want_amax) {
-                    double c = gb_abs(f / mx_s[up]);
+                    double c = gb_abs(div_ip(f, mx_s[up]));
                     lok = lok && (c < 1.0);
                     cmax = (c > cmax) ? c : cmax;
                 } else {
@@ -170,7 +170,7 @@ __global__ void __launch_bounds__(WARPS * 32) k_advect_x(XArgs A) {
             const int ntc = min(tc, nt - t0);
             for (int k = lane; k < n; k += GB_WARP) {
                 m_s[k] = mx_s[k];
-                minv_s[k] = 1.0 / mx_s[k];
+                minv_s[k] = div_ip(1.0, mx_s[k]);
                 for (int w = 0; w < 4; ++w)
                     for (int t = 0; t < ntc; ++t) {
                         double v = AT4(A.q[w], (int64_t)k * c, j, l, t0 + t);
@@ -199,7 +199,7 @@ __global__ void __launch_bounds__(WARPS * 32) k_advect_x(XArgs A) {
                     const double mo = m_s[i], alo = a_s[i], ahi = a_s[i + 1];
                     const double mn = (mo + alo) - ahi;
                     // 1 / mn, the next sub-step's Courant factor, also gives the slope's quotient
-                    const double inv = 1.0 / mn, y = recip_mark(mn, inv);
+                    const double inv = div_ip(1.0, mn), y = recip_mark(mn, inv);
                     for (int t = 0; t < ntc; ++t) {
                         double *f = F(0, t), *pf = F(1, t), *fy = F(2, t), *fz = F(3, t);
                         double rmn = Q(0, t)[i] - (f[i + 1] - f[lo]);
@@ -238,7 +238,7 @@ __global__ void __launch_bounds__(WARPS * 32) k_advect_x(XArgs A) {
                 for (int i = lane; i < im; i += GB_WARP) {
                     const int k = i / c;
                     const double mun = (AT(A.m, i, j, l) + AT(A.am, i, j, l)) - AT(A.am, i + 1, j, l);
-                    const double sc = mun / m_s[k];
+                    const double sc = div_ip(mun, m_s[k]);
                     for (int w = 0; w < 4; ++w)
                         for (int t = 0; t < ntc; ++t) AT4(A.q[w], i, j, l, t0 + t) = sc * Q(w, t)[k];
                     if (A.halo && i == im - 1)  // q(0) = q(im) after red2uni
@@ -347,7 +347,7 @@ __global__ void __launch_bounds__(WARPS * 32) k_adj_x(XArgs A) {
                 for (int p = 0; p < c; ++p) {
                     const int64_t i = (int64_t)k * c + p;
                     const double mun = (AT(A.m, i, j, l) + AT(A.am, i, j, l)) - AT(A.am, i + 1, j, l);
-                    acc = acc + (mun / L.mw[k]) * AT4(A.q[w], i, j, l, 0);
+                    acc = acc + div_ip(mun, L.mw[k]) * AT4(A.q[w], i, j, l, 0);
                 }
                 L.q[w][k] = acc;
             }

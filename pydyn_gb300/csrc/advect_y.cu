@@ -351,7 +351,7 @@ __global__ void __launch_bounds__(YMAX_THREADS, 2) k_y_steps(YArgs A) {
                 if (live && k >= 1) {  // the interior faces 1 .. nc-1
                     const double bk = b_s[k];
                     const int up = ge_zero(bk) ? k - 1 : k;
-                    const double beta = bk / m_s[up];
+                    const double beta = div_ip(bk, m_s[up]);
                     for (int t = 0; t < ntc; ++t) {
                         double f, pf, fx, fz;
                         // the along slope is rym, the cross slopes rxm, rzm
@@ -378,7 +378,7 @@ __global__ void __launch_bounds__(YMAX_THREADS, 2) k_y_steps(YArgs A) {
                     const int j = k;
                     const double mo = m_s[j], blo = b_s[j], bhi = b_s[j + 1];
                     const double mn = (mo + blo) - bhi;
-                    const double inv = 1.0 / mn;  // production dynamv hoists the reciprocal
+                    const double inv = div_ip(1.0, mn);  // production dynamv hoists the reciprocal
                     const double fc = blo - bhi;
                     const double fm = 3.0 * (blo + bhi);
                     const double mx3 = 3.0 * mo;

@@ -250,7 +250,7 @@ __global__ void __launch_bounds__(MAX_THREADS, 2) k_z_steps(ZArgs A) {
                 if (live && k >= 1) {
                     const double ck = c_s[k];
                     const int up = ge_zero(ck) ? k - 1 : k;
-                    const double gamma = ck / m_s[up];
+                    const double gamma = div_ip(ck, m_s[up]);
                     for (int t = 0; t < ntc; ++t) {
                         double f, pf, fx, fy;
                         // the along slope is rzm, the cross slopes rxm, rym

@@ -52,8 +52,11 @@ __device__ __forceinline__ double &E4(const DV &v, int64_t a, int64_t b, int64_t
 
 // the rate constants of a cell's temperature (chem.py:137-140): OH, 2.45e-12 exp(-1775 / T), and
 // tropospheric Cl, (2.36e-12 (T / 298)^1.37) exp(-939 / T)
-__device__ __forceinline__ double krate_ohf(double T) { return 2.45e-12 * gbm_exp(-1775.0 / T); }
-__device__ __forceinline__ double krate_cl(double T) { return (2.36e-12 * gbm_pow(T / 298.0, 1.37)) * gbm_exp(-939.0 / T); }
+constexpr double R298 = 1.0 / 298.0;  // correctly rounded: the divisor's reciprocal for div_by_recip
+__device__ __forceinline__ double krate_ohf(double T) { return 2.45e-12 * gbm_exp(div_ip(-1775.0, T)); }
+__device__ __forceinline__ double krate_cl(double T) {
+    return (2.36e-12 * gbm_pow(div_by_recip(T, 298.0, R298), 1.37)) * gbm_exp(div_ip(-939.0, T));
+}
 
 // the tropospheric Cl column's edges: pl_trop(i, j, 0 .. ntrop-1), then 0 (chem.py:135)
 struct TropEdges {
@@ -98,10 +101,10 @@ __device__ double rebin_layer(const Edges &ip, int first, int last, const double
     double overlap = 0.0;
     for (int k = first; k < last; ++k) {
         const double thickness = np_min(bot, ip[k]) - np_max(top, ip[k + 1]);
-        if (gb_gt0(thickness)) overlap = overlap + data[k * stride] * thickness;
+        if (gb_gt0(thickness)) overlap = add_ip(overlap, data[k * stride] * thickness);  // like-signed terms
     }
     const double width = bot - top;
-    return gb_gt0(width) ? overlap / width : overlap;
+    return gb_gt0(width) ? div_ip(overlap, width) : overlap;
 }
 
 // rebin_layer of three columns on the same edges at once (the zonal OH, Cl and O(1D) columns):
@@ -114,16 +117,17 @@ __device__ void rebin_layer3(const Edges &ip, int first, int last, const double 
     for (int k = first; k < last; ++k) {
         const double thickness = np_min(bot, ip[k]) - np_max(top, ip[k + 1]);
         if (gb_gt0(thickness)) {
-            o0 = o0 + d0[k * s0] * thickness;
-            o1 = o1 + d1[k * s1] * thickness;
-            o2 = o2 + d2[k * s2] * thickness;
+            o0 = add_ip(o0, d0[k * s0] * thickness);  // like-signed terms: the integer pipe's sums
+            o1 = add_ip(o1, d1[k * s1] * thickness);
+            o2 = add_ip(o2, d2[k * s2] * thickness);
         }
     }
     const double width = bot - top;
-    if (gb_gt0(width)) {
-        r0 = o0 / width;
-        r1 = o1 / width;
-        r2 = o2 / width;
+    if (gb_gt0(width)) {  // three quotients by one width: its reciprocal, then div_by_recip
+        const double y = recip_for(width);
+        r0 = div_by_recip(o0, width, y);
+        r1 = div_by_recip(o1, width, y);
+        r2 = div_by_recip(o2, width, y);
     } else {
         r0 = o0;
         r1 = o1;

@@ -192,7 +192,7 @@ __global__ void __launch_bounds__(GB_TUNE_MAX_CELL) k_convec_ratios(CArgs A) {
         if (act) {
             const double mu = amu[k - 1], eu = AT(A.entu, i, j, k - 1), du = AT(A.detu, i, j, k - 1);
             const double a = mu + eu - du;
-            z = gb_gt0(a) ? max0(1.0 - du / (mu + eu)) : 0.0;
+            z = gb_gt0(a) ? max0(1.0 - div_ip(du, mu + eu)) : 0.0;
         }
         zu[k] = z;
     }
@@ -202,7 +202,7 @@ __global__ void __launch_bounds__(GB_TUNE_MAX_CELL) k_convec_ratios(CArgs A) {
         if (act) {
             const double md = amd[k], ed = AT(A.entd, i, j, k - 1), dd = AT(A.detd, i, j, k - 1);
             const double a = md - ed + dd;
-            z = lt_zero(a) ? max0(1.0 + dd / (md - ed)) : 0.0;
+            z = lt_zero(a) ? max0(1.0 + div_ip(dd, md - ed)) : 0.0;
         }
         zd[k] = z;
     } else {
@@ -387,7 +387,7 @@ __global__ void __launch_bounds__(GB_TUNE_MAX_COLUMN) k_convec_tri(CArgs A) {
             const int r = r0 + u;
             if (r >= n) break;
             ok = ok && band_ok(sub[u]) && band_ok(dia[u]) && band_ok(sup[u]);
-            const double l = sub[u] / uprev;
+            const double l = div_ip(sub[u], uprev);
             const double v = dia[u] - l * sup[u];
             ud[r] = v;
             lb[r] = l;  // L(r, r-1): k_convec_apply builds L^-1 from it
@@ -503,7 +503,7 @@ __global__ void __launch_bounds__(GB_TUNE_MAX_LU_WARPS * 32) k_convec_lu(CArgs A
             const bool on = act && k < E;
             if (on) {
                 const double d = LU[(size_t)k * n + k];
-                for (int r = k + 1 + gl; r < E; r += G) LU[(size_t)r * n + k] = LU[(size_t)r * n + k] / d;
+                for (int r = k + 1 + gl; r < E; r += G) LU[(size_t)r * n + k] = div_ip(LU[(size_t)r * n + k], d);
             }
             // row k's non-zeros right of the diagonal inside the block, listed in order: the
             // columns step k updates
@@ -647,7 +647,7 @@ __global__ void __launch_bounds__(GB_TUNE_MAX_COLUMN) k_convec_tail(CArgs A) {
         for (int u = 0; u < B; ++u) {
             const int r = r0 + u;
             if (r >= n) break;
-            const double l = sub[u] / uprev;
+            const double l = div_ip(sub[u], uprev);
             const double v = dia[u] - l * sup[u];
             ud[r] = v;
             lb[r] = l;

@@ -128,10 +128,6 @@ __device__ __forceinline__ bool cfl_pass(double c, double mu) {
 // and any a, d or q0 outside that -- a zero d, subnormal, infinite or NaN operands, q0 at a
 // binade's edge or not normal -- take the division itself, on the FP64 pipe, through a call
 // (a predicated-off division beside the integer path would hold the FP64 pipe on every call).
-__device__ __forceinline__ double recip_for(double d) {
-    const int ed = (int)((__double_as_longlong(d) >> 52) & 0x7ff);
-    return (ed >= 23 && ed <= 2023) ? 1.0 / d : 0.0;
-}
 // recip_for(d) from an inv = 1.0 / d the caller makes anyway (an integer test, no division)
 __device__ __forceinline__ double recip_mark(double d, double inv) {
     const int ed = (int)((__double_as_longlong(d) >> 52) & 0x7ff);
@@ -160,6 +156,61 @@ __device__ __forceinline__ double div_by_recip(double a, double d, double y) {
     if (az) r = q0;
     else if (!fast) r = div_fp64_pipe(a, d);
     return r;
+}
+
+// a / d, correctly rounded, with three FP64 instructions where the FP64 pipe's own division
+// issues eight.  The seed is an FP32 reciprocal: d truncated to FP32 (relative error below
+// 2^-23) and rcp.approx.f32 (within one FP32 ulp, 2^-23), so y0 = 1 / d to within 2^-22.
+// q0 = RN(a y0) then carries a relative error below 2^-21.9, and one correction
+// q1 = RN(q0 + RN(a - q0 d) y0) squares it: below 2^-43.7, within 2^9.3 ulp of a / d.  Where
+// q1's significand is 2048 ulp or more inside its binade, a / d lies in that binade and the
+// correctly rounded quotient is q1 + k ulp, k = round(R / md), with R = ma 2^t - mq md the exact
+// residual in units of ulp(q1) d / md (as in div_by_recip: t = Ea - Eq - Ed, 52 or 53, and
+// |R| < 2^62.3, so the low 64 bits are all of it).  k comes from the top bits of R and md in FP32
+// (within 0.16 of R / md), then is made exact by one test of the integer remainder R - k md
+// against md / 2 (a tie would go to the even neighbour; a quotient of two doubles is never
+// one).  A zero a gives a y0, signed as a / d.  Outside d in [2^-125, 2^125] (where the FP32
+// seed and its reciprocal are normal), or with a, q1 not normal, or q1 near a binade's edge, the
+// division is the FP64 pipe's own, through a call.
+static __device__ __noinline__ double div_fp64_call(double a, double d) { return a / d; }
+__device__ __forceinline__ double div_ip(double a, double d) {
+    constexpr unsigned long long SIGN = 0x8000000000000000ULL, FRAC = 0xfffffffffffffULL, ONE = 0x10000000000000ULL;
+    const unsigned long long ua = (unsigned long long)__double_as_longlong(a),
+                             ud = (unsigned long long)__double_as_longlong(d);
+    const int ea = (int)((ua >> 52) & 0x7ff), ed = (int)((ud >> 52) & 0x7ff);
+    const bool seed_ok = (unsigned)(ed - 898) <= 250u;  // the FP32 image of d and its reciprocal normal
+    const uint32_t fd = ((uint32_t)(ed - 896) << 23) | ((uint32_t)(ud >> 29) & 0x7fffffu);
+    float rf;
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(rf) : "f"(__uint_as_float(fd)));
+    const uint32_t ur = __float_as_uint(rf);
+    const double y0 = __longlong_as_double((long long)((ud & SIGN) | ((unsigned long long)(((ur >> 23) & 0xffu) + 896u) << 52) |
+                                                       ((unsigned long long)(ur & 0x7fffffu) << 29)));
+    const double q0 = a * y0;
+    const double q1 = __fma_rn(__fma_rn(-q0, d, a), y0, q0);
+    const unsigned long long uq = (unsigned long long)__double_as_longlong(q1);
+    const int eq = (int)((uq >> 52) & 0x7ff);
+    const int t = ea - eq - ed + 1075;
+    const unsigned long long fq = uq & FRAC;
+    const bool fast = seed_ok && (unsigned)(ea - 1) < 2046u && (unsigned)(eq - 1) < 2046u && (t == 52 || t == 53) &&
+                      fq - 2048 < FRAC - 4095;  // 2048 <= fq <= 2^52 - 2049
+    const unsigned long long ma = (ua & FRAC) | ONE, md = (ud & FRAC) | ONE, mq = fq | ONE;
+    const long long R = (long long)((ma << (t & 63)) - mq * md), smd = (long long)md;
+    long long k = __float2int_rn(__fdividef((float)(int)(R >> 40), (float)(int)(md >> 40)));
+    const long long r2 = (R - k * smd) * 2;
+    k += (long long)(r2 > smd) - (long long)(r2 < -smd);
+    const long long t2 = (R - k * smd) * 2;
+    if ((t2 == smd || t2 == -smd) && ((mq + (unsigned long long)k) & 1) != 0) k += t2 > 0 ? 1 : -1;
+    double r = __longlong_as_double((long long)((uq & SIGN) | ((uq & ~SIGN) + (unsigned long long)k)));
+    if ((ua << 1) == 0 && seed_ok) r = q0;
+    else if (!fast) r = div_fp64_call(a, d);
+    return r;
+}
+
+// RN(1 / d) for div_by_recip where d is in [2^-1000, 2^1000]; else 0, the mark that makes
+// div_by_recip divide
+__device__ __forceinline__ double recip_for(double d) {
+    const int ed = (int)((__double_as_longlong(d) >> 52) & 0x7ff);
+    return (ed >= 23 && ed <= 2023) ? div_ip(1.0, d) : 0.0;
 }
 
 // ------------------------------------------------------------------ addition on the integer pipe
@@ -292,7 +343,7 @@ __device__ __forceinline__ double along_slope(double s, double pf_lo, double pf_
                                               double hi, double rm_new, double f_lo, double f_hi,
                                               double m_old, double m_new) {
     double num = ((pf_lo - pf_hi) - (lo - hi) * s) + 3.0 * ((lo + hi) * rm_new - (f_lo + f_hi) * m_old);
-    return s + num / m_new;
+    return s + div_ip(num, m_new);
 }
 // the same with the division num / m_new made from y_new = recip_for(m_new) (div_by_recip: the
 // division's bits), where the caller has the reciprocal of the new mass for other uses

@@ -21,6 +21,15 @@
 #define GBM_HD static inline
 #endif
 
+/* The quotients of the main paths.  On the device, div_ip of the kernels' common header (which a
+ * device translation unit includes before this file): the correctly rounded quotient, the same
+ * bits as a / b, with three FP64 instructions where the FP64 pipe's division issues eight. */
+#if defined(__CUDA_ARCH__)
+#define GBM_DIV(a, b) div_ip((a), (b))
+#else
+#define GBM_DIV(a, b) ((a) / (b))
+#endif
+
 GBM_HD uint64_t gbm_bits(double x) {
 #if defined(__CUDA_ARCH__)
     return (uint64_t)__double_as_longlong(x);
@@ -101,8 +110,8 @@ GBM_HD double gbm_exp(double x) {
     }
     t = x * x;
     c = x - t * (P1 + t * (P2 + t * (P3 + t * (P4 + t * P5))));
-    if (k == 0) return one - ((x * c) / (c - 2.0) - x);
-    y = one - ((lo - (x * c) / (2.0 - c)) - hi);
+    if (k == 0) return one - (GBM_DIV(x * c, c - 2.0) - x);
+    y = one - ((lo - GBM_DIV(x * c, 2.0 - c)) - hi);
     if (k >= -1021) return gbm_set_hi(y, gbm_hi(y) + (k << 20));
     return gbm_set_hi(y, gbm_hi(y) + ((k + 1000) << 20)) * twom1000;
 }
@@ -142,7 +151,7 @@ GBM_HD double gbm_log(double x) {
         dk = (double)k;
         return dk * ln2_hi - ((R - dk * ln2_lo) - f);
     }
-    s = f / (2.0 + f);
+    s = GBM_DIV(f, 2.0 + f);
     dk = (double)k;
     z = s * s;
     i = hx - 0x6147a;
@@ -267,7 +276,7 @@ GBM_HD double gbm_pow(double x, double y) {
         }
         ax = gbm_set_hi(ax, ix);
         u = ax - bp[k];
-        v = one / (ax + bp[k]);
+        v = GBM_DIV(one, ax + bp[k]);
         ss = u * v;
         s_h = gbm_set_lo(ss, 0);
         t_h = gbm_make(((ix >> 1) | 0x20000000) + 0x00080000 + (k << 18), 0);
@@ -322,7 +331,7 @@ GBM_HD double gbm_pow(double x, double y) {
     w = v - (z - u);
     t = z * z;
     t1 = z - t * (P1 + t * (P2 + t * (P3 + t * (P4 + t * P5))));
-    r = (z * t1) / (t1 - two) - (w + z * w);
+    r = GBM_DIV(z * t1, t1 - two) - (w + z * w);
     z = one - (r - z);
     j = gbm_hi(z);
     j += (n << 20);

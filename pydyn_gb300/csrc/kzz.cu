@@ -77,7 +77,7 @@ __global__ void __launch_bounds__(GB_TUNE_MAX_CELL) k_kzz_levels(KArgs A) {
     const double m = div_by_recip((ph0 - ph1) * A.dxyp[j], GRAV, RGRAV);
     const double pf = (ph0 + ph1) * 0.5;
     const double tl = S3(A.t, i, j, l), ql = S3(A.q, i, j, l);
-    const double wthm = tl * gbm_pow(APZERO / pf, ZKAPPA);
+    const double wthm = tl * gbm_pow(div_ip(APZERO, pf), ZKAPPA);
     A.wthm[t] = wthm;
     A.zthvk[t] = wthm * (1.0 + ZCRDQ * ql);
     A.lpf[t] = gbm_log(pf);
@@ -86,11 +86,11 @@ __global__ void __launch_bounds__(GB_TUNE_MAX_CELL) k_kzz_levels(KArgs A) {
         const double s = S2(A.sp, i, j);
         const double tv = tl * (1.0 + 0.608 * ql);
         const double pdown = A.at[l] + A.bt[l] * s, pup = A.at[l + 1] + A.bt[l + 1] * s;
-        A.dzg[t] = div_by_recip(tv * 287.05 * gbm_log(pdown / pup), GRAV, RGRAV);
+        A.dzg[t] = div_by_recip(tv * 287.05 * gbm_log(div_ip(pdown, pup)), GRAV, RGRAV);
     }
     const double dyy = AE * A.dy * (PI_ / 180.0);
-    A.uw[t] = A.dxx[j] * (S3(A.pu, i + 1, j, l) + S3(A.pu, i, j, l)) * 0.5 / m;
-    A.vw[t] = dyy * (S3(A.pv, i, j + 1, l) + S3(A.pv, i, j, l)) * 0.5 / m;
+    A.uw[t] = div_ip(A.dxx[j] * (S3(A.pu, i + 1, j, l) + S3(A.pu, i, j, l)) * 0.5, m);
+    A.vw[t] = div_ip(dyy * (S3(A.pv, i, j + 1, l) + S3(A.pv, i, j, l)) * 0.5, m);
 }
 
 // The bulk-Richardson sweep up a column (diffusion.py:123-152), split where its terms allow:
@@ -105,7 +105,7 @@ __device__ double sweep_carry(double pblh, const double *whm, const double *raw,
     for (int k = k0; k < lm; ++k) {
         const double zrino = jwork * raw[k];
         const double jq = jqif(RICR, zrino);
-        const double frac = (RICR - wrino) / (zrino - wrino);
+        const double frac = div_ip(RICR - wrino, zrino - wrino);
         const double at_ricr = (k == 0) ? frac * whm[k] : whm[k - 1] + frac * (whm[k] - whm[k - 1]);
         pblh = jq * pblh + (1.0 - jq) * at_ricr;
         jwork = jq * jwork;
@@ -190,7 +190,7 @@ __global__ void __launch_bounds__(GB_TUNE_MAX_CELL) k_kzz_heights(KArgs A) {
     const double du = uw[k] - uw[0], dv = vw[k] - vw[0];
     const double vvk = np_max(du * du + dv * dv + ZACB * ustr * ustr, TINY);
     const double dz = whk - wh0;
-    double zrino = GRAV * (A.zthvk[t] - wtseff) * dz / (wtseff * vvk);
+    double zrino = div_ip(GRAV * (A.zthvk[t] - wtseff) * dz, wtseff * vvk);
     zrino = zrino + copysign(1.0e-10, zrino);
     A.sw_vvk[t] = vvk;
     A.sw_dz[t] = dz;
@@ -223,7 +223,7 @@ __global__ void __launch_bounds__(GB_TUNE_MAX_CELL) k_kzz_raw2(KArgs A) {
     if (t % lm == 0) return;
     const double *cv = A.col + c * NCOLVAL;
     const double wtseff = cv[10], thvparc = cv[11];
-    double zrino = GRAV * (A.zthvk[t] - thvparc) * A.sw_dz[t] / (A.sw_vvk[t] * wtseff);
+    double zrino = div_ip(GRAV * (A.zthvk[t] - thvparc) * A.sw_dz[t], A.sw_vvk[t] * wtseff);
     zrino = zrino + copysign(1.0e-10, zrino);
     A.sw_raw[t] = zrino;
 }
@@ -282,21 +282,21 @@ __global__ void __launch_bounds__(GB_TUNE_MAX_CELL) k_kzz_interfaces(KArgs A) {
     const double z = gph[k] - z0;
     double jq = jqif(1000.0, z);
     const double zlambdac = jq * 300.0 + (1.0 - jq) * (30.0 + 270.0 * gbm_exp(1.0 - div_by_recip(z, 1000.0, 1.0e-3)));
-    const double rkz = 1.0 / (VKARMAN * z);
-    double cml2 = 1.0 / (1.0 / zlambdac + rkz);
+    const double rkz = div_ip(1.0, VKARMAN * z);
+    double cml2 = div_ip(1.0, div_ip(1.0, zlambdac) + rkz);
     cml2 = cml2 * cml2;
     const double du = A.uw[ck] - A.uw[ck - 1], dv = A.vw[ck] - A.vw[ck - 1];
     double zdup2 = np_max(du * du + dv * dv, 1.0e-10);
     const double whk = A.whm[ck], whk1 = A.whm[ck - 1];
     const double zdz = whk - whk1;
-    zdup2 = zdup2 / (zdz * zdz);
-    const double arg = (A.lphlb[ck] - A.lpf[ck - 1]) / (A.lpf[ck] - A.lpf[ck - 1]);
+    zdup2 = div_ip(zdup2, zdz * zdz);
+    const double arg = div_ip(A.lphlb[ck] - A.lpf[ck - 1], A.lpf[ck] - A.lpf[ck - 1]);
     const double dthv = A.zthvk[ck] - A.zthvk[ck - 1];
     const double zthva = A.zthvk[ck - 1] + arg * dthv;
-    const double zsstab = GRAV / zthva * dthv / zdz;
-    const double zrinub = zsstab / zdup2;
+    const double zsstab = div_ip(div_ip(GRAV, zthva) * dthv, zdz);
+    const double zrinub = div_ip(zsstab, zdup2);
     const double zfunst = sqrt(np_max(1.0 - 18.0 * zrinub, 0.0));
-    double zfstabh = 1.0 / (1.0 + 10.0 * zrinub * (1.0 + 8.0 * zrinub));
+    double zfstabh = div_ip(1.0, 1.0 + 10.0 * zrinub * (1.0 + 8.0 * zrinub));
     const double zkvn = cml2 * sqrt(zdup2);
     jq = jqif(zrinub, 0.0);
     const double wkvf = jq * np_max(CKMIN, zkvn * zfstabh) + (1.0 - jq) * np_max(CKMIN, zkvn * zfunst);
@@ -310,10 +310,10 @@ __global__ void __launch_bounds__(GB_TUNE_MAX_CELL) k_kzz_interfaces(KArgs A) {
     const double jq6 = jq1 * jqif(P, whk1) * jqif(whk, P);
     jq1 = jqif(SFFRAC, zh);
     const double jq4 = jq3 * jq1, jq5 = jq3 * (1.0 - jq1);
-    cml2 = 1.0 / (rkz + 1.0 / 450.0);
+    cml2 = div_ip(1.0, rkz + 1.0 / 450.0);
     cml2 = cml2 * cml2;
     const double jqq = jqif(zrinub, 0.0);
-    zfstabh = jqq / (1.0 + 10.0 * zrinub * sqrt(1.0 + jqq * zrinub)) + (1.0 - jqq);
+    zfstabh = div_ip(jqq, 1.0 + 10.0 * zrinub * sqrt(1.0 + jqq * zrinub)) + (1.0 - jqq);
     double zpblk = cml2 * sqrt(zdup2) * zfstabh;
     const double zkvh = jq2 * np_max(zpblk, KVHMIN) + (1.0 - jq2) * wkvf;
     double zslask = 1.0 - BETAH * zl;
@@ -336,8 +336,8 @@ __global__ void __launch_bounds__(GB_TUNE_MAX_CELL) k_kzz_interfaces(KArgs A) {
     // else none (div_by_recip divides)
     const double ypr = jq3_on ? cv[14] : (__double_as_longlong(pr) == 0x3ff0000000000000LL ? 1.0 : 0.0);
     const double kv = jq3 * np_max(div_by_recip(zpblk, pr, ypr), KVHMIN) + (1.0 - jq3) * zkvh;
-    const double thvgrad = dthv / zdz;
-    const double kvhentr = 0.2 * HV / thvgrad;
+    const double thvgrad = div_ip(dthv, zdz);
+    const double kvhentr = div_ip(0.2 * HV, thvgrad);
     const double kvh = jq6 * kvhentr + (1.0 - jq6) * kv;
 
     // dkg across interface l + 1 = k for l < lmax - 1, zero at lmax - 1 (diffusion.py:256-263)
@@ -349,7 +349,7 @@ __global__ void __launch_bounds__(GB_TUNE_MAX_CELL) k_kzz_interfaces(KArgs A) {
         const double m0 = div_by_recip((p0 - p1) * A.dxyp[j], GRAV, RGRAV),
                      m1 = div_by_recip((p1 - p2) * A.dxyp[j], GRAV, RGRAV);
         const double dz = gph[l + 2] - gph[l];
-        S3(A.dkg, i, j, l) = np_max(0.0, kvh) * 2.0 * (m1 + m0) / (dz * dz);
+        S3(A.dkg, i, j, l) = div_ip(np_max(0.0, kvh) * 2.0 * (m1 + m0), dz * dz);
     }
     if (k == 1) S3(A.dkg, i, j, A.lmax - 1) = 0.0;
 }

@@ -82,14 +82,14 @@ __global__ void k_m2phlb(DV m, DV sp, DV phlb, const double *dxyp, const double 
     const int i = (int)(k / jm), j = (int)(k % jm);
     double acc = AT(m, i, j, 0);
     for (int l = 1; l < lm; ++l) acc = acc + AT(m, i, j, l);
-    double p = (acc * GRAV) / dxyp[j];
+    double p = div_ip(acc * GRAV, dxyp[j]);
     if (xr > 0) {
         // the child's ring: rescaled to the parent cell's area (Fortran i, j from 1)
         const int fi = i + 1, fj = j + 1;
         const bool interior = (xr < fi && fi < im - xr + 1) && (yr < fj && fj < jm - yr + 1);
         if (!interior) {
             const int jpar = jbeg + (fj - 1) / yr;  // 1-based parent row
-            p = (((p * dxyp[j]) * (double)xr) * (double)yr) / dxyp_parent[jpar - 1];
+            p = div_ip(((p * dxyp[j]) * (double)xr) * (double)yr, dxyp_parent[jpar - 1]);
         }
     }
     sp.p[i * sp.s0 + j * sp.s1] = p;
