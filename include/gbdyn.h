@@ -377,7 +377,9 @@ int gb_m2phlb(gb_ctx *ctx, const gb_view *m, const gb_view *sp, const gb_view *p
 /* The device build of the library's exp / log / pow / cos / sin (op 0..4) on n values: the
  * check that it equals the host build (libgbmath.so) bit for bit; op 5 x / y through the
  * shared-reciprocal division the convection's back substitution uses, op 6 x / y by the
- * hardware division (the check that the two agree).  No reference counterpart. */
+ * hardware division (the check that the two agree), op 7 x / y by the integer-corrected
+ * division (div_ip), op 8 x + y and op 9 x - y by the integer-pipe sum (add_ip, sub_ip).  No
+ * reference counterpart. */
 int gb_math_eval(gb_ctx *ctx, int op, const double *x, const double *y, double *out, int64_t n);
 
 /* ------------------------------------------------------------------ the adjoint

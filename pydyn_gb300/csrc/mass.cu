@@ -139,6 +139,9 @@ __global__ void k_math_eval(int op, const double *x, const double *y, double *ou
         case 3: r = gbm_cos(x[k]); break;
         case 4: r = gbm_sin(x[k]); break;
         case 5: r = div_by_recip(x[k], y[k], recip_for(y[k])); break;
+        case 7: r = div_ip(x[k], y[k]); break;
+        case 8: r = add_ip(x[k], y[k]); break;
+        case 9: r = sub_ip(x[k], y[k]); break;
         default: r = x[k] / y[k]; break;
     }
     out[k] = r;

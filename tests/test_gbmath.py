@@ -124,3 +124,84 @@ def test_shared_reciprocal_division_is_the_division(dev):
     assert (bits(fast[ok]) == bits(want[ok])).all() and np.isnan(fast[~ok]).all()
     for x in (da, dd):
         x.free()
+
+
+def _eval(dev, op, a, b):
+    from pydyn_gb300 import _native as N
+    from pydyn_gb300.device import DevArray
+
+    da, db = DevArray.from_host(dev, a), DevArray.from_host(dev, b)
+    out = DevArray.zeros(dev, (0, len(a) - 1))
+    N.check(dev.L.gb_math_eval(dev.h, op, da.ptr, db.ptr, out.ptr, len(a)), "gb_math_eval")
+    got = out.host()
+    for x in (da, db, out):
+        x.free()
+    return got
+
+
+@pytest.mark.gpu
+def test_integer_corrected_division_is_the_division(dev):
+    """div_ip (an FP32 reciprocal seed, one FMA correction, the exact integer residual) equals the
+    hardware division bit for bit, NaNs included, over the whole range and at the edges of its
+    fast path: divisors at the ends of [2^-125, 2^125], significands at a binade's edges, exact
+    quotients."""
+    rng = np.random.default_rng(7)
+    a, d = _division_cases(rng)
+    n = 100_000
+    sig = lambda k: 1.0 + rng.integers(0, 2**52, k) / 2.0**52  # noqa: E731
+    edge = np.concatenate([1.0 + np.arange(0, 4096) / 2.0**52, 2.0 - np.arange(1, 4097) / 2.0**52])
+    d_edge = np.resize(edge, n) * np.exp2(rng.integers(-130, 130, n).astype(float))
+    a_edge = sig(n) * np.exp2(rng.integers(-60, 60, n).astype(float)) * rng.choice([-1.0, 1.0], n)
+    d_exact = sig(n)
+    a_exact = d_exact * rng.integers(1, 2**20, n).astype(float)
+    a = np.concatenate([a, a_edge, a_exact])
+    d = np.concatenate([d, d_edge, d_exact])
+    got, hw = _eval(dev, 7, a, d), _eval(dev, 6, a, d)
+    assert (bits(got) == bits(hw)).all()
+    with np.errstate(all="ignore"):
+        want = a / d
+    ok = ~np.isnan(want)
+    assert (bits(got[ok]) == bits(want[ok])).all() and np.isnan(got[~ok]).all()
+
+
+def _sum_cases(rng):
+    """(a, b) pairs for a + b: like signs at every exponent gap from 0 to 70, zeros of both signs
+    beside normal and subnormal numbers, subnormals, all-ones significands (carries), short
+    significands (ties), opposite signs, and every kind of special value."""
+    n = 100_000
+    sig = lambda k: 1.0 + rng.integers(0, 2**52, k) / 2.0**52  # noqa: E731
+    e = rng.integers(-900, 900, n).astype(float)
+    s = rng.choice([-1.0, 1.0], n)
+    a1 = sig(n) * np.exp2(e) * s
+    b1 = sig(n) * np.exp2(e - rng.integers(0, 71, n)) * s
+    a2 = sig(n) * np.exp2(rng.integers(-1074, 1023, n).astype(float)) * rng.choice([-1.0, 1.0], n)
+    b2 = rng.choice([0.0, -0.0], n)
+    a3 = rng.integers(1, 2**52, n) * 5e-324 * rng.choice([-1.0, 1.0], n)
+    b3 = sig(n) * np.exp2(rng.integers(-1022, -1000, n).astype(float)) * np.sign(a3)
+    ones = 2.0 - 2.0**-52
+    a4 = ones * np.exp2(e) * s
+    b4 = (2.0 - rng.integers(1, 8, n) * 2.0**-52) * np.exp2(e - rng.integers(0, 8, n)) * s
+    short = lambda k: np.round(sig(k) * 2.0**rng.integers(0, 30, k)) / 2.0**rng.integers(0, 30, k)  # noqa: E731
+    a5 = short(n) * np.exp2(e) * s
+    b5 = short(n) * np.exp2(e - rng.integers(0, 60, n)) * s
+    a6 = sig(n) * np.exp2(e) * s
+    b6 = -sig(n) * np.exp2(e - rng.integers(0, 60, n)) * s
+    special = np.array([0.0, -0.0, 5e-324, -5e-324, 2.2250738585072014e-308, 1.7976931348623157e308,
+                        8.98846567431158e307, np.inf, -np.inf, np.nan, 1.0, -1.0, 2.0 - 2.0**-52])
+    sa, sb = np.meshgrid(special, special)
+    a = np.concatenate([a1, a2, a3, a4, a5, a6, sa.ravel()])
+    b = np.concatenate([b1, b2, b3, b4, b5, b6, sb.ravel()])
+    return np.concatenate([a, b]), np.concatenate([b, a])
+
+
+@pytest.mark.gpu
+def test_integer_pipe_sum_is_the_sum(dev):
+    """add_ip / sub_ip equal IEEE a + b / a - b bit for bit (the host's, round to nearest even),
+    a NaN where it is a NaN: the integer path (like signs, zeros) and the FP64 fallback alike."""
+    a, b = _sum_cases(np.random.default_rng(13))
+    with np.errstate(all="ignore"):
+        want_add, want_sub = a + b, a - b
+    for op, want in ((8, want_add), (9, want_sub)):
+        got = _eval(dev, op, a, b)
+        ok = ~np.isnan(want)
+        assert (bits(got[ok]) == bits(want[ok])).all() and np.isnan(got[~ok]).all(), op
