@@ -65,16 +65,17 @@ BYTES_PER_CELL = {"_dynamu_region1": 12, "_dynamv_region1": 12, "_dynamw_region1
                   "dynam0": 5}  # fmt: skip  (values of 8 bytes per cell and application at nt = 1)
 
 
-# Per call of a convection body, from one ncu capture of an eager interval of each workload on
-# the current kernels (its seven k_convec launches, averaged over the body's calls in the
-# interval -- fresh and reusing its inverses; the parent's per v, both segments): DRAM bytes
+# Per call of a body, from one ncu capture of an eager interval of each workload on the current
+# kernels -- a convection body's seven k_convec launches, averaged over its calls in the interval
+# (fresh and reusing its inverses; the parent's per v, both segments), and the step's Calc_Kzz of
+# every region with the rate constants (the k_kzz and k_chem_krates launches): DRAM bytes
 # (dram__bytes_read.sum + dram__bytes_write.sum), the roofline's traffic, and FP64 warp
 # instructions (smsp__inst_executed_pipe_fp64.sum), whose issue bounds the step
 # (profiles/interval_dram_fp64_glb3x2+nam1x1.md, profiles/interval_dram_fp64_a100-case.md)
-TRAFFIC_PER_CALL = {"glb3x2+nam1x1": {"convec_region@2": 130.0e6, "convec_region@1": 243.3e6},
-                    "a100-case": {"convec_region@2": 48.57e6, "convec_region@1": 179.1e6}}
-FP64_PER_CALL = {"glb3x2+nam1x1": {"convec_region@2": 4.134e6, "convec_region@1": 5.257e6},
-                 "a100-case": {"convec_region@2": 2.262e6, "convec_region@1": 6.229e6}}
+TRAFFIC_PER_CALL = {"glb3x2+nam1x1": {"convec_region@2": 130.4e6, "convec_region@1": 240.2e6, "calc_kzz": 131.8e6},
+                    "a100-case": {"convec_region@2": 48.78e6, "convec_region@1": 181.0e6}}
+FP64_PER_CALL = {"glb3x2+nam1x1": {"convec_region@2": 2.658e6, "convec_region@1": 3.360e6, "calc_kzz": 15.451e6},
+                 "a100-case": {"convec_region@2": 1.425e6, "convec_region@1": 3.905e6}}
 
 
 def workload_config(workload, n_gpus):
@@ -658,7 +659,9 @@ def main():
     name, (calls, total_ms, nlaunch) = max(bodies.items(), key=lambda kv: kv[1][1])
     cells = {r: fw.zoom.g(r).im * fw.zoom.g(r).jm * lm for r in fw.zoom.regions()}
     body, _, region = name.partition("@")
-    per_call_bytes = 8 * BYTES_PER_CELL.get(body, 0) * cells[int(region) if region else 1]
+    # a body named without a region (calc_kzz: the step's Calc_Kzz of every region) covers them all
+    ncell = cells[int(region)] if region else sum(cells.values())
+    per_call_bytes = 8 * BYTES_PER_CELL.get(body, 0) * ncell
     achieved = per_call_bytes / (total_ms / calls / 1e3) / 1e9 if per_call_bytes else None
     roof = {"bound": "hbm", "kernel": name, "achieved": achieved, "peak": hbm, "unit": "GB/s",
             "frac": achieved / hbm if achieved else None,
