@@ -135,30 +135,34 @@ __device__ void rebin_layer3(const Edges &ip, int first, int last, const double 
     }
 }
 
-// thread per latitude: the zonal columns' edges (strat_edges, chem.py:91-98: midpoints, a half
-// layer below the first, 0 above the last, x100) and the tropopause pressure (chem.py:101-104)
-__global__ void k_chem_rows(CArgs A) {
-    const int j = blockIdx.x * blockDim.x + threadIdx.x;
-    if (j >= A.jm) return;
-    const int ns = A.ns;
-    double *edges = A.edges + (int64_t)j * (ns + 1);
-    bool ok = true;
-    for (int k = 0; k <= ns; ++k) {
-        double e;
-        if (k == 0) {
-            const double p0 = E2(A.sp, j, 0), p1 = E2(A.sp, j, 1);
-            e = p0 + 0.5 * (p0 - p1);
-        } else if (k < ns) {
-            e = (E2(A.sp, j, k - 1) + E2(A.sp, j, k)) / 2.0;
-        } else {
-            e = 0.0;
-        }
-        edges[k] = e * 100.0;
-        if (k > 0) ok = ok && gb_lt(edges[k], edges[k - 1]);  // = (edges[k] - edges[k-1] < 0) for every input
+// thread per (latitude, edge): the zonal columns' edges (strat_edges, chem.py:91-98: midpoints, a
+// half layer below the first, 0 above the last, x100), each checked below the one before it (made
+// again here by the same statements), and, at edge 0, the tropopause pressure (chem.py:101-104)
+__device__ __forceinline__ double strat_edge(const CArgs &A, int j, int k) {
+    double e;
+    if (k == 0) {
+        const double p0 = E2(A.sp, j, 0), p1 = E2(A.sp, j, 1);
+        e = p0 + 0.5 * (p0 - p1);
+    } else if (k < A.ns) {
+        e = (E2(A.sp, j, k - 1) + E2(A.sp, j, k)) / 2.0;
+    } else {
+        e = 0.0;
     }
-    if (!ok) raise_status(A.ctl, GB_ELEVELS);
-    const double cl = gbm_cos(A.lat[j]);
-    A.trop[j] = 30000.0 - 21500.0 * (cl * cl);
+    return e * 100.0;
+}
+__global__ void k_chem_rows(CArgs A) {
+    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const int ns = A.ns;
+    if (t >= (int64_t)A.jm * (ns + 1)) return;
+    const int j = (int)(t / (ns + 1)), k = (int)(t % (ns + 1));
+    const double e = strat_edge(A, j, k);
+    A.edges[(int64_t)j * (ns + 1) + k] = e;
+    if (k > 0 && !gb_lt(e, strat_edge(A, j, k - 1)))  // = (edges[k] - edges[k-1] < 0) for every input
+        raise_status(A.ctl, GB_ELEVELS);
+    if (k == 0) {
+        const double cl = gbm_cos(A.lat[j]);
+        A.trop[j] = 30000.0 - 21500.0 * (cl * cl);
+    }
 }
 
 // The cache of gb_chemistry, per (column, level) (value-major, then level, then column: a warp's
@@ -337,7 +341,7 @@ int launch_chem(gb_ctx *ctx, CArgs &A) {
     if (!w) return GB_ECUDA;
     A.edges = w;
     A.trop = w + (size_t)A.jm * (A.ns + 1);
-    k_chem_rows<<<(unsigned)((A.jm + 127) / 128), 128, 0, ctx->stream>>>(A);
+    k_chem_rows<<<(unsigned)(((int64_t)A.jm * (A.ns + 1) + 127) / 128), 128, 0, ctx->stream>>>(A);
     if (int rc = gb_after_launch(ctx, "chem_rows")) return rc;
     // blocks of 32 columns x (tcell / 32) levels
     const int tcell = ctx->tune[GB_TUNE_CELL_THREADS], lv = tcell / 32;
