@@ -74,7 +74,7 @@ BYTES_PER_CELL = {"_dynamu_region1": 12, "_dynamv_region1": 12, "_dynamw_region1
 # (profiles/interval_dram_fp64_glb3x2+nam1x1.md, profiles/interval_dram_fp64_a100-case.md)
 TRAFFIC_PER_CALL = {"glb3x2+nam1x1": {"convec_region@2": 130.4e6, "convec_region@1": 240.2e6, "calc_kzz": 131.8e6},
                     "a100-case": {"convec_region@2": 48.78e6, "convec_region@1": 181.0e6}}
-FP64_PER_CALL = {"glb3x2+nam1x1": {"convec_region@2": 2.658e6, "convec_region@1": 3.360e6, "calc_kzz": 15.451e6},
+FP64_PER_CALL = {"glb3x2+nam1x1": {"convec_region@2": 2.658e6, "convec_region@1": 3.360e6, "calc_kzz": 15.145e6},
                  "a100-case": {"convec_region@2": 1.425e6, "convec_region@1": 3.905e6}}
 
 

@@ -378,8 +378,9 @@ int gb_m2phlb(gb_ctx *ctx, const gb_view *m, const gb_view *sp, const gb_view *p
  * check that it equals the host build (libgbmath.so) bit for bit; op 5 x / y through the
  * shared-reciprocal division the convection's back substitution uses, op 6 x / y by the
  * hardware division (the check that the two agree), op 7 x / y by the integer-corrected
- * division (div_ip), op 8 x + y and op 9 x - y by the integer-pipe sum (add_ip, sub_ip).  No
- * reference counterpart. */
+ * division (div_ip), op 8 x + y and op 9 x - y by the integer-pipe sum (add_ip, sub_ip), op 10
+ * sqrt(x) by the integer-corrected root (sqrt_ip), op 11 by the hardware's.  No reference
+ * counterpart. */
 int gb_math_eval(gb_ctx *ctx, int op, const double *x, const double *y, double *out, int64_t n);
 
 /* ------------------------------------------------------------------ the adjoint
@@ -410,8 +411,10 @@ int gb_adjoint_sources(gb_ctx *ctx, const gb_view *rm_b, const gb_view *rzm_b, c
                        const double *area, double scale, int level, const int32_t *cols, int ncol);
 
 /* Measured FP64 issue rate of this GPU, instructions per second over all SMs: kind 0 a multiply
- * and an add (what -fmad=false emits), 1 a fused multiply-add, 2 a correctly rounded division.
- * The compute ceiling of the float64 step; not capturable.  No reference counterpart. */
+ * and an add (what -fmad=false emits), 1 a fused multiply-add, 2 a correctly rounded division;
+ * kind 3 the multiply with the add on the integer pipe (add_ip; the pair counted as two, as in
+ * kind 0), kind 4 the integer-corrected division (div_ip), divisions per second.  The compute
+ * ceiling of the float64 step; not capturable.  No reference counterpart. */
 int gb_fp64_rate(gb_ctx *ctx, int kind, double *rate);
 
 #ifdef __cplusplus

@@ -147,8 +147,10 @@ __device__ __forceinline__ double div_by_recip(double a, double d, double y) {
     const bool fast = (unsigned)(ea - 1) < 2046u && (unsigned)(ed - 1) < 2046u && (unsigned)(eq - 1) < 2046u &&
                       (t == 52 || t == 53) && fq - 1 < FRAC - 4;  // 1 <= fq <= 2^52 - 5
     const unsigned long long ma = (ua & FRAC) | ONE, md = (ud & FRAC) | ONE, mq = fq | ONE;
-    const long long R = (long long)((ma << (t & 63)) - mq * md);
-    const unsigned long long v = (unsigned long long)(R < 0 ? -R : R) << 1, m3 = md * 3, odd = mq & 1;
+    // (unsigned arithmetic throughout: outside the fast path the values are unused, and wrap)
+    const unsigned long long Ru = (ma << (t & 63)) - mq * md;
+    const long long R = (long long)Ru;
+    const unsigned long long v = (R < 0 ? 0ULL - Ru : Ru) << 1, m3 = md * 3, odd = mq & 1;
     const unsigned long long k = (unsigned long long)(v > md || (v == md && odd)) +
                                  (unsigned long long)(v > m3 || (v == m3 && !odd));
     const unsigned long long mag = (uq & ~SIGN) + (R < 0 ? 0ULL - k : k);
@@ -194,15 +196,68 @@ __device__ __forceinline__ double div_ip(double a, double d) {
     const bool fast = seed_ok && (unsigned)(ea - 1) < 2046u && (unsigned)(eq - 1) < 2046u && (t == 52 || t == 53) &&
                       fq - 2048 < FRAC - 4095;  // 2048 <= fq <= 2^52 - 2049
     const unsigned long long ma = (ua & FRAC) | ONE, md = (ud & FRAC) | ONE, mq = fq | ONE;
-    const long long R = (long long)((ma << (t & 63)) - mq * md), smd = (long long)md;
-    long long k = __float2int_rn(__fdividef((float)(int)(R >> 40), (float)(int)(md >> 40)));
-    const long long r2 = (R - k * smd) * 2;
-    k += (long long)(r2 > smd) - (long long)(r2 < -smd);
-    const long long t2 = (R - k * smd) * 2;
-    if ((t2 == smd || t2 == -smd) && ((mq + (unsigned long long)k) & 1) != 0) k += t2 > 0 ? 1 : -1;
-    double r = __longlong_as_double((long long)((uq & SIGN) | ((uq & ~SIGN) + (unsigned long long)k)));
+    // (the remainders in unsigned arithmetic, read as signed: outside the fast path the values are
+    // unused, and wrap)
+    const unsigned long long Ru = (ma << (t & 63)) - mq * md;
+    const long long R = (long long)Ru, smd = (long long)md;
+    unsigned long long k = (unsigned long long)(long long)__float2int_rn(
+        __fdividef((float)(int)(R >> 40), (float)(int)(md >> 40)));
+    const long long r2 = (long long)((Ru - k * md) << 1);
+    k += (unsigned long long)((long long)(r2 > smd) - (long long)(r2 < -smd));
+    const long long t2 = (long long)((Ru - k * md) << 1);
+    if ((t2 == smd || t2 == -smd) && ((mq + k) & 1) != 0) k += t2 > 0 ? 1ULL : 0ULL - 1ULL;
+    double r = __longlong_as_double((long long)((uq & SIGN) | ((uq & ~SIGN) + k)));
     if ((ua << 1) == 0 && seed_ok) r = q0;
     else if (!fast) r = div_fp64_call(a, d);
+    return r;
+}
+
+// sqrt(x), correctly rounded, with two FP64 instructions where the FP64 pipe's own square root
+// issues eight.  x = 1.f 2^(2q + p): the seed is the correctly rounded FP32 root of 1.f 2^p
+// (significand truncated to FP32: s0 within 2^-23 of sqrt(x) once scaled by 2^q) and the FP32
+// reciprocal of that root (rcp.approx.f32, within one ulp) for h0 = 1 / (2 s0).  One Newton step
+// s1 = RN(s0 + RN(x - s0^2) h0) leaves a relative error below 2^-44.6, within 2^8.4 ulp.  Where
+// s1's significand is 1024 ulp or more inside its binade, the root lies in that binade; with
+// x 2^-2Es = X = mx 2^t (t = Ex - 2 Es, 52 or 53) and c = ms + k the candidate significand, c is
+// the correctly rounded root exactly when (c - 1/2)^2 < X < (c + 1/2)^2, i.e. -c < X - c^2 <= c
+// for the integer X - c^2 (a root of a double is never a midpoint).  X - ms^2 is below 2^62.4 in
+// magnitude: its low 64 bits are all of it; k starts from its top bits over 2 ms in FP32 and is
+// moved by one until the test holds.  A zero is its own root.  Negative, subnormal, infinite and
+// NaN x, and s1 near a binade's edge, take the FP64 pipe's square root through a call.
+static __device__ __noinline__ double sqrt_fp64_call(double x) { return sqrt(x); }
+__device__ __forceinline__ double sqrt_ip(double x) {
+    constexpr unsigned long long FRAC = 0xfffffffffffffULL, ONE = 0x10000000000000ULL;
+    const unsigned long long ux = (unsigned long long)__double_as_longlong(x);
+    const int ex = (int)(ux >> 52);  // the sign bit included: >= 2048 for a negative x
+    const int E = ex - 1023, p = E & 1, q = (E - p) / 2;
+    const uint32_t fx = ((uint32_t)(127 + p) << 23) | ((uint32_t)(ux >> 29) & 0x7fffffu);
+    float sf, rf;
+    asm("sqrt.rn.f32 %0, %1;" : "=f"(sf) : "f"(__uint_as_float(fx)));
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(rf) : "f"(sf));
+    const uint32_t us = __float_as_uint(sf), ur = __float_as_uint(rf);
+    const double s0 = __longlong_as_double((long long)(((unsigned long long)((int)((us >> 23) & 0xffu) + 896 + q) << 52) |
+                                                       ((unsigned long long)(us & 0x7fffffu) << 29)));
+    const double h0 = __longlong_as_double((long long)(((unsigned long long)((int)((ur >> 23) & 0xffu) + 895 - q) << 52) |
+                                                       ((unsigned long long)(ur & 0x7fffffu) << 29)));
+    const double s1 = __fma_rn(__fma_rn(-s0, s0, x), h0, s0);
+    const unsigned long long us1 = (unsigned long long)__double_as_longlong(s1);
+    const int es = (int)((us1 >> 52) & 0x7ff);
+    const int t = ex - 2 * es + 1075;
+    const unsigned long long fs = us1 & FRAC;
+    const bool fast = ex >= 1 && ex <= 2046 && (t == 52 || t == 53) && fs - 1024 < FRAC - 2047;  // 1024 <= fs <= 2^52 - 1025
+    const unsigned long long mx = (ux & FRAC) | ONE, ms = fs | ONE;
+    const unsigned long long Ru = (mx << (t & 63)) - ms * ms;  // X - ms^2 (unsigned: wraps off the fast path)
+    unsigned long long k = (unsigned long long)(long long)__float2int_rn(
+        __fdividef((float)(int)((long long)Ru >> 40), (float)(int)(ms >> 39)));
+#pragma unroll
+    for (int it = 0; it < 2; ++it) {
+        const unsigned long long c = ms + k;
+        const long long D = (long long)(Ru - 2 * ms * k - k * k);  // X - c^2
+        k += (unsigned long long)((long long)(D > (long long)c) - (long long)(D <= -(long long)c));
+    }
+    double r = __longlong_as_double((long long)(us1 + k));
+    if ((ux << 1) == 0) r = x;  // sqrt(+-0) = +-0
+    else if (!fast) r = sqrt_fp64_call(x);
     return r;
 }
 

@@ -138,10 +138,10 @@ __global__ void __launch_bounds__(GB_TUNE_MAX_COLUMN) k_kzz_surface(KArgs A) {
 
     const double xland = S2(A.surf[1], i, j) / 100.0;
     const double ew = S2(A.surf[8], i, j), ns = S2(A.surf[9], i, j);
-    const double tau = sqrt(ew * ew + ns * ns);
-    const double ustar_sea = np_max(0.001, sqrt(tau / RHO_AIR));
+    const double tau = sqrt_ip(ew * ew + ns * ns);
+    const double ustar_sea = np_max(0.001, sqrt_ip(div_ip(tau, RHO_AIR)));
     const double u10 = S2(A.surf[4], i, j), v10 = S2(A.surf[5], i, j);
-    const double wind10m = sqrt(u10 * u10 + v10 * v10);
+    const double wind10m = sqrt_ip(u10 * u10 + v10 * v10);
     const double sr_land = np_max(1e-2, S2(A.surf[3], i, j));
     const double sr_help = np_min(S2(A.surf[2], i, j), 0.03);
     double land = VKARMAN * wind10m / gbm_log(10.0 / sr_help) * gbm_log(75.0 / sr_help);
@@ -246,9 +246,9 @@ __global__ void __launch_bounds__(GB_TUNE_MAX_COLUMN) k_kzz_sweep2(KArgs A) {
     const double stab0 = 1.0 - SSFRAC * BETAH * pblh / (0.0 * wobkl - 1.0);
     const double stab1 = 1.0 - SSFRAC * BETAH * pblh / (1.0 * wobkl - 0.0);
     cv[6] = gbm_pow(stab0, ONET);
-    cv[7] = sqrt(stab0);
+    cv[7] = sqrt_ip(stab0);
     cv[8] = gbm_pow(stab1, ONET);
-    cv[9] = sqrt(stab1);
+    cv[9] = sqrt_ip(stab1);
     // the interface's pr = jq3 (t1 / t2 + CCON FAKN w* / (U t1)) + (1 - jq3) takes t1, t2 from one of
     // the two pairs above: both sums, each in the statement's own order
     const double CCON = SFFRAC * VKARMAN, zwstr = cv[5], U = cv[4];
@@ -295,9 +295,10 @@ __global__ void __launch_bounds__(GB_TUNE_MAX_CELL) k_kzz_interfaces(KArgs A) {
     const double zthva = A.zthvk[ck - 1] + arg * dthv;
     const double zsstab = div_ip(div_ip(GRAV, zthva) * dthv, zdz);
     const double zrinub = div_ip(zsstab, zdup2);
-    const double zfunst = sqrt(np_max(1.0 - 18.0 * zrinub, 0.0));
+    const double zfunst = sqrt_ip(np_max(1.0 - 18.0 * zrinub, 0.0));
     double zfstabh = div_ip(1.0, 1.0 + 10.0 * zrinub * (1.0 + 8.0 * zrinub));
-    const double zkvn = cml2 * sqrt(zdup2);
+    const double rdup = sqrt_ip(zdup2);
+    const double zkvn = cml2 * rdup;
     jq = jqif(zrinub, 0.0);
     const double wkvf = jq * np_max(CKMIN, zkvn * zfstabh) + (1.0 - jq) * np_max(CKMIN, zkvn * zfunst);
     jq = jqif(P, z);
@@ -313,8 +314,8 @@ __global__ void __launch_bounds__(GB_TUNE_MAX_CELL) k_kzz_interfaces(KArgs A) {
     cml2 = div_ip(1.0, rkz + 1.0 / 450.0);
     cml2 = cml2 * cml2;
     const double jqq = jqif(zrinub, 0.0);
-    zfstabh = div_ip(jqq, 1.0 + 10.0 * zrinub * sqrt(1.0 + jqq * zrinub)) + (1.0 - jqq);
-    double zpblk = cml2 * sqrt(zdup2) * zfstabh;
+    zfstabh = div_ip(jqq, 1.0 + 10.0 * zrinub * sqrt_ip(1.0 + jqq * zrinub)) + (1.0 - jqq);
+    double zpblk = cml2 * rdup * zfstabh;
     const double zkvh = jq2 * np_max(zpblk, KVHMIN) + (1.0 - jq2) * wkvf;
     double zslask = 1.0 - BETAH * zl;
     zslask = jq4 * zslask + (1.0 - jq4);

@@ -142,6 +142,8 @@ __global__ void k_math_eval(int op, const double *x, const double *y, double *ou
         case 7: r = div_ip(x[k], y[k]); break;
         case 8: r = add_ip(x[k], y[k]); break;
         case 9: r = sub_ip(x[k], y[k]); break;
+        case 10: r = sqrt_ip(x[k]); break;
+        case 11: r = sqrt(x[k]); break;
         default: r = x[k] / y[k]; break;
     }
     out[k] = r;

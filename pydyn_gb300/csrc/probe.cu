@@ -59,11 +59,42 @@ __global__ void k_probe_div(double *out, int iters, double a) {
     out[tid] = ((x[0] + x[1]) + x[2]) + x[3];
 }
 
+// 8 chains of a multiply on the FP64 pipe and an add on the integer pipe (add_ip): the pair
+// counted as two instructions, as kind 0 counts it
+__global__ void k_probe_muladd_ip(double *out, int iters, double a, double b) {
+    int tid = blockIdx.x * blockDim.x + threadIdx.x;
+    double x[8];
+#pragma unroll
+    for (int c = 0; c < 8; ++c) x[c] = tid * 1e-9 + c + 1.0;
+    for (int i = 0; i < iters; ++i) {
+#pragma unroll
+        for (int c = 0; c < 8; ++c) x[c] = add_ip(x[c] * a, b);
+    }
+    double s = 0.0;
+#pragma unroll
+    for (int c = 0; c < 8; ++c) s = s + x[c];
+    out[tid] = s;
+}
+
+// 4 chains of the integer-corrected division (div_ip)
+__global__ void k_probe_div_ip(double *out, int iters, double a) {
+    int tid = blockIdx.x * blockDim.x + threadIdx.x;
+    double x[4];
+#pragma unroll
+    for (int c = 0; c < 4; ++c) x[c] = 1.0 + tid * 1e-9 + c;
+    for (int i = 0; i < iters; ++i) {
+#pragma unroll
+        for (int c = 0; c < 4; ++c) x[c] = div_ip(a, x[c]);
+    }
+    out[tid] = ((x[0] + x[1]) + x[2]) + x[3];
+}
+
 }  // namespace
 
-// kind 0: DMUL + DADD, 1: DFMA, 2: DDIV.  *rate = instructions per second over the whole GPU.
+// kind 0: DMUL + DADD, 1: DFMA, 2: DDIV, 3: DMUL + add_ip (counted as two instructions, as kind 0),
+// 4: div_ip.  *rate = instructions (kinds 2 and 4: divisions) per second over the whole GPU.
 extern "C" int gb_fp64_rate(gb_ctx *ctx, int kind, double *rate) {
-    if (!ctx || !rate || kind < 0 || kind > 2) return GB_EARG;
+    if (!ctx || !rate || kind < 0 || kind > 4) return GB_EARG;
     if (ctx->capturing) {
         gb_set_error("fp64_rate: cannot be captured");
         return GB_EARG;
@@ -74,8 +105,8 @@ extern "C" int gb_fp64_rate(gb_ctx *ctx, int kind, double *rate) {
     const int64_t threads = (int64_t)blocks * PROBE_THREADS;
     double *out = gb_work(ctx, threads * sizeof(double));
     if (!out) return GB_ECUDA;
-    const int iters = kind == 2 ? 200 : 2000;
-    const double per_iter = kind == 0 ? 16.0 : kind == 1 ? 8.0 : 4.0;
+    const int iters = (kind == 2 || kind == 4) ? 200 : 2000;
+    const double per_iter = (kind == 0 || kind == 3) ? 16.0 : kind == 1 ? 8.0 : 4.0;
     cudaEvent_t e0, e1;
     GB_CHECK_CUDA(cudaEventCreate(&e0));
     GB_CHECK_CUDA(cudaEventCreate(&e1));
@@ -87,8 +118,12 @@ extern "C" int gb_fp64_rate(gb_ctx *ctx, int kind, double *rate) {
             k_probe_muladd<<<blocks, PROBE_THREADS, 0, ctx->stream>>>(out, iters, 0.999999, 1e-7);
         else if (kind == 1)
             k_probe_fma<<<blocks, PROBE_THREADS, 0, ctx->stream>>>(out, iters, 0.999999, 1e-7);
-        else
+        else if (kind == 2)
             k_probe_div<<<blocks, PROBE_THREADS, 0, ctx->stream>>>(out, iters, 1.000001);
+        else if (kind == 3)
+            k_probe_muladd_ip<<<blocks, PROBE_THREADS, 0, ctx->stream>>>(out, iters, 0.999999, 1e-7);
+        else
+            k_probe_div_ip<<<blocks, PROBE_THREADS, 0, ctx->stream>>>(out, iters, 1.000001);
         rc = gb_after_launch(ctx, "fp64_rate");
         cudaEventRecord(e1, ctx->stream);
         cudaError_t e = cudaEventSynchronize(e1);

@@ -152,9 +152,11 @@ class Device:
     # -------------------------------------------------------------- FP64 ceiling
     def fp64_rates(self):
         """Measured FP64 issue rates of this GPU in G instructions/s: multiply + add pairs,
-        fused multiply-adds, correctly rounded divisions."""
+        fused multiply-adds, correctly rounded divisions; and the same pair with the add on the
+        integer pipe (add_ip, counted as two instructions) and the integer-corrected division
+        (div_ip, divisions/s)."""
         out = {}
-        for kind, name in enumerate(("dmul_dadd", "dfma", "ddiv")):
+        for kind, name in enumerate(("dmul_dadd", "dfma", "ddiv", "dmul_add_ip", "div_ip")):
             r = ctypes.c_double()
             N.check(self.L.gb_fp64_rate(self.h, kind, ctypes.byref(r)), "gb_fp64_rate")
             out[name] = r.value / 1e9

@@ -205,3 +205,37 @@ def test_integer_pipe_sum_is_the_sum(dev):
         got = _eval(dev, op, a, b)
         ok = ~np.isnan(want)
         assert (bits(got[ok]) == bits(want[ok])).all() and np.isnan(got[~ok]).all(), op
+
+
+@pytest.mark.gpu
+def test_integer_corrected_root_is_the_root(dev):
+    """sqrt_ip (a correctly rounded FP32 seed, one Newton step, the exact integer residual) equals
+    the hardware square root and IEEE sqrt bit for bit: over the whole range, exact squares and
+    their neighbours, significands at a binade's edges, zeros, negatives, subnormals, specials."""
+    rng = np.random.default_rng(17)
+    n = 200_000
+    sig = lambda k: 1.0 + rng.integers(0, 2**52, k) / 2.0**52  # noqa: E731
+    x1 = sig(n) * np.exp2(rng.integers(-1022, 1024, n).astype(float))
+    s = sig(n) * np.exp2(rng.integers(-200, 200, n).astype(float))
+    sq = s * s
+    x2 = np.concatenate([sq, np.nextafter(sq, 0.0), np.nextafter(sq, np.inf)])
+    x3 = (rng.integers(1, 2**26, n).astype(float)) ** 2
+    edge = np.concatenate([1.0 + np.arange(0, 4096) / 2.0**52, 2.0 - np.arange(1, 4097) / 2.0**52])
+    x4 = np.resize(edge, n) * np.exp2(rng.integers(-300, 300, n).astype(float))
+    special = np.array([0.0, -0.0, 5e-324, 2.2250738585072014e-308, 1.7976931348623157e308, np.inf, -np.inf,
+                        np.nan, -1.0, 1.0, 4.0, 2.0, 0.25, -5e-324])
+    x = np.concatenate([x1, x2, x3, x4, special])
+    got, hw = _eval(dev, 10, x, x), _eval(dev, 11, x, x)
+    assert (bits(got) == bits(hw)).all()
+    with np.errstate(all="ignore"):
+        want = np.sqrt(x)
+    ok = ~np.isnan(want)
+    assert (bits(got[ok]) == bits(want[ok])).all() and np.isnan(got[~ok]).all()
+
+
+@pytest.mark.gpu
+def test_fp64_rates(dev):
+    """The rate probe's five kinds run and report positive rates."""
+    r = dev.fp64_rates()
+    assert set(r) == {"dmul_dadd", "dfma", "ddiv", "dmul_add_ip", "div_ip"}
+    assert all(v > 0.0 for v in r.values())
