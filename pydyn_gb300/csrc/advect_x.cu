@@ -88,7 +88,7 @@ __device__ int row_search(double *m_s, double *mx_s, double *a_s, int n, bool he
             return nloop;
         }
         nloop += 1;
-        for (int k = k0 + lane; k <= k1; k += GB_WARP) a_s[k] = (a_s[k] * (double)(nloop - 1)) / (double)nloop;
+        for (int k = k0 + lane; k <= k1; k += GB_WARP) a_s[k] = div_ip(a_s[k] * (double)(nloop - 1), (double)nloop);
         __syncwarp();
         if (nloop > nmax) {
             amax_out = 0.0;

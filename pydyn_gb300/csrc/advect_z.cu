@@ -79,7 +79,7 @@ __device__ void z_trials(const ZArgs &A, ZCol *zc, double *mx, double *cf, int p
             const int64_t col = col0 + q;
             const int i = (int)(col / A.jm), j = (int)(col % A.jm);
             const double v = AT(A.cm, i, j, kk);
-            cf[q * NC + kk] = zc[q].n == 1 ? v : v / (double)zc[q].n;
+            cf[q * NC + kk] = zc[q].n == 1 ? v : div_ip(v, (double)zc[q].n);
         }
     }
     const bool mine = p < ncols && zc[p].state == 1;
@@ -212,7 +212,7 @@ __global__ void __launch_bounds__(MAX_THREADS, 2) k_z_steps(ZArgs A) {
     for (int e = threadIdx.x; e < ncols * (lm + 1); e += blockDim.x) {
         const int q = e / (lm + 1), kk = e % (lm + 1);
         const int64_t cq = col0 + q;
-        smem[q * per + NC + kk] = AT(A.cm, A.si0 + (int)(cq / ns), A.sj0 + (int)(cq % ns), kk) / (double)n;
+        smem[q * per + NC + kk] = div_ip(AT(A.cm, A.si0 + (int)(cq / ns), A.sj0 + (int)(cq % ns), kk), (double)n);
     }
     double *m_s = smem + p * per;
     double *c_s = m_s + NC;

@@ -127,9 +127,9 @@ __global__ void k_uncompress_x(RA R, int xr, int js, int je, int ls, int le, int
     const int j = js + rest / nl, l = ls + rest % nl;
     const int f = ft == 0 ? 0 : 1 + (ft - 1) / R.nt, t = ft == 0 ? 0 : (ft - 1) % R.nt;
     const int imr = R.im;
-    const double w = Xc(R, f, xr, j, l, t) / (double)xr;
+    const double w = div_ip(Xc(R, f, xr, j, l, t), (double)xr);
     for (int i = 1; i <= xr; ++i) Xc(R, f, i, j, l, t) = w;
-    const double e = Xc(R, f, imr - xr + 1, j, l, t) / (double)xr;
+    const double e = div_ip(Xc(R, f, imr - xr + 1, j, l, t), (double)xr);
     for (int i = imr - xr + 1; i <= imr; ++i) Xc(R, f, i, j, l, t) = e;
 }
 
@@ -164,9 +164,9 @@ __global__ void k_uncompress_y(RA R, int yr, int is, int ie, int ls, int le, int
     const int i = is + rest / nl, l = ls + rest % nl;
     const int f = ft == 0 ? 0 : 1 + (ft - 1) / R.nt, t = ft == 0 ? 0 : (ft - 1) % R.nt;
     const int jmr = R.jm;
-    const double w = Xc(R, f, i, yr, l, t) / (double)yr;
+    const double w = div_ip(Xc(R, f, i, yr, l, t), (double)yr);
     for (int j = 1; j <= yr; ++j) Xc(R, f, i, j, l, t) = w;
-    const double e = Xc(R, f, i, jmr - yr + 1, l, t) / (double)yr;
+    const double e = div_ip(Xc(R, f, i, jmr - yr + 1, l, t), (double)yr);
     for (int j = jmr - yr + 1; j <= jmr; ++j) Xc(R, f, i, j, l, t) = e;
 }
 
@@ -291,8 +291,8 @@ __global__ void k_coarsen_ambm(RA P, RA C, int ib, int ie, int jb, int je, int l
         if (!xedges) return;
         const int j = jb + (int)(k / nl), lev = lb + (int)(k % nl);
         const int jc = (j - jb) * yr + 1, lc = (lev - lb) * zr + 1;
-        const double cell1 = Fc(P.am, ib - 1, j, lev) / (double)(yr * zr);
-        const double cellm = Fc(P.am, ie, j, lev) / (double)(yr * zr);
+        const double cell1 = div_ip(Fc(P.am, ib - 1, j, lev), (double)(yr * zr));
+        const double cellm = div_ip(Fc(P.am, ie, j, lev), (double)(yr * zr));
         for (int jj = jc; jj <= jc + yr - 1; ++jj)
             for (int ll = lc; ll <= lc + zr - 1; ++ll) {
                 Fc(C.am, xr - 1, jj, ll) = cell1;
@@ -304,8 +304,8 @@ __global__ void k_coarsen_ambm(RA P, RA C, int ib, int ie, int jb, int je, int l
     if (k >= (int64_t)ni * nl) return;
     const int i = ib + (int)(k / nl), lev = lb + (int)(k % nl);
     const int ic = (i - ib) * xr + 1, lc = (lev - lb) * zr + 1;
-    const double cell1 = Fc(P.bm, i, jb, lev) / (double)(xr * zr);
-    const double cellm = Fc(P.bm, i, je + 1, lev) / (double)(xr * zr);
+    const double cell1 = div_ip(Fc(P.bm, i, jb, lev), (double)(xr * zr));
+    const double cellm = div_ip(Fc(P.bm, i, je + 1, lev), (double)(xr * zr));
     for (int ii = ic; ii <= ic + xr - 1; ++ii)
         for (int ll = lc; ll <= lc + zr - 1; ++ll) {
             if (sp_edge) Fc(C.bm, ii, yr, ll) = cell1;

@@ -412,7 +412,7 @@ __device__ __forceinline__ double along_slope_y(double s, double pf_lo, double p
 // The progressive rescale of dynamu / dynamv (ops.py:304-307): f * (n - 1) / n, evaluated
 // left to right, applied once per retry n = 2 .. nloop.
 __device__ __forceinline__ double progressive_chain(double f, int nloop) {
-    for (int n = 2; n <= nloop; ++n) f = (f * (double)(n - 1)) / (double)n;
+    for (int n = 2; n <= nloop; ++n) f = div_ip(f * (double)(n - 1), (double)n);
     return f;
 }
 
