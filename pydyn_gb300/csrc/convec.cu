@@ -301,7 +301,10 @@ __global__ void __launch_bounds__(GB_TUNE_MAX_CELL) k_convec_matrix(CArgs A) {
         // the diagonal's terms (l == k: - qamu, then - qdk2) and the sub-diagonal's (l == k - 1:
         // - qamd, then + qdk1) as f = (f - s1) + s2, where the other lanes' s1 = +0 and s2 = -0
         // leave every f as it is (x - +0 = x, x + -0 = x, zeros and NaNs included)
-        double u = 0.0;
+        // The diagonal element (row k = l + 1, 1-based) takes e + 1.0: its e is kept and the sum made
+        // once after the loop -- a sum inside it would be issued every row for the warp, its other
+        // lanes predicated off.
+        double u = 0.0, ediag = 0.0;
         for (int k = 1; k <= kg; ++k) {
             const double z = zu[k];
             // the updraft chain from l + 1 up: qeu z at k = l + 1, then u z; zero below
@@ -314,11 +317,12 @@ __global__ void __launch_bounds__(GB_TUNE_MAX_CELL) k_convec_matrix(CArgs A) {
                 f = (f - s1) + s2;
                 fk = f;
             }
-            double e = mdt * (fprev - fk);
-            if (l == k - 1) e = e + 1.0;
-            out[(size_t)(k - 1) * n + l] = e;
+            const double e = mdt * (fprev - fk);
+            if (l == k - 1) ediag = e;
+            else out[(size_t)(k - 1) * n + l] = e;
             fprev = fk;
         }
+        if (l + 1 <= kg) out[(size_t)l * n + l] = ediag + 1.0;
     }
     // rows kg+1 .. kend (a lane whose band lies above R): f(k, l) is the band's, +0 below row l;
     // f(l-1, l) is the chains' last value when row l-1 is kg, else +0

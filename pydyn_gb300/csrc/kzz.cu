@@ -51,6 +51,37 @@ __device__ __forceinline__ double &S3(const DV &v, int i, int j, int l) {
 }
 // jqif(x, y) = nint(0.5 + sign(0.5, x - y)): 1 where x - y has a clear sign bit
 __device__ __forceinline__ double jqif(double x, double y) { return signbit(x - y) ? 0.0 : 1.0; }
+
+// The statements blend by flags that are exactly +0.0 or 1.0 (jqif's values, their products and
+// complements), so the flag arithmetic runs on the integer pipe:
+//   jq a jq' and jq (1 - jq')  ->  the flags' AND (+0.0 or 1.0, as the products are);
+//   jq x + (1 - jq) y          ->  x or y, for finite x and y, with the zero the other product
+//                                  adds: x + (+0 y) is x but for x = -0 beside a y of clear sign
+//                                  (-0 + +0 = +0), and (+0 x) + y the same way round;
+//   jq v                       ->  v, or the zero of v's sign, for finite v.
+// A non-finite operand takes the FP64 statement itself, through a call.
+__device__ __forceinline__ bool on(double f) { return __double_as_longlong(f) != 0; }  // 1.0, not +0.0
+__device__ __forceinline__ double flag(bool b) { return b ? 1.0 : 0.0; }
+__device__ __forceinline__ bool finite_bits(unsigned long long b) { return ((b >> 52) & 0x7ff) != 0x7ff; }
+static __device__ __noinline__ double blend_fp64(double jq, double x, double y) { return jq * x + (1.0 - jq) * y; }
+__device__ __forceinline__ double blend01(double jq, double x, double y) {
+    const unsigned long long bx = (unsigned long long)__double_as_longlong(x), by = (unsigned long long)__double_as_longlong(y);
+    constexpr unsigned long long SIGN = 0x8000000000000000ULL;
+    if (!finite_bits(bx) || !finite_bits(by)) return blend_fp64(jq, x, y);
+    const unsigned long long r = on(jq) ? ((bx == SIGN && (by >> 63) == 0) ? 0ULL : bx)
+                                        : ((by == SIGN && (bx >> 63) == 0) ? 0ULL : by);
+    return __longlong_as_double((long long)r);
+}
+static __device__ __noinline__ double mul_fp64(double a, double b) { return a * b; }
+// the interfaces' free-convection blend as the reference writes it, for non-finite operands
+static __device__ __noinline__ double zpblk_jq5_fp64(double jq5, double zpblk, double wsc, double z, double zzh) {
+    return (1.0 - jq5) * zpblk + jq5 * wsc * VKARMAN * z * zzh;
+}
+__device__ __forceinline__ double mul01(double jq, double v) {
+    const unsigned long long bv = (unsigned long long)__double_as_longlong(v);
+    if (!finite_bits(bv)) return mul_fp64(jq, v);
+    return __longlong_as_double((long long)(on(jq) ? bv : (bv & 0x8000000000000000ULL)));
+}
 __device__ __forceinline__ double cube(double x) { return (x * x) * x; }
 
 __device__ __forceinline__ double rair() { return RGAS * 1.0e3 / XMAIR; }
@@ -281,7 +312,7 @@ __global__ void __launch_bounds__(GB_TUNE_MAX_CELL) k_kzz_interfaces(KArgs A) {
 
     const double z = gph[k] - z0;
     double jq = jqif(1000.0, z);
-    const double zlambdac = jq * 300.0 + (1.0 - jq) * (30.0 + 270.0 * gbm_exp(1.0 - div_by_recip(z, 1000.0, 1.0e-3)));
+    const double zlambdac = blend01(jq, 300.0, 30.0 + 270.0 * gbm_exp(1.0 - div_by_recip(z, 1000.0, 1.0e-3)));
     const double rkz = div_ip(1.0, VKARMAN * z);
     double cml2 = div_ip(1.0, div_ip(1.0, zlambdac) + rkz);
     cml2 = cml2 * cml2;
@@ -300,46 +331,59 @@ __global__ void __launch_bounds__(GB_TUNE_MAX_CELL) k_kzz_interfaces(KArgs A) {
     const double rdup = sqrt_ip(zdup2);
     const double zkvn = cml2 * rdup;
     jq = jqif(zrinub, 0.0);
-    const double wkvf = jq * np_max(CKMIN, zkvn * zfstabh) + (1.0 - jq) * np_max(CKMIN, zkvn * zfunst);
+    const double wkvf = blend01(jq, np_max(CKMIN, zkvn * zfstabh), np_max(CKMIN, zkvn * zfunst));
     jq = jqif(P, z);
-    const double jz = jq * z;
+    const double jz = mul01(jq, z);
     const double zh = div_by_recip(jz, P, yP);
     const double zl = div_by_recip(jz, Wb, yWb) + (1.0 - jq);
-    const double zzh = jq * ((1.0 - zh) * (1.0 - zh));
+    const double zzh = mul01(jq, (1.0 - zh) * (1.0 - zh));
     double jq1 = jqif(HV, 0.0);
-    const double jq2 = jq * (1.0 - jq1), jq3 = jq * jq1;
-    const double jq6 = jq1 * jqif(P, whk1) * jqif(whk, P);
+    const double jq2 = flag(on(jq) && !on(jq1)), jq3 = flag(on(jq) && on(jq1));
+    const double jq6 = flag(on(jq1) && on(jqif(P, whk1)) && on(jqif(whk, P)));
     jq1 = jqif(SFFRAC, zh);
-    const double jq4 = jq3 * jq1, jq5 = jq3 * (1.0 - jq1);
+    const double jq4 = flag(on(jq3) && on(jq1)), jq5 = flag(on(jq3) && !on(jq1));
     cml2 = div_ip(1.0, rkz + 1.0 / 450.0);
     cml2 = cml2 * cml2;
     const double jqq = jqif(zrinub, 0.0);
-    zfstabh = div_ip(jqq, 1.0 + 10.0 * zrinub * sqrt_ip(1.0 + jqq * zrinub)) + (1.0 - jqq);
+    zfstabh = div_ip(jqq, 1.0 + 10.0 * zrinub * sqrt_ip(1.0 + mul01(jqq, zrinub))) + (1.0 - jqq);
     double zpblk = cml2 * rdup * zfstabh;
-    const double zkvh = jq2 * np_max(zpblk, KVHMIN) + (1.0 - jq2) * wkvf;
+    const double zkvh = blend01(jq2, np_max(zpblk, KVHMIN), wkvf);
     double zslask = 1.0 - BETAH * zl;
-    zslask = jq4 * zslask + (1.0 - jq4);
-    zpblk = (1.0 - jq4) * zkvh + jq4 * (U * VKARMAN * z * zzh * gbm_pow(zslask, ONET));
+    zslask = blend01(jq4, zslask, 1.0);
+    zpblk = blend01(jq4, U * VKARMAN * z * zzh * gbm_pow(zslask, ONET), zkvh);  // (1 - jq4) zkvh + jq4 (...)
     // jq5 is 0 or 1: at 1 the base is the column's stabw (stabw + 0.0, whose cube root is stabw's)
     const bool jq5_on = (__double_as_longlong(jq5) << 1) != 0;
     double fmt;
     if (jq5_on) {
         fmt = cv[16];
     } else {
-        zslask = jq5 * cv[15] + (1.0 - jq5);
+        zslask = blend01(jq5, cv[15], 1.0);
         fmt = gbm_pow(zslask, ONET);
     }
     const double wsc = U * fmt;
-    zpblk = (1.0 - jq5) * zpblk + jq5 * wsc * VKARMAN * z * zzh;
+    // (1 - jq5) zpblk + (((jq5 wsc) VKARMAN) z) zzh: at jq5 = 1 the product (1 wsc = wsc) plus +0
+    // zpblk; at jq5 = 0 zpblk plus a zero of the sign of wsc z zzh (a NaN if any is not finite)
+    {
+        const unsigned long long bw = (unsigned long long)__double_as_longlong(wsc), bz = (unsigned long long)__double_as_longlong(z),
+                                 bh = (unsigned long long)__double_as_longlong(zzh), bp = (unsigned long long)__double_as_longlong(zpblk);
+        if (jq5_on) {
+            zpblk = blend01(1.0, wsc * VKARMAN * z * zzh, zpblk);
+        } else if (finite_bits(bw) && finite_bits(bz) && finite_bits(bh) && finite_bits(bp)) {
+            const unsigned long long zs = (bw ^ bz ^ bh) & 0x8000000000000000ULL;  // the zero's sign
+            if (bp == 0x8000000000000000ULL && zs == 0) zpblk = 0.0;               // -0 + +0 = +0
+        } else {
+            zpblk = zpblk_jq5_fp64(jq5, zpblk, wsc, z, zzh);
+        }
+    }
     const bool jq3_on = (__double_as_longlong(jq3) << 1) != 0;  // jq3 != 0.0, on the integer pipe
-    const double pr = jq3 * (jq3_on ? cv[13] : cv[12]) + (1.0 - jq3);
+    const double pr = blend01(jq3, jq3_on ? cv[13] : cv[12], 1.0);
     // pr's reciprocal: the sum's at jq3 = 1 (pr = sum + 0.0), 1 where jq3 = 0 left pr at exactly 1,
     // else none (div_by_recip divides)
     const double ypr = jq3_on ? cv[14] : (__double_as_longlong(pr) == 0x3ff0000000000000LL ? 1.0 : 0.0);
-    const double kv = jq3 * np_max(div_by_recip(zpblk, pr, ypr), KVHMIN) + (1.0 - jq3) * zkvh;
+    const double kv = blend01(jq3, np_max(div_by_recip(zpblk, pr, ypr), KVHMIN), zkvh);
     const double thvgrad = div_ip(dthv, zdz);
     const double kvhentr = div_ip(0.2 * HV, thvgrad);
-    const double kvh = jq6 * kvhentr + (1.0 - jq6) * kv;
+    const double kvh = blend01(jq6, kvhentr, kv);
 
     // dkg across interface l + 1 = k for l < lmax - 1, zero at lmax - 1 (diffusion.py:256-263)
     const int l = k - 1;
