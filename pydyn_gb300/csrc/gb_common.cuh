@@ -173,7 +173,8 @@ __device__ __forceinline__ double div_by_recip(double a, double d, double y) {
 // against md / 2 (a tie would go to the even neighbour; a quotient of two doubles is never
 // one).  A zero a gives a y0, signed as a / d.  Outside d in [2^-125, 2^125] (where the FP32
 // seed and its reciprocal are normal), or with a, q1 not normal, or q1 near a binade's edge, the
-// division is the FP64 pipe's own, through a call.
+// division is the FP64 pipe's own, through a call (a quotient that is always near a power of two,
+// such as a midpoint's fraction 1/2, is better left to the plain division).
 static __device__ __noinline__ double div_fp64_call(double a, double d) { return a / d; }
 __device__ __forceinline__ double div_ip(double a, double d) {
     constexpr unsigned long long SIGN = 0x8000000000000000ULL, FRAC = 0xfffffffffffffULL, ONE = 0x10000000000000ULL;

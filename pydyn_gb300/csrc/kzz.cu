@@ -51,6 +51,18 @@ __device__ __forceinline__ double &S3(const DV &v, int i, int j, int l) {
 }
 // jqif(x, y) = nint(0.5 + sign(0.5, x - y)): 1 where x - y has a clear sign bit
 __device__ __forceinline__ double jqif(double x, double y) { return signbit(x - y) ? 0.0 : 1.0; }
+// The same on the integer pipe, for the column sweep's serial chain (where the subtraction's
+// latency is on the path): for finite x and y the sign of x - y is their order (x - x = +0; an
+// overflowing difference keeps its sign), but for two zeros, where only -0 - +0 = -0 has it set.
+// An infinite or NaN operand takes the subtraction itself.  (Where the FP64 pipe's throughput,
+// not its latency, is the bound, the plain subtraction measured better.)
+static __device__ __noinline__ double jqif_fp64(double x, double y) { return signbit(x - y) ? 0.0 : 1.0; }
+__device__ __forceinline__ double jqif_ip(double x, double y) {
+    const unsigned long long bx = (unsigned long long)__double_as_longlong(x), by = (unsigned long long)__double_as_longlong(y);
+    if (((bx >> 52) & 0x7ff) == 0x7ff || ((by >> 52) & 0x7ff) == 0x7ff) return jqif_fp64(x, y);
+    if (((bx | by) << 1) == 0) return (bx >> 63) && !(by >> 63) ? 0.0 : 1.0;  // two zeros
+    return gb_ge(x, y) ? 1.0 : 0.0;
+}
 
 // The statements blend by flags that are exactly +0.0 or 1.0 (jqif's values, their products and
 // complements), so the flag arithmetic runs on the integer pipe:
@@ -132,17 +144,20 @@ __global__ void __launch_bounds__(GB_TUNE_MAX_CELL) k_kzz_levels(KArgs A) {
 // k_kzz_raw2); the carried part -- the mask jwork, the last Richardson number, pblh -- runs a
 // thread per column (sweep_carry).
 __device__ double sweep_carry(double pblh, const double *whm, const double *raw, int k0, int lm) {
+    // jwork and jq are flags (+0.0 or 1.0): their products and blends are integer selects
+    // (mul01, blend01); wrino = zrino + (1 - jwork) 0.1 is zrino + +0 while jwork is 1
     double jwork = 1.0, wrino = 0.0;
     for (int k = k0; k < lm; ++k) {
-        const double zrino = jwork * raw[k];
-        const double jq = jqif(RICR, zrino);
+        const double zrino = mul01(jwork, raw[k]);
+        const double jq = jqif_ip(RICR, zrino);
         const double frac = div_ip(RICR - wrino, zrino - wrino);
         const double at_ricr = (k == 0) ? frac * whm[k] : whm[k - 1] + frac * (whm[k] - whm[k - 1]);
-        pblh = jq * pblh + (1.0 - jq) * at_ricr;
-        jwork = jq * jwork;
-        wrino = zrino + (1.0 - jwork) * 0.1;
+        pblh = blend01(jq, pblh, at_ricr);
+        jwork = flag(on(jq) && on(jwork));
+        wrino = on(jwork) ? blend01(1.0, zrino, 0.1) : zrino + 0.1;  // zrino + (1 - jwork) 0.1
     }
-    return k0 == 0 ? (1.0 - jwork) * pblh + whm[lm - 1] * jwork : (1.0 - jwork) * pblh + jwork * whm[lm - 1];
+    // (1 - jwork) pblh + whm(lm-1) jwork, or with the second product's factors swapped (the same value)
+    return blend01(jwork, whm[lm - 1], pblh);
 }
 
 // thread per column: the geopotential's running sum, ustar (diffusion.py:76-89), the surface
@@ -157,7 +172,7 @@ __global__ void __launch_bounds__(GB_TUNE_MAX_COLUMN) k_kzz_surface(KArgs A) {
     const double *dzg = A.dzg + c * lm, *wthm = A.wthm + c * lm;
     const double sm = S2(A.spm, i, j);
 
-    const double g0 = S2(A.surf[0], i, j) / GRAV;
+    const double g0 = div_by_recip(S2(A.surf[0], i, j), GRAV, RGRAV);
     gph[0] = g0;
     double g = g0, g1 = g0;
     for (int k = 0; k < lm - 1; ++k) {
@@ -167,7 +182,7 @@ __global__ void __launch_bounds__(GB_TUNE_MAX_COLUMN) k_kzz_surface(KArgs A) {
     }
     gph[lm] = 200000.0;
 
-    const double xland = S2(A.surf[1], i, j) / 100.0;
+    const double xland = div_by_recip(S2(A.surf[1], i, j), 100.0, 0.01);  // 0.01 = RN(1 / 100)
     const double ew = S2(A.surf[8], i, j), ns = S2(A.surf[9], i, j);
     const double tau = sqrt_ip(ew * ew + ns * ns);
     const double ustar_sea = np_max(0.001, sqrt_ip(div_ip(tau, RHO_AIR)));
@@ -175,19 +190,19 @@ __global__ void __launch_bounds__(GB_TUNE_MAX_COLUMN) k_kzz_surface(KArgs A) {
     const double wind10m = sqrt_ip(u10 * u10 + v10 * v10);
     const double sr_land = np_max(1e-2, S2(A.surf[3], i, j));
     const double sr_help = np_min(S2(A.surf[2], i, j), 0.03);
-    double land = VKARMAN * wind10m / gbm_log(10.0 / sr_help) * gbm_log(75.0 / sr_help);
-    land = land / gbm_log(10.0 / sr_land);
+    double land = div_ip(VKARMAN * wind10m, gbm_log(div_ip(10.0, sr_help))) * gbm_log(div_ip(75.0, sr_help));
+    land = div_ip(land, gbm_log(div_ip(10.0, sr_land)));
     const double ustar_land = gb_gt0(xland) ? land : 0.0;
     const double ustar_loc = xland * ustar_land + (1.0 - xland) * ustar_sea;
 
     const double ph0 = A.at[0] + A.bt[0] * sm, ph1 = A.at[1] + A.bt[1] * sm;
     const double dz1 = (lm > 1 ? g1 : gph[1]) - g0, dp1 = ph0 - ph1;
-    const double wheat = -S2(A.surf[6], i, j) * dz1 * GRAV / dp1 / CP_AIR;
-    const double wqflx = -S2(A.surf[7], i, j) * dz1 * GRAV / dp1 / LVAP;
+    const double wheat = div_ip(div_ip(-S2(A.surf[6], i, j) * dz1 * GRAV, dp1), CP_AIR);
+    const double wqflx = div_ip(div_ip(-S2(A.surf[7], i, j) * dz1 * GRAV, dp1), LVAP);
     const double ustr = np_max(ustar_loc, 0.01);
     const double wtseff = wthm[0] * (1.0 + ZCRDQ * S3(A.q, i, j, 0));
     const double wheatv = wheat + ZCRDQ * wthm[0] * wqflx;
-    const double wobkl = -wtseff * cube(ustr) / (GRAV * VKARMAN * (wheatv + copysign(1.0e-10, wheatv)));
+    const double wobkl = div_ip(-wtseff * cube(ustr), GRAV * VKARMAN * (wheatv + copysign(1.0e-10, wheatv)));
     double *cv = A.col + c * NCOLVAL;
     cv[0] = g0;
     cv[2] = wobkl;
@@ -200,6 +215,7 @@ __global__ void __launch_bounds__(GB_TUNE_MAX_COLUMN) k_kzz_surface(KArgs A) {
 __device__ __forceinline__ double level_height(const KArgs &A, const double *gph, double z0, double sm, int l) {
     const double ph0 = A.at[l] + A.bt[l] * sm, ph1 = A.at[l + 1] + A.bt[l + 1] * sm;
     const double pf = (ph0 + ph1) * 0.5;
+    // about 0.5, at a binade's edge, where div_ip would take the division itself after its own work
     const double intfac = (ph0 - pf) / (ph0 - ph1);
     return (gph[l] - z0) * (1.0 - intfac) + (gph[l + 1] - z0) * intfac;
 }
@@ -222,7 +238,7 @@ __global__ void __launch_bounds__(GB_TUNE_MAX_CELL) k_kzz_heights(KArgs A) {
     const double vvk = np_max(du * du + dv * dv + ZACB * ustr * ustr, TINY);
     const double dz = whk - wh0;
     double zrino = div_ip(GRAV * (A.zthvk[t] - wtseff) * dz, wtseff * vvk);
-    zrino = zrino + copysign(1.0e-10, zrino);
+    zrino = add_ip(zrino, copysign(1.0e-10, zrino));  // like-signed: the integer pipe's sum
     A.sw_vvk[t] = vvk;
     A.sw_dz[t] = dz;
     A.sw_raw[t] = zrino;
@@ -238,11 +254,11 @@ __global__ void __launch_bounds__(GB_TUNE_MAX_COLUMN) k_kzz_sweep1(KArgs A) {
     const double wobkl = cv[2], wheatv = cv[3], ustr = cv[4], wtseff = cv[10];
     const double pblh = sweep_carry(0.0, A.whm + c * lm, A.sw_raw + c * lm, 0, lm);
     const double jq = jqif(wheatv, 0.0);
-    const double fmt = gbm_pow(jq * (1.0 - BINM * pblh / wobkl) + (1.0 - jq), ONET);
+    const double fmt = gbm_pow(blend01(jq, 1.0 - div_ip(BINM * pblh, wobkl), 1.0), ONET);
     const double wsc = ustr * fmt;
-    const double zexcess = wheatv * FAK / wsc;
+    const double zexcess = div_ip(wheatv * FAK, wsc);
     cv[1] = pblh;
-    cv[11] = wtseff + jq * zexcess;  // thvparc
+    cv[11] = wtseff + mul01(jq, zexcess);  // thvparc
 }
 
 // thread per (column, level >= 1): the second sweep's level terms
@@ -255,7 +271,7 @@ __global__ void __launch_bounds__(GB_TUNE_MAX_CELL) k_kzz_raw2(KArgs A) {
     const double *cv = A.col + c * NCOLVAL;
     const double wtseff = cv[10], thvparc = cv[11];
     double zrino = div_ip(GRAV * (A.zthvk[t] - thvparc) * A.sw_dz[t], A.sw_vvk[t] * wtseff);
-    zrino = zrino + copysign(1.0e-10, zrino);
+    zrino = add_ip(zrino, copysign(1.0e-10, zrino));  // like-signed: the integer pipe's sum
     A.sw_raw[t] = zrino;
 }
 
