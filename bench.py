@@ -72,10 +72,10 @@ BYTES_PER_CELL = {"_dynamu_region1": 12, "_dynamv_region1": 12, "_dynamw_region1
 # (dram__bytes_read.sum + dram__bytes_write.sum), the roofline's traffic, and FP64 warp
 # instructions (smsp__inst_executed_pipe_fp64.sum), whose issue bounds the step
 # (profiles/interval_dram_fp64_glb3x2+nam1x1.md, profiles/interval_dram_fp64_a100-case.md)
-TRAFFIC_PER_CALL = {"glb3x2+nam1x1": {"convec_region@2": 130.4e6, "convec_region@1": 240.2e6, "calc_kzz": 131.8e6},
-                    "a100-case": {"convec_region@2": 48.78e6, "convec_region@1": 181.0e6}}
-FP64_PER_CALL = {"glb3x2+nam1x1": {"convec_region@2": 2.658e6, "convec_region@1": 3.360e6, "calc_kzz": 15.145e6},
-                 "a100-case": {"convec_region@2": 1.425e6, "convec_region@1": 3.905e6}}
+TRAFFIC_PER_CALL = {"glb3x2+nam1x1": {"convec_region@2": 131.5e6, "convec_region@1": 240.9e6, "calc_kzz": 131.8e6},
+                    "a100-case": {"convec_region@2": 49.66e6, "convec_region@1": 182.7e6}}
+FP64_PER_CALL = {"glb3x2+nam1x1": {"convec_region@2": 2.623e6, "convec_region@1": 3.319e6, "calc_kzz": 13.866e6},
+                 "a100-case": {"convec_region@2": 1.394e6, "convec_region@1": 3.827e6}}
 
 
 def workload_config(workload, n_gpus):

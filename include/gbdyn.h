@@ -410,7 +410,7 @@ int gb_adjoint_convec(gb_ctx *ctx, const gb_view *rm_b, const gb_view *rxm_b, co
 int gb_adjoint_sources(gb_ctx *ctx, const gb_view *rm_b, const gb_view *rzm_b, const gb_view *grad,
                        const double *area, double scale, int level, const int32_t *cols, int ncol);
 
-/* Measured FP64 issue rate of this GPU, instructions per second over all SMs: kind 0 a multiply
+/* Measured FP64 issue rate of the device, instructions per second over all SMs: kind 0 a multiply
  * and an add (what -fmad=false emits), 1 a fused multiply-add, 2 a correctly rounded division;
  * kind 3 the multiply with the add on the integer pipe (add_ip; the pair counted as two, as in
  * kind 0), kind 4 the integer-corrected division (div_ip), divisions per second.  The compute

@@ -243,7 +243,7 @@ __global__ void __launch_bounds__(GB_TUNE_MAX_CELL) k_chem(CArgs A) {
                 const double krate = A.krates.p ? E4(A.krates, i, j, l, 1) : krate_cl(T);
                 trop_cl = (v * krate) * A.cl_scale;
             }
-            L1 = strat ? s_cl : s_cl + trop_cl;
+            L1 = strat ? s_cl : add_ip(s_cl, trop_cl);  // rates: like-signed sums
             L2 = s_od * A.o1d_scale;
         }
         double L0 = s_oh;
@@ -254,7 +254,9 @@ __global__ void __launch_bounds__(GB_TUNE_MAX_CELL) k_chem(CArgs A) {
             L0 = (krate_oh * oh) * A.oh_scale;
         }
         const double L3 = (A.has_soil && l == 0) ? -(A.soil_rate * E2(A.soil, i, j)) : 0.0;
-        const double d = (hit && strat) ? cc[6 * ncell] : gbm_exp(-((((L0 + L1) + L2) + L3) * A.dt));
+        // the rates are >= 0 and L3 is +0 but at the surface: the sums are the integer pipe's (add_ip;
+        // the surface's soil uptake, of the other sign, takes its FP64 fallback)
+        const double d = (hit && strat) ? cc[6 * ncell] : gbm_exp(-(add_ip(add_ip(add_ip(L0, L1), L2), L3) * A.dt));
         if (cc && !hit) {
             cc[0] = bot;
             cc[ncell] = top;

@@ -1,7 +1,7 @@
 // convec: implicit convection with Kzz diffusion folded into one matrix per column, inverted
 // by Crout LU without pivoting, applied to the tracer mass and (by its diagonal) the slopes.
 //
-// Seven launches, shaped so that the FP64 pipe -- this GPU's scarcest unit -- issues with its
+// Seven launches, shaped so that the FP64 pipe -- GB300's scarcest unit -- issues with its
 // lanes full:
 //   k_convec_chains  three threads per owned column: whether its kept inverse still holds, the
 //                    updraft and the downdraft mass fluxes carried level to level

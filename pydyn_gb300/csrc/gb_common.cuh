@@ -69,7 +69,7 @@ static inline DV dv(const gb_view *v) {
 }
 
 // ------------------------------------------------------------------ bit tests
-// isnan, |x| and -x on the integer pipe: on this GPU the FP64 pipe is the scarce unit, and a
+// isnan, |x| and -x on the integer pipe: on GB300 the FP64 pipe is the scarce unit, and a
 // compare or a sign change issued there costs as much as a multiply.  Exact for every input.
 __device__ __forceinline__ bool gb_isnan(double x) {
     return (unsigned long long)(__double_as_longlong(x) & 0x7fffffffffffffffLL) > 0x7ff0000000000000ULL;
@@ -270,7 +270,7 @@ __device__ __forceinline__ double recip_for(double d) {
 }
 
 // ------------------------------------------------------------------ addition on the integer pipe
-// a + b, IEEE binary64 round to nearest even, bit for bit the FP64 pipe's sum.  On this GPU the
+// a + b, IEEE binary64 round to nearest even, bit for bit the FP64 pipe's sum.  On GB300 the
 // FP64 pipe issues a warp instruction about every 76 cycles of a sub-partition while the integer
 // ALU issues one every two: a chain of products and sums (x = x + c q) that keeps the multiply on
 // the FP64 pipe and moves the sum here runs well above the rate of both on the FP64 pipe.

@@ -1,7 +1,7 @@
 // Calc_Kzz: the vertical diffusion exchange rate dkg of every column of a region.
 //
 // Eight launches, each with every lane on its own cell, column or interface (FP64 issue slots
-// are this GPU's scarcest resource, so no lane idles through another's serial work), the
+// are GB300's scarcest resource, so no lane idles through another's serial work), the
 // column-serial parts reduced to the recurrences that carry from level to level:
 //   k_kzz_rows        thread per latitude: the zonal wind factor dxx (a cosine per row)
 //   k_kzz_levels      thread per (column, level): potential temperature, the logarithms, the

@@ -151,7 +151,7 @@ class Device:
 
     # -------------------------------------------------------------- FP64 ceiling
     def fp64_rates(self):
-        """Measured FP64 issue rates of this GPU in G instructions/s: multiply + add pairs,
+        """Measured FP64 issue rates of the device in G instructions/s: multiply + add pairs,
         fused multiply-adds, correctly rounded divisions; and the same pair with the add on the
         integer pipe (add_ip, counted as two instructions) and the integer-corrected division
         (div_ip, divisions/s)."""

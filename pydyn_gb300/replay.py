@@ -80,7 +80,7 @@ def _bits_to_float(b):
 
 # ------------------------------------------------------------------ the engine
 class DeviceEngine:
-    """pydyn's replay engine for a state on this GPU (see the module's docstring)."""
+    """pydyn's replay engine for a state on the device (see the module's docstring)."""
 
     name = "gb300"
     fingerprint = False
