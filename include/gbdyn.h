@@ -379,8 +379,9 @@ int gb_m2phlb(gb_ctx *ctx, const gb_view *m, const gb_view *sp, const gb_view *p
  * shared-reciprocal division the convection's back substitution uses, op 6 x / y by the
  * hardware division (the check that the two agree), op 7 x / y by the integer-corrected
  * division (div_ip), op 8 x + y and op 9 x - y by the integer-pipe sum (add_ip, sub_ip), op 10
- * sqrt(x) by the integer-corrected root (sqrt_ip), op 11 by the hardware's.  No reference
- * counterpart. */
+ * sqrt(x) by the integer-corrected root (sqrt_ip), op 11 by the hardware's; Calc_Kzz's flag
+ * arithmetic on the integer pipe: op 12 1 x + (1 - 1) y and op 13 0 x + (1 - 0) y (blend01), op 14
+ * 0 x (mul01), op 15 jqif(x, y) (jqif_ip).  No reference counterpart. */
 int gb_math_eval(gb_ctx *ctx, int op, const double *x, const double *y, double *out, int64_t n);
 
 /* ------------------------------------------------------------------ the adjoint

@@ -334,6 +334,48 @@ __device__ __forceinline__ double zero_plus(double p) {
 }
 __device__ __forceinline__ double zero_minus(double p) { return zero_plus(gb_neg(p)); }
 
+// ------------------------------------------------------------------ 0/1 flags (Calc_Kzz's jqif)
+// jqif(x, y) = nint(0.5 + sign(0.5, x - y)) (1 where x - y has a clear sign bit) on the integer
+// pipe, for the Kzz column sweep's serial chain (where the subtraction's latency is on the
+// path): for finite x and y the sign of x - y is their order (x - x = +0; an
+// overflowing difference keeps its sign), but for two zeros, where only -0 - +0 = -0 has it set.
+// An infinite or NaN operand takes the subtraction itself.  (Where the FP64 pipe's throughput,
+// not its latency, is the bound, the plain subtraction measured better.)
+static __device__ __noinline__ double jqif_fp64(double x, double y) { return signbit(x - y) ? 0.0 : 1.0; }
+__device__ __forceinline__ double jqif_ip(double x, double y) {
+    const unsigned long long bx = (unsigned long long)__double_as_longlong(x), by = (unsigned long long)__double_as_longlong(y);
+    if (((bx >> 52) & 0x7ff) == 0x7ff || ((by >> 52) & 0x7ff) == 0x7ff) return jqif_fp64(x, y);
+    if (((bx | by) << 1) == 0) return (bx >> 63) && !(by >> 63) ? 0.0 : 1.0;  // two zeros
+    return gb_ge(x, y) ? 1.0 : 0.0;
+}
+
+// Calc_Kzz's statements blend by flags that are exactly +0.0 or 1.0 (jqif's values, their
+// products and complements), so the flag arithmetic runs on the integer pipe:
+//   jq a jq' and jq (1 - jq')  ->  the flags' AND (+0.0 or 1.0, as the products are);
+//   jq x + (1 - jq) y          ->  x or y, for finite x and y, with the zero the other product
+//                                  adds: x + (+0 y) is x but for x = -0 beside a y of clear sign
+//                                  (-0 + +0 = +0), and (+0 x) + y the same way round;
+//   jq v                       ->  v, or the zero of v's sign, for finite v.
+// A non-finite operand takes the FP64 statement itself, through a call.
+__device__ __forceinline__ bool on(double f) { return __double_as_longlong(f) != 0; }  // 1.0, not +0.0
+__device__ __forceinline__ double flag(bool b) { return b ? 1.0 : 0.0; }
+__device__ __forceinline__ bool finite_bits(unsigned long long b) { return ((b >> 52) & 0x7ff) != 0x7ff; }
+static __device__ __noinline__ double blend_fp64(double jq, double x, double y) { return jq * x + (1.0 - jq) * y; }
+__device__ __forceinline__ double blend01(double jq, double x, double y) {
+    const unsigned long long bx = (unsigned long long)__double_as_longlong(x), by = (unsigned long long)__double_as_longlong(y);
+    constexpr unsigned long long SIGN = 0x8000000000000000ULL;
+    if (!finite_bits(bx) || !finite_bits(by)) return blend_fp64(jq, x, y);
+    const unsigned long long r = on(jq) ? ((bx == SIGN && (by >> 63) == 0) ? 0ULL : bx)
+                                        : ((by == SIGN && (bx >> 63) == 0) ? 0ULL : by);
+    return __longlong_as_double((long long)r);
+}
+static __device__ __noinline__ double mul_fp64(double a, double b) { return a * b; }
+__device__ __forceinline__ double mul01(double jq, double v) {
+    const unsigned long long bv = (unsigned long long)__double_as_longlong(v);
+    if (!finite_bits(bv)) return mul_fp64(jq, v);
+    return __longlong_as_double((long long)(on(jq) ? bv : (bv & 0x8000000000000000ULL)));
+}
+
 // x >= 0.0 and x < 0.0 on the integer pipe (an FP64 compare issues on the FP64 pipe): >= holds
 // from +0 to +inf and at -0; < from the smallest negative to -inf; a NaN fails both
 __device__ __forceinline__ bool ge_zero(double x) {

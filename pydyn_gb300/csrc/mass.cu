@@ -144,6 +144,10 @@ __global__ void k_math_eval(int op, const double *x, const double *y, double *ou
         case 9: r = sub_ip(x[k], y[k]); break;
         case 10: r = sqrt_ip(x[k]); break;
         case 11: r = sqrt(x[k]); break;
+        case 12: r = blend01(1.0, x[k], y[k]); break;  // 1 x + (1 - 1) y
+        case 13: r = blend01(0.0, x[k], y[k]); break;  // 0 x + (1 - 0) y
+        case 14: r = mul01(0.0, x[k]); break;          // 0 x
+        case 15: r = jqif_ip(x[k], y[k]); break;
         default: r = x[k] / y[k]; break;
     }
     out[k] = r;

@@ -239,3 +239,28 @@ def test_fp64_rates(dev):
     r = dev.fp64_rates()
     assert set(r) == {"dmul_dadd", "dfma", "ddiv", "dmul_add_ip", "div_ip"}
     assert all(v > 0.0 for v in r.values())
+
+
+@pytest.mark.gpu
+def test_flag_arithmetic_is_the_statements(dev):
+    """Calc_Kzz's flag arithmetic on the integer pipe equals the FP64 statements bit for bit (NaNs
+    as NaNs), signed zeros, infinities and NaNs included: jq x + (1 - jq) y at jq = 1.0 and +0.0
+    (blend01), +0.0 x (mul01), and jqif(x, y) = nint(0.5 + sign(0.5, x - y)) (jqif_ip)."""
+    rng = np.random.default_rng(23)
+    special = np.array([0.0, -0.0, 5e-324, -5e-324, 1.0, -1.0, 0.3, -0.3, 1.7976931348623157e308,
+                        -1.7976931348623157e308, np.inf, -np.inf, np.nan, 2.2250738585072014e-308])
+    sa, sb = np.meshgrid(special, special)
+    n = 100_000
+    a = np.concatenate([sa.ravel(), rng.standard_normal(n) * np.exp2(rng.integers(-60, 60, n).astype(float)),
+                        rng.choice(special, n)])
+    b = np.concatenate([sb.ravel(), rng.standard_normal(n) * np.exp2(rng.integers(-60, 60, n).astype(float)),
+                        rng.choice(special, n)])
+    with np.errstate(all="ignore"):
+        want = {12: 1.0 * a + (1.0 - 1.0) * b, 13: 0.0 * a + (1.0 - 0.0) * b, 14: 0.0 * a,
+                15: np.where(np.signbit(a - b), 0.0, 1.0)}
+    for op, w in want.items():
+        got = _eval(dev, op, a, b)
+        ok = ~np.isnan(w)
+        if op == 15:  # the sign of a NaN difference is the hardware's; compare the finite operands
+            ok = np.isfinite(a) & np.isfinite(b)
+        assert (bits(got[ok]) == bits(w[ok])).all() and np.isnan(got[~ok & np.isnan(w)]).all(), op
