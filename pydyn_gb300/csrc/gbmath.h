@@ -161,13 +161,16 @@ GBM_HD double gbm_log(double x) {
     t2 = z * (Lg1 + w * (Lg3 + w * (Lg5 + w * Lg7)));
     i |= j;
     R = t2 + t1;
+    /* dk ln2_hi and dk ln2_lo, the two tails' common products, made once before the tails split
+       (a warp whose lanes take both tails then issues them once) */
+    const double dhi = dk * ln2_hi, dlo = dk * ln2_lo;
     if (i > 0) {
         hfsq = 0.5 * f * f;
         if (k == 0) return f - (hfsq - s * (hfsq + R));
-        return dk * ln2_hi - ((hfsq - (s * (hfsq + R) + dk * ln2_lo)) - f);
+        return dhi - ((hfsq - (s * (hfsq + R) + dlo)) - f);
     }
     if (k == 0) return f - s * (f - R);
-    return dk * ln2_hi - ((s * (f - R) - dk * ln2_lo) - f);
+    return dhi - ((s * (f - R) - dlo) - f);
 }
 
 /* ------------------------------------------------------------------ pow */
