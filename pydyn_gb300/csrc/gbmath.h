@@ -175,8 +175,9 @@ GBM_HD double gbm_log(double x) {
 
 /* ------------------------------------------------------------------ pow */
 GBM_HD double gbm_pow(double x, double y) {
-    const double bp[2] = {1.0, 1.5}, dp_h[2] = {0.0, 5.84962487220764160156e-01},
-                 dp_l[2] = {0.0, 1.35003920212974897128e-08};
+    /* bp, dp_h, dp_l of fdlibm's two-entry tables (k = 0, 1), picked by selects rather than an
+       index (an indexed table lives in local memory on the device) */
+    const double dp_h1 = 5.84962487220764160156e-01, dp_l1 = 1.35003920212974897128e-08;
     const double zero = 0.0, one = 1.0, two = 2.0, two53 = 9007199254740992.0, huge = 1.0e300, tiny = 1.0e-300;
     const double L1 = 5.99999999999994648725e-01, L2 = 4.28571428578550184252e-01, L3 = 3.33333329818377432918e-01,
                  L4 = 2.72728123808534006489e-01, L5 = 2.30660745775561754067e-01, L6 = 2.06975017800338417784e-01;
@@ -278,12 +279,13 @@ GBM_HD double gbm_pow(double x, double y) {
             ix -= 0x00100000;
         }
         ax = gbm_set_hi(ax, ix);
-        u = ax - bp[k];
-        v = GBM_DIV(one, ax + bp[k]);
+        const double bpk = k ? 1.5 : 1.0, dphk = k ? dp_h1 : 0.0, dplk = k ? dp_l1 : 0.0;
+        u = ax - bpk;
+        v = GBM_DIV(one, ax + bpk);
         ss = u * v;
         s_h = gbm_set_lo(ss, 0);
         t_h = gbm_make(((ix >> 1) | 0x20000000) + 0x00080000 + (k << 18), 0);
-        t_l = ax - (t_h - bp[k]);
+        t_l = ax - (t_h - bpk);
         s_l = v * ((u - s_h * t_h) - s_h * t_l);
         s2 = ss * ss;
         r = s2 * s2 * (L1 + s2 * (L2 + s2 * (L3 + s2 * (L4 + s2 * (L5 + s2 * L6)))));
@@ -296,10 +298,10 @@ GBM_HD double gbm_pow(double x, double y) {
         p_h = gbm_set_lo(u + v, 0);
         p_l = v - (p_h - u);
         z_h = cp_h * p_h;
-        z_l = cp_l * p_h + p_l * cp + dp_l[k];
+        z_l = cp_l * p_h + p_l * cp + dplk;
         t = (double)n;
-        t1 = gbm_set_lo(((z_h + z_l) + dp_h[k]) + t, 0);
-        t2 = z_l - (((t1 - t) - dp_h[k]) - z_h);
+        t1 = gbm_set_lo(((z_h + z_l) + dphk) + t, 0);
+        t2 = z_l - (((t1 - t) - dphk) - z_h);
     }
     /* (y1 + y2) * (t1 + t2) */
     y1 = gbm_set_lo(y, 0);
