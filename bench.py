@@ -71,10 +71,12 @@ BYTES_PER_CELL = {"_dynamu_region1": 12, "_dynamv_region1": 12, "_dynamw_region1
 # every region with the rate constants (the k_kzz and k_chem_krates launches): DRAM bytes
 # (dram__bytes_read.sum + dram__bytes_write.sum), the roofline's traffic, and FP64 warp
 # instructions (smsp__inst_executed_pipe_fp64.sum), whose issue bounds the step
-# (profiles/interval_dram_fp64_glb3x2+nam1x1.md, profiles/interval_dram_fp64_a100-case.md)
+# (profiles/interval_dram_fp64_glb3x2+nam1x1.md, profiles/interval_dram_fp64_a100-case.md);
+# Calc_Kzz's FP64 count with its levels and interfaces kernels re-captured after log's tails
+# were given their common products (the same file's single-kernel capture)
 TRAFFIC_PER_CALL = {"glb3x2+nam1x1": {"convec_region@2": 131.5e6, "convec_region@1": 240.9e6, "calc_kzz": 131.8e6},
                     "a100-case": {"convec_region@2": 49.66e6, "convec_region@1": 182.7e6}}
-FP64_PER_CALL = {"glb3x2+nam1x1": {"convec_region@2": 2.623e6, "convec_region@1": 3.319e6, "calc_kzz": 13.866e6},
+FP64_PER_CALL = {"glb3x2+nam1x1": {"convec_region@2": 2.623e6, "convec_region@1": 3.319e6, "calc_kzz": 13.603e6},
                  "a100-case": {"convec_region@2": 1.394e6, "convec_region@1": 3.827e6}}
 
 
